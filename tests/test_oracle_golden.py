@@ -1,0 +1,81 @@
+"""Pin the CPU oracle against the reference's own golden vectors (no GPU).
+
+Fixtures come from tests/golden/make_golden.py: the (r, fval, U) tables of the
+reference's unit tests and outputs of the reference's own header-only
+routines (Hilbert map, DSFUN) compiled from its source tree.
+"""
+import struct
+
+import numpy as np
+import pytest
+
+import oracle
+
+EPS64 = np.finfo(np.float64).eps
+
+
+@pytest.mark.parametrize("trunc", ["sharp", "shifted", "force_shifted", "smooth_r4"])
+def test_lj_tables(golden, trunc):
+    g = golden("lj_tables.json")
+    pot = oracle.Potential(g["epsilon"], g["sigma"], g["r_cut_sigma"], trunc, h=g["h"])
+    tol = g["tolerance_eps_double"] * EPS64
+    for pair, (a, b) in {"aa": (0, 0), "ab": (0, 1), "bb": (1, 1)}.items():
+        for r, fval, en in g["tables"][trunc][pair]:
+            f, e = pot(r * r, a, b)
+            # BOOST_CHECK_CLOSE_FRACTION semantics: |x-y| <= tol*|y| (exact zeros compare absolutely)
+            assert abs(f - fval) <= tol * abs(fval) or (fval == 0 and abs(f) < 1e-30), (trunc, pair, r, f, fval)
+            assert abs(e - en) <= tol * abs(en) or (en == 0 and abs(e) < 1e-12), (trunc, pair, r, e, en)
+
+
+def test_smooth_r4_near_cutoff(golden):
+    g = golden("smooth_r4_tables.json")
+    pot = oracle.Potential(g["epsilon"], g["sigma"], g["r_cut_sigma"], "smooth_r4", h=g["h"])
+    rcut = pot.r_cut
+    for pair, (a, b), k, kf in (("aa", (0, 0), 8, 1), ("ab", (0, 1), 8, 1), ("bb", (1, 1), 9, 2)):
+        rc = rcut[a, b]
+        for r, fval, en in g["tables"][pair]:
+            f, e = pot(r * r, a, b)
+            tol = k * EPS64 * (1 + rc / (rc - r))
+            assert abs(f - fval) <= kf * tol * abs(fval), (pair, r, f, fval)
+            assert abs(e - en) <= tol * abs(en), (pair, r, e, en)
+
+
+def test_accumulator(golden):
+    g = golden("accumulator.json")
+    s = oracle.accumulate(g["values"])
+    assert s["count"] == g["count"]
+    for key in ("mean", "variance", "sigma", "error_of_mean", "sum"):
+        assert abs(s[key] - g[key]) <= g["tolerance"] * abs(g[key])
+
+
+def test_hilbert_map_matches_reference(golden):
+    g = golden("hilbert_keys.json")
+    for case in g["cases"]:
+        pts = np.asarray(case["points"], dtype=np.float32)
+        keys = oracle.hilbert_map_unit(pts, case["depth"])
+        assert keys.tolist() == case["keys"], case["depth"]
+
+
+def _f(u):
+    return struct.unpack("<f", struct.pack("<I", u))[0]
+
+
+@pytest.mark.parametrize("op", ["add", "sub", "mul"])
+def test_dsfun_matches_reference(golden, op):
+    rows = np.asarray(golden("dsfun.json")[op], dtype=np.uint64).astype(np.uint32)
+    a = rows[:, 0:2].copy().view(np.float32)
+    b = rows[:, 2:4].copy().view(np.float32)
+    c = oracle.dsfun(op, a, b)
+    assert np.array_equal(c.view(np.uint32), rows[:, 4:6])
+
+
+def test_philox_known_answers():
+    # Random123 known-answer vectors for philox4x32-10
+    cases = [
+        ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+        ((0xFFFFFFFF,) * 4, (0xFFFFFFFF, 0xFFFFFFFF), (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+        ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+         (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+    ]
+    for ctr, key, want in cases:
+        assert oracle.philox4x32_10(ctr, key).tolist() == list(want)
