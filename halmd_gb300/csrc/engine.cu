@@ -1,0 +1,933 @@
+// engine.cu — host runtime: layout, buffers, step graph, overflow recovery.
+#include "engine.h"
+#include "kernels.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace hmd {
+
+void cuda_check(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw Error(HMD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+static uint32_t ceil_log2(uint64_t x)
+{
+    uint32_t b = 0;
+    while ((1ull << b) < x) ++b;
+    return b;
+}
+
+static uint32_t round_up(uint32_t x, uint32_t m) { return (x + m - 1) / m * m; }
+
+Engine::Engine(int precision, int device) : precision_(precision), device_(device)
+{
+    if (precision != HMD_PRECISION_FLOAT && precision != HMD_PRECISION_DSFLOAT)
+        throw Error(HMD_ERR_INVALID, "precision must be HMD_PRECISION_FLOAT or HMD_PRECISION_DSFLOAT");
+    int ndev = 0;
+    HMD_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) throw Error(HMD_ERR_INVALID, "no such CUDA device");
+    HMD_CUDA(cudaSetDevice(device));
+    HMD_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    HMD_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+}
+
+Engine::~Engine()
+{
+    cudaSetDevice(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    destroy_graphs();
+    if (stream_) cudaStreamDestroy(stream_);
+    if (side_) cudaStreamDestroy(side_);
+}
+
+void Engine::check_committed() const
+{
+    if (!committed_) throw Error(HMD_ERR_STATE, "engine is not committed");
+}
+
+void Engine::check_sys(uint32_t s) const
+{
+    check_committed();
+    if (s >= sys_.size()) throw Error(HMD_ERR_INVALID, "no such system");
+}
+
+const SysHost& Engine::system(uint32_t s) const
+{
+    check_sys(s);
+    return sys_[s];
+}
+
+void Engine::sync() { HMD_CUDA(cudaStreamSynchronize(stream_)); }
+
+// LJ in double for the cut-off constants (lennard_jones.hpp:56-66)
+static void lj_double(double eps, double sigma2, double rr, double& fval, double& en)
+{
+    const double rri = sigma2 / rr;
+    const double r6i = rri * rri * rri;
+    const double eps_r6i = eps * r6i;
+    fval = 48 * rri * eps_r6i * (r6i - 0.5) / sigma2;
+    en = 4 * eps_r6i * (r6i - 1);
+}
+
+uint32_t Engine::add_system(const hmd_system_desc& d)
+{
+    if (committed_) throw Error(HMD_ERR_STATE, "systems must be added before commit");
+    if (d.nparticle == 0) throw Error(HMD_ERR_INVALID, "nparticle must be positive");
+    if (d.nspecies < 1 || d.nspecies > HMD_MAX_SPECIES) throw Error(HMD_ERR_INVALID, "nspecies out of range [1, 4]");
+    if (d.truncation < 0 || d.truncation > 3) throw Error(HMD_ERR_INVALID, "unknown truncation");
+    if (d.integrator != HMD_INTEGRATOR_VERLET && d.integrator != HMD_INTEGRATOR_ANDERSEN)
+        throw Error(HMD_ERR_INVALID, "unknown integrator");
+    if (!(d.timestep > 0)) throw Error(HMD_ERR_INVALID, "timestep must be positive");
+    if (!(d.skin >= 0)) throw Error(HMD_ERR_INVALID, "skin must be non-negative");
+    if (!(d.cell_occupancy > 0) || !(d.neighbour_occupancy > 0)) throw Error(HMD_ERR_INVALID, "occupancy must be positive");
+    if (d.truncation == HMD_TRUNC_SMOOTH_R4 && !(d.smoothing > 0)) throw Error(HMD_ERR_INVALID, "smooth_r4 needs h > 0");
+    const uint32_t ns = d.nspecies;
+    for (uint32_t ab = 0; ab < ns * ns; ++ab) {
+        if (!(d.sigma[ab] > 0) || !(d.r_cut[ab] > 0) || !(d.epsilon[ab] >= 0))
+            throw Error(HMD_ERR_INVALID, "bad potential parameters");
+    }
+    for (int q = 0; q < 3; ++q)
+        if (!(d.box[q] > 0)) throw Error(HMD_ERR_INVALID, "box edges must be positive");
+    if (d.integrator == HMD_INTEGRATOR_ANDERSEN && (!(d.temperature >= 0) || !(d.collision_rate >= 0)))
+        throw Error(HMD_ERR_INVALID, "bad thermostat parameters");
+    if (sys_.size() >= 65536) throw Error(HMD_ERR_INVALID, "too many systems");
+    SysHost h;
+    std::memset(&h.P, 0, sizeof(h.P));
+    h.desc = d;
+    sys_.push_back(h);
+    return (uint32_t)(sys_.size() - 1);
+}
+
+void Engine::layout_system(SysHost& h, uint32_t rank)
+{
+    const hmd_system_desc& d = h.desc;
+    SysParam& P = h.P;
+    const uint32_t ns = d.nspecies;
+    P.n = d.nparticle;
+    P.A = round_up(std::max<uint32_t>(d.nparticle, 1), SLOT_ALIGN);
+    P.ns = ns;
+    P.trunc = (uint32_t)d.truncation;
+    P.rank = rank;
+    P.active = 1;
+    P.sort_enable = d.sort ? 1u : 0u;
+    P.integrator = (uint32_t)d.integrator;
+    double rc_max = 0, rcs_max = 0;
+    h.pairs.resize(ns * ns);
+    for (uint32_t ab = 0; ab < ns * ns; ++ab) {
+        const double sigma = d.sigma[ab], eps = d.epsilon[ab];
+        const double sigma2 = sigma * sigma;
+        const double rc = sigma * d.r_cut[ab];
+        const double rcs = rc + d.skin;
+        double fc, ec;
+        lj_double(eps, sigma2, rc * rc, fc, ec);
+        PairParam& p = h.pairs[ab];
+        p.eps4 = (float)(4 * eps);
+        p.c48 = (float)(48 * eps / sigma2);
+        p.sigma2 = (float)sigma2;
+        p.rr_cut = (float)(rc * rc);
+        p.r_cut = (float)rc;
+        p.rr_cut_skin = (float)(rcs * rcs);
+        p.en_cut = (d.truncation == HMD_TRUNC_SHARP) ? 0.0f : (float)ec;
+        p.f_cut = (d.truncation == HMD_TRUNC_FORCE_SHIFTED) ? (float)(fc * rc) : 0.0f;
+        rc_max = std::max(rc_max, rc);
+        rcs_max = std::max(rcs_max, rcs);
+    }
+    P.rri_smooth = (d.truncation == HMD_TRUNC_SMOOTH_R4) ? (float)std::pow(d.smoothing, -2) : 0.0f;
+    P.dt = (float)d.timestep;
+    P.dt_half = (float)(d.timestep / 2);
+    P.rr_half_skin = (float)(0.25 * d.skin * d.skin);
+    P.sqrt_T = (float)std::sqrt(d.temperature);
+    {
+        const double q = d.collision_rate * d.timestep;
+        P.coll_threshold = (d.integrator == HMD_INTEGRATOR_ANDERSEN)
+                               ? (uint32_t)std::min(4294967295.0, std::floor(q * 4294967296.0)) : 0u;
+    }
+    P.seed_lo = (uint32_t)d.seed;
+    P.seed_hi = (uint32_t)(d.seed >> 32);
+    float Lmax = 0;
+    for (int q = 0; q < 3; ++q) {
+        const float Lf = (float)d.box[q];
+        P.L[q] = Lf;
+        P.Linv[q] = (float)(1.0 / (double)Lf);
+        Lmax = std::max(Lmax, Lf);
+        if (!(d.box[q] > 2 * rc_max))
+            throw Error(HMD_ERR_INVALID, "box edge must exceed twice the largest cutoff (minimum image)");
+    }
+    // Hilbert depth (gpu/sorts/hilbert.cpp:51-54)
+    P.depth = std::min(10u, (uint32_t)std::ceil(std::log((double)Lmax) / M_LN2));
+    // binning sizing (gpu/binning.cpp:81-101)
+    const double warp = 32;
+    const double nwarps = d.nparticle / (d.cell_occupancy * warp);
+    const double volume = d.box[0] * d.box[1] * d.box[2];
+    uint32_t ncells = 1;
+    for (int q = 0; q < 3; ++q) {
+        const int nmax = (int)(d.box[q] / rcs_max);
+        const int nc = (int)std::ceil(d.box[q] * std::pow(nwarps / volume, 1.0 / 3));
+        P.ncell[q] = std::max(1, std::min(nc, nmax));
+        P.cell_len[q] = P.L[q] / (float)P.ncell[q];
+        ncells *= (uint32_t)P.ncell[q];
+    }
+    P.ncells = ncells;
+    P.cell_size = (uint32_t)(warp * std::ceil(nwarps / ncells));
+    P.cell_size = std::max<uint32_t>(32, P.cell_size);
+    if (P.cell_size > 256) throw Error(HMD_ERR_INVALID, "cell size above 256 slots; lower the density or occupancy");
+    // neighbour list capacity (from_binning.cpp:96-119)
+    const float sphere = (float)(4 * M_PI / 3) * std::pow((float)rcs_max, 3.0f);
+    const float density = (float)(d.nparticle / volume);
+    h.nbr_size = (uint32_t)std::ceil(sphere * (density / (float)d.neighbour_occupancy));
+    h.nbr_size = std::max<uint32_t>(h.nbr_size, 32);
+}
+
+void Engine::commit()
+{
+    if (committed_) throw Error(HMD_ERR_STATE, "engine already committed");
+    if (sys_.empty()) throw Error(HMD_ERR_STATE, "no systems");
+    HMD_CUDA(cudaSetDevice(device_));
+    S_ = 0;
+    total_cells_ = 0;
+    uint32_t cell_words = 0;
+    nbr_cap_ = 0;
+    uint32_t shift = 0;
+    any_sort_ = false;
+    for (uint32_t s = 0; s < sys_.size(); ++s) {
+        SysHost& h = sys_[s];
+        layout_system(h, s);
+        h.P.off = S_;
+        S_ += h.P.A;
+        h.P.cell_off = total_cells_;
+        h.P.cell_word_off = cell_words;
+        total_cells_ += h.P.ncells;
+        cell_words += h.P.ncells * h.P.cell_size;
+        nbr_cap_ = std::max(nbr_cap_, h.nbr_size);
+        shift = std::max(shift, std::max(3 * h.P.depth, ceil_log2(h.P.A)));
+        any_sort_ = any_sort_ || h.P.sort_enable;
+    }
+    const uint32_t rank_bits = ceil_log2(sys_.size());
+    if (shift + rank_bits > 32) {
+        // reduce the Hilbert depth of the deepest systems until the key fits
+        const uint32_t avail = 32 - rank_bits;
+        shift = 0;
+        for (auto& h : sys_) {
+            while (3 * h.P.depth > avail && h.P.depth > 1) --h.P.depth;
+            if (ceil_log2(h.P.A) > avail) throw Error(HMD_ERR_INVALID, "too many slots for the sort key");
+            shift = std::max(shift, std::max(3 * h.P.depth, ceil_log2(h.P.A)));
+        }
+    }
+    key_bits_ = shift + rank_bits;
+    for (auto& h : sys_) h.P.key_shift = shift;
+
+    const size_t S = S_;
+    pos_.alloc(2 * S); vel_.alloc(2 * S); img_.alloc(S); force_.alloc(S); r0_.alloc(S);
+    tpos_.alloc(2 * S); tvel_.alloc(2 * S); timg_.alloc(S); tid_.alloc(S);
+    en_pot_.alloc(S); stress_.alloc(6 * S);
+    id_.alloc(S); rid_.alloc(S);
+    nbr_.alloc((size_t)nbr_cap_ * S); nbr_count_.alloc(S);
+    cell_.alloc(std::max<uint32_t>(cell_words, 1)); cell_count_.alloc(total_cells_); cell_sys_.alloc(total_cells_);
+    chunk_sys_.alloc(S / CHUNK);
+    key0_.alloc(S); key1_.alloc(S); val0_.alloc(S); val1_.alloc(S); hist_.alloc(radix_hist_words(S_));
+    status_.alloc(1); done_.alloc(1); any_rebuild_.alloc(1);
+    dsys_.alloc(sys_.size()); dst_.alloc(sys_.size());
+    {
+        size_t np = 0;
+        for (auto& h : sys_) np += h.pairs.size();
+        dpair_.alloc(np);
+    }
+    partial_.alloc((S / 256) * NTHERMO + 1); thermo_.alloc(sys_.size() * NTHERMO);
+
+    // initial contents: ghosts everywhere, real particles at slot = off + tag
+    std::vector<float4> hpos(2 * S), hvel(2 * S, make_float4(0, 0, 0, 0));
+    std::vector<uint32_t> hid(S, PLACEHOLDER), hrid(S, 0), hchunk(S / CHUNK), hcs(total_cells_);
+    float ghost;
+    {
+        uint32_t g = PLACEHOLDER;
+        std::memcpy(&ghost, &g, 4);
+    }
+    for (size_t k = 0; k < 2 * S; ++k) hpos[k] = make_float4(0, 0, 0, k < S ? ghost : 0.0f);
+    for (uint32_t s = 0; s < sys_.size(); ++s) {
+        const SysParam& P = sys_[s].P;
+        for (uint32_t c = P.off / CHUNK; c < (P.off + P.A) / CHUNK; ++c) hchunk[c] = s;
+        for (uint32_t c = P.cell_off; c < P.cell_off + P.ncells; ++c) hcs[c] = s;
+        for (uint32_t t = 0; t < P.A; ++t) {
+            const uint32_t slot = P.off + t;
+            hrid[slot] = slot;
+            if (t < P.n) {
+                hid[slot] = t;
+                float zero = 0.0f;
+                hpos[slot].w = zero;   // species 0
+                hvel[slot].w = 1.0f;   // unit mass (particle.cpp:56-160)
+            }
+        }
+    }
+    HMD_CUDA(cudaMemcpyAsync(pos_.p, hpos.data(), pos_.bytes(), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(vel_.p, hvel.data(), vel_.bytes(), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(r0_.p, hpos.data(), r0_.bytes(), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemsetAsync(img_.p, 0, img_.bytes(), stream_));
+    HMD_CUDA(cudaMemsetAsync(force_.p, 0, force_.bytes(), stream_));
+    HMD_CUDA(cudaMemsetAsync(en_pot_.p, 0, en_pot_.bytes(), stream_));
+    HMD_CUDA(cudaMemsetAsync(stress_.p, 0, stress_.bytes(), stream_));
+    HMD_CUDA(cudaMemsetAsync(nbr_count_.p, 0, nbr_count_.bytes(), stream_));
+    HMD_CUDA(cudaMemsetAsync(cell_count_.p, 0, cell_count_.bytes(), stream_));
+    HMD_CUDA(cudaMemsetAsync(status_.p, 0, status_.bytes(), stream_));
+    HMD_CUDA(cudaMemsetAsync(done_.p, 0, done_.bytes(), stream_));
+    HMD_CUDA(cudaMemsetAsync(any_rebuild_.p, 0, any_rebuild_.bytes(), stream_));
+    HMD_CUDA(cudaMemcpyAsync(id_.p, hid.data(), id_.bytes(), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(rid_.p, hrid.data(), rid_.bytes(), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(chunk_sys_.p, hchunk.data(), chunk_sys_.bytes(), cudaMemcpyHostToDevice, stream_));
+    if (total_cells_) HMD_CUDA(cudaMemcpyAsync(cell_sys_.p, hcs.data(), cell_sys_.bytes(), cudaMemcpyHostToDevice, stream_));
+    std::vector<SysState> st(sys_.size());
+    for (auto& t : st) {
+        std::memset(&t, 0, sizeof(t));
+        t.steps_left = 0xFFFFFFFFu;
+        t.rebuild_request = 1u;
+    }
+    HMD_CUDA(cudaMemcpyAsync(dst_.p, st.data(), dst_.bytes(), cudaMemcpyHostToDevice, stream_));
+    upload_tables();
+    sync();
+    committed_ = true;
+}
+
+void Engine::upload_tables()
+{
+    std::vector<SysParam> P(sys_.size());
+    std::vector<PairParam> pp;
+    for (uint32_t s = 0; s < sys_.size(); ++s) {
+        sys_[s].P.pair_off = (uint32_t)pp.size();
+        P[s] = sys_[s].P;
+        pp.insert(pp.end(), sys_[s].pairs.begin(), sys_[s].pairs.end());
+    }
+    HMD_CUDA(cudaMemcpyAsync(dsys_.p, P.data(), dsys_.bytes(), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(dpair_.p, pp.data(), pp.size() * sizeof(PairParam), cudaMemcpyHostToDevice, stream_));
+}
+
+Dev Engine::dev() const
+{
+    Dev d;
+    std::memset(&d, 0, sizeof(d));
+    d.pos = pos_.p; d.vel = vel_.p; d.img = img_.p; d.force = force_.p; d.r0 = r0_.p;
+    d.en_pot = en_pot_.p; d.stress = stress_.p; d.id = id_.p; d.rid = rid_.p;
+    d.nbr = nbr_.p; d.nbr_count = nbr_count_.p; d.nbr_cap = nbr_cap_;
+    d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
+    d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
+    d.S = S_; d.nsys = (uint32_t)sys_.size();
+    d.status = status_.p; d.done = done_.p; d.any_rebuild = any_rebuild_.p;
+    d.key[0] = key0_.p; d.key[1] = key1_.p; d.val[0] = val0_.p; d.val[1] = val1_.p; d.hist = hist_.p;
+    d.tpos = tpos_.p; d.tvel = tvel_.p; d.timg = timg_.p; d.tid = tid_.p;
+    d.partial = partial_.p; d.thermo = thermo_.p;
+    return d;
+}
+
+template <typename T>
+void Engine::download(const DevBuf<T>& b, size_t first, size_t count, T* host)
+{
+    if (count == 0) return;
+    HMD_CUDA(cudaMemcpyAsync(host, b.p + first, count * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+    sync();
+}
+
+template <typename T>
+void Engine::upload(DevBuf<T>& b, size_t first, size_t count, const T* host)
+{
+    if (count == 0) return;
+    HMD_CUDA(cudaMemcpyAsync(b.p + first, host, count * sizeof(T), cudaMemcpyHostToDevice, stream_));
+    sync();
+}
+
+std::vector<SysState> Engine::read_state()
+{
+    std::vector<SysState> st(sys_.size());
+    download(dst_, 0, st.size(), st.data());
+    return st;
+}
+
+void Engine::write_state(const std::vector<SysState>& st) { upload(dst_, 0, st.size(), st.data()); }
+
+std::vector<uint32_t> Engine::slots_of(uint32_t s)
+{
+    const SysParam& P = sys_[s].P;
+    std::vector<uint32_t> r(P.n);
+    download(rid_, P.off, P.n, r.data());
+    return r;
+}
+
+static float f32_from_bits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+static uint32_t bits_of(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+
+void Engine::set(uint32_t s, const std::string& name, const void* host, size_t count)
+{
+    check_sys(s);
+    const SysParam& P = sys_[s].P;
+    const uint32_t n = P.n;
+    const size_t S = S_;
+    std::vector<uint32_t> slot = slots_of(s);
+    auto need = [&](size_t k) {
+        if (count != k) throw Error(HMD_ERR_INVALID, "array '" + name + "' needs " + std::to_string(k) + " elements");
+    };
+    if (name == "position") {
+        need(3 * (size_t)n);
+        const double* x = static_cast<const double*>(host);
+        std::vector<float4> hi(P.A), lo(P.A), im(P.A);
+        download(pos_, P.off, P.A, hi.data());
+        download(pos_, S + P.off, P.A, lo.data());
+        download(img_, P.off, P.A, im.data());
+        for (uint32_t t = 0; t < n; ++t) {
+            const uint32_t k = slot[t] - P.off;
+            float* h = &hi[k].x;
+            float* l = &lo[k].x;
+            float* g = &im[k].x;
+            for (int q = 0; q < 3; ++q) {
+                const double L = (double)P.L[q];
+                const double w = std::rint(x[3 * t + q] / L);
+                const double xr = x[3 * t + q] - w * L;
+                h[q] = (float)xr;
+                l[q] = ds() ? (float)(xr - (double)h[q]) : 0.0f;
+                g[q] = (float)((double)g[q] + w);
+            }
+        }
+        upload(pos_, P.off, P.A, hi.data());
+        upload(pos_, S + P.off, P.A, lo.data());
+        upload(img_, P.off, P.A, im.data());
+        forces_valid_ = false;
+        request_rebuild(s);
+    } else if (name == "velocity") {
+        need(3 * (size_t)n);
+        const double* x = static_cast<const double*>(host);
+        std::vector<float4> hi(P.A), lo(P.A);
+        download(vel_, P.off, P.A, hi.data());
+        download(vel_, S + P.off, P.A, lo.data());
+        for (uint32_t t = 0; t < n; ++t) {
+            const uint32_t k = slot[t] - P.off;
+            float* h = &hi[k].x;
+            float* l = &lo[k].x;
+            for (int q = 0; q < 3; ++q) {
+                h[q] = (float)x[3 * t + q];
+                l[q] = ds() ? (float)(x[3 * t + q] - (double)h[q]) : 0.0f;
+            }
+        }
+        upload(vel_, P.off, P.A, hi.data());
+        upload(vel_, S + P.off, P.A, lo.data());
+    } else if (name == "mass") {
+        need(n);
+        const double* x = static_cast<const double*>(host);
+        std::vector<float4> hi(P.A);
+        download(vel_, P.off, P.A, hi.data());
+        for (uint32_t t = 0; t < n; ++t) {
+            if (!(x[t] > 0)) throw Error(HMD_ERR_INVALID, "mass must be positive");
+            hi[slot[t] - P.off].w = (float)x[t];
+        }
+        upload(vel_, P.off, P.A, hi.data());
+    } else if (name == "species") {
+        need(n);
+        const uint32_t* x = static_cast<const uint32_t*>(host);
+        std::vector<float4> hi(P.A);
+        download(pos_, P.off, P.A, hi.data());
+        for (uint32_t t = 0; t < n; ++t) {
+            if (x[t] >= P.ns) throw Error(HMD_ERR_INVALID, "species out of range");
+            hi[slot[t] - P.off].w = f32_from_bits(x[t]);
+        }
+        upload(pos_, P.off, P.A, hi.data());
+        forces_valid_ = false;
+        request_rebuild(s);
+    } else if (name == "image") {
+        need(3 * (size_t)n);
+        const double* x = static_cast<const double*>(host);
+        std::vector<float4> im(P.A);
+        download(img_, P.off, P.A, im.data());
+        for (uint32_t t = 0; t < n; ++t) {
+            float* g = &im[slot[t] - P.off].x;
+            for (int q = 0; q < 3; ++q) g[q] = (float)x[3 * t + q];
+        }
+        upload(img_, P.off, P.A, im.data());
+    } else {
+        throw Error(HMD_ERR_INVALID, "unknown or read-only array '" + name + "'");
+    }
+}
+
+void Engine::get(uint32_t s, const std::string& name, void* host, size_t count)
+{
+    check_sys(s);
+    const SysParam& P = sys_[s].P;
+    const uint32_t n = P.n;
+    const size_t S = S_;
+    auto need = [&](size_t k) {
+        if (count != k) throw Error(HMD_ERR_INVALID, "array '" + name + "' needs " + std::to_string(k) + " elements");
+    };
+    if (name == "id") {
+        need(P.A);
+        download(id_, P.off, P.A, static_cast<uint32_t*>(host));
+        return;
+    }
+    std::vector<uint32_t> slot = slots_of(s);
+    if (name == "reverse_id") {
+        need(n);
+        uint32_t* o = static_cast<uint32_t*>(host);
+        for (uint32_t t = 0; t < n; ++t) o[t] = slot[t] - P.off;
+    } else if (name == "position" || name == "unwrapped_position") {
+        need(3 * (size_t)n);
+        std::vector<float4> hi(P.A), lo(P.A), im(P.A);
+        download(pos_, P.off, P.A, hi.data());
+        download(pos_, S + P.off, P.A, lo.data());
+        download(img_, P.off, P.A, im.data());
+        double* o = static_cast<double*>(host);
+        const bool unwrap = name == "unwrapped_position";
+        for (uint32_t t = 0; t < n; ++t) {
+            const uint32_t k = slot[t] - P.off;
+            const float* h = &hi[k].x;
+            const float* l = &lo[k].x;
+            const float* g = &im[k].x;
+            for (int q = 0; q < 3; ++q)
+                o[3 * t + q] = (double)h[q] + (double)l[q] + (unwrap ? (double)g[q] * (double)P.L[q] : 0.0);
+        }
+    } else if (name == "velocity") {
+        need(3 * (size_t)n);
+        std::vector<float4> hi(P.A), lo(P.A);
+        download(vel_, P.off, P.A, hi.data());
+        download(vel_, S + P.off, P.A, lo.data());
+        double* o = static_cast<double*>(host);
+        for (uint32_t t = 0; t < n; ++t) {
+            const uint32_t k = slot[t] - P.off;
+            const float* h = &hi[k].x;
+            const float* l = &lo[k].x;
+            for (int q = 0; q < 3; ++q) o[3 * t + q] = (double)h[q] + (double)l[q];
+        }
+    } else if (name == "mass" || name == "species") {
+        need(n);
+        std::vector<float4> b(P.A);
+        if (name == "mass") download(vel_, P.off, P.A, b.data());
+        else download(pos_, P.off, P.A, b.data());
+        for (uint32_t t = 0; t < n; ++t) {
+            const float w = b[slot[t] - P.off].w;
+            if (name == "mass") static_cast<double*>(host)[t] = w;
+            else static_cast<uint32_t*>(host)[t] = bits_of(w);
+        }
+    } else if (name == "image" || name == "force") {
+        need(3 * (size_t)n);
+        std::vector<float4> b(P.A);
+        download(name == "image" ? img_ : force_, P.off, P.A, b.data());
+        double* o = static_cast<double*>(host);
+        for (uint32_t t = 0; t < n; ++t) {
+            const float* g = &b[slot[t] - P.off].x;
+            for (int q = 0; q < 3; ++q) o[3 * t + q] = g[q];
+        }
+    } else if (name == "potential_energy") {
+        need(n);
+        std::vector<float> b(P.A);
+        download(en_pot_, P.off, P.A, b.data());
+        double* o = static_cast<double*>(host);
+        for (uint32_t t = 0; t < n; ++t) o[t] = b[slot[t] - P.off];
+    } else if (name == "stress_pot") {
+        need(6 * (size_t)n);
+        double* o = static_cast<double*>(host);
+        std::vector<float> b(P.A);
+        for (int c = 0; c < 6; ++c) {
+            download(stress_, (size_t)c * S + P.off, P.A, b.data());
+            for (uint32_t t = 0; t < n; ++t) o[6 * t + c] = b[slot[t] - P.off];
+        }
+    } else {
+        throw Error(HMD_ERR_INVALID, "unknown array '" + name + "'");
+    }
+}
+
+void Engine::get_raw(uint32_t s, const std::string& name, void* host, size_t bytes)
+{
+    check_sys(s);
+    const SysParam& P = sys_[s].P;
+    const size_t S = S_;
+    auto need = [&](size_t b) {
+        if (bytes != b) throw Error(HMD_ERR_INVALID, "raw array '" + name + "' has " + std::to_string(b) + " bytes");
+    };
+    if (name == "cells") {
+        need((size_t)P.ncells * P.cell_size * 4);
+        uint32_t* o = static_cast<uint32_t*>(host);
+        download(cell_, P.cell_word_off, (size_t)P.ncells * P.cell_size, o);
+        for (size_t k = 0; k < (size_t)P.ncells * P.cell_size; ++k)
+            if (o[k] != PLACEHOLDER) o[k] -= P.off;
+        return;
+    }
+    need((size_t)P.A * 16);
+    float4* o = static_cast<float4*>(host);
+    if (name == "position_hi") download(pos_, P.off, P.A, o);
+    else if (name == "position_lo") download(pos_, S + P.off, P.A, o);
+    else if (name == "velocity_hi") download(vel_, P.off, P.A, o);
+    else if (name == "velocity_lo") download(vel_, S + P.off, P.A, o);
+    else if (name == "image") download(img_, P.off, P.A, o);
+    else if (name == "force") download(force_, P.off, P.A, o);
+    else if (name == "r0") download(r0_, P.off, P.A, o);
+    else throw Error(HMD_ERR_INVALID, "unknown raw array '" + name + "'");
+}
+
+void Engine::info(uint32_t s, hmd_system_info* out)
+{
+    check_sys(s);
+    const SysHost& h = sys_[s];
+    std::vector<SysState> st = read_state();
+    std::memset(out, 0, sizeof(*out));
+    out->nparticle = h.P.n;
+    out->nspecies = h.P.ns;
+    out->slot_offset = h.P.off;
+    out->slots = h.P.A;
+    for (int q = 0; q < 3; ++q) { out->ncell[q] = h.P.ncell[q]; out->box_f32[q] = h.P.L[q]; }
+    out->cell_size = h.P.cell_size;
+    out->neighbour_capacity = nbr_cap_;
+    out->hilbert_depth = h.P.depth;
+    out->max_neighbours = st[s].max_nbr;
+    out->max_cell_occupancy = st[s].max_cell;
+    out->step = st[s].step;
+    out->rebuilds = st[s].rebuilds;
+    for (size_t ab = 0; ab < h.pairs.size(); ++ab) {
+        out->rr_cut_skin[ab] = h.pairs[ab].rr_cut_skin;
+        out->rr_cut[ab] = h.pairs[ab].rr_cut;
+    }
+}
+
+void Engine::request_rebuild(uint32_t s)
+{
+    check_sys(s);
+    std::vector<SysState> st = read_state();
+    st[s].rebuild_request = 1u;
+    write_state(st);
+    forces_valid_ = false;
+}
+
+void Engine::set_steps_left(uint32_t s, uint32_t steps)
+{
+    check_sys(s);
+    std::vector<SysState> st = read_state();
+    st[s].steps_left = steps;
+    write_state(st);
+}
+
+// ---- the step --------------------------------------------------------------
+
+void Engine::rebuild_chain(cudaStream_t st)
+{
+    const Dev d = dev();
+    if (any_sort_) {
+        const int cur = launch_sort(d, key_bits_, st);
+        launch_rearrange(d, ds(), cur == 0 ? d.val[0] : d.val[1], st);
+    }
+    launch_binning(d, st);
+    launch_neighbour(d, st);
+}
+
+void Engine::ensure_forces(bool aux)
+{
+    if (forces_valid_ && (!aux || aux_valid_)) return;
+    const Dev d = dev();
+    launch_mark(d, false, stream_);
+    rebuild_chain(stream_);
+    launch_force(d, aux, stream_);
+    HMD_CUDA(cudaGetLastError());
+    uint32_t status = 0;
+    download(status_, 0, 1, &status);
+    if (status != 0) {
+        if (!grow_after_overflow(status)) throw Error(HMD_ERR_OVERFLOW, "capacity overflow in the initial list build");
+        HMD_CUDA(cudaMemsetAsync(status_.p, 0, 4, stream_));
+        std::vector<SysState> st = read_state();
+        for (auto& t : st) t.rebuild_request = 1u;
+        write_state(st);
+        forces_valid_ = false;
+        ensure_forces(aux);
+        return;
+    }
+    forces_valid_ = true;
+    aux_valid_ = aux;
+    integrated_ = false;
+}
+
+cudaGraphExec_t Engine::capture(int nsteps, bool aux_last)
+{
+    const Dev d = dev();
+    cudaGraph_t g;
+    HMD_CUDA(cudaGraphCreate(&g, 0));
+    HMD_CUDA(cudaStreamBeginCaptureToGraph(stream_, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    try {
+        for (int k = 0; k < nsteps; ++k) {
+            cudaGraphConditionalHandle h;
+            HMD_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+            launch_integrate(d, ds(), h, true, stream_);
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t cg;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t nd = 0;
+            HMD_CUDA(cudaStreamGetCaptureInfo(stream_, &cs, nullptr, &cg, &deps, nullptr, &nd));
+            cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeIf;
+            cp.conditional.size = 1;
+            cudaGraphNode_t cn;
+            HMD_CUDA(cudaGraphAddNode(&cn, cg, deps, nullptr, nd, &cp));
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            HMD_CUDA(cudaStreamUpdateCaptureDependencies(stream_, &cn, nullptr, 1, cudaStreamSetCaptureDependencies));
+            HMD_CUDA(cudaStreamBeginCaptureToGraph(side_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            rebuild_chain(side_);
+            cudaGraph_t body_out;
+            HMD_CUDA(cudaStreamEndCapture(side_, &body_out));
+            launch_force(d, aux_last && k == nsteps - 1, stream_);
+            launch_finalize(d, ds(), stream_);
+        }
+    } catch (...) {
+        cudaGraph_t tmp;
+        cudaStreamEndCapture(stream_, &tmp);
+        cudaGraphDestroy(g);
+        throw;
+    }
+    cudaGraph_t out;
+    HMD_CUDA(cudaStreamEndCapture(stream_, &out));
+    cudaGraphExec_t exec;
+    HMD_CUDA(cudaGraphInstantiate(&exec, out, 0));
+    HMD_CUDA(cudaGraphDestroy(out));
+    return exec;
+}
+
+void Engine::destroy_graphs()
+{
+    if (g_chunk_) cudaGraphExecDestroy(g_chunk_);
+    if (g_one_) cudaGraphExecDestroy(g_one_);
+    if (g_one_aux_) cudaGraphExecDestroy(g_one_aux_);
+    g_chunk_ = g_one_ = g_one_aux_ = nullptr;
+}
+
+void Engine::build_graphs()
+{
+    destroy_graphs();
+    g_chunk_ = capture(CHUNK_STEPS, false);
+    g_one_ = capture(1, false);
+    g_one_aux_ = capture(1, true);
+}
+
+void Engine::snapshot()
+{
+    const size_t S = S_;
+    if (!snap_pos_.p) {
+        snap_pos_.alloc(2 * S); snap_vel_.alloc(2 * S); snap_img_.alloc(S); snap_force_.alloc(S);
+        snap_id_.alloc(S); snap_rid_.alloc(S); snap_st_.alloc(sys_.size());
+    }
+    HMD_CUDA(cudaMemcpyAsync(snap_pos_.p, pos_.p, pos_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(snap_vel_.p, vel_.p, vel_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(snap_img_.p, img_.p, img_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(snap_force_.p, force_.p, force_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(snap_id_.p, id_.p, id_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(snap_rid_.p, rid_.p, rid_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(snap_st_.p, dst_.p, dst_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+}
+
+void Engine::restore()
+{
+    HMD_CUDA(cudaMemcpyAsync(pos_.p, snap_pos_.p, pos_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(vel_.p, snap_vel_.p, vel_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(img_.p, snap_img_.p, img_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(force_.p, snap_force_.p, force_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(id_.p, snap_id_.p, id_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(rid_.p, snap_rid_.p, rid_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(dst_.p, snap_st_.p, dst_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    HMD_CUDA(cudaMemsetAsync(status_.p, 0, 4, stream_));
+    HMD_CUDA(cudaMemsetAsync(done_.p, 0, 4, stream_));
+    sync();
+}
+
+// grow cell or list capacity from the occupancies the failed build recorded
+bool Engine::grow_after_overflow(uint32_t status)
+{
+    std::vector<SysState> st = read_state();
+    bool changed = false;
+    if (status & ST_CELL_OVERFLOW) {
+        uint32_t words = 0;
+        for (uint32_t s = 0; s < sys_.size(); ++s) {
+            SysParam& P = sys_[s].P;
+            if (st[s].max_cell > P.cell_size) {
+                const uint32_t want = round_up((uint32_t)std::ceil(st[s].max_cell * 1.25), 32);
+                if (want > 256 || want <= P.cell_size) return false;
+                P.cell_size = want;
+                changed = true;
+            }
+            P.cell_word_off = words;
+            words += P.ncells * P.cell_size;
+        }
+        cell_.alloc(std::max<uint32_t>(words, 1));
+        upload_tables();
+    }
+    if (status & ST_NBR_OVERFLOW) {
+        uint32_t m = 0;
+        for (auto& t : st) m = std::max(m, t.max_nbr);
+        const uint32_t want = (uint32_t)std::ceil(m * 1.2) + 8;
+        if (want <= nbr_cap_) return false;
+        nbr_cap_ = want;
+        nbr_.alloc((size_t)nbr_cap_ * S_);
+        changed = true;
+    }
+    for (auto& t : st) { t.max_cell = 0; t.max_nbr = 0; }
+    write_state(st);
+    if (changed) destroy_graphs();
+    return changed;
+}
+
+void Engine::run_steps(uint64_t nsteps, bool aux_last)
+{
+    if (!g_chunk_) build_graphs();
+    uint64_t left = nsteps;
+    while (left > 0) {
+        if (left >= (uint64_t)CHUNK_STEPS && !(aux_last && left == (uint64_t)CHUNK_STEPS)) {
+            HMD_CUDA(cudaGraphLaunch(g_chunk_, stream_));
+            left -= CHUNK_STEPS;
+        } else if (left == 1 && aux_last) {
+            HMD_CUDA(cudaGraphLaunch(g_one_aux_, stream_));
+            left -= 1;
+        } else {
+            HMD_CUDA(cudaGraphLaunch(g_one_, stream_));
+            left -= 1;
+        }
+    }
+}
+
+void Engine::step(uint64_t nsteps, bool aux_last)
+{
+    check_committed();
+    if (nsteps == 0) return;
+    ensure_forces(false);
+    uint64_t left = nsteps;
+    while (left > 0) {
+        const uint64_t seg = std::min(left, SEGMENT_STEPS);
+        const bool aux = aux_last && seg == left;
+        snapshot();
+        int tries = 0;
+        for (;;) {
+            run_steps(seg, aux);
+            uint32_t status = 0;
+            download(status_, 0, 1, &status);
+            if (status == 0) break;
+            if (++tries > 6 || !grow_after_overflow(status))
+                throw Error(HMD_ERR_OVERFLOW, "neighbour or cell capacity overflow could not be resolved");
+            restore();
+            std::vector<SysState> st = read_state();
+            for (auto& t : st) t.rebuild_request = 1u;
+            write_state(st);
+        }
+        left -= seg;
+    }
+    aux_valid_ = aux_last;
+    forces_valid_ = true;
+    integrated_ = false;
+}
+
+void Engine::integrate()
+{
+    check_committed();
+    ensure_forces(false);
+    launch_integrate(dev(), ds(), 0, false, stream_);
+    HMD_CUDA(cudaGetLastError());
+    integrated_ = true;
+    forces_valid_ = false;
+}
+
+void Engine::force(bool aux)
+{
+    check_committed();
+    if (!integrated_) {
+        forces_valid_ = forces_valid_ && (!aux || aux_valid_);
+        ensure_forces(aux);
+        return;
+    }
+    const Dev d = dev();
+    rebuild_chain(stream_);
+    launch_force(d, aux, stream_);
+    HMD_CUDA(cudaGetLastError());
+    uint32_t status = 0;
+    download(status_, 0, 1, &status);
+    if (status != 0) {
+        if (!grow_after_overflow(status)) throw Error(HMD_ERR_OVERFLOW, "capacity overflow in list rebuild");
+        HMD_CUDA(cudaMemsetAsync(status_.p, 0, 4, stream_));
+        launch_mark(d, true, stream_);
+        const Dev d2 = dev();
+        rebuild_chain(stream_);
+        launch_force(d2, aux, stream_);
+        download(status_, 0, 1, &status);
+        if (status != 0) throw Error(HMD_ERR_OVERFLOW, "capacity overflow in list rebuild");
+    }
+    forces_valid_ = true;
+    aux_valid_ = aux;
+    integrated_ = false;
+}
+
+void Engine::finalize()
+{
+    check_committed();
+    launch_finalize(dev(), ds(), stream_);
+    HMD_CUDA(cudaGetLastError());
+    sync();
+}
+
+double Engine::max_displacement(uint32_t s)
+{
+    check_sys(s);
+    const SysParam& P = sys_[s].P;
+    std::vector<float4> r(P.A), q(P.A);
+    download(pos_, P.off, P.A, r.data());
+    download(r0_, P.off, P.A, q.data());
+    float m = 0;
+    for (uint32_t k = 0; k < P.A; ++k) {
+        if (bits_of(r[k].w) == PLACEHOLDER) continue;
+        float dd[3] = {r[k].x - q[k].x, r[k].y - q[k].y, r[k].z - q[k].z};
+        float rr = 0;
+        for (int c = 0; c < 3; ++c) {
+            const float kk = std::rint(dd[c] * P.Linv[c]);
+            dd[c] = dd[c] - kk * P.L[c];
+            rr += dd[c] * dd[c];
+        }
+        m = std::max(m, rr);
+    }
+    return std::sqrt((double)m);
+}
+
+void Engine::thermo(uint32_t s, double* out)
+{
+    check_sys(s);
+    launch_thermo(dev(), stream_);
+    HMD_CUDA(cudaGetLastError());
+    download(thermo_, (size_t)s * NTHERMO, NTHERMO, out);
+}
+
+void Engine::neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint32_t maxn)
+{
+    check_sys(s);
+    ensure_forces(false);
+    const SysParam& P = sys_[s].P;
+    std::vector<uint32_t> slot = slots_of(s);
+    std::vector<uint32_t> cnt(P.A), id(P.A);
+    download(nbr_count_, P.off, P.A, cnt.data());
+    download(id_, P.off, P.A, id.data());
+    std::vector<uint32_t> col(P.A);
+    for (uint32_t t = 0; t < P.n; ++t) {
+        const uint32_t k = slot[t] - P.off;
+        if (cnt[k] > maxn) throw Error(HMD_ERR_INVALID, "maxn smaller than a neighbour count");
+    }
+    std::vector<uint32_t> all((size_t)nbr_cap_ * P.A);
+    for (uint32_t k = 0; k < nbr_cap_; ++k) download(nbr_, (size_t)k * S_ + P.off, P.A, all.data() + (size_t)k * P.A);
+    for (uint32_t t = 0; t < P.n; ++t) {
+        const uint32_t k = slot[t] - P.off;
+        counts[t] = cnt[k];
+        std::vector<uint32_t> v(cnt[k]);
+        for (uint32_t q = 0; q < cnt[k]; ++q) v[q] = id[all[(size_t)q * P.A + k] - P.off];
+        std::sort(v.begin(), v.end());
+        for (uint32_t q = 0; q < maxn; ++q) lists[(size_t)t * maxn + q] = q < cnt[k] ? v[q] : PLACEHOLDER;
+    }
+}
+
+void Engine::hilbert_keys(uint32_t s, uint32_t* keys)
+{
+    check_sys(s);
+    const SysParam& P = sys_[s].P;
+    launch_hilbert_keys(dev(), key0_.p, stream_);
+    HMD_CUDA(cudaGetLastError());
+    std::vector<uint32_t> k(P.A);
+    download(key0_, P.off, P.A, k.data());
+    std::vector<uint32_t> slot = slots_of(s);
+    for (uint32_t t = 0; t < P.n; ++t) keys[t] = k[slot[t] - P.off];
+}
+
+} // namespace hmd

@@ -1,0 +1,148 @@
+// engine.h — host runtime of the GB300 MD step: layout of the systems in HBM,
+// device buffers, the captured step graph with its on-device rebuild
+// decision, and recovery from capacity overflow.
+#pragma once
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "hmd_device.cuh"
+#include "halmd_gb300.h"
+
+namespace hmd {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char* what);
+#define HMD_CUDA(x) ::hmd::cuda_check((x), #x)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void alloc(size_t count)
+    {
+        release();
+        if (count == 0) return;
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            (void)cudaGetLastError();
+            throw Error(HMD_ERR_NOMEM, std::string("device allocation of ") + std::to_string(count * sizeof(T)) +
+                                           " bytes failed: " + cudaGetErrorString(e));
+        }
+        n = count;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+struct SysHost {
+    hmd_system_desc desc;
+    SysParam P;
+    std::vector<PairParam> pairs;
+    uint32_t nbr_size;   // list capacity estimate (from_binning.cpp:96-119)
+};
+
+class Engine {
+public:
+    Engine(int precision, int device);
+    ~Engine();
+
+    uint32_t add_system(const hmd_system_desc& desc);
+    void commit();
+    void set(uint32_t s, const std::string& name, const void* host, size_t count);
+    void get(uint32_t s, const std::string& name, void* host, size_t count);
+    void get_raw(uint32_t s, const std::string& name, void* host, size_t bytes);
+    void info(uint32_t s, hmd_system_info* out);
+
+    void step(uint64_t nsteps, bool aux_last);
+    void integrate();
+    void force(bool aux);
+    void finalize();
+    void request_rebuild(uint32_t s);
+    void set_steps_left(uint32_t s, uint32_t steps);
+    double max_displacement(uint32_t s);
+    void thermo(uint32_t s, double* out);
+    void neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint32_t maxn);
+    void hilbert_keys(uint32_t s, uint32_t* keys);
+
+    // used by the dynamics module
+    Dev dev() const;
+    cudaStream_t stream() const { return stream_; }
+    const SysHost& system(uint32_t s) const;
+    uint32_t nsys() const { return (uint32_t)sys_.size(); }
+    uint32_t slots() const { return S_; }
+    bool ds() const { return precision_ == HMD_PRECISION_DSFLOAT; }
+    void sync();
+
+    std::string err;
+
+private:
+    void check_committed() const;
+    void check_sys(uint32_t s) const;
+    void layout_system(SysHost& h, uint32_t rank);
+    void upload_tables();
+    void ensure_forces(bool aux);
+    void rebuild_chain(cudaStream_t st);
+    void build_graphs();
+    void destroy_graphs();
+    cudaGraphExec_t capture(int nsteps, bool aux_last);
+    void snapshot();
+    void restore();
+    bool grow_after_overflow(uint32_t status);
+    void run_steps(uint64_t nsteps, bool aux_last);
+    std::vector<SysState> read_state();
+    void write_state(const std::vector<SysState>& st);
+    template <typename T> void download(const DevBuf<T>& b, size_t first, size_t count, T* host);
+    template <typename T> void upload(DevBuf<T>& b, size_t first, size_t count, const T* host);
+    std::vector<uint32_t> slots_of(uint32_t s);   // slot (absolute) of each tag
+
+    int precision_;
+    int device_;
+    bool committed_ = false;
+    bool forces_valid_ = false;
+    bool aux_valid_ = false;
+    bool integrated_ = false;   // hmd_integrate since the last force
+    std::vector<SysHost> sys_;
+    uint32_t S_ = 0;
+    uint32_t total_cells_ = 0;
+    uint32_t nbr_cap_ = 0;
+    uint32_t key_bits_ = 0;
+    bool any_sort_ = false;
+    cudaStream_t stream_ = nullptr;
+    cudaStream_t side_ = nullptr;
+
+    DevBuf<float4> pos_, vel_, img_, force_, r0_, tpos_, tvel_, timg_;
+    DevBuf<float> en_pot_, stress_;
+    DevBuf<uint32_t> id_, rid_, nbr_, nbr_count_, cell_, cell_count_, cell_sys_, chunk_sys_, tid_;
+    DevBuf<uint32_t> key0_, key1_, val0_, val1_, hist_, status_, done_, any_rebuild_;
+    DevBuf<SysParam> dsys_;
+    DevBuf<SysState> dst_;
+    DevBuf<PairParam> dpair_;
+    DevBuf<double> partial_, thermo_;
+    // overflow snapshot
+    DevBuf<float4> snap_pos_, snap_vel_, snap_img_, snap_force_;
+    DevBuf<uint32_t> snap_id_, snap_rid_;
+    DevBuf<SysState> snap_st_;
+
+    static constexpr int CHUNK_STEPS = 50;
+    static constexpr uint64_t SEGMENT_STEPS = 5000;
+    cudaGraphExec_t g_chunk_ = nullptr, g_one_ = nullptr, g_one_aux_ = nullptr;
+};
+
+} // namespace hmd

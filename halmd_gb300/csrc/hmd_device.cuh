@@ -1,0 +1,223 @@
+// hmd_device.cuh — device-side types and arithmetic shared by the MD kernels.
+//
+// Layout (HBM, flat over all systems of an engine):
+//   slots      every system s owns slots [off_s, off_s + A_s), A_s = n_s rounded
+//              up to SLOT_ALIGN; slots past n_s are ghosts (species 0xFFFFFFFF),
+//              following mdsim/gpu/particle.cpp:67-88 (ghost padding).
+//   position   float4 [2*S]: hi words (x, y, z, species bits), then lo words
+//              (dsfloat split, mdsim/gpu/particle.hpp:56-88).  FP32 engines
+//              keep only the hi half.
+//   velocity   float4 [2*S]: (vx, vy, vz, mass) hi, then lo.
+//   image      float4 [S]; force float4 [S]; en_pot float [S];
+//              stress float [6*S] column-major (mdsim/force_kernel.hpp:64-80).
+//   neighbours uint32 [cap * S] transposed: entry k of slot i at k*S + i
+//              (from_binning_kernel.cu:154-158), plus a count per slot.
+//
+// All float arithmetic that must agree bit-for-bit with the CPU oracle
+// (minimum image, squared distance, cell index, Hilbert key, dsfloat
+// integrator) uses the __f*_rn intrinsics so nvcc cannot contract it.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hmd {
+
+constexpr uint32_t PLACEHOLDER = 0xFFFFFFFFu;
+constexpr int MAX_SPECIES = 4;
+constexpr int SLOT_ALIGN = 256;   // slots per system are a multiple of this
+constexpr int CHUNK = 64;         // granularity of the slot -> system map
+
+enum Trunc : uint32_t { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3 };
+enum Integrator : uint32_t { INTEG_VERLET = 0, INTEG_ANDERSEN = 1 };
+enum Status : uint32_t {
+    ST_CELL_OVERFLOW = 1u,
+    ST_NBR_OVERFLOW = 2u,
+};
+
+// per species pair of one system (LJ parameters + truncation constants)
+struct PairParam {
+    float eps4;        // 4 eps
+    float c48;         // 48 eps / sigma^2
+    float sigma2;
+    float rr_cut;      // (float)(r_c^2)
+    float en_cut;      // U(r_c) (0 for sharp)
+    float r_cut;
+    float rr_cut_skin; // (float)((r_c + skin)^2)
+    float f_cut;       // force_shifted: F_c = fval(r_c) r_c
+};
+
+struct SysParam {
+    uint32_t off, n, A;        // slot range and real particle count
+    uint32_t ns, trunc, pair_off;
+    float L[3], Linv[3];
+    int32_t ncell[3];
+    float cell_len[3];
+    uint32_t cell_off;         // first cell of this system in the cell arrays
+    uint32_t cell_size;        // slots per cell (multiple of 32)
+    uint32_t ncells;
+    uint32_t cell_word_off;    // first word of this system's cell contents
+    float rri_smooth;          // h^-2 for smooth_r4
+    float dt, dt_half;
+    float rr_half_skin;        // (skin/2)^2 rebuild threshold on squared displacement
+    uint32_t depth;            // Hilbert recursion depth
+    uint32_t key_shift;        // sort key = (rank << key_shift) | local key
+    uint32_t integrator;
+    float sqrt_T;
+    uint32_t coll_threshold;   // collision iff philox word < threshold
+    uint32_t seed_lo, seed_hi;
+    uint32_t active;           // 0: all slots are ghosts, kernels skip
+    uint32_t sort_enable;      // Hilbert reorder on rebuild
+    uint32_t rank;             // position among systems (sort key prefix)
+};
+
+// mutable per-system device state
+struct SysState {
+    uint32_t disp2_bits;       // running max |r - r0|^2 (float bits, >= 0)
+    uint32_t rebuild;          // 1: rebuild lists in this step
+    uint32_t max_nbr;          // largest neighbour count of the last build
+    uint32_t max_cell;         // largest cell occupancy of the last build
+    unsigned long long step;   // completed integration steps
+    unsigned long long rebuilds;
+    uint32_t steps_left;       // integration steps still to do (0: frozen, ~0u: unbounded)
+    uint32_t live;             // 1: the system advances in the current step
+    uint32_t rebuild_request;  // host-set: rebuild at the next opportunity
+    uint32_t pad;
+};
+
+// device pointers of one engine (passed by value to every kernel)
+struct Dev {
+    float4* pos;               // [2S] hi | lo
+    float4* vel;               // [2S] hi | lo
+    float4* img;               // [S]
+    float4* force;             // [S]
+    float4* r0;                // [S] hi positions at the last list build
+    float* en_pot;             // [S]
+    float* stress;             // [6S]
+    uint32_t* id;              // [S] tag of the particle within its system
+    uint32_t* rid;             // [S] slot of (off + tag)
+    uint32_t* nbr;             // [nbr_cap * S]
+    uint32_t* nbr_count;       // [S]
+    uint32_t nbr_cap;
+    uint32_t* cell;            // cell contents
+    uint32_t* cell_count;      // [total_cells]
+    const uint32_t* cell_sys;  // [total_cells] owning system
+    uint32_t total_cells;
+    const SysParam* sys;
+    SysState* st;
+    const PairParam* pair;
+    const uint32_t* chunk_sys; // [S / CHUNK]
+    uint32_t S, nsys;
+    uint32_t* status;          // ST_* bits
+    uint32_t* done;            // last-block ticket counter
+    uint32_t* any_rebuild;
+    // sort scratch
+    uint32_t* key[2];
+    uint32_t* val[2];
+    uint32_t* hist;
+    // rearrange temporaries
+    float4* tpos;
+    float4* tvel;
+    float4* timg;
+    uint32_t* tid;
+    // reductions
+    double* partial;           // [S / 256 * NTHERMO]
+    double* thermo;            // [nsys * NTHERMO]
+};
+
+constexpr int NTHERMO = 14;    // see k_thermo_partial
+
+__device__ __forceinline__ uint32_t species_bits(float w) { return __float_as_uint(w); }
+
+// minimum image: k = rint(dr / L) via dr * (1/L); dr - k L (box_kernel.cuh:37-47)
+__device__ __forceinline__ float min_image(float dr, float L, float Linv)
+{
+    float k = rintf(__fmul_rn(dr, Linv));
+    return __fsub_rn(dr, __fmul_rn(k, L));
+}
+
+__device__ __forceinline__ float rr_exact(float dx, float dy, float dz)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// ---- double-single arithmetic: Knuth TwoSum / Dekker split (DSFUN) --------
+
+__device__ __forceinline__ void ds_add(float& c0, float& c1, float a0, float a1, float b0, float b1)
+{
+    float t1 = __fadd_rn(a0, b0);
+    float e = __fsub_rn(t1, a0);
+    float t2 = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(b0, e), __fsub_rn(a0, __fsub_rn(t1, e))), a1), b1);
+    e = __fadd_rn(t1, t2);
+    c0 = e;
+    c1 = __fsub_rn(t2, __fsub_rn(e, t1));
+}
+
+__device__ __forceinline__ void ds_sub(float& c0, float& c1, float a0, float a1, float b0, float b1)
+{
+    float t1 = __fsub_rn(a0, b0);
+    float e = __fsub_rn(t1, a0);
+    float t2 = __fsub_rn(__fadd_rn(__fadd_rn(__fsub_rn(-b0, e), __fsub_rn(a0, __fsub_rn(t1, e))), a1), b1);
+    e = __fadd_rn(t1, t2);
+    c0 = e;
+    c1 = __fsub_rn(t2, __fsub_rn(e, t1));
+}
+
+__device__ __forceinline__ void ds_mul(float& c0, float& c1, float a0, float a1, float b0, float b1)
+{
+    float cona = __fmul_rn(a0, 8193.0f);
+    float conb = __fmul_rn(b0, 8193.0f);
+    float sa1 = __fsub_rn(cona, __fsub_rn(cona, a0));
+    float sb1 = __fsub_rn(conb, __fsub_rn(conb, b0));
+    float sa2 = __fsub_rn(a0, sa1);
+    float sb2 = __fsub_rn(b0, sb1);
+    float c11 = __fmul_rn(a0, b0);
+    float c21 = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fmul_rn(sa1, sb1), c11), __fmul_rn(sa1, sb2)),
+                                    __fmul_rn(sa2, sb1)), __fmul_rn(sa2, sb2));
+    float c2 = __fadd_rn(__fmul_rn(a0, b1), __fmul_rn(a1, b0));
+    float t1 = __fadd_rn(c11, c2);
+    float e = __fsub_rn(t1, c11);
+    float t2 = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(c2, e), __fsub_rn(c11, __fsub_rn(t1, e))), c21),
+                         __fmul_rn(a1, b1));
+    e = __fadd_rn(t1, t2);
+    c0 = e;
+    c1 = __fsub_rn(t2, __fsub_rn(e, t1));
+}
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) ---------------------
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t lo0 = 0xD2511F53u * c.x;
+        uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
+        uint32_t lo1 = 0xCD9E8D57u * c.z;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// uniform in (0, 1) from the top 24 bits
+__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f) + (0.5f / 16777216.0f); }
+
+// ---- warp / block helpers -------------------------------------------------
+
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+} // namespace hmd

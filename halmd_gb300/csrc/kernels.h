@@ -1,0 +1,37 @@
+// kernels.h — host-side launchers of the MD kernels (one engine = struct Dev).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hmd {
+
+struct Dev;
+
+// step (kernels_step.cu)
+void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool use_handle, cudaStream_t st);
+void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st);
+void launch_force(const Dev& d, bool aux, cudaStream_t st);
+void launch_finalize(const Dev& d, bool ds, cudaStream_t st);
+void launch_thermo(const Dev& d, cudaStream_t st);
+
+// rebuild (kernels_rebuild.cu)
+int radix_passes(uint32_t key_bits);
+int launch_sort(const Dev& d, uint32_t key_bits, cudaStream_t st);
+void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st);
+void launch_binning(const Dev& d, cudaStream_t st);
+void launch_neighbour(const Dev& d, cudaStream_t st);
+void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st);
+void launch_radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t* hist, uint32_t n,
+                             uint32_t key_bits, cudaStream_t st, int* result_buffer);
+uint32_t radix_hist_words(uint32_t n);
+
+// observables (kernels_obs.cu)
+void launch_sample_position(const Dev& d, uint32_t first, uint32_t count, double* out, cudaStream_t st);
+void launch_msd(const double* r1, const double* r2, const uint32_t* range, uint32_t nrange, const uint32_t* blk_range,
+                const uint32_t* blk_begin, uint32_t nblk, double* partial, double* out, cudaStream_t st);
+void launch_density_modes(const Dev& d, const uint32_t* range, uint32_t nrange, const uint32_t* blk_range,
+                          const uint32_t* blk_begin, uint32_t nblk, const float4* q, uint32_t nq, double* partial,
+                          double* out, cudaStream_t st);
+
+} // namespace hmd

@@ -1,0 +1,450 @@
+// kernels_rebuild.cu — neighbour-list rebuild chain, run for the systems whose
+// maximum displacement exceeded skin/2 (SysState::rebuild):
+//   Hilbert keys -> stable LSD radix sort -> rearrange (mdsim/gpu/sorts/hilbert.cpp:71-117,
+//   particle.cpp:173-218) -> cell binning (binning.cpp:166-221) -> full Verlet
+//   list (neighbours/from_binning_kernel.cu:99-267).
+#include "hmd_device.cuh"
+#include "kernels.h"
+
+namespace hmd {
+
+// ---------------------------------------------------------------------------
+// Hilbert key (mdsim/sorts/hilbert_kernel.hpp:70-230; Wang & Shan, 2005):
+// the position, scaled to the unit cube, is snapped to the centre of its cell
+// on a 2^depth grid and descended vertex by vertex.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void hswap(uint32_t& v, uint32_t& a, uint32_t& b)
+{
+    const uint32_t va = (v >> a) & 7u;
+    const uint32_t vb = (v >> b) & 7u;
+    v = v ^ (va << a) ^ (vb << b) ^ (va << b) ^ (vb << a);
+    const uint32_t t = a; a = b; b = t;
+}
+
+__device__ uint32_t hilbert_key(float x0, float x1, float x2, uint32_t depth)
+{
+    const float n = (float)(1u << depth);
+    float r[3] = {x0, x1, x2};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        r[q] = __fmul_rn(__fsub_rn(r[q], floorf(r[q])), n);
+        r[q] = __fsub_rn(__fdiv_rn(__fadd_rn(floorf(r[q]), 0.5f), n), 0.5f);
+    }
+    uint32_t a = 21, b = 18, c = 12, d = 15, e = 3, f = 0, g = 6, h = 9;
+    uint32_t vc = (1u << b) ^ (2u << c) ^ (3u << d) ^ (4u << e) ^ (5u << f) ^ (6u << g) ^ (7u << h);
+    uint32_t code = 0;
+    for (uint32_t i = 0; i < depth; ++i) {
+        const uint32_t x = signbit(r[0]) ? 1u : 0u;
+        const uint32_t y = signbit(r[1]) ? 1u : 0u;
+        const uint32_t z = signbit(r[2]) ? 1u : 0u;
+        const uint32_t v = (vc >> (3u * (x + (y << 1) + (z << 2)))) & 7u;
+        r[0] = __fsub_rn(__fadd_rn(__fmul_rn(r[0], 2.0f), (float)x), 0.5f);
+        r[1] = __fsub_rn(__fadd_rn(__fmul_rn(r[1], 2.0f), (float)y), 0.5f);
+        r[2] = __fsub_rn(__fadd_rn(__fmul_rn(r[2], 2.0f), (float)z), 0.5f);
+        if (v == 0) { hswap(vc, b, h); hswap(vc, c, e); }
+        else if (v == 1 || v == 2) { hswap(vc, c, g); hswap(vc, d, h); }
+        else if (v == 3 || v == 4) { hswap(vc, a, c); hswap(vc, f, h); }
+        else if (v == 5 || v == 6) { hswap(vc, a, e); hswap(vc, b, f); }
+        else { hswap(vc, a, g); hswap(vc, d, f); }
+        code = (code << 3) + v;
+    }
+    return code;
+}
+
+// sort key per slot: (system rank, Hilbert code) for systems that rebuild with
+// sorting on; (rank, slot) otherwise so those systems keep their order.
+__global__ void __launch_bounds__(256) k_sort_keys(Dev d, uint32_t* keys, uint32_t* vals)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    const uint32_t local = i - P.off;
+    uint32_t lk = local;
+    if (P.active && P.sort_enable && d.st[s].rebuild) {
+        const float4 r = d.pos[i];
+        if (species_bits(r.w) == PLACEHOLDER) {
+            lk = (P.key_shift >= 32) ? 0xFFFFFFFFu : ((1u << P.key_shift) - 1u);
+        } else {
+            lk = hilbert_key(__fdiv_rn(r.x, P.L[0]), __fdiv_rn(r.y, P.L[1]), __fdiv_rn(r.z, P.L[2]), P.depth);
+        }
+    }
+    keys[i] = (P.key_shift >= 32) ? lk : ((P.rank << P.key_shift) | lk);
+    vals[i] = i;
+}
+
+// Hilbert keys of all real particles of every system (module interface)
+__global__ void k_hilbert_keys(Dev d, uint32_t* keys)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.S) return;
+    const SysParam& P = d.sys[d.chunk_sys[i / CHUNK]];
+    const float4 r = d.pos[i];
+    keys[i] = (species_bits(r.w) == PLACEHOLDER)
+        ? PLACEHOLDER
+        : hilbert_key(__fdiv_rn(r.x, P.L[0]), __fdiv_rn(r.y, P.L[1]), __fdiv_rn(r.z, P.L[2]), P.depth);
+}
+
+// ---------------------------------------------------------------------------
+// stable LSD radix sort, 8-bit digits (algorithm/gpu/radix_sort_kernel.cu:76-230
+// restated): per-tile digit histograms, one scan, stable scatter with
+// warp-match ranking.  Tiles of 2048 keys (256 threads x 8 rounds).
+// ---------------------------------------------------------------------------
+
+constexpr int RADIX_THREADS = 256;
+constexpr int RADIX_ROUNDS = 8;
+constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;
+
+__global__ void __launch_bounds__(RADIX_THREADS) k_radix_hist(const uint32_t* keys, uint32_t n, uint32_t shift,
+                                                              uint32_t* hist, uint32_t ntiles)
+{
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * RADIX_TILE;
+#pragma unroll
+    for (int r = 0; r < RADIX_ROUNDS; ++r) {
+        const uint32_t idx = base + r * RADIX_THREADS + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// exclusive scan of hist[0 .. 256*ntiles) by one block of 1024 threads
+__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t* hist, uint32_t total)
+{
+    __shared__ uint32_t part[1024];
+    const uint32_t per = (total + blockDim.x - 1) / blockDim.x;
+    const uint32_t b = threadIdx.x * per;
+    const uint32_t e = min(b + per, total);
+    uint32_t sum = 0;
+    for (uint32_t k = b; k < e; ++k) sum += hist[k];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (uint32_t o = 1; o < blockDim.x; o <<= 1) {
+        uint32_t v = (threadIdx.x >= o) ? part[threadIdx.x - o] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - sum;
+    for (uint32_t k = b; k < e; ++k) {
+        const uint32_t v = hist[k];
+        hist[k] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint32_t* kin, const uint32_t* vin,
+                                                                 uint32_t* kout, uint32_t* vout, uint32_t n,
+                                                                 uint32_t shift, const uint32_t* hist, uint32_t ntiles)
+{
+    __shared__ uint32_t s_w[RADIX_THREADS / 32][256];
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_goff[256];
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    s_base[t] = 0;
+    s_goff[t] = hist[t * ntiles + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < RADIX_THREADS / 32; ++w) s_w[w][t] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * RADIX_TILE;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (int r = 0; r < RADIX_ROUNDS; ++r) {
+        const uint32_t idx = base + r * RADIX_THREADS + t;
+        const bool valid = idx < n;
+        uint32_t key = 0, val = 0, dg = 256u;
+        if (valid) { key = kin[idx]; val = vin[idx]; dg = (key >> shift) & 255u; }
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, dg);
+        const uint32_t rank = __popc(peers & lt);
+        if (valid && rank == 0) s_w[warp][dg] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t run = s_base[t];
+#pragma unroll
+            for (int w = 0; w < RADIX_THREADS / 32; ++w) {
+                const uint32_t c = s_w[w][t];
+                s_w[w][t] = run;
+                run += c;
+            }
+            s_base[t] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t pos = s_goff[dg] + s_w[warp][dg] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int w = 0; w < RADIX_THREADS / 32; ++w) s_w[w][t] = 0;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// rearrange (particle.cpp:173-218, particle_kernel.cu:45): gather phase space
+// by the sort permutation into temporaries, then copy back, for the systems
+// that rebuild; reverse ids follow.
+// ---------------------------------------------------------------------------
+
+template <bool DS>
+__global__ void __launch_bounds__(256) k_rearrange(Dev d, const uint32_t* perm)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    if (!(P.active && P.sort_enable && d.st[s].rebuild)) return;
+    const uint32_t src = perm[i];
+    d.tpos[i] = d.pos[src];
+    d.tvel[i] = d.vel[src];
+    if (DS) {
+        d.tpos[d.S + i] = d.pos[d.S + src];
+        d.tvel[d.S + i] = d.vel[d.S + src];
+    }
+    d.timg[i] = d.img[src];
+    const uint32_t tag = d.id[src];
+    d.tid[i] = tag;
+    if (tag != PLACEHOLDER) d.rid[P.off + tag] = i;
+}
+
+template <bool DS>
+__global__ void __launch_bounds__(256) k_copyback(Dev d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    if (!(P.active && P.sort_enable && d.st[s].rebuild)) return;
+    d.pos[i] = d.tpos[i];
+    d.vel[i] = d.tvel[i];
+    if (DS) {
+        d.pos[d.S + i] = d.tpos[d.S + i];
+        d.vel[d.S + i] = d.tvel[d.S + i];
+    }
+    d.img[i] = d.timg[i];
+    d.id[i] = d.tid[i];
+}
+
+// ---------------------------------------------------------------------------
+// cell binning: cell index (binning_kernel.cu:36-75) -> atomic slot in
+// fixed-capacity cells -> each cell sorted ascending (the same contents as
+// the reference's stable radix sort + assign_cells, binning_kernel.cu:94-123)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void cell_coords(const SysParam& P, float4 r, int& cx, int& cy, int& cz)
+{
+    const float x = __fadd_rn(__fdiv_rn(r.x, P.cell_len[0]), (float)P.ncell[0]);
+    const float y = __fadd_rn(__fdiv_rn(r.y, P.cell_len[1]), (float)P.ncell[1]);
+    const float z = __fadd_rn(__fdiv_rn(r.z, P.cell_len[2]), (float)P.ncell[2]);
+    cx = (int)(((uint32_t)x) % (uint32_t)P.ncell[0]);
+    cy = (int)(((uint32_t)y) % (uint32_t)P.ncell[1]);
+    cz = (int)(((uint32_t)z) % (uint32_t)P.ncell[2]);
+}
+
+__global__ void k_cell_clear(Dev d)
+{
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.total_cells) return;
+    const uint32_t s = d.cell_sys[c];
+    if (d.st[s].rebuild) d.cell_count[c] = 0;
+}
+
+__global__ void __launch_bounds__(256) k_bin(Dev d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    if (!(P.active && d.st[s].rebuild)) return;
+    const float4 r = d.pos[i];
+    if (species_bits(r.w) == PLACEHOLDER) return;
+    int cx, cy, cz;
+    cell_coords(P, r, cx, cy, cz);
+    const uint32_t c = ((uint32_t)cz * P.ncell[1] + cy) * P.ncell[0] + cx;
+    const uint32_t k = atomicAdd(&d.cell_count[P.cell_off + c], 1u);
+    if (k < P.cell_size) d.cell[P.cell_word_off + c * P.cell_size + k] = i;
+}
+
+// one warp per cell: sort the occupied slots ascending, pad with placeholders
+__global__ void __launch_bounds__(128) k_cell_sort(Dev d)
+{
+    __shared__ uint32_t s_buf[4][256];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t c = blockIdx.x * 4 + warp;
+    if (c >= d.total_cells) return;
+    const uint32_t s = d.cell_sys[c];
+    const SysParam& P = d.sys[s];
+    if (!(P.active && d.st[s].rebuild)) return;
+    const uint32_t cs = P.cell_size;
+    const uint32_t cnt = d.cell_count[c];
+    if (lane == 0) {
+        atomicMax(&d.st[s].max_cell, cnt);
+        if (cnt > cs) atomicOr(d.status, ST_CELL_OVERFLOW);
+    }
+    const uint32_t n = min(cnt, cs);
+    uint32_t* cell = d.cell + P.cell_word_off + (c - P.cell_off) * cs;
+    uint32_t* buf = s_buf[warp];
+    for (uint32_t k = lane; k < n; k += 32) buf[k] = cell[k];
+    __syncwarp();
+    uint32_t mine[8];
+    uint32_t rk[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t k = lane + 32u * q;
+        mine[q] = (k < n) ? buf[k] : PLACEHOLDER;
+        rk[q] = 0;
+    }
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t x = buf[k];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) rk[q] += (x < mine[q]) ? 1u : 0u;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t k = lane + 32u * q;
+        if (k < n) cell[rk[q]] = mine[q];
+        else if (k < cs) cell[k] = PLACEHOLDER;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// full Verlet list, one thread per particle: the 27 cells around the
+// particle's cell (each distinct cell once when a dimension has fewer than
+// 3 cells), criterion rr <= (r_c + skin)^2 in float
+// (from_binning_kernel.cu:144-163), transposed layout k*S + i.
+// Also stores r0 = r for the displacement check (max_displacement.cpp:60-72).
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128) k_neighbour(Dev d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
+    if (threadIdx.x < P.ns * P.ns) s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
+    __syncthreads();
+    if (!(P.active && d.st[s].rebuild)) return;   // block-uniform
+    const float4 ri = d.pos[i];
+    const uint32_t a = species_bits(ri.w);
+    uint32_t count = 0;
+    if (a != PLACEHOLDER) {
+        d.r0[i] = ri;
+        int cx, cy, cz;
+        cell_coords(P, ri, cx, cy, cz);
+        const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
+        const int lox = nx >= 3 ? -1 : 0, hix = nx >= 2 ? 1 : 0;
+        const int loy = ny >= 3 ? -1 : 0, hiy = ny >= 2 ? 1 : 0;
+        const int loz = nz >= 3 ? -1 : 0, hiz = nz >= 2 ? 1 : 0;
+        const uint32_t cs = P.cell_size;
+        const uint32_t cap = d.nbr_cap;
+        const size_t stride = d.S;
+        uint32_t* out = d.nbr + i;
+        const float* rrcs = s_rrcs + a * P.ns;
+        for (int oz = loz; oz <= hiz; ++oz) {
+            const int z = (cz + oz + nz) % nz;
+            for (int oy = loy; oy <= hiy; ++oy) {
+                const int y = (cy + oy + ny) % ny;
+                for (int ox = lox; ox <= hix; ++ox) {
+                    const int x = (cx + ox + nx) % nx;
+                    const uint32_t* cell = d.cell + P.cell_word_off + ((uint32_t)(z * ny + y) * nx + x) * cs;
+                    for (uint32_t k = 0; k < cs; ++k) {
+                        const uint32_t j = __ldg(cell + k);
+                        if (j == PLACEHOLDER) break;
+                        if (j == i) continue;
+                        const float4 rj = __ldg(d.pos + j);
+                        const float dx = min_image(__fsub_rn(ri.x, rj.x), P.L[0], P.Linv[0]);
+                        const float dy = min_image(__fsub_rn(ri.y, rj.y), P.L[1], P.Linv[1]);
+                        const float dz = min_image(__fsub_rn(ri.z, rj.z), P.L[2], P.Linv[2]);
+                        const float rr = rr_exact(dx, dy, dz);
+                        const uint32_t b = species_bits(rj.w);
+                        if (b < P.ns && rr <= rrcs[b]) {
+                            if (count < cap) out[count * stride] = j;
+                            ++count;
+                        }
+                    }
+                }
+            }
+        }
+        d.nbr_count[i] = min(count, cap);
+    }
+    // warp-aggregated maximum and overflow flag (all lanes of the warp are here)
+    uint32_t m = count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+    if ((threadIdx.x & 31u) == 0) {
+        if (m > 0) atomicMax(&d.st[s].max_nbr, m);
+        if (m > d.nbr_cap) atomicOr(d.status, ST_NBR_OVERFLOW);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+
+int radix_passes(uint32_t key_bits) { return (int)((key_bits + 7) / 8); }
+
+// sort keys/values of all S slots; returns the buffer index holding the result
+int launch_sort(const Dev& d, uint32_t key_bits, cudaStream_t st)
+{
+    const uint32_t n = d.S;
+    const uint32_t ntiles = (n + RADIX_TILE - 1) / RADIX_TILE;
+    k_sort_keys<<<n / 256, 256, 0, st>>>(d, d.key[0], d.val[0]);
+    int cur = 0;
+    const int passes = radix_passes(key_bits);
+    for (int p = 0; p < passes; ++p) {
+        const uint32_t shift = 8u * p;
+        k_radix_hist<<<ntiles, RADIX_THREADS, 0, st>>>(d.key[cur], n, shift, d.hist, ntiles);
+        k_radix_scan<<<1, 1024, 0, st>>>(d.hist, 256u * ntiles);
+        k_radix_scatter<<<ntiles, RADIX_THREADS, 0, st>>>(d.key[cur], d.val[cur], d.key[1 - cur], d.val[1 - cur],
+                                                           n, shift, d.hist, ntiles);
+        cur = 1 - cur;
+    }
+    return cur;
+}
+
+void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st)
+{
+    const unsigned grid = d.S / 256;
+    if (ds) { k_rearrange<true><<<grid, 256, 0, st>>>(d, perm); k_copyback<true><<<grid, 256, 0, st>>>(d); }
+    else { k_rearrange<false><<<grid, 256, 0, st>>>(d, perm); k_copyback<false><<<grid, 256, 0, st>>>(d); }
+}
+
+void launch_binning(const Dev& d, cudaStream_t st)
+{
+    k_cell_clear<<<(d.total_cells + 255) / 256, 256, 0, st>>>(d);
+    k_bin<<<d.S / 256, 256, 0, st>>>(d);
+    k_cell_sort<<<(d.total_cells + 3) / 4, 128, 0, st>>>(d);
+}
+
+void launch_neighbour(const Dev& d, cudaStream_t st)
+{
+    k_neighbour<<<d.S / 128, 128, 0, st>>>(d);
+}
+
+void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
+{
+    k_hilbert_keys<<<(d.S + 255) / 256, 256, 0, st>>>(d, keys);
+}
+
+void launch_radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t* hist, uint32_t n,
+                             uint32_t key_bits, cudaStream_t st, int* result_buffer)
+{
+    const uint32_t ntiles = (n + RADIX_TILE - 1) / RADIX_TILE;
+    uint32_t* kk[2] = {k0, k1};
+    uint32_t* vv[2] = {v0, v1};
+    int cur = 0;
+    for (int p = 0; p < radix_passes(key_bits); ++p) {
+        const uint32_t shift = 8u * p;
+        k_radix_hist<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], n, shift, hist, ntiles);
+        k_radix_scan<<<1, 1024, 0, st>>>(hist, 256u * ntiles);
+        k_radix_scatter<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], vv[cur], kk[1 - cur], vv[1 - cur], n, shift,
+                                                           hist, ntiles);
+        cur = 1 - cur;
+    }
+    *result_buffer = cur;
+}
+
+uint32_t radix_hist_words(uint32_t n) { return 256u * ((n + RADIX_TILE - 1) / RADIX_TILE); }
+
+} // namespace hmd

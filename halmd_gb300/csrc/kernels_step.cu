@@ -1,0 +1,421 @@
+// kernels_step.cu — per-step kernels: velocity-Verlet integrate (fused with the
+// maximum-displacement reduction and the rebuild decision), truncated LJ pair
+// force from the neighbour list, Verlet / Andersen finalize, FP64 reductions.
+//
+// Every kernel runs over all slots of all systems of an engine; a block never
+// straddles two systems (blocks of <= 256 threads, systems padded to 256
+// slots), so per-system parameters are block-uniform.
+#include "hmd_device.cuh"
+#include "kernels.h"
+
+namespace hmd {
+
+// ---------------------------------------------------------------------------
+// integrate: first half of velocity Verlet (mdsim/gpu/integrators/verlet_kernel.cu:38-72)
+//   v += F dt/(2m); r += v dt; image += rint(r/L); r -= image L
+// fused with |r - r0|^2 (mdsim/gpu/max_displacement_kernel.cu:37-68) and,
+// in the last block to finish, the per-system rebuild decision
+// (from_binning.cpp:130: displacement > skin/2), which also drives the
+// conditional rebuild node of a captured step graph.
+// ---------------------------------------------------------------------------
+
+template <bool DS>
+__device__ __forceinline__ void integrate_component(float& rh, float& rl, float& vh, float& vl, float& im,
+                                                    float f, float m, float dt, float dt_half, float L, float Linv)
+{
+    float a = __fdiv_rn(__fmul_rn(f, dt_half), m);
+    float k;
+    if (DS) {
+        float v0, v1, d0, d1, r0, r1;
+        ds_add(v0, v1, vh, vl, a, 0.0f);
+        ds_mul(d0, d1, v0, v1, dt, 0.0f);
+        ds_add(r0, r1, rh, rl, d0, d1);
+        k = rintf(__fmul_rn(r0, Linv));
+        ds_sub(r0, r1, r0, r1, __fmul_rn(k, L), 0.0f);
+        vh = v0; vl = v1; rh = r0; rl = r1;
+    } else {
+        float v = __fadd_rn(vh, a);
+        float r = __fadd_rn(rh, __fmul_rn(v, dt));
+        k = rintf(__fmul_rn(r, Linv));
+        r = __fsub_rn(r, __fmul_rn(k, L));
+        vh = v; rh = r;
+    }
+    im = __fadd_rn(im, k);
+}
+
+template <bool DS>
+__global__ void __launch_bounds__(256) k_integrate(Dev d, cudaGraphConditionalHandle h, int use_handle)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    SysState& st = d.st[s];
+    const bool live = P.active && st.steps_left != 0u && (*d.status == 0u);
+    float rr = 0.0f;
+    if (live) {
+        float4 r = d.pos[i];
+        if (species_bits(r.w) != PLACEHOLDER) {
+            float4 v = d.vel[i];
+            const float4 f = d.force[i];
+            float4 im = d.img[i];
+            const float4 im_old = im;
+            float4 rl = make_float4(0, 0, 0, 0), vl = make_float4(0, 0, 0, 0);
+            if (DS) { rl = d.pos[d.S + i]; vl = d.vel[d.S + i]; }
+            const float m = v.w;
+            integrate_component<DS>(r.x, rl.x, v.x, vl.x, im.x, f.x, m, P.dt, P.dt_half, P.L[0], P.Linv[0]);
+            integrate_component<DS>(r.y, rl.y, v.y, vl.y, im.y, f.y, m, P.dt, P.dt_half, P.L[1], P.Linv[1]);
+            integrate_component<DS>(r.z, rl.z, v.z, vl.z, im.z, f.z, m, P.dt, P.dt_half, P.L[2], P.Linv[2]);
+            d.pos[i] = r;
+            d.vel[i] = v;
+            if (DS) { d.pos[d.S + i] = rl; d.vel[d.S + i] = vl; }
+            if (im.x != im_old.x || im.y != im_old.y || im.z != im_old.z) d.img[i] = im;
+            const float4 q = d.r0[i];
+            float dx = min_image(__fsub_rn(r.x, q.x), P.L[0], P.Linv[0]);
+            float dy = min_image(__fsub_rn(r.y, q.y), P.L[1], P.Linv[1]);
+            float dz = min_image(__fsub_rn(r.z, q.z), P.L[2], P.Linv[2]);
+            rr = rr_exact(dx, dy, dz);
+        }
+    }
+    __shared__ float s_max[8];
+    __shared__ bool s_last;
+    rr = warp_max(rr);
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = rr;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float b = s_max[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = fmaxf(b, s_max[w]);
+        if (b > 0.0f) atomicMax(&st.disp2_bits, __float_as_uint(b));
+        __threadfence();
+        s_last = (atomicAdd(d.done, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const bool ok = (*(volatile uint32_t*)d.status == 0u);
+    uint32_t any = 0;
+    for (uint32_t q = threadIdx.x; q < d.nsys; q += blockDim.x) {
+        SysState& t = d.st[q];
+        const SysParam& Q = d.sys[q];
+        const bool lv = ok && Q.active && t.steps_left != 0u;
+        const float disp = __uint_as_float(atomicExch(&t.disp2_bits, 0u));
+        const uint32_t rb = lv && (disp > Q.rr_half_skin || t.rebuild_request != 0u);
+        t.rebuild = rb;
+        t.live = lv;
+        if (lv) {
+            t.rebuild_request = 0u;
+            t.step += 1ull;
+            if (t.steps_left != 0xFFFFFFFFu) t.steps_left -= 1u;
+            if (rb) t.rebuilds += 1ull;
+        }
+        any |= rb;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) {
+        *d.done = 0u;
+        *d.any_rebuild = any ? 1u : 0u;
+        if (use_handle) cudaGraphSetConditional(h, any ? 1u : 0u);
+    }
+}
+
+// Mark systems live for a force evaluation outside a step (set-up, or a
+// force requested through the module interface); `rebuild_all` also flags
+// every active system for a list rebuild.
+__global__ void k_mark(Dev d, int rebuild_all)
+{
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < d.nsys; q += gridDim.x * blockDim.x) {
+        SysState& t = d.st[q];
+        const bool lv = d.sys[q].active != 0u;
+        t.live = lv;
+        t.rebuild = (lv && (rebuild_all || t.rebuild_request)) ? 1u : 0u;
+        if (t.rebuild) { t.rebuild_request = 0u; t.rebuilds += 1ull; }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pair force (mdsim/gpu/forces/pair_trunc_kernel.cuh:165-255)
+//   F_i = Σ_j fval(r_ij²) r_ij over list entries with r_ij² < r_c²;
+//   aux: E_i = ½ Σ U, stress_i = ½ Σ fval r⊗r (full list, weight ½,
+//   pair_trunc.hpp:291-294).
+// FP32 math; each force component is accumulated with Knuth's TwoSum and
+// a running compensation term, so the per-particle sum is as accurate as a
+// double-single accumulator (the reference uses dsfloat, :194).
+// The within-range test uses the same rounded squared distance as the list
+// build, so the pair set is reproducible on the CPU.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float x)
+{
+    const float t = __fadd_rn(s, x);
+    const float z = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z));
+    s = t;
+    c = __fadd_rn(c, e);
+}
+
+// LJ + truncation (lennard_jones_kernel.hpp:44-56, truncations/*_kernel.cuh)
+template <int TR>
+__device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rri_smooth, float& fval, float& en)
+{
+    const float rri = __fdiv_rn(p.sigma2, rr);
+    const float ri6 = rri * rri * rri;
+    fval = p.c48 * rri * ri6 * (ri6 - 0.5f);
+    en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
+    if (TR == TRUNC_SMOOTH_R4) {
+        const float r = __fsqrt_rn(rr);
+        const float dr = r - p.r_cut;
+        const float x2 = dr * dr * rri_smooth;
+        const float x4 = x2 * x2;
+        const float x4i = __fdiv_rn(1.0f, 1.0f + x4);
+        const float h0 = x4 * x4i;
+        const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
+        fval = h0 * fval - h1 * __fdiv_rn(en, r);
+        en = h0 * en;
+    } else if (TR == TRUNC_FORCE_SHIFTED) {
+        const float r = __fsqrt_rn(rr);
+        fval = fval - __fdiv_rn(p.f_cut, r);
+        en = en + (r - p.r_cut) * p.f_cut;
+    }
+}
+
+template <int TR, bool AUX>
+__device__ __forceinline__ void force_particle(const Dev& d, uint32_t i, const SysParam& P, const PairParam* spp,
+                                               float4 ri, uint32_t a)
+{
+    const uint32_t cnt = d.nbr_count[i];
+    const uint32_t* lst = d.nbr + i;
+    const size_t stride = d.S;
+    const uint32_t ns = P.ns;
+    const float Lx = P.L[0], Ly = P.L[1], Lz = P.L[2];
+    const float Ix = P.Linv[0], Iy = P.Linv[1], Iz = P.Linv[2];
+    const float rri_smooth = P.rri_smooth;
+    float fx = 0, fy = 0, fz = 0, cx = 0, cy = 0, cz = 0;
+    float en = 0;
+    float s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
+#pragma unroll 4
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t j = __ldg(lst + k * stride);
+        const float4 rj = __ldg(d.pos + j);
+        const uint32_t b = species_bits(rj.w);
+        const float dx = min_image(__fsub_rn(ri.x, rj.x), Lx, Ix);
+        const float dy = min_image(__fsub_rn(ri.y, rj.y), Ly, Iy);
+        const float dz = min_image(__fsub_rn(ri.z, rj.z), Lz, Iz);
+        const float rr = rr_exact(dx, dy, dz);
+        if (b >= ns) continue;   // lists hold real particles only; keep the table lookup in bounds
+        const PairParam& p = spp[a * ns + b];
+        if (!(rr < p.rr_cut)) continue;
+        float fval, e;
+        pair_eval<TR>(p, rr, rri_smooth, fval, e);
+        two_sum_acc(fx, cx, fval * dx);
+        two_sum_acc(fy, cy, fval * dy);
+        two_sum_acc(fz, cz, fval * dz);
+        if (AUX) {
+            en += e;
+            s0 += fval * dx * dx;
+            s1 += fval * dy * dy;
+            s2 += fval * dz * dz;
+            s3 += fval * dx * dy;
+            s4 += fval * dx * dz;
+            s5 += fval * dy * dz;
+        }
+    }
+    d.force[i] = make_float4(fx + cx, fy + cy, fz + cz, 0.0f);
+    if (AUX) {
+        d.en_pot[i] = 0.5f * en;
+        float* sp = d.stress + i;
+        sp[0 * stride] = 0.5f * s0;
+        sp[1 * stride] = 0.5f * s1;
+        sp[2 * stride] = 0.5f * s2;
+        sp[3 * stride] = 0.5f * s3;
+        sp[4 * stride] = 0.5f * s4;
+        sp[5 * stride] = 0.5f * s5;
+    }
+}
+
+template <bool AUX>
+__global__ void __launch_bounds__(128) k_force(Dev d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    __shared__ PairParam spp[MAX_SPECIES * MAX_SPECIES];
+    const uint32_t np = P.ns * P.ns;
+    if (threadIdx.x < np) spp[threadIdx.x] = d.pair[P.pair_off + threadIdx.x];
+    __syncthreads();
+    if (!P.active || !d.st[s].live || *d.status != 0u) return;
+    const float4 ri = d.pos[i];
+    const uint32_t a = species_bits(ri.w);
+    if (a == PLACEHOLDER) return;
+    switch (P.trunc) {
+    case TRUNC_SHARP:
+    case TRUNC_SHIFTED: force_particle<TRUNC_SHIFTED, AUX>(d, i, P, spp, ri, a); break;
+    case TRUNC_SMOOTH_R4: force_particle<TRUNC_SMOOTH_R4, AUX>(d, i, P, spp, ri, a); break;
+    default: force_particle<TRUNC_FORCE_SHIFTED, AUX>(d, i, P, spp, ri, a); break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// finalize: second half-kick (verlet_kernel.cu:78-98) or Andersen
+// (per-particle collisions with the heat bath, host convention
+// mdsim/host/integrators/verlet_nvt_andersen.cpp:111-137; Philox4x32-10
+// streams keyed by (seed, particle tag, step) so results do not depend on
+// particle order or on which other systems share the launch)
+// ---------------------------------------------------------------------------
+
+template <bool DS>
+__device__ __forceinline__ void half_kick(float& vh, float& vl, float f, float m, float dt_half)
+{
+    const float a = __fdiv_rn(__fmul_rn(f, dt_half), m);
+    if (DS) {
+        float v0, v1;
+        ds_add(v0, v1, vh, vl, a, 0.0f);
+        vh = v0; vl = v1;
+    } else {
+        vh = __fadd_rn(vh, a);
+    }
+}
+
+template <bool DS>
+__global__ void __launch_bounds__(256) k_finalize(Dev d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    const SysState& st = d.st[s];
+    if (!P.active || !st.live || *d.status != 0u) return;
+    if (species_bits(d.pos[i].w) == PLACEHOLDER) return;
+    float4 v = d.vel[i];
+    float4 vl = make_float4(0, 0, 0, 0);
+    if (DS) vl = d.vel[d.S + i];
+    const float4 f = d.force[i];
+    if (P.integrator == INTEG_ANDERSEN) {
+        const unsigned long long step = st.step - 1ull;
+        const uint4 ctr = make_uint4(d.id[i], (uint32_t)step, (uint32_t)(step >> 32), 0x414E4452u);
+        const uint4 u = philox4x32_10(ctr, P.seed_lo, P.seed_hi);
+        if (u.x < P.coll_threshold) {
+            const uint4 w = philox4x32_10(make_uint4(ctr.x, ctr.y, ctr.z, 0x414E4453u), P.seed_lo, P.seed_hi);
+            const float rad0 = sqrtf(-2.0f * logf(u01(w.x)));
+            const float rad1 = sqrtf(-2.0f * logf(u01(w.z)));
+            float sn0, cs0, sn1, cs1;
+            sincospif(2.0f * u01(w.y), &sn0, &cs0);
+            sincospif(2.0f * u01(w.w), &sn1, &cs1);
+            v.x = P.sqrt_T * rad0 * cs0;
+            v.y = P.sqrt_T * rad0 * sn0;
+            v.z = P.sqrt_T * rad1 * cs1;
+            d.vel[i] = v;
+            if (DS) d.vel[d.S + i] = make_float4(0, 0, 0, vl.w);
+            return;
+        }
+    }
+    half_kick<DS>(v.x, vl.x, f.x, v.w, P.dt_half);
+    half_kick<DS>(v.y, vl.y, f.y, v.w, P.dt_half);
+    half_kick<DS>(v.z, vl.z, f.z, v.w, P.dt_half);
+    d.vel[i] = v;
+    if (DS) d.vel[d.S + i] = vl;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 reductions (observables/gpu/thermodynamics_kernel.cu:35-106 and
+// algorithm/gpu/reduce_kernel.cuh:126): per-block partial sums, then a
+// fixed-order per-system reduction (deterministic, no double atomics).
+//   0: Σ m v²   1-3: Σ m v   4: Σ m   5: Σ E_pot   6: Σ tr(stress)
+//   7-12: Σ stress (xx yy zz xy xz yz)   13: particle count
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_thermo_partial(Dev d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[NTHERMO];
+#pragma unroll
+    for (int k = 0; k < NTHERMO; ++k) acc[k] = 0.0;
+    const float4 r = d.pos[i];
+    if (species_bits(r.w) != PLACEHOLDER && d.sys[d.chunk_sys[i / CHUNK]].active) {
+        const float4 vh = d.vel[i];
+        const float4 vl = d.vel[d.S + i];
+        const double m = vh.w;
+        const double vx = (double)vh.x + (double)vl.x;
+        const double vy = (double)vh.y + (double)vl.y;
+        const double vz = (double)vh.z + (double)vl.z;
+        acc[0] = m * (vx * vx + vy * vy + vz * vz);
+        acc[1] = m * vx; acc[2] = m * vy; acc[3] = m * vz;
+        acc[4] = m;
+        acc[5] = d.en_pot[i];
+        const size_t S = d.S;
+        double sxx = d.stress[i], syy = d.stress[S + i], szz = d.stress[2 * S + i];
+        acc[6] = sxx + syy + szz;
+        acc[7] = sxx; acc[8] = syy; acc[9] = szz;
+        acc[10] = d.stress[3 * S + i]; acc[11] = d.stress[4 * S + i]; acc[12] = d.stress[5 * S + i];
+        acc[13] = 1.0;
+    }
+    __shared__ double s_acc[8][NTHERMO];
+#pragma unroll
+    for (int k = 0; k < NTHERMO; ++k) {
+        double v = warp_sum(acc[k]);
+        if ((threadIdx.x & 31) == 0) s_acc[threadIdx.x >> 5][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NTHERMO) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += s_acc[w][threadIdx.x];
+        d.partial[(size_t)blockIdx.x * NTHERMO + threadIdx.x] = v;
+    }
+}
+
+// one block per system; `velocity_lo` is ignored for FP32 engines by the
+// caller zeroing the lo half once
+__global__ void __launch_bounds__(256) k_thermo_reduce(Dev d)
+{
+    const uint32_t s = blockIdx.x;
+    const SysParam& P = d.sys[s];
+    const uint32_t b0 = P.off / 256, nb = P.A / 256;
+    __shared__ double s_red[256];
+    for (int k = 0; k < NTHERMO; ++k) {
+        double v = 0.0;
+        for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) v += d.partial[(size_t)(b0 + b) * NTHERMO + k];
+        s_red[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+            if ((int)threadIdx.x < o) s_red[threadIdx.x] += s_red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) d.thermo[(size_t)s * NTHERMO + k] = s_red[0];
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+
+void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool use_handle, cudaStream_t st)
+{
+    const unsigned grid = d.S / 256;
+    if (ds) k_integrate<true><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
+    else k_integrate<false><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
+}
+
+void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st)
+{
+    k_mark<<<(d.nsys + 255) / 256, 256, 0, st>>>(d, rebuild_all ? 1 : 0);
+}
+
+void launch_force(const Dev& d, bool aux, cudaStream_t st)
+{
+    const unsigned grid = d.S / 128;
+    if (aux) k_force<true><<<grid, 128, 0, st>>>(d);
+    else k_force<false><<<grid, 128, 0, st>>>(d);
+}
+
+void launch_finalize(const Dev& d, bool ds, cudaStream_t st)
+{
+    const unsigned grid = d.S / 256;
+    if (ds) k_finalize<true><<<grid, 256, 0, st>>>(d);
+    else k_finalize<false><<<grid, 256, 0, st>>>(d);
+}
+
+void launch_thermo(const Dev& d, cudaStream_t st)
+{
+    k_thermo_partial<<<d.S / 256, 256, 0, st>>>(d);
+    k_thermo_reduce<<<d.nsys, 256, 0, st>>>(d);
+}
+
+} // namespace hmd

@@ -1,0 +1,222 @@
+/*
+ * halmd_gb300.h — C ABI of the GB300-native molecular-dynamics step.
+ *
+ * Drop-in boundary for HALMD's mdsim/gpu backend.  The reference exposes its
+ * modules to Lua through luaponte bindings (luaopen_libhalmd_mdsim_gpu_*, e.g.
+ * halmd/mdsim/gpu/particle.cpp:304-357); this library exports plain C entry
+ * points with opaque handles, host pointers and sizes, and integer status
+ * codes (0 = ok, negative = error, message via hmd_last_error).  One handle
+ * (an "engine") holds one or more independent systems that advance together
+ * on one GPU; a single reference simulation is an engine with one system.
+ *
+ * Threading: an engine is thread-compatible (one thread at a time per
+ * handle), like the reference's single-threaded module graph.  All array
+ * accessors take and return data in particle-tag order (the reference's
+ * particle id), independent of the device's internal Hilbert order.
+ */
+#ifndef HALMD_GB300_H
+#define HALMD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define HMD_API __attribute__((visibility("default")))
+#else
+#define HMD_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HMD_OK 0
+#define HMD_ERR_INVALID (-1)   /* bad argument (std::invalid_argument in the reference) */
+#define HMD_ERR_CUDA (-2)      /* CUDA runtime error */
+#define HMD_ERR_STATE (-3)     /* call not valid in the current state (std::logic_error) */
+#define HMD_ERR_NOMEM (-4)     /* device allocation failed */
+#define HMD_ERR_OVERFLOW (-5)  /* capacity overflow that retries could not resolve */
+
+#define HMD_PRECISION_FLOAT 0     /* particle_3_float   (particle.lua.in:46-57) */
+#define HMD_PRECISION_DSFLOAT 1   /* particle_3_dsfloat (default precision) */
+
+#define HMD_TRUNC_SHARP 0          /* truncations/sharp.hpp */
+#define HMD_TRUNC_SHIFTED 1        /* truncations/shifted.hpp (truncate.lua.in:289 default) */
+#define HMD_TRUNC_SMOOTH_R4 2      /* truncations/smooth_r4.hpp */
+#define HMD_TRUNC_FORCE_SHIFTED 3  /* truncations/force_shifted.hpp */
+
+#define HMD_INTEGRATOR_VERLET 0    /* integrators/verlet.cpp */
+#define HMD_INTEGRATOR_ANDERSEN 1  /* integrators/verlet_nvt_andersen.cpp */
+
+#define HMD_MAX_SPECIES 4
+#define HMD_NTHERMO 14
+
+typedef struct hmd_engine hmd_engine;
+typedef struct hmd_dynamics hmd_dynamics;
+
+/*
+ * Parameters of one system.  Replaces the constructor arguments of
+ * particle(nparticle, nspecies)            lua/halmd/mdsim/particle.lua.in:229-290
+ * box(edges)                               mdsim/box.cpp:40-60
+ * lennard_jones(epsilon, sigma)            mdsim/gpu/potentials/pair/lennard_jones.cpp:45-71
+ *   :truncate{kind, cutoff, h}             lua/halmd/mdsim/potentials/pair/adapters/truncate.lua.in:287-305
+ * neighbour{skin, occupancy, sort}         lua/halmd/mdsim/neighbour.lua.in:151-306, from_binning.cpp:96-119
+ * binning{occupancy}                       mdsim/gpu/binning.cpp:47-116
+ * verlet(dt) / verlet_nvt_andersen(dt, T, rate)
+ *                                          lua/halmd/mdsim/integrators/{verlet,verlet_nvt_andersen}.lua.in
+ * Matrices are nspecies x nspecies, row-major; r_cut in units of sigma.
+ */
+typedef struct hmd_system_desc {
+    uint32_t nparticle;
+    uint32_t nspecies;
+    double box[3];
+    double epsilon[HMD_MAX_SPECIES * HMD_MAX_SPECIES];
+    double sigma[HMD_MAX_SPECIES * HMD_MAX_SPECIES];
+    double r_cut[HMD_MAX_SPECIES * HMD_MAX_SPECIES];
+    int32_t truncation;
+    double smoothing;            /* h of smooth_r4 */
+    double skin;                 /* neighbour list skin (default 0.5) */
+    double cell_occupancy;       /* binning occupancy (default 0.5) */
+    double neighbour_occupancy;  /* list occupancy (default 0.4, from_binning.cpp:285-287) */
+    double timestep;
+    int32_t integrator;
+    double temperature;          /* Andersen heat bath */
+    double collision_rate;       /* Andersen collision rate nu */
+    uint64_t seed;               /* Andersen random stream */
+    int32_t sort;                /* 1: Hilbert reorder at every list rebuild (default) */
+} hmd_system_desc;
+
+/* per-system state readable after any call (hmd_info) */
+typedef struct hmd_system_info {
+    uint32_t nparticle, nspecies;
+    uint32_t slot_offset, slots;     /* device slot range */
+    int32_t ncell[3];
+    uint32_t cell_size;
+    uint32_t neighbour_capacity;
+    uint32_t hilbert_depth;
+    uint32_t max_neighbours;         /* largest list of the last build */
+    uint32_t max_cell_occupancy;     /* largest cell of the last build */
+    uint64_t step;                   /* completed integration steps */
+    uint64_t rebuilds;               /* neighbour-list builds so far */
+    float box_f32[3];                /* box edges as the device stores them */
+    float rr_cut_skin[HMD_MAX_SPECIES * HMD_MAX_SPECIES];  /* float (r_c + skin)^2 table */
+    float rr_cut[HMD_MAX_SPECIES * HMD_MAX_SPECIES];       /* float r_c^2 table */
+} hmd_system_info;
+
+/* fill with the reference's defaults (Lua module defaults) */
+HMD_API void hmd_system_desc_init(hmd_system_desc* desc);
+
+/* last error of an engine (engine == NULL: last error of this thread) */
+HMD_API int hmd_last_error(const hmd_engine* engine, char* buf, size_t size);
+
+/* ---- engine lifecycle --------------------------------------------------- */
+
+/* precision HMD_PRECISION_*; device = CUDA ordinal (main.cpp:56-63 --device) */
+HMD_API int hmd_engine_create(int precision, int device, hmd_engine** out);
+HMD_API int hmd_engine_destroy(hmd_engine* engine);
+/* add a system before hmd_engine_commit; *index receives its number */
+HMD_API int hmd_engine_add_system(hmd_engine* engine, const hmd_system_desc* desc, uint32_t* index);
+/* lay out and allocate all device arrays (particle.cpp:56-160 ctor) */
+HMD_API int hmd_engine_commit(hmd_engine* engine);
+/* CUDA stream all work of the engine is issued on (cudaStream_t) */
+HMD_API int hmd_engine_stream(hmd_engine* engine, void** stream);
+HMD_API int hmd_info(hmd_engine* engine, uint32_t sys, hmd_system_info* info);
+
+/*
+ * Phase-space access in tag order (particle.cpp get/set_{position,velocity,
+ * species,mass,image,force,potential_energy,stress_pot,id,reverse_id}):
+ *   "position"  double[3n] (wrapped into the box on set; the image absorbs the shift)
+ *   "velocity"  double[3n]     "mass" double[n]     "species" uint32[n]
+ *   "image"     double[3n]     "force" double[3n] (get)
+ *   "potential_energy" double[n] (get)   "stress_pot" double[6n] (get)
+ *   "unwrapped_position" double[3n] (get; position + image * box)
+ *   "reverse_id" uint32[n] (get; slot of each tag, relative to the system)
+ *   "id"        uint32[slots] (get; tag of each slot, 0xFFFFFFFF for ghosts)
+ * count is the number of elements of the host array.
+ */
+HMD_API int hmd_set(hmd_engine* engine, uint32_t sys, const char* name, const void* host, size_t count);
+HMD_API int hmd_get(hmd_engine* engine, uint32_t sys, const char* name, void* host, size_t count);
+
+/*
+ * Raw device arrays in slot order (float words as stored), for checking:
+ *   "position_hi" / "position_lo" / "velocity_hi" / "velocity_lo" / "image" /
+ *   "force" / "r0": float[4*slots];  "cells": uint32[ncells*cell_size]
+ *   (slot numbers relative to the system).
+ */
+HMD_API int hmd_get_raw(hmd_engine* engine, uint32_t sys, const char* name, void* host, size_t bytes);
+
+/* ---- the MD step -------------------------------------------------------- */
+
+/*
+ * Advance every system by nsteps velocity-Verlet steps (sampler.cpp:49-83 ->
+ * core.cpp:30-63 mdstep: integrate, lazy neighbour rebuild, force, finalize),
+ * as replays of a captured CUDA graph; rebuilds are decided on the device.
+ * aux_last != 0: the last step also computes potential energy and stress
+ * (particle::aux_enable, particle.cpp:221-253).
+ */
+HMD_API int hmd_step(hmd_engine* engine, uint64_t nsteps, int aux_last);
+/* module-level calls (integrators/verlet.cpp integrate()/finalize(),
+ * forces/pair_trunc.hpp apply()), launched one at a time */
+HMD_API int hmd_integrate(hmd_engine* engine);
+HMD_API int hmd_force(hmd_engine* engine, int aux);
+HMD_API int hmd_finalize(hmd_engine* engine);
+/* request a neighbour-list rebuild (with sort) before the next force */
+HMD_API int hmd_request_rebuild(hmd_engine* engine, uint32_t sys);
+/* steps a system still has to do (serving); ~0u = unbounded */
+HMD_API int hmd_set_steps_left(hmd_engine* engine, uint32_t sys, uint32_t steps);
+
+/* maximum displacement since the last build (max_displacement.cpp:77-106) */
+HMD_API int hmd_max_displacement(hmd_engine* engine, uint32_t sys, double* displacement);
+
+/*
+ * FP64 sums (observables/gpu/thermodynamics.cpp:68-190), valid after a step
+ * or force call with aux: out[HMD_NTHERMO] =
+ *   Σ m v², Σ m v (3), Σ m, Σ E_pot, Σ tr(stress), stress (6), N
+ */
+HMD_API int hmd_thermo(hmd_engine* engine, uint32_t sys, double* out);
+
+/*
+ * Neighbour lists of the last build (neighbours/from_binning.cpp g_neighbour()):
+ * counts[n] and lists[n*maxn] in tag numbering, each list ascending, padded
+ * with 0xFFFFFFFF.  Returns HMD_ERR_INVALID if maxn is too small.
+ */
+HMD_API int hmd_neighbour_lists(hmd_engine* engine, uint32_t sys, uint32_t* counts, uint32_t* lists, uint32_t maxn);
+
+/* Hilbert keys of the current positions, tag order (hilbert_kernel.cu:39-66) */
+HMD_API int hmd_hilbert_keys(hmd_engine* engine, uint32_t sys, uint32_t* keys);
+
+/* ---- dynamic correlations (observables/dynamics) ------------------------ */
+
+/*
+ * Blocking scheme (observables/dynamics/blocking_scheme.cpp:35-200) over one
+ * system: max_lag_time and resolution in time units, block_size, shift,
+ * separation as the reference.
+ */
+HMD_API int hmd_dynamics_create(hmd_engine* engine, uint32_t sys, double max_lag_time, double resolution,
+                        uint32_t block_size, uint32_t shift, uint32_t separation, hmd_dynamics** out);
+HMD_API int hmd_dynamics_destroy(hmd_dynamics* dyn);
+/* number of levels and the time grid [levels*block_size] */
+HMD_API int hmd_dynamics_levels(hmd_dynamics* dyn, uint32_t* levels, uint32_t* block_size);
+HMD_API int hmd_dynamics_time(hmd_dynamics* dyn, double* time);
+/* MSD of the particles with tag in [first, last) (id_range particle group) */
+HMD_API int hmd_dynamics_add_msd(hmd_dynamics* dyn, uint32_t first, uint32_t last, int32_t* tcf);
+/*
+ * ISF of a particle group at the given wavenumbers (wavevector.cpp:40-160:
+ * shells of reciprocal-lattice vectors within tolerance, <= max_count each),
+ * normalised by `norm` (intermediate_scattering_function.hpp:89-113)
+ */
+HMD_API int hmd_dynamics_add_isf(hmd_dynamics* dyn, const double* wavenumber, uint32_t nk, double tolerance,
+                         uint32_t max_count, uint32_t first, uint32_t last, double norm, int32_t* tcf);
+/* sample at the current step (blocking_scheme::sample) / drain (finalise) */
+HMD_API int hmd_dynamics_sample(hmd_dynamics* dyn);
+HMD_API int hmd_dynamics_finalise(hmd_dynamics* dyn);
+/* result of a correlation: mean, error of mean and count per (level, lag,
+ * shell); arrays of levels*block_size*nshell (nshell = 1 for MSD) */
+HMD_API int hmd_dynamics_result(hmd_dynamics* dyn, int32_t tcf, double* mean, double* error, uint64_t* count);
+HMD_API int hmd_dynamics_shells(hmd_dynamics* dyn, int32_t tcf, uint32_t* nshell, double* wavenumber);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HALMD_GB300_H */

@@ -1,0 +1,62 @@
+"""The C-ABI library loads and exports every entry point of include/halmd_gb300.h (no GPU needed)."""
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+from halmd_gb300 import _lib
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        from halmd_gb300 import build
+        build.build()
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    names = _lib.header_symbols()
+    assert "hmd_engine_create" in names and "hmd_step" in names
+    assert len(names) >= 30
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [s for s in _lib.header_symbols() if s not in exported]
+    assert not missing, missing
+    for s in _lib.header_symbols():
+        assert hasattr(lib, s)
+
+
+def test_desc_defaults_match_reference(lib):
+    d = _lib.SystemDesc()
+    lib.hmd_system_desc_init(ctypes.byref(d))
+    assert d.skin == 0.5            # neighbour.lua.in: skin default 0.5
+    assert d.neighbour_occupancy == 0.4   # from_binning.cpp:285-287
+    assert d.cell_occupancy == 0.5  # binning.lua.in:83
+    assert d.truncation == _lib.TRUNCATION["shifted"]   # truncate.lua.in:289
+    assert d.sort == 1
+
+
+def test_null_handles_are_rejected(lib):
+    assert lib.hmd_step(None, 1, 0) == -1
+    assert lib.hmd_engine_create(0, 0, None) == -1
+    assert "null" in _lib.last_error()
+
+
+def test_struct_layout_matches_header(lib):
+    # the ctypes mirrors must have the C sizes (catches drift between header and binding)
+    exe = os.path.join(_lib.REPO, "_build", "sizeof_check")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    code =('#include "halmd_gb300.h"\n#include <stdio.h>\nint main(void){printf("%zu %zu\\n",'
+            'sizeof(hmd_system_desc), sizeof(hmd_system_info));return 0;}\n')
+    c_path = os.path.join(_lib.REPO, "_build", "sizeof_check.c")
+    with open(c_path, "w") as fh:
+        fh.write(code)
+    subprocess.run(["gcc", "-I", os.path.join(_lib.REPO, "include"), "-o", exe, c_path], check=True)
+    a, b = map(int, subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split())
+    assert a == ctypes.sizeof(_lib.SystemDesc)
+    assert b == ctypes.sizeof(_lib.SystemInfo)

@@ -1,0 +1,256 @@
+"""GPU parity of the MD step against the CPU oracle (calls through the C ABI).
+
+Bars: bit-exact for integer/index work (cells, neighbour sets, Hilbert keys,
+sort permutation) and for the float/dsfloat integrator, which rounds every
+operation like the oracle; forces within the stated tolerance of an FP64
+evaluation on the same float positions.
+"""
+import numpy as np
+import pytest
+
+import halmd_gb300 as hg
+import oracle
+from _systems import KA_EPS, KA_SIGMA, ka_system, lj_system, rel_force_error
+
+pytestmark = pytest.mark.gpu
+
+# per-particle force error bound: max_i |F_i - F64_i| / max(|F64_i|, F_rms)
+FORCE_TOL = 2e-6
+
+
+def lj_engine(precision="dsfloat", ncell=6, skin=0.3, dt=0.005, **kw):
+    r, v, L = lj_system(ncell=ncell)
+    n = r.shape[0]
+    eng = hg.Engine(precision)
+    eng.add_system(hg.system_desc(n, L, r_cut=2.5, truncation="shifted", skin=skin, timestep=dt, **kw))
+    eng.commit()
+    eng.set("position", r)
+    eng.set("velocity", v)
+    return eng, r, v, L
+
+
+def ka_engine(precision="dsfloat", ncell=6, dt=0.002, **kw):
+    r, v, sp, L = ka_system(ncell=ncell)
+    n = r.shape[0]
+    eng = hg.Engine(precision)
+    rc = 2.5 * np.asarray(KA_SIGMA) / np.asarray(KA_SIGMA)  # r_c = 2.5 sigma_ab
+    eng.add_system(hg.system_desc(n, L, epsilon=KA_EPS, sigma=KA_SIGMA, r_cut=rc, truncation="smooth_r4",
+                                  smoothing=0.005, skin=0.3, timestep=dt, **kw))
+    eng.commit()
+    eng.set("species", sp)
+    eng.set("position", r)
+    eng.set("velocity", v)
+    return eng, r, v, sp, L
+
+
+def tag_order(eng, raw):
+    rid = eng.get("reverse_id")
+    return raw[rid]
+
+
+def oracle_forces(eng, species, pot):
+    inf = eng.info()
+    Lf = np.array(inf.box_f32, dtype=np.float32)
+    pos4 = tag_order(eng, eng.get_raw("position_hi"))
+    r = pos4[:, :3].astype(np.float64)
+    return oracle.forces(r, species, Lf.astype(np.float64), pot, pos4=pos4, Lf=Lf), pos4
+
+
+@pytest.mark.parametrize("precision", ["dsfloat", "float"])
+def test_lj_force_parity(precision):
+    eng, r, v, L = lj_engine(precision)
+    n = r.shape[0]
+    eng.force(aux=True)
+    f = eng.get("force")
+    pot = oracle.Potential(1.0, 1.0, 2.5, "shifted")
+    ref, _ = oracle_forces(eng, np.zeros(n), pot)
+    emax, emed = rel_force_error(f, ref["force"])
+    print("LJ force rel err max %.3g median %.3g" % (emax, emed))
+    assert emax < FORCE_TOL
+    en = eng.get("potential_energy")
+    assert abs(en.sum() - ref["epot"]) < 1e-6 * abs(ref["epot"])
+    np.testing.assert_allclose(en, ref["en_pot"], rtol=1e-5, atol=1e-5)
+    st = eng.get("stress_pot")
+    srms = np.sqrt(np.mean(ref["stress"] ** 2))
+    assert np.max(np.abs(st - ref["stress"])) < 1e-5 * srms * 10
+    th = eng.thermo()
+    assert abs(th["epot"] - ref["epot"]) < 1e-6 * abs(ref["epot"])
+    assert abs(th["virial"] - ref["virial"]) < 1e-6 * abs(ref["virial"])
+    vv = eng.get("velocity")
+    assert abs(th["mv2"] - np.sum(vv * vv)) < 1e-12 * np.sum(vv * vv)
+    eng.close()
+
+
+def test_ka_smooth_r4_force_parity():
+    eng, r, v, sp, L = ka_engine()
+    eng.force(aux=True)
+    f = eng.get("force")
+    pot = oracle.Potential(KA_EPS, KA_SIGMA, 2.5 * np.ones((2, 2)) * 1.0, "smooth_r4", h=0.005)
+    # r_cut = 2.5 sigma_ab: in units of sigma the cutoff matrix is 2.5 everywhere
+    ref, _ = oracle_forces(eng, sp, pot)
+    emax, emed = rel_force_error(f, ref["force"])
+    print("KA force rel err max %.3g median %.3g" % (emax, emed))
+    assert emax < FORCE_TOL
+    en = eng.get("potential_energy")
+    assert abs(en.sum() - ref["epot"]) < 1e-6 * abs(ref["epot"])
+    eng.close()
+
+
+@pytest.mark.parametrize("make", ["lj", "ka"])
+def test_neighbour_lists_bit_exact(make):
+    if make == "lj":
+        eng, r, v, L = lj_engine()
+    else:
+        eng, r, v, sp, L = ka_engine()
+    eng.force()
+    inf = eng.info()
+    ns = inf.nspecies
+    rrcs = np.array(inf.rr_cut_skin[: ns * ns], dtype=np.float32)
+    pos4 = tag_order(eng, eng.get_raw("r0"))   # positions of the last build
+    maxn = inf.neighbour_capacity
+    counts, lists = eng.neighbour_lists(maxn)
+    rc, rl, mx = oracle.neighbour_full_f32(pos4, np.array(inf.box_f32), rrcs, maxn)
+    assert np.array_equal(counts, rc)
+    assert np.array_equal(lists, rl)
+    assert inf.max_neighbours == mx
+    eng.close()
+
+
+def test_binning_bit_exact():
+    eng, r, v, L = lj_engine(ncell=8)
+    eng.force()
+    inf = eng.info()
+    ncell = np.array(inf.ncell[:], dtype=np.int32)
+    Lf = np.array(inf.box_f32, dtype=np.float32)
+    cell_len = Lf / ncell.astype(np.float32)
+    pos4 = eng.get_raw("position_hi")
+    cells, _, maxocc = oracle.binning_f32(pos4, ncell, cell_len, inf.cell_size)
+    assert maxocc == inf.max_cell_occupancy
+    assert np.array_equal(eng.get_raw("cells"), cells)
+    eng.close()
+
+
+def test_hilbert_keys_and_sort_permutation():
+    eng, r, v, L = lj_engine(ncell=8)
+    n = r.shape[0]
+    inf = eng.info()
+    pos4 = eng.get_raw("position_hi")[:n]          # slot order == tag order before the first sort
+    keys = oracle.hilbert_keys_f32(pos4, np.array(inf.box_f32), inf.hilbert_depth)
+    assert inf.hilbert_depth == oracle.hilbert_depth(float(max(inf.box_f32)))
+    assert np.array_equal(eng.hilbert_keys(), keys)
+    eng.force()                                    # first list build sorts the particles
+    ids = eng.get("id")[:n]
+    assert np.array_equal(ids, oracle.stable_argsort_u32(keys))
+    # the phase space moved with the particles (tag-order view unchanged)
+    np.testing.assert_allclose(eng.get("velocity"), v, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(eng.get("position"), r, rtol=1e-12, atol=1e-12)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["dsfloat", "float"])
+def test_integrate_finalize_bit_exact(precision):
+    eng, r, v, L = lj_engine(precision)
+    ds = precision == "dsfloat"
+    eng.force()
+    inf = eng.info()
+    Lf = np.array(inf.box_f32, dtype=np.float32)
+    r4 = np.concatenate([eng.get_raw("position_hi"), eng.get_raw("position_lo")])
+    v4 = np.concatenate([eng.get_raw("velocity_hi"), eng.get_raw("velocity_lo")])
+    img = eng.get_raw("image")
+    f4 = eng.get_raw("force")
+    eng.integrate()
+    r_ref, v_ref, img_ref = oracle.integrate_f32(r4, v4, img, f4, 0.005, Lf, ds=ds)
+    A = inf.slots
+    assert np.array_equal(eng.get_raw("position_hi").view(np.uint32), r_ref[:A].view(np.uint32))
+    assert np.array_equal(eng.get_raw("velocity_hi").view(np.uint32), v_ref[:A].view(np.uint32))
+    if ds:
+        assert np.array_equal(eng.get_raw("position_lo").view(np.uint32), r_ref[A:].view(np.uint32))
+        assert np.array_equal(eng.get_raw("velocity_lo").view(np.uint32), v_ref[A:].view(np.uint32))
+    assert np.array_equal(eng.get_raw("image"), img_ref)
+    eng.force()
+    r4 = np.concatenate([eng.get_raw("position_hi"), eng.get_raw("position_lo")])
+    v4 = np.concatenate([eng.get_raw("velocity_hi"), eng.get_raw("velocity_lo")])
+    f4 = eng.get_raw("force")
+    eng.finalize()
+    v_ref = oracle.finalize_f32(r4, v4, f4, 0.005, ds=ds)
+    assert np.array_equal(eng.get_raw("velocity_hi").view(np.uint32), v_ref[:A].view(np.uint32))
+    if ds:
+        assert np.array_equal(eng.get_raw("velocity_lo").view(np.uint32), v_ref[A:].view(np.uint32))
+    eng.close()
+
+
+def test_andersen_collisions():
+    T, rate, dt, seed = 0.7, 60.0, 0.005, 1234
+    eng, r, v, L = lj_engine(integrator="andersen", temperature=T, collision_rate=rate, seed=seed)
+    eng.force()
+    eng.integrate()
+    eng.force()
+    A = eng.info().slots
+    r4 = np.concatenate([eng.get_raw("position_hi"), eng.get_raw("position_lo")])
+    v4 = np.concatenate([eng.get_raw("velocity_hi"), eng.get_raw("velocity_lo")])
+    f4 = eng.get_raw("force")
+    ids = eng.get("id")
+    eng.finalize()
+    v_ref, coll = oracle.andersen_finalize_f32(r4, v4, f4, ids, dt, T, rate * dt, seed, step=0)
+    got = eng.get_raw("velocity_hi")
+    assert 0.2 < coll[:len(ids)].mean() < 0.4       # p = 0.3 per particle and step
+    keep = ~coll[:A]
+    assert np.array_equal(got[keep].view(np.uint32), v_ref[:A][keep].view(np.uint32))
+    np.testing.assert_allclose(got[coll[:A], :3], v_ref[:A][coll[:A], :3], rtol=2e-6, atol=2e-6)
+    eng.close()
+
+
+def test_graph_step_equals_module_calls():
+    a, r, v, L = lj_engine()
+    b, *_ = lj_engine()
+    a.step(7)
+    for _ in range(7):
+        b.integrate()
+        b.force()
+        b.finalize()
+    for name in ("position", "velocity", "image"):
+        assert np.array_equal(a.get(name), b.get(name)), name
+    assert a.info().step == b.info().step == 7
+    a.close()
+    b.close()
+
+
+def test_short_trajectory_against_fp64_host_backend():
+    eng, r, v, L = lj_engine(ncell=5, dt=0.002)
+    n = r.shape[0]
+    nsteps = 50
+    eng.step(nsteps)
+    pot = oracle.Potential(1.0, 1.0, 2.5, "shifted")
+    Lf = float(np.float32(L))
+    r_ref, v_ref, img_ref, st = oracle.md_run(r, v, np.zeros(n), np.ones(n), [Lf] * 3, pot, 0.3, 0.002, nsteps)
+    got = eng.get("unwrapped_position")
+    ref = r_ref + img_ref * Lf
+    assert np.max(np.abs(got - ref)) < 1e-5
+    np.testing.assert_allclose(eng.get("velocity"), v_ref, atol=1e-4)
+    eng.close()
+
+
+def test_nve_energy_conservation_dsfloat():
+    eng, r, v, L = lj_engine(ncell=10, dt=0.005)
+    eng.force(aux=True)
+    th = eng.thermo()
+    e0 = 0.5 * th["mv2"] + th["epot"]
+    eng.step(1000, aux_last=True)
+    th = eng.thermo()
+    e1 = 0.5 * th["mv2"] + th["epot"]
+    assert abs(e1 - e0) / abs(e0) < 2e-3
+    assert np.max(np.abs(th["momentum"])) < 1e-6 * r.shape[0]
+    assert eng.info().rebuilds >= 2
+    eng.close()
+
+
+def test_overflow_recovery_matches_ample_capacity():
+    a, r, v, L = lj_engine(neighbour_occupancy=20.0)   # list capacity 32 < ~78 needed
+    b, *_ = lj_engine()
+    a.step(20)
+    b.step(20)
+    assert a.info().neighbour_capacity > 32
+    assert np.array_equal(a.get("position"), b.get("position"))
+    assert np.array_equal(a.get("velocity"), b.get("velocity"))
+    a.close()
+    b.close()
