@@ -1,0 +1,337 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 MD step (particle-steps/s).
+
+Workload (default): the Kob-Andersen binary mixture, N = 64000 at density 1.2
+(A:B = 80:20), LJ with smooth_r4 cut-off (h = 0.005, r_c = 2.5 sigma_ab),
+skin 0.3, Andersen NVT at T = 0.7 (collision rate 1), dt = 0.002, dsfloat
+positions and velocities.  One bench step = one captured graph of
+`--md-steps` MD steps (integrate, device-decided list rebuild, force,
+finalize); L2 is flushed between bench steps.  `--workload lj1m` runs the
+LJ fluid with N = 1,048,576.
+
+Arms:
+  default           the CUDA engine through the C ABI (this repository)
+  --impl reference  the reference's host backend restated on the CPU
+                    (single thread, FP64, half list; the reference itself
+                    cannot be built: no Boost / Lua / HDF5 in the image)
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+MEASURED = os.path.join(REPO, "MEASURED_PEAKS.json")
+
+KA = dict(eps=[[1.0, 1.5], [1.5, 0.5]], sigma=[[1.0, 0.8], [0.8, 0.88]])
+
+
+def workload(name):
+    if name == "ka64k":
+        return dict(name="KA-64k", n=64000, rho=1.2, T=0.7, dt=0.002, trunc="smooth_r4", skin=0.3, nspecies=2,
+                    rate=1.0)
+    if name == "lj1m":
+        return dict(name="LJ-1M", n=1048576, rho=0.8442, T=0.722, dt=0.002, trunc="shifted", skin=0.3, nspecies=1,
+                    rate=0.0)
+    if name == "lj4k":
+        return dict(name="LJ-4k", n=4000, rho=0.8442, T=1.5, dt=0.005, trunc="shifted", skin=0.3, nspecies=1,
+                    rate=0.0)
+    raise SystemExit("unknown workload " + name)
+
+
+def initial_state(w, seed=2024):
+    """Seeded synthetic input: fcc lattice (LJ) or lattice sites with random
+    80:20 species (KA), Maxwell-Boltzmann velocities with zero momentum."""
+    n = w["n"]
+    rng = np.random.default_rng(seed)
+    ncell = int(round((n / 4) ** (1 / 3)))
+    if 4 * ncell ** 3 != n:
+        # KA-64k: 40^3 simple-cubic sites
+        m = int(round(n ** (1 / 3)))
+        assert m ** 3 == n
+        L = (n / w["rho"]) ** (1 / 3)
+        g = (np.arange(m) + 0.5) * (L / m) - 0.5 * L
+        r = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    else:
+        L = ncell * (4 / w["rho"]) ** (1 / 3)
+        a = L / ncell
+        basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+        c = np.stack(np.meshgrid(*(np.arange(ncell),) * 3, indexing="ij"), -1).reshape(-1, 1, 3)
+        r = ((c + basis[None] + 0.25) * a - 0.5 * L).reshape(-1, 3)
+    r = r + rng.uniform(-0.02, 0.02, size=r.shape)
+    v = rng.normal(0, np.sqrt(w["T"]), size=(n, 3))
+    v -= v.mean(axis=0)
+    v *= np.sqrt(3 * (n - 1) * w["T"] / np.sum(v * v))
+    species = np.zeros(n, dtype=np.uint32)
+    if w["nspecies"] == 2:
+        species[rng.permutation(n)[: n // 5]] = 1
+    return r, v, species, L
+
+
+def make_engine(w, L, seed=7):
+    import halmd_gb300 as hg
+    eng = hg.Engine("dsfloat")
+    if w["nspecies"] == 2:
+        d = hg.system_desc(w["n"], L, epsilon=KA["eps"], sigma=KA["sigma"], r_cut=2.5, truncation="smooth_r4",
+                           smoothing=0.005, skin=w["skin"], timestep=w["dt"],
+                           integrator="andersen" if w["rate"] > 0 else "verlet", temperature=w["T"],
+                           collision_rate=w["rate"], seed=seed)
+    else:
+        d = hg.system_desc(w["n"], L, r_cut=2.5, truncation=w["trunc"], skin=w["skin"], timestep=w["dt"],
+                           integrator="andersen" if w["rate"] > 0 else "verlet", temperature=w["T"],
+                           collision_rate=w["rate"], seed=seed)
+    eng.add_system(d)
+    eng.commit()
+    return eng
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        rows = [[x.strip() for x in line.split(",")] for line in out.strip().splitlines() if line.strip()]
+        rows = [r for r in rows if len(r) == 7]
+        if not rows:
+            return None
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, name in enumerate(names):
+                if r[3 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": float(rows[0][1]),
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def peaks():
+    try:
+        with open(MEASURED) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(w, r, v, species, L, budget_s=15.0):
+    """FP64 single-thread host backend restatement on a bounded sample."""
+    import oracle
+    if w["nspecies"] == 2:
+        pot = oracle.Potential(KA["eps"], KA["sigma"], 2.5, "smooth_r4", h=0.005)
+    else:
+        pot = oracle.Potential(1.0, 1.0, 2.5, w["trunc"])
+    n = w["n"]
+    mass = np.ones(n)
+    t0 = time.perf_counter()
+    oracle.md_run(r, v, species, mass, [L] * 3, pot, w["skin"], w["dt"], 2, temperature=w["T"],
+                  coll_rate=w["rate"], seed=1)
+    t_probe = time.perf_counter() - t0
+    steps = int(max(2, min(2000, (budget_s / max(t_probe, 1e-3)) * 2)))
+    t0 = time.perf_counter()
+    oracle.md_run(r, v, species, mass, [L] * 3, pot, w["skin"], w["dt"], steps, temperature=w["T"],
+                  coll_rate=w["rate"], seed=1)
+    dt = time.perf_counter() - t0
+    return {"value": n * steps / dt, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+            "sample": "%s, %d MD steps from the synthetic start (list builds included), FP64, 1 thread" %
+                      (w["name"], steps)}
+
+
+def run_reference(args, w):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    r, v, species, L = initial_state(w)
+    import oracle
+    if w["nspecies"] == 2:
+        pot = oracle.Potential(KA["eps"], KA["sigma"], 2.5, "smooth_r4", h=0.005)
+    else:
+        pot = oracle.Potential(1.0, 1.0, 2.5, w["trunc"])
+    n = w["n"]
+    mass = np.ones(n)
+    # sample size per bench step: a few MD steps so the whole run stays within minutes
+    per = max(1, int(args.ref_steps))
+    for _ in range(args.warmup):
+        oracle.md_run(r, v, species, mass, [L] * 3, pot, w["skin"], w["dt"], 1, temperature=w["T"],
+                      coll_rate=w["rate"], seed=1)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        oracle.md_run(r, v, species, mass, [L] * 3, pot, w["skin"], w["dt"], per, temperature=w["T"],
+                      coll_rate=w["rate"], seed=1 + k)
+    dt = time.perf_counter() - t0
+    value = n * per * args.steps / dt
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / (per * args.steps), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "n": n, "md_steps_per_bench_step": per},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+                             "sample": "%s, %d x %d MD steps, FP64 host-backend restatement, 1 thread "
+                                       "(the reference host backend is single-threaded)" % (w["name"], args.steps, per)},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--workload", default="ka64k")
+    ap.add_argument("--md-steps", type=int, default=100, help="MD steps per bench step")
+    ap.add_argument("--ref-steps", type=int, default=2, help="MD steps per bench step of the reference arm")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = workload(args.workload)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, w)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    r, v, species, L = initial_state(w, seed=2024 + rank)
+    eng = make_engine(w, L, seed=7 + rank)
+    n = w["n"]
+    eng.set("species", species)
+    eng.set("position", r)
+    eng.set("velocity", v)
+    eng.step(max(1, args.md_steps))   # equilibrate lists / first rebuilds
+    stream = torch.cuda.ExternalStream(eng.stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    M = args.md_steps
+    for _ in range(args.warmup):
+        eng.step(M)
+    inf0 = eng.info()
+    barrier()
+    clocks = ClockSampler(local)
+    total_ms = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.step(M)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    barrier()
+    clk = clocks.stop()
+    inf1 = eng.info()
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    md_steps = M * args.steps
+    value = world * n * md_steps / (total_ms * 1e-3)
+    rebuilds = int(inf1.rebuilds - inf0.rebuilds)
+    launches = md_steps * 3 + rebuilds * inf1.rebuild_kernels
+
+    # e2e: the public API with host buffers; H2D of the phase space, M steps, D2H of it
+    e2e_ms = 0.0
+    h2d = d2h = 0
+    pos = eng.get("position")
+    vel = eng.get("velocity")
+    A = inf1.slots
+    for _ in range(max(1, args.steps // 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.set("position", pos)
+        eng.set("velocity", vel)
+        eng.step(M)
+        pos = eng.get("position")
+        vel = eng.get("velocity")
+        e2e_ms += 1e3 * (time.perf_counter() - t0)
+    e2e_steps = M * max(1, args.steps // 2)
+    # bytes the API moves per call: set(position) 3 float4[A] up, set(velocity) 2 up (each after a read-back
+    # of the same arrays); get(position) 3 down, get(velocity) 2 down; reverse ids 4 B/particle per call
+    h2d = (3 + 2) * 16 * A
+    d2h = (3 + 2) * 16 * A + (3 + 2) * 16 * A + 4 * 4 * n
+    e2e_value = world * n * e2e_steps / (e2e_ms * 1e-3)
+
+    # dominant kernel: the pair force, timed alone with events on the engine stream
+    eng.profile(True)
+    for _ in range(20):
+        eng.force()
+    f_ms, f_cnt = eng.profile_get("force")
+    eng.profile(False)
+    counts, _ = eng.neighbour_lists()
+    K_l = float(counts.mean())
+    bytes_per_launch = n * (16 + 4 * K_l + 16)
+    achieved = bytes_per_launch / (f_ms / f_cnt * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, r, v, species, L)
+
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / md_steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (dsfloat state)",
+            "data": "synthetic",
+            "config": {"workload": w["name"], "n": n, "density": w["rho"], "temperature": w["T"], "dt": w["dt"],
+                       "md_steps_per_bench_step": M, "truncation": w["trunc"], "skin": w["skin"],
+                       "precision": "dsfloat", "l2": "flushed (256 MB write) between timed bench steps",
+                       "rebuilds_in_timed_region": rebuilds, "parallelism": "replicas" if world > 1 else "single"},
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d / M,
+                    "d2h_bytes_per_step": d2h / M,
+                    "note": "hmd_set(position, velocity) + hmd_step(%d) + hmd_get(position, velocity) per call" % M},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "k_force",
+                         "peak_source": peak_kind,
+                         "bytes_per_launch": bytes_per_launch, "mean_list_length": K_l,
+                         "force_ms": f_ms / f_cnt},
+            "clocks": clk}
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line))
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

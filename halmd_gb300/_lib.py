@@ -67,6 +67,8 @@ class SystemInfo(ctypes.Structure):
         ("max_cell_occupancy", ctypes.c_uint32),
         ("step", ctypes.c_uint64),
         ("rebuilds", ctypes.c_uint64),
+        ("sort_key_bits", ctypes.c_uint32),
+        ("rebuild_kernels", ctypes.c_uint32),
         ("box_f32", ctypes.c_float * 3),
         ("rr_cut_skin", ctypes.c_float * 16),
         ("rr_cut", ctypes.c_float * 16),
@@ -117,6 +119,8 @@ def load():
         "hmd_thermo": (I, [P, U, P]),
         "hmd_neighbour_lists": (I, [P, U, P, P, U]),
         "hmd_hilbert_keys": (I, [P, U, P]),
+        "hmd_profile_enable": (I, [P, I]),
+        "hmd_profile_get": (I, [P, ctypes.c_char_p, P, P]),
         "hmd_dynamics_create": (I, [P, U, D, D, U, U, U, P]),
         "hmd_dynamics_destroy": (I, [P]),
         "hmd_dynamics_levels": (I, [P, P, P]),
@@ -300,6 +304,15 @@ class Engine:
         lists = np.zeros((n, maxn), dtype=np.uint32)
         self._check(self._L.hmd_neighbour_lists(self._h, s, _ptr(counts), _ptr(lists), maxn))
         return counts, lists
+
+    def profile(self, enable=True):
+        self._check(self._L.hmd_profile_enable(self._h, 1 if enable else 0))
+
+    def profile_get(self, phase):
+        ms = ctypes.c_double()
+        cnt = ctypes.c_uint64()
+        self._check(self._L.hmd_profile_get(self._h, phase.encode(), ctypes.byref(ms), ctypes.byref(cnt)))
+        return ms.value, cnt.value
 
     def hilbert_keys(self, s=0):
         k = np.zeros(self.n(s), dtype=np.uint32)

@@ -210,6 +210,19 @@ int hmd_neighbour_lists(hmd_engine* h, uint32_t sys, uint32_t* counts, uint32_t*
     return guard(h, [&] { h->e->neighbour_lists(sys, counts, lists, maxn); });
 }
 
+int hmd_profile_enable(hmd_engine* h, int enable)
+{
+    ENGINE_OR_FAIL(h);
+    return guard(h, [&] { h->e->profile_enable(enable != 0); });
+}
+
+int hmd_profile_get(hmd_engine* h, const char* phase, double* total_ms, uint64_t* count)
+{
+    ENGINE_OR_FAIL(h);
+    if (!phase || !total_ms || !count) return HMD_ERR_INVALID;
+    return guard(h, [&] { h->e->profile_get(phase, total_ms, count); });
+}
+
 int hmd_hilbert_keys(hmd_engine* h, uint32_t sys, uint32_t* keys)
 {
     ENGINE_OR_FAIL(h);

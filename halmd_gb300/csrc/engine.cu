@@ -42,6 +42,8 @@ Engine::~Engine()
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
     destroy_graphs();
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
     if (stream_) cudaStreamDestroy(stream_);
     if (side_) cudaStreamDestroy(side_);
 }
@@ -579,6 +581,8 @@ void Engine::info(uint32_t s, hmd_system_info* out)
     out->max_cell_occupancy = st[s].max_cell;
     out->step = st[s].step;
     out->rebuilds = st[s].rebuilds;
+    out->sort_key_bits = key_bits_;
+    out->rebuild_kernels = rebuild_kernel_count();
     for (size_t ab = 0; ab < h.pairs.size(); ++ab) {
         out->rr_cut_skin[ab] = h.pairs[ab].rr_cut_skin;
         out->rr_cut[ab] = h.pairs[ab].rr_cut;
@@ -815,28 +819,74 @@ void Engine::step(uint64_t nsteps, bool aux_last)
     integrated_ = false;
 }
 
+void Engine::tic()
+{
+    if (!profile_) return;
+    HMD_CUDA(cudaEventRecord(ev0_, stream_));
+}
+
+void Engine::toc(const char* phase)
+{
+    if (!profile_) return;
+    HMD_CUDA(cudaEventRecord(ev1_, stream_));
+    HMD_CUDA(cudaEventSynchronize(ev1_));
+    float ms = 0;
+    HMD_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    for (auto& t : timers_)
+        if (t.first == phase) { t.second.ms += ms; t.second.count += 1; return; }
+    timers_.push_back({phase, Timer{ms, 1}});
+}
+
+void Engine::profile_enable(bool on)
+{
+    if (on && !ev0_) {
+        HMD_CUDA(cudaEventCreate(&ev0_));
+        HMD_CUDA(cudaEventCreate(&ev1_));
+    }
+    profile_ = on;
+    if (on) timers_.clear();
+}
+
+void Engine::profile_get(const std::string& phase, double* total_ms, uint64_t* count)
+{
+    *total_ms = 0;
+    *count = 0;
+    for (auto& t : timers_)
+        if (t.first == phase) { *total_ms = t.second.ms; *count = t.second.count; }
+}
+
+uint32_t Engine::rebuild_kernel_count() const
+{
+    // sort keys + (hist, scan, scatter) per pass + rearrange + copy back; cell clear, bin, sort; list build
+    return (any_sort_ ? 1u + 3u * (uint32_t)radix_passes(key_bits_) + 2u : 0u) + 3u + 1u;
+}
+
 void Engine::integrate()
 {
     check_committed();
     ensure_forces(false);
+    tic();
     launch_integrate(dev(), ds(), 0, false, stream_);
     HMD_CUDA(cudaGetLastError());
+    toc("integrate");
     integrated_ = true;
     forces_valid_ = false;
 }
 
+// pair_trunc::apply (forces/pair_trunc.hpp:192-216): always evaluates; the
+// lists are rebuilt first where a step flagged it or a rebuild is pending
 void Engine::force(bool aux)
 {
     check_committed();
-    if (!integrated_) {
-        forces_valid_ = forces_valid_ && (!aux || aux_valid_);
-        ensure_forces(aux);
-        return;
-    }
     const Dev d = dev();
+    if (!integrated_) launch_mark(d, false, stream_);
+    tic();
     rebuild_chain(stream_);
+    toc("rebuild");
+    tic();
     launch_force(d, aux, stream_);
     HMD_CUDA(cudaGetLastError());
+    toc(aux ? "force_aux" : "force");
     uint32_t status = 0;
     download(status_, 0, 1, &status);
     if (status != 0) {
@@ -857,8 +907,10 @@ void Engine::force(bool aux)
 void Engine::finalize()
 {
     check_committed();
+    tic();
     launch_finalize(dev(), ds(), stream_);
     HMD_CUDA(cudaGetLastError());
+    toc("finalize");
     sync();
 }
 

@@ -80,6 +80,8 @@ public:
     void thermo(uint32_t s, double* out);
     void neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint32_t maxn);
     void hilbert_keys(uint32_t s, uint32_t* keys);
+    void profile_enable(bool on);
+    void profile_get(const std::string& phase, double* total_ms, uint64_t* count);
 
     // used by the dynamics module
     Dev dev() const;
@@ -139,6 +141,18 @@ private:
     DevBuf<float4> snap_pos_, snap_vel_, snap_img_, snap_force_;
     DevBuf<uint32_t> snap_id_, snap_rid_;
     DevBuf<SysState> snap_st_;
+
+    // per-phase CUDA-event timers of the module-level calls
+    struct Timer {
+        double ms = 0;
+        uint64_t count = 0;
+    };
+    bool profile_ = false;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    std::vector<std::pair<std::string, Timer>> timers_;
+    void tic();
+    void toc(const char* phase);
+    uint32_t rebuild_kernel_count() const;
 
     static constexpr int CHUNK_STEPS = 50;
     static constexpr uint64_t SEGMENT_STEPS = 5000;

@@ -177,6 +177,49 @@ __device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rr
     }
 }
 
+// error of s = fl(a + b) (Knuth TwoSum)
+__device__ __forceinline__ float two_sum_err(float a, float b, float s)
+{
+    const float bp = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// Compensated LJ: the pair distance and its square are carried as
+// (hi, lo) pairs (TwoSum of the position difference, FMA residuals of the
+// squares), the reciprocal is refined by one Newton step against rr_hi +
+// rr_lo, and fval gets the first-order term d fval / d rri * rri_lo.  The
+// steep r^-14 law otherwise amplifies the float rounding of r^2 seven-fold.
+template <int TR>
+__device__ __forceinline__ void pair_eval_precise(const PairParam& p, float rr, float rrl, float rri_smooth,
+                                                  float& fval, float& en)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(rr));
+    const float res = __fmaf_rn(-rrl, y, __fmaf_rn(-rr, y, 1.0f));
+    const float ylo = __fmul_rn(y, res);
+    const float rri = __fmul_rn(p.sigma2, y);
+    const float rril = __fmaf_rn(p.sigma2, ylo, __fmaf_rn(p.sigma2, y, -rri));
+    const float ri6 = rri * rri * rri;
+    fval = p.c48 * rri * ri6 * (ri6 - 0.5f);
+    fval = __fmaf_rn(p.c48 * ri6 * __fmaf_rn(7.0f, ri6, -2.0f), rril, fval);
+    en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
+    if (TR == TRUNC_SMOOTH_R4) {
+        const float r = __fsqrt_rn(rr);
+        const float dr = r - p.r_cut;
+        const float x2 = dr * dr * rri_smooth;
+        const float x4 = x2 * x2;
+        const float x4i = __fdiv_rn(1.0f, 1.0f + x4);
+        const float h0 = x4 * x4i;
+        const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
+        fval = h0 * fval - h1 * __fdiv_rn(en, r);
+        en = h0 * en;
+    } else if (TR == TRUNC_FORCE_SHIFTED) {
+        const float r = __fsqrt_rn(rr);
+        fval = fval - __fdiv_rn(p.f_cut, r);
+        en = en + (r - p.r_cut) * p.f_cut;
+    }
+}
+
 template <int TR, bool AUX>
 __device__ __forceinline__ void force_particle(const Dev& d, uint32_t i, const SysParam& P, const PairParam* spp,
                                                float4 ri, uint32_t a)
@@ -196,18 +239,35 @@ __device__ __forceinline__ void force_particle(const Dev& d, uint32_t i, const S
         const uint32_t j = __ldg(lst + k * stride);
         const float4 rj = __ldg(d.pos + j);
         const uint32_t b = species_bits(rj.w);
-        const float dx = min_image(__fsub_rn(ri.x, rj.x), Lx, Ix);
-        const float dy = min_image(__fsub_rn(ri.y, rj.y), Ly, Iy);
-        const float dz = min_image(__fsub_rn(ri.z, rj.z), Lz, Iz);
-        const float rr = rr_exact(dx, dy, dz);
+        const float sx = __fsub_rn(ri.x, rj.x);
+        const float sy = __fsub_rn(ri.y, rj.y);
+        const float sz = __fsub_rn(ri.z, rj.z);
+        const float dx = min_image(sx, Lx, Ix);
+        const float dy = min_image(sy, Ly, Iy);
+        const float dz = min_image(sz, Lz, Iz);
+        const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
+        const float pxy = __fadd_rn(px, py);
+        const float rr = __fadd_rn(pxy, pz);   // == rr_exact(dx, dy, dz)
         if (b >= ns) continue;   // lists hold real particles only; keep the table lookup in bounds
         const PairParam& p = spp[a * ns + b];
         if (!(rr < p.rr_cut)) continue;
+        // dx - k L is exact (k = 0, or Sterbenz for k = +-1): the difference
+        // error is the TwoSum error of ri - rj
+        const float dxl = two_sum_err(ri.x, -rj.x, sx);
+        const float dyl = two_sum_err(ri.y, -rj.y, sy);
+        const float dzl = two_sum_err(ri.z, -rj.z, sz);
+        float rrl = __fadd_rn(__fadd_rn(__fmaf_rn(dx, dx, -px), __fmaf_rn(dy, dy, -py)), __fmaf_rn(dz, dz, -pz));
+        rrl = __fadd_rn(rrl, __fadd_rn(two_sum_err(px, py, pxy), two_sum_err(pxy, pz, rr)));
+        rrl = __fmaf_rn(2.0f * dx, dxl, __fmaf_rn(2.0f * dy, dyl, __fmaf_rn(2.0f * dz, dzl, rrl)));
         float fval, e;
-        pair_eval<TR>(p, rr, rri_smooth, fval, e);
-        two_sum_acc(fx, cx, fval * dx);
-        two_sum_acc(fy, cy, fval * dy);
-        two_sum_acc(fz, cz, fval * dz);
+        pair_eval_precise<TR>(p, rr, rrl, rri_smooth, fval, e);
+        const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
+        two_sum_acc(fx, cx, tx);
+        two_sum_acc(fy, cy, ty);
+        two_sum_acc(fz, cz, tz);
+        cx = __fmaf_rn(fval, dxl, __fadd_rn(cx, __fmaf_rn(fval, dx, -tx)));
+        cy = __fmaf_rn(fval, dyl, __fadd_rn(cy, __fmaf_rn(fval, dy, -ty)));
+        cz = __fmaf_rn(fval, dzl, __fadd_rn(cz, __fmaf_rn(fval, dz, -tz)));
         if (AUX) {
             en += e;
             s0 += fval * dx * dx;

@@ -98,6 +98,8 @@ typedef struct hmd_system_info {
     uint32_t max_cell_occupancy;     /* largest cell of the last build */
     uint64_t step;                   /* completed integration steps */
     uint64_t rebuilds;               /* neighbour-list builds so far */
+    uint32_t sort_key_bits;          /* bits of the engine's sort key (radix passes = ceil(bits/8)) */
+    uint32_t rebuild_kernels;        /* kernels one conditional rebuild launches */
     float box_f32[3];                /* box edges as the device stores them */
     float rr_cut_skin[HMD_MAX_SPECIES * HMD_MAX_SPECIES];  /* float (r_c + skin)^2 table */
     float rr_cut[HMD_MAX_SPECIES * HMD_MAX_SPECIES];       /* float r_c^2 table */
@@ -164,6 +166,16 @@ HMD_API int hmd_finalize(hmd_engine* engine);
 HMD_API int hmd_request_rebuild(hmd_engine* engine, uint32_t sys);
 /* steps a system still has to do (serving); ~0u = unbounded */
 HMD_API int hmd_set_steps_left(hmd_engine* engine, uint32_t sys, uint32_t steps);
+
+/*
+ * Per-phase runtime accumulators (utility/profiler.hpp:56-99, the modules'
+ * scoped_timer runtime structs, e.g. forces/pair_trunc.hpp:141-148):
+ * while enabled, hmd_integrate / hmd_force / hmd_finalize bracket their
+ * kernels with CUDA events on the engine stream.  Phases: "integrate",
+ * "force", "force_aux", "finalize", "rebuild".
+ */
+HMD_API int hmd_profile_enable(hmd_engine* engine, int enable);
+HMD_API int hmd_profile_get(hmd_engine* engine, const char* phase, double* total_ms, uint64_t* count);
 
 /* maximum displacement since the last build (max_displacement.cpp:77-106) */
 HMD_API int hmd_max_displacement(hmd_engine* engine, uint32_t sys, double* displacement);

@@ -15,7 +15,7 @@ from _systems import KA_EPS, KA_SIGMA, ka_system, lj_system, rel_force_error
 pytestmark = pytest.mark.gpu
 
 # per-particle force error bound: max_i |F_i - F64_i| / max(|F64_i|, F_rms)
-FORCE_TOL = 2e-6
+FORCE_TOL = 1e-6
 
 
 def lj_engine(precision="dsfloat", ncell=6, skin=0.3, dt=0.005, **kw):
