@@ -231,6 +231,8 @@ def main():
     eng.set("position", r)
     eng.set("velocity", v)
     eng.step(max(1, args.md_steps))   # equilibrate lists / first rebuilds
+    from halmd_gb300.tune import autotune_force_lanes
+    lanes, lane_ms = autotune_force_lanes(eng, use_cache=False)
     stream = torch.cuda.ExternalStream(eng.stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -313,7 +315,8 @@ def main():
             "config": {"workload": w["name"], "n": n, "density": w["rho"], "temperature": w["T"], "dt": w["dt"],
                        "md_steps_per_bench_step": M, "truncation": w["trunc"], "skin": w["skin"],
                        "precision": "dsfloat", "l2": "flushed (256 MB write) between timed bench steps",
-                       "rebuilds_in_timed_region": rebuilds, "parallelism": "replicas" if world > 1 else "single"},
+                       "rebuilds_in_timed_region": rebuilds, "parallelism": "replicas" if world > 1 else "single",
+                       "force_lanes": lanes, "autotune_force_ms": {str(k): v for k, v in lane_ms.items()}},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d / M,
                     "d2h_bytes_per_step": d2h / M,
                     "note": "hmd_set(position, velocity) + hmd_step(%d) + hmd_get(position, velocity) per call" % M},

@@ -105,6 +105,8 @@ def load():
         "hmd_engine_add_system": (I, [P, P, P]),
         "hmd_engine_commit": (I, [P]),
         "hmd_engine_stream": (I, [P, P]),
+        "hmd_engine_set_option": (I, [P, ctypes.c_char_p, ctypes.c_int64]),
+        "hmd_engine_get_option": (I, [P, ctypes.c_char_p, P]),
         "hmd_info": (I, [P, U, P]),
         "hmd_set": (I, [P, U, ctypes.c_char_p, P, S]),
         "hmd_get": (I, [P, U, ctypes.c_char_p, P, S]),
@@ -229,6 +231,14 @@ class Engine:
     def commit(self):
         self._check(self._L.hmd_engine_commit(self._h))
         self.committed = True
+
+    def set_option(self, name, value):
+        self._check(self._L.hmd_engine_set_option(self._h, name.encode(), int(value)))
+
+    def get_option(self, name):
+        v = ctypes.c_int64()
+        self._check(self._L.hmd_engine_get_option(self._h, name.encode(), ctypes.byref(v)))
+        return v.value
 
     @property
     def stream(self):

@@ -117,6 +117,20 @@ int hmd_engine_commit(hmd_engine* h)
     return guard(h, [&] { h->e->commit(); });
 }
 
+int hmd_engine_set_option(hmd_engine* h, const char* name, int64_t value)
+{
+    ENGINE_OR_FAIL(h);
+    if (!name) return HMD_ERR_INVALID;
+    return guard(h, [&] { h->e->set_option(name, value); });
+}
+
+int hmd_engine_get_option(hmd_engine* h, const char* name, int64_t* value)
+{
+    ENGINE_OR_FAIL(h);
+    if (!name || !value) return HMD_ERR_INVALID;
+    return guard(h, [&] { *value = h->e->get_option(name); });
+}
+
 int hmd_engine_stream(hmd_engine* h, void** stream)
 {
     ENGINE_OR_FAIL(h);

@@ -152,6 +152,13 @@ void Engine::layout_system(SysHost& h, uint32_t rank)
     }
     P.seed_lo = (uint32_t)d.seed;
     P.seed_hi = (uint32_t)(d.seed >> 32);
+    for (int q = 0; q < 3; ++q) {
+        // a list pair is within r_c + skin of each other at force time (each
+        // particle moved < skin/2 since the build); particles farther than
+        // that from every face have no partner across the box
+        const double in = 0.5 * d.box[q] - (rcs_max + d.skin) - 1e-4 * d.box[q];
+        P.inner[q] = in > 0 ? (float)in : 0.0f;
+    }
     float Lmax = 0;
     for (int q = 0; q < 3; ++q) {
         const float Lf = (float)d.box[q];
@@ -206,7 +213,7 @@ void Engine::commit()
         h.P.cell_word_off = cell_words;
         total_cells_ += h.P.ncells;
         cell_words += h.P.ncells * h.P.cell_size;
-        nbr_cap_ = std::max(nbr_cap_, h.nbr_size);
+        nbr_cap_ = std::max(nbr_cap_, round_up(h.nbr_size, 8));
         shift = std::max(shift, std::max(3 * h.P.depth, ceil_log2(h.P.A)));
         any_sort_ = any_sort_ || h.P.sort_enable;
     }
@@ -222,6 +229,9 @@ void Engine::commit()
         }
     }
     key_bits_ = shift + rank_bits;
+    // lanes per particle in the force kernel: enough threads to fill 152 SMs
+    // for small engines, fewer lanes (less reduction work) for large ones
+    if (lanes_ == 0) lanes_ = S_ <= (1u << 19) ? 8u : 4u;
     for (auto& h : sys_) h.P.key_shift = shift;
 
     const size_t S = S_;
@@ -314,6 +324,8 @@ Dev Engine::dev() const
     d.pos = pos_.p; d.vel = vel_.p; d.img = img_.p; d.force = force_.p; d.r0 = r0_.p;
     d.en_pot = en_pot_.p; d.stress = stress_.p; d.id = id_.p; d.rid = rid_.p;
     d.nbr = nbr_.p; d.nbr_count = nbr_count_.p; d.nbr_cap = nbr_cap_;
+    d.lanes = lanes_;
+    d.lanes_log2 = lanes_ == 8 ? 3u : lanes_ == 4 ? 2u : lanes_ == 2 ? 1u : 0u;
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
     d.S = S_; d.nsys = (uint32_t)sys_.size();
@@ -598,6 +610,35 @@ void Engine::request_rebuild(uint32_t s)
     forces_valid_ = false;
 }
 
+void Engine::set_option(const std::string& name, int64_t value)
+{
+    if (name == "force_lanes") {
+        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
+            throw Error(HMD_ERR_INVALID, "force_lanes must be 0 (auto), 1, 2, 4 or 8");
+        if (!committed_) {
+            lanes_ = (uint32_t)value;
+            return;
+        }
+        const uint32_t w = value == 0 ? 4u : (uint32_t)value;
+        if (w == lanes_) return;
+        lanes_ = w;   // the list layout changes: rebuild every list before the next force
+        destroy_graphs();
+        std::vector<SysState> st = read_state();
+        for (auto& t : st) t.rebuild_request = 1u;
+        write_state(st);
+        forces_valid_ = false;
+        return;
+    }
+    throw Error(HMD_ERR_INVALID, "unknown option '" + name + "'");
+}
+
+int64_t Engine::get_option(const std::string& name) const
+{
+    if (name == "force_lanes") return lanes_;
+    if (name == "neighbour_capacity") return nbr_cap_;
+    throw Error(HMD_ERR_INVALID, "unknown option '" + name + "'");
+}
+
 void Engine::set_steps_left(uint32_t s, uint32_t steps)
 {
     check_sys(s);
@@ -759,7 +800,7 @@ bool Engine::grow_after_overflow(uint32_t status)
     if (status & ST_NBR_OVERFLOW) {
         uint32_t m = 0;
         for (auto& t : st) m = std::max(m, t.max_nbr);
-        const uint32_t want = (uint32_t)std::ceil(m * 1.2) + 8;
+        const uint32_t want = round_up((uint32_t)std::ceil(m * 1.2) + 8, 8);
         if (want <= nbr_cap_) return false;
         nbr_cap_ = want;
         nbr_.alloc((size_t)nbr_cap_ * S_);
@@ -953,18 +994,22 @@ void Engine::neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint
     std::vector<uint32_t> cnt(P.A), id(P.A);
     download(nbr_count_, P.off, P.A, cnt.data());
     download(id_, P.off, P.A, id.data());
-    std::vector<uint32_t> col(P.A);
     for (uint32_t t = 0; t < P.n; ++t) {
         const uint32_t k = slot[t] - P.off;
         if (cnt[k] > maxn) throw Error(HMD_ERR_INVALID, "maxn smaller than a neighbour count");
     }
+    // lane-blocked layout: block b holds entries [b*W, b*W + W) of every slot
+    const uint32_t W = lanes_;
+    const uint32_t nblk = nbr_cap_ / W;
     std::vector<uint32_t> all((size_t)nbr_cap_ * P.A);
-    for (uint32_t k = 0; k < nbr_cap_; ++k) download(nbr_, (size_t)k * S_ + P.off, P.A, all.data() + (size_t)k * P.A);
+    for (uint32_t b = 0; b < nblk; ++b)
+        download(nbr_, ((size_t)b * S_ + P.off) * W, (size_t)P.A * W, all.data() + (size_t)b * P.A * W);
     for (uint32_t t = 0; t < P.n; ++t) {
         const uint32_t k = slot[t] - P.off;
         counts[t] = cnt[k];
         std::vector<uint32_t> v(cnt[k]);
-        for (uint32_t q = 0; q < cnt[k]; ++q) v[q] = id[all[(size_t)q * P.A + k] - P.off];
+        for (uint32_t q = 0; q < cnt[k]; ++q)
+            v[q] = id[all[((size_t)(q / W) * P.A + k) * W + q % W] - P.off];
         std::sort(v.begin(), v.end());
         for (uint32_t q = 0; q < maxn; ++q) lists[(size_t)t * maxn + q] = q < cnt[k] ? v[q] : PLACEHOLDER;
     }

@@ -76,6 +76,8 @@ public:
     void finalize();
     void request_rebuild(uint32_t s);
     void set_steps_left(uint32_t s, uint32_t steps);
+    void set_option(const std::string& name, int64_t value);
+    int64_t get_option(const std::string& name) const;
     double max_displacement(uint32_t s);
     void thermo(uint32_t s, double* out);
     void neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint32_t maxn);
@@ -124,6 +126,7 @@ private:
     uint32_t S_ = 0;
     uint32_t total_cells_ = 0;
     uint32_t nbr_cap_ = 0;
+    uint32_t lanes_ = 0;        // force-kernel lanes per particle (0: choose at commit)
     uint32_t key_bits_ = 0;
     bool any_sort_ = false;
     cudaStream_t stream_ = nullptr;

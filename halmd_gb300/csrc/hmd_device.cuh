@@ -69,6 +69,7 @@ struct SysParam {
     uint32_t active;           // 0: all slots are ghosts, kernels skip
     uint32_t sort_enable;      // Hilbert reorder on rebuild
     uint32_t rank;             // position among systems (sort key prefix)
+    float inner[3];            // |r| below this in every dimension: no list pair wraps the box
 };
 
 // mutable per-system device state
@@ -96,9 +97,11 @@ struct Dev {
     float* stress;             // [6S]
     uint32_t* id;              // [S] tag of the particle within its system
     uint32_t* rid;             // [S] slot of (off + tag)
-    uint32_t* nbr;             // [nbr_cap * S]
+    uint32_t* nbr;             // [nbr_cap * S], lane-blocked: entry k of slot i at ((k/lanes)*S + i)*lanes + k%lanes
     uint32_t* nbr_count;       // [S]
-    uint32_t nbr_cap;
+    uint32_t nbr_cap;          // multiple of 8
+    uint32_t lanes;            // threads per particle in the force kernel (1, 2, 4, 8)
+    uint32_t lanes_log2;
     uint32_t* cell;            // cell contents
     uint32_t* cell_count;      // [total_cells]
     const uint32_t* cell_sys;  // [total_cells] owning system

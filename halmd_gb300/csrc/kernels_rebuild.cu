@@ -338,8 +338,9 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
         const int loz = nz >= 3 ? -1 : 0, hiz = nz >= 2 ? 1 : 0;
         const uint32_t cs = P.cell_size;
         const uint32_t cap = d.nbr_cap;
-        const size_t stride = d.S;
-        uint32_t* out = d.nbr + i;
+        const uint32_t lw = d.lanes_log2, lmask = d.lanes - 1u;
+        const size_t bstride = (size_t)d.S << lw;
+        uint32_t* out = d.nbr + ((size_t)i << lw);
         const float* rrcs = s_rrcs + a * P.ns;
         for (int oz = loz; oz <= hiz; ++oz) {
             const int z = (cz + oz + nz) % nz;
@@ -359,7 +360,7 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
                         const float rr = rr_exact(dx, dy, dz);
                         const uint32_t b = species_bits(rj.w);
                         if (b < P.ns && rr <= rrcs[b]) {
-                            if (count < cap) out[count * stride] = j;
+                            if (count < cap) out[(count >> lw) * bstride + (count & lmask)] = j;
                             ++count;
                         }
                     }

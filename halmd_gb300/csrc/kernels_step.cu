@@ -152,31 +152,6 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float x)
     c = __fadd_rn(c, e);
 }
 
-// LJ + truncation (lennard_jones_kernel.hpp:44-56, truncations/*_kernel.cuh)
-template <int TR>
-__device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rri_smooth, float& fval, float& en)
-{
-    const float rri = __fdiv_rn(p.sigma2, rr);
-    const float ri6 = rri * rri * rri;
-    fval = p.c48 * rri * ri6 * (ri6 - 0.5f);
-    en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
-    if (TR == TRUNC_SMOOTH_R4) {
-        const float r = __fsqrt_rn(rr);
-        const float dr = r - p.r_cut;
-        const float x2 = dr * dr * rri_smooth;
-        const float x4 = x2 * x2;
-        const float x4i = __fdiv_rn(1.0f, 1.0f + x4);
-        const float h0 = x4 * x4i;
-        const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
-        fval = h0 * fval - h1 * __fdiv_rn(en, r);
-        en = h0 * en;
-    } else if (TR == TRUNC_FORCE_SHIFTED) {
-        const float r = __fsqrt_rn(rr);
-        fval = fval - __fdiv_rn(p.f_cut, r);
-        en = en + (r - p.r_cut) * p.f_cut;
-    }
-}
-
 // error of s = fl(a + b) (Knuth TwoSum)
 __device__ __forceinline__ float two_sum_err(float a, float b, float s)
 {
@@ -184,14 +159,17 @@ __device__ __forceinline__ float two_sum_err(float a, float b, float s)
     return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
 }
 
-// Compensated LJ: the pair distance and its square are carried as
-// (hi, lo) pairs (TwoSum of the position difference, FMA residuals of the
-// squares), the reciprocal is refined by one Newton step against rr_hi +
-// rr_lo, and fval gets the first-order term d fval / d rri * rri_lo.  The
-// steep r^-14 law otherwise amplifies the float rounding of r^2 seven-fold.
+// LJ + truncation (lennard_jones_kernel.hpp:44-56, truncations/*_kernel.cuh).
+// Compensated LJ: the squared distance arrives as a (hi, lo) pair, the
+// reciprocal is refined by one Newton step against rr_hi + rr_lo, and fval
+// gets the first-order term d fval / d rri * rri_lo; the steep r^-14 law
+// would otherwise amplify the float rounding of r^2 seven-fold.  The
+// smoothing factors (smooth_r4) and the force shift use approximate
+// reciprocal / square-root intrinsics: their errors scale forces that are
+// already small near r_c.
 template <int TR>
-__device__ __forceinline__ void pair_eval_precise(const PairParam& p, float rr, float rrl, float rri_smooth,
-                                                  float& fval, float& en)
+__device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rrl, float rri_smooth,
+                                          float& fval, float& en)
 {
     float y;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(rr));
@@ -204,52 +182,60 @@ __device__ __forceinline__ void pair_eval_precise(const PairParam& p, float rr, 
     fval = __fmaf_rn(p.c48 * ri6 * __fmaf_rn(7.0f, ri6, -2.0f), rril, fval);
     en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
     if (TR == TRUNC_SMOOTH_R4) {
-        const float r = __fsqrt_rn(rr);
+        const float rinv = rsqrtf(rr);
+        const float r = rr * rinv;
         const float dr = r - p.r_cut;
         const float x2 = dr * dr * rri_smooth;
         const float x4 = x2 * x2;
-        const float x4i = __fdiv_rn(1.0f, 1.0f + x4);
+        const float x4i = __fdividef(1.0f, 1.0f + x4);
         const float h0 = x4 * x4i;
         const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
-        fval = h0 * fval - h1 * __fdiv_rn(en, r);
+        fval = h0 * fval - h1 * (en * rinv);
         en = h0 * en;
     } else if (TR == TRUNC_FORCE_SHIFTED) {
-        const float r = __fsqrt_rn(rr);
-        fval = fval - __fdiv_rn(p.f_cut, r);
-        en = en + (r - p.r_cut) * p.f_cut;
+        const float rinv = rsqrtf(rr);
+        fval = fval - p.f_cut * rinv;
+        en = en + (rr * rinv - p.r_cut) * p.f_cut;
     }
 }
 
-template <int TR, bool AUX>
-__device__ __forceinline__ void force_particle(const Dev& d, uint32_t i, const SysParam& P, const PairParam* spp,
-                                               float4 ri, uint32_t a)
+struct ForceAcc {
+    float fx = 0, fy = 0, fz = 0, cx = 0, cy = 0, cz = 0;
+    float en = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
+};
+
+// W lanes per particle; lane q takes list entries q, q+W, ...  The list is
+// stored lane-blocked: entry k of slot i at ((k/W)*S + i)*W + k%W, so a warp
+// reads 128 contiguous bytes per load.  WRAP = false when no particle of the
+// warp can see a neighbour across the box: then rint(s/L) = 0 for every pair
+// and the minimum-image arithmetic is skipped without changing any result.
+template <int W, int TR, bool AUX, bool WRAP>
+__device__ __forceinline__ void force_loop(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
+                                           const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
 {
-    const uint32_t cnt = d.nbr_count[i];
-    const uint32_t* lst = d.nbr + i;
-    const size_t stride = d.S;
+    const uint32_t* lst = d.nbr + (size_t)i * W + q;
+    const size_t bstride = (size_t)d.S * W;
     const uint32_t ns = P.ns;
     const float Lx = P.L[0], Ly = P.L[1], Lz = P.L[2];
     const float Ix = P.Linv[0], Iy = P.Linv[1], Iz = P.Linv[2];
     const float rri_smooth = P.rri_smooth;
-    float fx = 0, fy = 0, fz = 0, cx = 0, cy = 0, cz = 0;
-    float en = 0;
-    float s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
-#pragma unroll 4
-    for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t j = __ldg(lst + k * stride);
+    const PairParam* row = spp + a * ns;
+#pragma unroll 2
+    for (uint32_t k = q; k < cnt; k += W, lst += bstride) {
+        const uint32_t j = __ldg(lst);
         const float4 rj = __ldg(d.pos + j);
         const uint32_t b = species_bits(rj.w);
         const float sx = __fsub_rn(ri.x, rj.x);
         const float sy = __fsub_rn(ri.y, rj.y);
         const float sz = __fsub_rn(ri.z, rj.z);
-        const float dx = min_image(sx, Lx, Ix);
-        const float dy = min_image(sy, Ly, Iy);
-        const float dz = min_image(sz, Lz, Iz);
+        const float dx = WRAP ? min_image(sx, Lx, Ix) : sx;
+        const float dy = WRAP ? min_image(sy, Ly, Iy) : sy;
+        const float dz = WRAP ? min_image(sz, Lz, Iz) : sz;
         const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
         const float pxy = __fadd_rn(px, py);
         const float rr = __fadd_rn(pxy, pz);   // == rr_exact(dx, dy, dz)
         if (b >= ns) continue;   // lists hold real particles only; keep the table lookup in bounds
-        const PairParam& p = spp[a * ns + b];
+        const PairParam& p = row[b];
         if (!(rr < p.rr_cut)) continue;
         // dx - k L is exact (k = 0, or Sterbenz for k = +-1): the difference
         // error is the TwoSum error of ri - rj
@@ -260,56 +246,104 @@ __device__ __forceinline__ void force_particle(const Dev& d, uint32_t i, const S
         rrl = __fadd_rn(rrl, __fadd_rn(two_sum_err(px, py, pxy), two_sum_err(pxy, pz, rr)));
         rrl = __fmaf_rn(2.0f * dx, dxl, __fmaf_rn(2.0f * dy, dyl, __fmaf_rn(2.0f * dz, dzl, rrl)));
         float fval, e;
-        pair_eval_precise<TR>(p, rr, rrl, rri_smooth, fval, e);
+        pair_eval<TR>(p, rr, rrl, rri_smooth, fval, e);
         const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
-        two_sum_acc(fx, cx, tx);
-        two_sum_acc(fy, cy, ty);
-        two_sum_acc(fz, cz, tz);
-        cx = __fmaf_rn(fval, dxl, __fadd_rn(cx, __fmaf_rn(fval, dx, -tx)));
-        cy = __fmaf_rn(fval, dyl, __fadd_rn(cy, __fmaf_rn(fval, dy, -ty)));
-        cz = __fmaf_rn(fval, dzl, __fadd_rn(cz, __fmaf_rn(fval, dz, -tz)));
+        two_sum_acc(A.fx, A.cx, tx);
+        two_sum_acc(A.fy, A.cy, ty);
+        two_sum_acc(A.fz, A.cz, tz);
+        A.cx = __fmaf_rn(fval, dxl, __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx)));
+        A.cy = __fmaf_rn(fval, dyl, __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty)));
+        A.cz = __fmaf_rn(fval, dzl, __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz)));
         if (AUX) {
-            en += e;
-            s0 += fval * dx * dx;
-            s1 += fval * dy * dy;
-            s2 += fval * dz * dz;
-            s3 += fval * dx * dy;
-            s4 += fval * dx * dz;
-            s5 += fval * dy * dz;
+            A.en += e;
+            A.s0 += fval * dx * dx;
+            A.s1 += fval * dy * dy;
+            A.s2 += fval * dz * dz;
+            A.s3 += fval * dx * dy;
+            A.s4 += fval * dx * dz;
+            A.s5 += fval * dy * dz;
         }
-    }
-    d.force[i] = make_float4(fx + cx, fy + cy, fz + cz, 0.0f);
-    if (AUX) {
-        d.en_pot[i] = 0.5f * en;
-        float* sp = d.stress + i;
-        sp[0 * stride] = 0.5f * s0;
-        sp[1 * stride] = 0.5f * s1;
-        sp[2 * stride] = 0.5f * s2;
-        sp[3 * stride] = 0.5f * s3;
-        sp[4 * stride] = 0.5f * s4;
-        sp[5 * stride] = 0.5f * s5;
     }
 }
 
-template <bool AUX>
+template <int W, int TR, bool AUX>
+__device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, bool wrap,
+                                               const SysParam& P, const PairParam* spp, float4 ri, uint32_t a,
+                                               ForceAcc& A)
+{
+    if (wrap) force_loop<W, TR, AUX, true>(d, i, q, cnt, P, spp, ri, a, A);
+    else force_loop<W, TR, AUX, false>(d, i, q, cnt, P, spp, ri, a, A);
+}
+
+// merge the compensated sums of the W lanes of a particle (fixed tree: deterministic)
+template <int W>
+__device__ __forceinline__ void lane_merge(float& s, float& c)
+{
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xFFFFFFFFu, s, o, W);
+        const float c2 = __shfl_xor_sync(0xFFFFFFFFu, c, o, W);
+        const float t = __fadd_rn(s, s2);
+        c = __fadd_rn(__fadd_rn(c, c2), two_sum_err(s, s2, t));
+        s = t;
+    }
+}
+
+template <int W>
+__device__ __forceinline__ float lane_sum(float v)
+{
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o, W);
+    return v;
+}
+
+template <int W, bool AUX>
 __global__ void __launch_bounds__(128) k_force(Dev d)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = t / W, q = t % W;
+    const uint32_t s = d.chunk_sys[(blockIdx.x * (blockDim.x / W)) / CHUNK];
     const SysParam& P = d.sys[s];
     __shared__ PairParam spp[MAX_SPECIES * MAX_SPECIES];
     const uint32_t np = P.ns * P.ns;
     if (threadIdx.x < np) spp[threadIdx.x] = d.pair[P.pair_off + threadIdx.x];
     __syncthreads();
-    if (!P.active || !d.st[s].live || *d.status != 0u) return;
+    if (!P.active || !d.st[s].live || *d.status != 0u) return;   // block-uniform
     const float4 ri = d.pos[i];
     const uint32_t a = species_bits(ri.w);
-    if (a == PLACEHOLDER) return;
-    switch (P.trunc) {
-    case TRUNC_SHARP:
-    case TRUNC_SHIFTED: force_particle<TRUNC_SHIFTED, AUX>(d, i, P, spp, ri, a); break;
-    case TRUNC_SMOOTH_R4: force_particle<TRUNC_SMOOTH_R4, AUX>(d, i, P, spp, ri, a); break;
-    default: force_particle<TRUNC_FORCE_SHIFTED, AUX>(d, i, P, spp, ri, a); break;
+    const bool real = a != PLACEHOLDER;
+    const uint32_t cnt = real ? d.nbr_count[i] : 0u;
+    const bool inner = !real || (fabsf(ri.x) < P.inner[0] && fabsf(ri.y) < P.inner[1] && fabsf(ri.z) < P.inner[2]);
+    const bool wrap = __any_sync(0xFFFFFFFFu, !inner);
+    ForceAcc A;
+    if (real) {
+        switch (P.trunc) {
+        case TRUNC_SHARP:
+        case TRUNC_SHIFTED: force_dispatch<W, TRUNC_SHIFTED, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A); break;
+        case TRUNC_SMOOTH_R4: force_dispatch<W, TRUNC_SMOOTH_R4, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A); break;
+        default: force_dispatch<W, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A); break;
+        }
+    }
+    lane_merge<W>(A.fx, A.cx);
+    lane_merge<W>(A.fy, A.cy);
+    lane_merge<W>(A.fz, A.cz);
+    if (AUX) {
+        A.en = lane_sum<W>(A.en);
+        A.s0 = lane_sum<W>(A.s0); A.s1 = lane_sum<W>(A.s1); A.s2 = lane_sum<W>(A.s2);
+        A.s3 = lane_sum<W>(A.s3); A.s4 = lane_sum<W>(A.s4); A.s5 = lane_sum<W>(A.s5);
+    }
+    if (!real || q != 0) return;
+    d.force[i] = make_float4(A.fx + A.cx, A.fy + A.cy, A.fz + A.cz, 0.0f);
+    if (AUX) {
+        const size_t stride = d.S;
+        d.en_pot[i] = 0.5f * A.en;
+        float* sp = d.stress + i;
+        sp[0 * stride] = 0.5f * A.s0;
+        sp[1 * stride] = 0.5f * A.s1;
+        sp[2 * stride] = 0.5f * A.s2;
+        sp[3 * stride] = 0.5f * A.s3;
+        sp[4 * stride] = 0.5f * A.s4;
+        sp[5 * stride] = 0.5f * A.s5;
     }
 }
 
@@ -458,11 +492,22 @@ void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st)
     k_mark<<<(d.nsys + 255) / 256, 256, 0, st>>>(d, rebuild_all ? 1 : 0);
 }
 
+template <int W>
+static void launch_force_w(const Dev& d, bool aux, cudaStream_t st)
+{
+    const unsigned grid = (unsigned)((size_t)d.S * W / 128);
+    if (aux) k_force<W, true><<<grid, 128, 0, st>>>(d);
+    else k_force<W, false><<<grid, 128, 0, st>>>(d);
+}
+
 void launch_force(const Dev& d, bool aux, cudaStream_t st)
 {
-    const unsigned grid = d.S / 128;
-    if (aux) k_force<true><<<grid, 128, 0, st>>>(d);
-    else k_force<false><<<grid, 128, 0, st>>>(d);
+    switch (d.lanes) {
+    case 1: launch_force_w<1>(d, aux, st); break;
+    case 2: launch_force_w<2>(d, aux, st); break;
+    case 4: launch_force_w<4>(d, aux, st); break;
+    default: launch_force_w<8>(d, aux, st); break;
+    }
 }
 
 void launch_finalize(const Dev& d, bool ds, cudaStream_t st)

@@ -1,0 +1,74 @@
+"""Autotuner for the engine's launch shapes.
+
+Picks the force kernel's lanes per particle (1, 2, 4 or 8 threads share one
+particle's neighbour list) by timing the force kernel on the engine's own
+systems with CUDA events (the engine's per-phase profiler).  Results are
+cached as JSON keyed by (GPU name, slots bucket, mean list length bucket)
+so a later engine of similar size reuses the choice without timing.
+"""
+import json
+import math
+import os
+
+CACHE = os.environ.get("HMD_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "halmd_gb300_tune.json"))
+CHOICES = (1, 2, 4, 8)
+
+
+def _gpu_name():
+    try:
+        import torch
+        return torch.cuda.get_device_name()
+    except Exception:
+        return "unknown"
+
+
+def _key(engine):
+    slots = sum(engine.info(s).slots for s in range(len(engine.systems)))
+    cap = engine.get_option("neighbour_capacity")
+    return "%s|slots2^%d|cap%d" % (_gpu_name(), int(round(math.log2(max(slots, 1)))), cap // 16 * 16)
+
+
+def _load():
+    try:
+        with open(CACHE) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(db):
+    try:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        with open(CACHE, "w") as fh:
+            json.dump(db, fh, indent=1)
+    except OSError:
+        pass
+
+
+def autotune_force_lanes(engine, repeats=10, use_cache=True):
+    """Time the force kernel for every lane count; keep the fastest.
+
+    Returns (lanes, {lanes: ms per launch}).  The engine must be committed and
+    hold a representative state (positions set)."""
+    key = _key(engine)
+    db = _load() if use_cache else {}
+    if use_cache and key in db:
+        engine.set_option("force_lanes", db[key]["lanes"])
+        return db[key]["lanes"], db[key]["ms"]
+    timings = {}
+    for w in CHOICES:
+        engine.set_option("force_lanes", w)
+        engine.force()            # rebuilds the lists in this layout
+        engine.profile(True)
+        for _ in range(repeats):
+            engine.force()
+        ms, n = engine.profile_get("force")
+        engine.profile(False)
+        timings[w] = ms / max(n, 1)
+    best = min(timings, key=timings.get)
+    engine.set_option("force_lanes", best)
+    engine.force()
+    if use_cache:
+        db[key] = {"lanes": best, "ms": {str(k): v for k, v in timings.items()}}
+        _store(db)
+    return best, timings

@@ -120,6 +120,14 @@ HMD_API int hmd_engine_destroy(hmd_engine* engine);
 HMD_API int hmd_engine_add_system(hmd_engine* engine, const hmd_system_desc* desc, uint32_t* index);
 /* lay out and allocate all device arrays (particle.cpp:56-160 ctor) */
 HMD_API int hmd_engine_commit(hmd_engine* engine);
+/*
+ * Tuning options (autotuned or set by the caller):
+ *   "force_lanes"   threads per particle in the force kernel: 0 (auto), 1, 2, 4, 8
+ *                   (the reference's unroll_force_loop, neighbour.lua.in:98-101, is 32)
+ *   "neighbour_capacity" (get only) list slots per particle
+ */
+HMD_API int hmd_engine_set_option(hmd_engine* engine, const char* name, int64_t value);
+HMD_API int hmd_engine_get_option(hmd_engine* engine, const char* name, int64_t* value);
 /* CUDA stream all work of the engine is issued on (cudaStream_t) */
 HMD_API int hmd_engine_stream(hmd_engine* engine, void** stream);
 HMD_API int hmd_info(hmd_engine* engine, uint32_t sys, hmd_system_info* info);

@@ -81,6 +81,27 @@ def test_lj_force_parity(precision):
     eng.close()
 
 
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+def test_force_lanes_agree(lanes):
+    eng, r, v, L = lj_engine(ncell=7)
+    eng.set_option("force_lanes", lanes)
+    eng.force()
+    assert eng.get_option("force_lanes") == lanes
+    f = eng.get("force")
+    pot = oracle.Potential(1.0, 1.0, 2.5, "shifted")
+    ref, _ = oracle_forces(eng, np.zeros(r.shape[0]), pot)
+    emax, _ = rel_force_error(f, ref["force"])
+    assert emax < FORCE_TOL
+    counts, lists = eng.neighbour_lists()
+    inf = eng.info()
+    rc, rl, _ = oracle.neighbour_full_f32(tag_order(eng, eng.get_raw("r0")), np.array(inf.box_f32),
+                                         np.array(inf.rr_cut_skin[:1], dtype=np.float32), inf.neighbour_capacity)
+    assert np.array_equal(counts, rc) and np.array_equal(lists, rl)
+    eng.step(5)
+    assert np.all(np.isfinite(eng.get("position")))
+    eng.close()
+
+
 def test_ka_smooth_r4_force_parity():
     eng, r, v, sp, L = ka_engine()
     eng.force(aux=True)
