@@ -198,6 +198,33 @@ def run_reference(args, w):
     print(json.dumps(line))
 
 
+def run_phases(args, w):
+    """Per-phase breakdown of the MD step through the module-level calls."""
+    r, v, species, L = initial_state(w)
+    eng = make_engine(w, L)
+    eng.set("species", species)
+    eng.set("position", r)
+    eng.set("velocity", v)
+    eng.step(50)
+    for _ in range(5):
+        eng.integrate(); eng.force(); eng.finalize()
+    inf0 = eng.info()
+    eng.profile(True)
+    for _ in range(args.phases):
+        eng.integrate()
+        eng.force()
+        eng.finalize()
+    inf1 = eng.info()
+    out = {"workload": w["name"], "n": w["n"], "md_steps": args.phases,
+           "rebuilds": int(inf1.rebuilds - inf0.rebuilds), "force_lanes": eng.get_option("force_lanes")}
+    for ph in ("integrate", "rebuild", "force", "finalize"):
+        ms, cnt = eng.profile_get(ph)
+        out[ph + "_ms_per_call"] = ms / max(cnt, 1)
+        out[ph + "_ms_per_step"] = ms / max(args.phases, 1)
+    print(json.dumps(out))
+    eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -208,8 +235,14 @@ def main():
     ap.add_argument("--md-steps", type=int, default=100, help="MD steps per bench step")
     ap.add_argument("--ref-steps", type=int, default=2, help="MD steps per bench step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--phases", type=int, default=0,
+                    help="run N MD steps through the module calls (integrate / force / finalize, one launch "
+                         "each, no graph) with the per-phase CUDA-event timers, print the breakdown and exit; "
+                         "this is the run profilers can attribute kernel by kernel")
     args = ap.parse_args()
     w = workload(args.workload)
+    if args.phases:
+        return run_phases(args, w)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

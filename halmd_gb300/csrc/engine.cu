@@ -920,10 +920,22 @@ void Engine::force(bool aux)
 {
     check_committed();
     const Dev d = dev();
-    if (!integrated_) launch_mark(d, false, stream_);
-    tic();
-    rebuild_chain(stream_);
-    toc("rebuild");
+    bool need = true;
+    if (!integrated_) {
+        launch_mark(d, false, stream_);
+    } else {
+        // the integrate kernel's last block decided on the device; one word
+        // comes back (the reference reads its displacement maxima every step,
+        // max_displacement.cpp:96)
+        uint32_t any = 0;
+        download(any_rebuild_, 0, 1, &any);
+        need = any != 0;
+    }
+    if (need) {
+        tic();
+        rebuild_chain(stream_);
+        toc("rebuild");
+    }
     tic();
     launch_force(d, aux, stream_);
     HMD_CUDA(cudaGetLastError());

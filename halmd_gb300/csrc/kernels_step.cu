@@ -159,6 +159,12 @@ __device__ __forceinline__ float two_sum_err(float a, float b, float s)
     return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
 }
 
+// error of s = fl(a + b) for a, b >= 0 (Dekker's Fast2Sum on the ordered pair)
+__device__ __forceinline__ float fast_err_pos(float a, float b, float s)
+{
+    return __fsub_rn(fminf(a, b), __fsub_rn(s, fmaxf(a, b)));
+}
+
 // LJ + truncation (lennard_jones_kernel.hpp:44-56, truncations/*_kernel.cuh).
 // Compensated LJ: the squared distance arrives as a (hi, lo) pair, the
 // reciprocal is refined by one Newton step against rr_hi + rr_lo, and fval
@@ -209,10 +215,15 @@ struct ForceAcc {
 // reads 128 contiguous bytes per load.  WRAP = false when no particle of the
 // warp can see a neighbour across the box: then rint(s/L) = 0 for every pair
 // and the minimum-image arithmetic is skipped without changing any result.
-template <int W, int TR, bool AUX, bool WRAP>
+// TR >= ONE_SPECIES: single-species system, the pair table has one entry
+constexpr int ONE_SPECIES = 16;
+
+template <int W, int TRX, bool AUX, bool WRAP>
 __device__ __forceinline__ void force_loop(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
                                            const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
 {
+    constexpr bool NS1 = TRX >= ONE_SPECIES;
+    constexpr int TR = TRX & (ONE_SPECIES - 1);
     const uint32_t* lst = d.nbr + (size_t)i * W + q;
     const size_t bstride = (size_t)d.S * W;
     const uint32_t ns = P.ns;
@@ -220,11 +231,12 @@ __device__ __forceinline__ void force_loop(const Dev& d, uint32_t i, uint32_t q,
     const float Ix = P.Linv[0], Iy = P.Linv[1], Iz = P.Linv[2];
     const float rri_smooth = P.rri_smooth;
     const PairParam* row = spp + a * ns;
+    PairParam p1;
+    if (NS1) p1 = spp[0];
 #pragma unroll 2
     for (uint32_t k = q; k < cnt; k += W, lst += bstride) {
         const uint32_t j = __ldg(lst);
         const float4 rj = __ldg(d.pos + j);
-        const uint32_t b = species_bits(rj.w);
         const float sx = __fsub_rn(ri.x, rj.x);
         const float sy = __fsub_rn(ri.y, rj.y);
         const float sz = __fsub_rn(ri.z, rj.z);
@@ -234,8 +246,15 @@ __device__ __forceinline__ void force_loop(const Dev& d, uint32_t i, uint32_t q,
         const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
         const float pxy = __fadd_rn(px, py);
         const float rr = __fadd_rn(pxy, pz);   // == rr_exact(dx, dy, dz)
-        if (b >= ns) continue;   // lists hold real particles only; keep the table lookup in bounds
-        const PairParam& p = row[b];
+        const PairParam* pp;
+        if (NS1) {
+            pp = &p1;
+        } else {
+            const uint32_t b = species_bits(rj.w);
+            if (b >= ns) continue;   // lists hold real particles only; keep the table lookup in bounds
+            pp = row + b;
+        }
+        const PairParam& p = *pp;
         if (!(rr < p.rr_cut)) continue;
         // dx - k L is exact (k = 0, or Sterbenz for k = +-1): the difference
         // error is the TwoSum error of ri - rj
@@ -243,8 +262,8 @@ __device__ __forceinline__ void force_loop(const Dev& d, uint32_t i, uint32_t q,
         const float dyl = two_sum_err(ri.y, -rj.y, sy);
         const float dzl = two_sum_err(ri.z, -rj.z, sz);
         float rrl = __fadd_rn(__fadd_rn(__fmaf_rn(dx, dx, -px), __fmaf_rn(dy, dy, -py)), __fmaf_rn(dz, dz, -pz));
-        rrl = __fadd_rn(rrl, __fadd_rn(two_sum_err(px, py, pxy), two_sum_err(pxy, pz, rr)));
-        rrl = __fmaf_rn(2.0f * dx, dxl, __fmaf_rn(2.0f * dy, dyl, __fmaf_rn(2.0f * dz, dzl, rrl)));
+        rrl = __fadd_rn(rrl, __fadd_rn(fast_err_pos(px, py, pxy), fast_err_pos(pxy, pz, rr)));
+        rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
         float fval, e;
         pair_eval<TR>(p, rr, rrl, rri_smooth, fval, e);
         const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
@@ -319,7 +338,10 @@ __global__ void __launch_bounds__(128) k_force(Dev d)
     if (real) {
         switch (P.trunc) {
         case TRUNC_SHARP:
-        case TRUNC_SHIFTED: force_dispatch<W, TRUNC_SHIFTED, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A); break;
+        case TRUNC_SHIFTED:
+            if (P.ns == 1) force_dispatch<W, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A);
+            else force_dispatch<W, TRUNC_SHIFTED, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A);
+            break;
         case TRUNC_SMOOTH_R4: force_dispatch<W, TRUNC_SMOOTH_R4, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A); break;
         default: force_dispatch<W, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A); break;
         }
