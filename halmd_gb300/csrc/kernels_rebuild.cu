@@ -111,28 +111,44 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_hist(const uint32_t* ke
     hist[threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// exclusive scan of hist[0 .. 256*ntiles) by one block of 1024 threads
+// exclusive scan of hist[0 .. 256*ntiles) by one block of 1024 threads: each
+// warp owns a contiguous chunk, reads it lane-strided (coalesced) once to
+// total it and once more to scan it with warp shuffles and a running carry
 __global__ void __launch_bounds__(1024) k_radix_scan(uint32_t* hist, uint32_t total)
 {
-    __shared__ uint32_t part[1024];
-    const uint32_t per = (total + blockDim.x - 1) / blockDim.x;
-    const uint32_t b = threadIdx.x * per;
-    const uint32_t e = min(b + per, total);
+    __shared__ uint32_t s_warp[32];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t chunk = (total + nw - 1) / nw;
+    const uint32_t b = min(warp * chunk, total), e = min(b + chunk, total);
     uint32_t sum = 0;
-    for (uint32_t k = b; k < e; ++k) sum += hist[k];
-    part[threadIdx.x] = sum;
+    for (uint32_t k = b + lane; k < e; k += 32) sum += hist[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, o);
+    if (lane == 0) s_warp[warp] = sum;
     __syncthreads();
-    for (uint32_t o = 1; o < blockDim.x; o <<= 1) {
-        uint32_t v = (threadIdx.x >= o) ? part[threadIdx.x - o] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
+    if (warp == 0) {
+        const uint32_t v = lane < nw ? s_warp[lane] : 0u;
+        uint32_t incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += t;
+        }
+        if (lane < nw) s_warp[lane] = incl - v;
     }
-    uint32_t run = part[threadIdx.x] - sum;
-    for (uint32_t k = b; k < e; ++k) {
-        const uint32_t v = hist[k];
-        hist[k] = run;
-        run += v;
+    __syncthreads();
+    uint32_t carry = s_warp[warp];
+    for (uint32_t k0 = b; k0 < e; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        const uint32_t v = (k < e) ? hist[k] : 0u;
+        uint32_t incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += t;
+        }
+        if (k < e) hist[k] = carry + incl - v;
+        carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
 }
 
@@ -348,20 +364,32 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
                 const int y = (cy + oy + ny) % ny;
                 for (int ox = lox; ox <= hix; ++ox) {
                     const int x = (cx + ox + nx) % nx;
-                    const uint32_t* cell = d.cell + P.cell_word_off + ((uint32_t)(z * ny + y) * nx + x) * cs;
-                    for (uint32_t k = 0; k < cs; ++k) {
-                        const uint32_t j = __ldg(cell + k);
-                        if (j == PLACEHOLDER) break;
-                        if (j == i) continue;
-                        const float4 rj = __ldg(d.pos + j);
-                        const float dx = min_image(__fsub_rn(ri.x, rj.x), P.L[0], P.Linv[0]);
-                        const float dy = min_image(__fsub_rn(ri.y, rj.y), P.L[1], P.Linv[1]);
-                        const float dz = min_image(__fsub_rn(ri.z, rj.z), P.L[2], P.Linv[2]);
-                        const float rr = rr_exact(dx, dy, dz);
-                        const uint32_t b = species_bits(rj.w);
-                        if (b < P.ns && rr <= rrcs[b]) {
-                            if (count < cap) out[(count >> lw) * bstride + (count & lmask)] = j;
-                            ++count;
+                    const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
+                    // occupied slots of the cell (ascending); read four at a time
+                    // so the position gathers are independent of one another
+                    const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
+                    const uint4* cell4 = reinterpret_cast<const uint4*>(d.cell + P.cell_word_off + c * cs);
+                    for (uint32_t k = 0; k < nc; k += 4) {
+                        const uint4 jj = __ldg(cell4 + (k >> 2));
+                        const uint32_t jv[4] = {jj.x, jj.y, jj.z, jj.w};
+                        float4 rv[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            rv[u] = (k + u < nc) ? __ldg(d.pos + jv[u]) : make_float4(0, 0, 0, 0);
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const uint32_t j = jv[u];
+                            if (k + u >= nc || j == i) continue;
+                            const float4 rj = rv[u];
+                            const float dx = min_image(__fsub_rn(ri.x, rj.x), P.L[0], P.Linv[0]);
+                            const float dy = min_image(__fsub_rn(ri.y, rj.y), P.L[1], P.Linv[1]);
+                            const float dz = min_image(__fsub_rn(ri.z, rj.z), P.L[2], P.Linv[2]);
+                            const float rr = rr_exact(dx, dy, dz);
+                            const uint32_t b = species_bits(rj.w);
+                            if (b < P.ns && rr <= rrcs[b]) {
+                                if (count < cap) out[(count >> lw) * bstride + (count & lmask)] = j;
+                                ++count;
+                            }
                         }
                     }
                 }

@@ -57,18 +57,24 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d, cudaGraphConditionalHa
         if (species_bits(r.w) != PLACEHOLDER) {
             float4 v = d.vel[i];
             const float4 f = d.force[i];
-            float4 im = d.img[i];
-            const float4 im_old = im;
+            float4 k = make_float4(0, 0, 0, 0);   // box images crossed in this step
             float4 rl = make_float4(0, 0, 0, 0), vl = make_float4(0, 0, 0, 0);
             if (DS) { rl = d.pos[d.S + i]; vl = d.vel[d.S + i]; }
             const float m = v.w;
-            integrate_component<DS>(r.x, rl.x, v.x, vl.x, im.x, f.x, m, P.dt, P.dt_half, P.L[0], P.Linv[0]);
-            integrate_component<DS>(r.y, rl.y, v.y, vl.y, im.y, f.y, m, P.dt, P.dt_half, P.L[1], P.Linv[1]);
-            integrate_component<DS>(r.z, rl.z, v.z, vl.z, im.z, f.z, m, P.dt, P.dt_half, P.L[2], P.Linv[2]);
+            integrate_component<DS>(r.x, rl.x, v.x, vl.x, k.x, f.x, m, P.dt, P.dt_half, P.L[0], P.Linv[0]);
+            integrate_component<DS>(r.y, rl.y, v.y, vl.y, k.y, f.y, m, P.dt, P.dt_half, P.L[1], P.Linv[1]);
+            integrate_component<DS>(r.z, rl.z, v.z, vl.z, k.z, f.z, m, P.dt, P.dt_half, P.L[2], P.Linv[2]);
             d.pos[i] = r;
             d.vel[i] = v;
             if (DS) { d.pos[d.S + i] = rl; d.vel[d.S + i] = vl; }
-            if (im.x != im_old.x || im.y != im_old.y || im.z != im_old.z) d.img[i] = im;
+            if (k.x != 0.0f || k.y != 0.0f || k.z != 0.0f) {
+                // image counters are read and written only on a wrap
+                float4 im = d.img[i];
+                im.x = __fadd_rn(im.x, k.x);
+                im.y = __fadd_rn(im.y, k.y);
+                im.z = __fadd_rn(im.z, k.z);
+                d.img[i] = im;
+            }
             const float4 q = d.r0[i];
             float dx = min_image(__fsub_rn(r.x, q.x), P.L[0], P.Linv[0]);
             float dy = min_image(__fsub_rn(r.y, q.y), P.L[1], P.Linv[1]);
