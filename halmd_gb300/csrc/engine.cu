@@ -137,6 +137,8 @@ void Engine::layout_system(SysHost& h, uint32_t rank)
         p.rr_cut_skin = (float)(rcs * rcs);
         p.en_cut = (d.truncation == HMD_TRUNC_SHARP) ? 0.0f : (float)ec;
         p.f_cut = (d.truncation == HMD_TRUNC_FORCE_SHIFTED) ? (float)(fc * rc) : 0.0f;
+        p.rr_near = (float)(NEAR_SIGMA * NEAR_SIGMA * sigma2);
+        p.pad[0] = p.pad[1] = p.pad[2] = 0.0f;
         rc_max = std::max(rc_max, rc);
         rcs_max = std::max(rcs_max, rcs);
     }
@@ -1006,9 +1008,11 @@ void Engine::neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint
     std::vector<uint32_t> cnt(P.A), id(P.A);
     download(nbr_count_, P.off, P.A, cnt.data());
     download(id_, P.off, P.A, id.data());
+    // counts are packed (near | far << 16): near entries from the front of a
+    // list, far entries from its back
     for (uint32_t t = 0; t < P.n; ++t) {
         const uint32_t k = slot[t] - P.off;
-        if (cnt[k] > maxn) throw Error(HMD_ERR_INVALID, "maxn smaller than a neighbour count");
+        if ((cnt[k] & 0xFFFFu) + (cnt[k] >> 16) > maxn) throw Error(HMD_ERR_INVALID, "maxn smaller than a neighbour count");
     }
     // lane-blocked layout: block b holds entries [b*W, b*W + W) of every slot
     const uint32_t W = lanes_;
@@ -1018,12 +1022,15 @@ void Engine::neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint
         download(nbr_, ((size_t)b * S_ + P.off) * W, (size_t)P.A * W, all.data() + (size_t)b * P.A * W);
     for (uint32_t t = 0; t < P.n; ++t) {
         const uint32_t k = slot[t] - P.off;
-        counts[t] = cnt[k];
-        std::vector<uint32_t> v(cnt[k]);
-        for (uint32_t q = 0; q < cnt[k]; ++q)
-            v[q] = id[all[((size_t)(q / W) * P.A + k) * W + q % W] - P.off];
+        const uint32_t nn = cnt[k] & 0xFFFFu, nf = cnt[k] >> 16;
+        counts[t] = nn + nf;
+        std::vector<uint32_t> v(nn + nf);
+        for (uint32_t q = 0; q < nn + nf; ++q) {
+            const uint32_t e = q < nn ? q : nbr_cap_ - 1u - (q - nn);
+            v[q] = id[all[((size_t)(e / W) * P.A + k) * W + e % W] - P.off];
+        }
         std::sort(v.begin(), v.end());
-        for (uint32_t q = 0; q < maxn; ++q) lists[(size_t)t * maxn + q] = q < cnt[k] ? v[q] : PLACEHOLDER;
+        for (uint32_t q = 0; q < maxn; ++q) lists[(size_t)t * maxn + q] = q < counts[t] ? v[q] : PLACEHOLDER;
     }
 }
 

@@ -45,7 +45,14 @@ struct PairParam {
     float r_cut;
     float rr_cut_skin; // (float)((r_c + skin)^2)
     float f_cut;       // force_shifted: F_c = fval(r_c) r_c
+    float rr_near;     // (float)((NEAR_SIGMA sigma)^2): list pairs closer at build time get the compensated path
+    float pad[3];
 };
+
+// pairs closer than NEAR_SIGMA sigma at list build time are evaluated with
+// the compensated arithmetic; the rest (|F| below ~2 eps / sigma even after
+// closing in by the skin) in plain FP32
+constexpr double NEAR_SIGMA = 1.5;
 
 struct SysParam {
     uint32_t off, n, A;        // slot range and real particle count
@@ -98,7 +105,7 @@ struct Dev {
     uint32_t* id;              // [S] tag of the particle within its system
     uint32_t* rid;             // [S] slot of (off + tag)
     uint32_t* nbr;             // [nbr_cap * S], lane-blocked: entry k of slot i at ((k/lanes)*S + i)*lanes + k%lanes
-    uint32_t* nbr_count;       // [S]
+    uint32_t* nbr_count;       // [S] near count | far count << 16 (near entries from the front, far from the back)
     uint32_t nbr_cap;          // multiple of 8
     uint32_t lanes;            // threads per particle in the force kernel (1, 2, 4, 8)
     uint32_t lanes_log2;

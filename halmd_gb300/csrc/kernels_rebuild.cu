@@ -338,12 +338,17 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
     const uint32_t s = d.chunk_sys[i / CHUNK];
     const SysParam& P = d.sys[s];
     __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
-    if (threadIdx.x < P.ns * P.ns) s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
+    __shared__ float s_rrnear[MAX_SPECIES * MAX_SPECIES];
+    if (threadIdx.x < P.ns * P.ns) {
+        s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
+        s_rrnear[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_near;
+    }
     __syncthreads();
     if (!(P.active && d.st[s].rebuild)) return;   // block-uniform
     const float4 ri = d.pos[i];
     const uint32_t a = species_bits(ri.w);
     uint32_t count = 0;
+    uint32_t nn = 0, nf = 0;   // near entries from the front, far entries from the back
     if (a != PLACEHOLDER) {
         d.r0[i] = ri;
         int cx, cy, cz;
@@ -358,6 +363,7 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
         const size_t bstride = (size_t)d.S << lw;
         uint32_t* out = d.nbr + ((size_t)i << lw);
         const float* rrcs = s_rrcs + a * P.ns;
+        const float* rrnear = s_rrnear + a * P.ns;
         for (int oz = loz; oz <= hiz; ++oz) {
             const int z = (cz + oz + nz) % nz;
             for (int oy = loy; oy <= hiy; ++oy) {
@@ -387,15 +393,20 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
                             const float rr = rr_exact(dx, dy, dz);
                             const uint32_t b = species_bits(rj.w);
                             if (b < P.ns && rr <= rrcs[b]) {
-                                if (count < cap) out[(count >> lw) * bstride + (count & lmask)] = j;
-                                ++count;
+                                const bool near = rr < rrnear[b];
+                                const uint32_t e = near ? nn : cap - 1u - nf;
+                                if (nn + nf < cap) out[(e >> lw) * bstride + (e & lmask)] = j;
+                                if (near) ++nn; else ++nf;
                             }
                         }
                     }
                 }
             }
         }
-        d.nbr_count[i] = min(count, cap);
+        count = nn + nf;
+        const uint32_t sn = min(nn, cap);
+        const uint32_t sf = min(nf, cap - sn);   // stored regions never overlap
+        d.nbr_count[i] = sn | (sf << 16);
     }
     // warp-aggregated maximum and overflow flag (all lanes of the warp are here)
     uint32_t m = count;

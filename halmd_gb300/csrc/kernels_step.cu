@@ -211,8 +211,37 @@ __device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rr
     }
 }
 
+// plain FP32 evaluation for pairs that were farther than NEAR_SIGMA sigma at
+// list build time (forces of order eps / sigma or less)
+template <int TR>
+__device__ __forceinline__ void pair_eval_fast(const PairParam& p, float rr, float rri_smooth, float& fval, float& en)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(rr));
+    const float rri = p.sigma2 * y;
+    const float ri6 = rri * rri * rri;
+    fval = p.c48 * rri * ri6 * (ri6 - 0.5f);
+    en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
+    if (TR == TRUNC_SMOOTH_R4) {
+        const float rinv = rsqrtf(rr);
+        const float dr = rr * rinv - p.r_cut;
+        const float x2 = dr * dr * rri_smooth;
+        const float x4 = x2 * x2;
+        const float x4i = __fdividef(1.0f, 1.0f + x4);
+        const float h0 = x4 * x4i;
+        const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
+        fval = h0 * fval - h1 * (en * rinv);
+        en = h0 * en;
+    } else if (TR == TRUNC_FORCE_SHIFTED) {
+        const float rinv = rsqrtf(rr);
+        fval = fval - p.f_cut * rinv;
+        en = en + (rr * rinv - p.r_cut) * p.f_cut;
+    }
+}
+
 struct ForceAcc {
-    float fx = 0, fy = 0, fz = 0, cx = 0, cy = 0, cz = 0;
+    float fx = 0, fy = 0, fz = 0, cx = 0, cy = 0, cz = 0;   // compensated (near pairs)
+    float gx = 0, gy = 0, gz = 0;                           // plain sums (far pairs)
     float en = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
 };
 
@@ -291,13 +320,77 @@ __device__ __forceinline__ void force_loop(const Dev& d, uint32_t i, uint32_t q,
     }
 }
 
-template <int W, int TR, bool AUX>
-__device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, bool wrap,
-                                               const SysParam& P, const PairParam* spp, float4 ri, uint32_t a,
-                                               ForceAcc& A)
+// far part of the list: entry k at list position cap-1-k (stored from the
+// back), lane q walks its own lane column backwards
+template <int W, int TRX, bool AUX, bool WRAP>
+__device__ __forceinline__ void force_loop_far(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
+                                               const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
 {
-    if (wrap) force_loop<W, TR, AUX, true>(d, i, q, cnt, P, spp, ri, a, A);
-    else force_loop<W, TR, AUX, false>(d, i, q, cnt, P, spp, ri, a, A);
+    constexpr bool NS1 = TRX >= ONE_SPECIES;
+    constexpr int TR = TRX & (ONE_SPECIES - 1);
+    const size_t bstride = (size_t)d.S * W;
+    const uint32_t* lst = d.nbr + (size_t)(d.nbr_cap / W - 1) * bstride + (size_t)i * W + (W - 1 - q);
+    const uint32_t ns = P.ns;
+    const float Lx = P.L[0], Ly = P.L[1], Lz = P.L[2];
+    const float Ix = P.Linv[0], Iy = P.Linv[1], Iz = P.Linv[2];
+    const float rri_smooth = P.rri_smooth;
+    const PairParam* row = spp + a * ns;
+    PairParam p1;
+    if (NS1) p1 = spp[0];
+#pragma unroll 2
+    for (uint32_t k = q; k < cnt; k += W, lst -= bstride) {
+        const uint32_t j = __ldg(lst);
+        const float4 rj = __ldg(d.pos + j);
+        const float sx = __fsub_rn(ri.x, rj.x);
+        const float sy = __fsub_rn(ri.y, rj.y);
+        const float sz = __fsub_rn(ri.z, rj.z);
+        const float dx = WRAP ? min_image(sx, Lx, Ix) : sx;
+        const float dy = WRAP ? min_image(sy, Ly, Iy) : sy;
+        const float dz = WRAP ? min_image(sz, Lz, Iz) : sz;
+        const float rr = rr_exact(dx, dy, dz);
+        const PairParam* pp;
+        if (NS1) {
+            pp = &p1;
+        } else {
+            const uint32_t b = species_bits(rj.w);
+            if (b >= ns) continue;
+            pp = row + b;
+        }
+        const PairParam& p = *pp;
+        if (!(rr < p.rr_cut)) continue;
+        float fval, e;
+        pair_eval_fast<TR>(p, rr, rri_smooth, fval, e);
+        A.gx = __fmaf_rn(fval, dx, A.gx);
+        A.gy = __fmaf_rn(fval, dy, A.gy);
+        A.gz = __fmaf_rn(fval, dz, A.gz);
+        if (AUX) {
+            A.en += e;
+            A.s0 += fval * dx * dx;
+            A.s1 += fval * dy * dy;
+            A.s2 += fval * dz * dz;
+            A.s3 += fval * dx * dy;
+            A.s4 += fval * dx * dz;
+            A.s5 += fval * dy * dz;
+        }
+    }
+}
+
+template <int W, int TR, bool AUX>
+__device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf,
+                                               bool wrap, const SysParam& P, const PairParam* spp, float4 ri,
+                                               uint32_t a, ForceAcc& A)
+{
+    if (wrap) {
+        force_loop<W, TR, AUX, true>(d, i, q, nn, P, spp, ri, a, A);
+        force_loop_far<W, TR, AUX, true>(d, i, q, nf, P, spp, ri, a, A);
+    } else {
+        force_loop<W, TR, AUX, false>(d, i, q, nn, P, spp, ri, a, A);
+        force_loop_far<W, TR, AUX, false>(d, i, q, nf, P, spp, ri, a, A);
+    }
+    // fold the plain far-pair sums into the compensated accumulators
+    two_sum_acc(A.fx, A.cx, A.gx);
+    two_sum_acc(A.fy, A.cy, A.gy);
+    two_sum_acc(A.fz, A.cz, A.gz);
 }
 
 // merge the compensated sums of the W lanes of a particle (fixed tree: deterministic)
@@ -337,7 +430,8 @@ __global__ void __launch_bounds__(128) k_force(Dev d)
     const float4 ri = d.pos[i];
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;
-    const uint32_t cnt = real ? d.nbr_count[i] : 0u;
+    const uint32_t packed = real ? d.nbr_count[i] : 0u;
+    const uint32_t nn = packed & 0xFFFFu, nf = packed >> 16;   // near / far list parts
     const bool inner = !real || (fabsf(ri.x) < P.inner[0] && fabsf(ri.y) < P.inner[1] && fabsf(ri.z) < P.inner[2]);
     const bool wrap = __any_sync(0xFFFFFFFFu, !inner);
     ForceAcc A;
@@ -345,11 +439,11 @@ __global__ void __launch_bounds__(128) k_force(Dev d)
         switch (P.trunc) {
         case TRUNC_SHARP:
         case TRUNC_SHIFTED:
-            if (P.ns == 1) force_dispatch<W, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A);
-            else force_dispatch<W, TRUNC_SHIFTED, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A);
+            if (P.ns == 1) force_dispatch<W, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
+            else force_dispatch<W, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
             break;
-        case TRUNC_SMOOTH_R4: force_dispatch<W, TRUNC_SMOOTH_R4, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A); break;
-        default: force_dispatch<W, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, cnt, wrap, P, spp, ri, a, A); break;
+        case TRUNC_SMOOTH_R4: force_dispatch<W, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
+        default: force_dispatch<W, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
         }
     }
     lane_merge<W>(A.fx, A.cx);
