@@ -16,13 +16,6 @@ void cuda_check(cudaError_t e, const char* what)
     }
 }
 
-static uint32_t ceil_log2(uint64_t x)
-{
-    uint32_t b = 0;
-    while ((1ull << b) < x) ++b;
-    return b;
-}
-
 static uint32_t round_up(uint32_t x, uint32_t m) { return (x + m - 1) / m * m; }
 
 Engine::Engine(int precision, int device) : precision_(precision), device_(device)
@@ -216,21 +209,16 @@ void Engine::commit()
         total_cells_ += h.P.ncells;
         cell_words += h.P.ncells * h.P.cell_size;
         nbr_cap_ = std::max(nbr_cap_, round_up(h.nbr_size, 8));
-        shift = std::max(shift, std::max(3 * h.P.depth, ceil_log2(h.P.A)));
+        shift = std::max(shift, 3 * h.P.depth);
         any_sort_ = any_sort_ || h.P.sort_enable;
     }
-    const uint32_t rank_bits = ceil_log2(sys_.size());
-    if (shift + rank_bits > 32) {
-        // reduce the Hilbert depth of the deepest systems until the key fits
-        const uint32_t avail = 32 - rank_bits;
-        shift = 0;
-        for (auto& h : sys_) {
-            while (3 * h.P.depth > avail && h.P.depth > 1) --h.P.depth;
-            if (ceil_log2(h.P.A) > avail) throw Error(HMD_ERR_INVALID, "too many slots for the sort key");
-            shift = std::max(shift, std::max(3 * h.P.depth, ceil_log2(h.P.A)));
-        }
+    // each system sorts its own slot range with 3*depth-bit Hilbert keys
+    key_bits_ = shift;
+    big_.clear();
+    for (uint32_t s = 0; s < sys_.size(); ++s) {
+        const SysParam& P = sys_[s].P;
+        if (P.sort_enable && P.A > SORT_SEG_MAX) big_.push_back(SortSeg{s, P.off, P.A, P.depth});
     }
-    key_bits_ = shift + rank_bits;
     // lanes per particle in the force kernel: enough threads to fill 152 SMs
     // for small engines, fewer lanes (less reduction work) for large ones
     if (lanes_ == 0) lanes_ = S_ <= (1u << 19) ? 8u : 4u;
@@ -655,8 +643,8 @@ void Engine::rebuild_chain(cudaStream_t st)
 {
     const Dev d = dev();
     if (any_sort_) {
-        const int cur = launch_sort(d, key_bits_, st);
-        launch_rearrange(d, ds(), cur == 0 ? d.val[0] : d.val[1], st);
+        launch_sort(d, big_.data(), (int)big_.size(), d.nsys, st);
+        launch_rearrange(d, ds(), d.val[0], st);
     }
     launch_binning(d, st);
     launch_neighbour(d, st);
@@ -901,7 +889,7 @@ void Engine::profile_get(const std::string& phase, double* total_ms, uint64_t* c
 uint32_t Engine::rebuild_kernel_count() const
 {
     // sort keys + (hist, scan, scatter) per pass + rearrange + copy back; cell clear, bin, sort; list build
-    return (any_sort_ ? 1u + 3u * (uint32_t)radix_passes(key_bits_) + 2u : 0u) + 3u + 1u;
+    return (any_sort_ ? (uint32_t)sort_kernel_count(big_.data(), (int)big_.size()) + 2u : 0u) + 3u + 1u;
 }
 
 void Engine::integrate()

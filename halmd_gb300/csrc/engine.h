@@ -10,6 +10,7 @@
 
 #include "hmd_device.cuh"
 #include "halmd_gb300.h"
+#include "kernels.h"
 
 namespace hmd {
 
@@ -127,6 +128,7 @@ private:
     uint32_t total_cells_ = 0;
     uint32_t nbr_cap_ = 0;
     uint32_t lanes_ = 0;        // force-kernel lanes per particle (0: choose at commit)
+    std::vector<SortSeg> big_;  // systems sorted by the multi-block radix sort
     uint32_t key_bits_ = 0;
     bool any_sort_ = false;
     cudaStream_t stream_ = nullptr;

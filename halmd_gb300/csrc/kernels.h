@@ -17,7 +17,13 @@ void launch_thermo(const Dev& d, cudaStream_t st);
 
 // rebuild (kernels_rebuild.cu)
 int radix_passes(uint32_t key_bits);
-int launch_sort(const Dev& d, uint32_t key_bits, cudaStream_t st);
+// a system sorted by the multi-block radix sort (larger than one block handles)
+struct SortSeg {
+    uint32_t sys, off, slots, depth;
+};
+constexpr uint32_t SORT_SEG_MAX = 262144;   // systems up to this many slots sort in one block each
+void launch_sort(const Dev& d, const SortSeg* big, int nbig, uint32_t nsys_grid, cudaStream_t st);
+int sort_kernel_count(const SortSeg* big, int nbig);
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st);
 void launch_binning(const Dev& d, cudaStream_t st);
 void launch_neighbour(const Dev& d, cudaStream_t st);

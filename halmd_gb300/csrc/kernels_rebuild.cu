@@ -52,25 +52,118 @@ __device__ uint32_t hilbert_key(float x0, float x1, float x2, uint32_t depth)
     return code;
 }
 
-// sort key per slot: (system rank, Hilbert code) for systems that rebuild with
-// sorting on; (rank, slot) otherwise so those systems keep their order.
-__global__ void __launch_bounds__(256) k_sort_keys(Dev d, uint32_t* keys, uint32_t* vals)
+// Hilbert sort key of a slot; ghosts get the largest key of the 3*depth-bit
+// range so the (stable) sort keeps them behind every real particle
+__device__ __forceinline__ uint32_t slot_key(const Dev& d, const SysParam& P, uint32_t i)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const float4 r = d.pos[i];
+    const uint32_t bits = 3u * P.depth;
+    if (species_bits(r.w) == PLACEHOLDER) return (1u << bits) - 1u;
+    return hilbert_key(__fdiv_rn(r.x, P.L[0]), __fdiv_rn(r.y, P.L[1]), __fdiv_rn(r.z, P.L[2]), P.depth);
+}
+
+// keys and identity values of one (large) system's slot range
+__global__ void __launch_bounds__(256) k_segment_keys(Dev d, uint32_t s)
+{
     const SysParam& P = d.sys[s];
-    const uint32_t local = i - P.off;
-    uint32_t lk = local;
-    if (P.active && P.sort_enable && d.st[s].rebuild) {
-        const float4 r = d.pos[i];
-        if (species_bits(r.w) == PLACEHOLDER) {
-            lk = (P.key_shift >= 32) ? 0xFFFFFFFFu : ((1u << P.key_shift) - 1u);
-        } else {
-            lk = hilbert_key(__fdiv_rn(r.x, P.L[0]), __fdiv_rn(r.y, P.L[1]), __fdiv_rn(r.z, P.L[2]), P.depth);
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.A || !(P.active && P.sort_enable && d.st[s].rebuild)) return;
+    d.key[0][P.off + t] = slot_key(d, P, P.off + t);
+    d.val[0][P.off + t] = P.off + t;
+}
+
+// ---------------------------------------------------------------------------
+// Per-system sort: one thread block sorts the slot range of one system that
+// rebuilds (stable LSD radix sort, 9-bit digits, an even number of passes so
+// the permutation ends in val[0]).  All systems up to SEG_MAX slots sort in
+// a single launch, each at the cost of its own size.
+// ---------------------------------------------------------------------------
+
+constexpr uint32_t SEG_MAX = SORT_SEG_MAX;
+constexpr int SEG_THREADS = 512;
+constexpr int SEG_WARPS = SEG_THREADS / 32;
+constexpr int SEG_BITS = 9;
+constexpr int SEG_BINS = 1 << SEG_BITS;
+
+__global__ void __launch_bounds__(SEG_THREADS) k_segment_sort(Dev d)
+{
+    const uint32_t s = blockIdx.x;
+    if (s >= d.nsys) return;
+    const SysParam& P = d.sys[s];
+    if (!(P.active && P.sort_enable && d.st[s].rebuild) || P.A > SEG_MAX) return;   // block-uniform
+    __shared__ uint32_t s_w[SEG_WARPS][SEG_BINS];
+    __shared__ uint32_t s_off[SEG_BINS];
+    __shared__ uint32_t s_tot[SEG_WARPS];
+    const uint32_t off = P.off, n = P.A;
+    uint32_t* kb[2] = {d.key[0] + off, d.key[1] + off};
+    uint32_t* vb[2] = {d.val[0] + off, d.val[1] + off};
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, lt = (1u << lane) - 1u;
+    for (uint32_t t = tid; t < n; t += SEG_THREADS) {
+        kb[0][t] = slot_key(d, P, off + t);
+        vb[0][t] = off + t;
+    }
+    for (int w = 0; w < SEG_WARPS; ++w) s_w[w][tid] = 0;
+    const uint32_t bits = 3u * P.depth;
+    uint32_t passes = (bits + SEG_BITS - 1) / SEG_BITS;
+    passes += passes & 1u;
+    for (uint32_t p = 0; p < passes; ++p) {
+        const uint32_t shift = SEG_BITS * p;
+        const uint32_t* kin = kb[p & 1u];
+        const uint32_t* vin = vb[p & 1u];
+        uint32_t* kout = kb[(p + 1) & 1u];
+        uint32_t* vout = vb[(p + 1) & 1u];
+        s_off[tid] = 0;
+        __syncthreads();
+        for (uint32_t t = tid; t < n; t += SEG_THREADS) atomicAdd(&s_off[(kin[t] >> shift) & (SEG_BINS - 1u)], 1u);
+        __syncthreads();
+        // exclusive scan of the SEG_BINS counts (one per thread)
+        {
+            const uint32_t v = s_off[tid];
+            uint32_t incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= (uint32_t)o) incl += x;
+            }
+            if (lane == 31) s_tot[warp] = incl;
+            __syncthreads();
+            uint32_t before = 0;
+            for (uint32_t w = 0; w < warp; ++w) before += s_tot[w];
+            __syncthreads();
+            s_off[tid] = before + incl - v;
+        }
+        __syncthreads();
+        for (uint32_t base = 0; base < n; base += SEG_THREADS) {
+            const uint32_t idx = base + tid;
+            const bool valid = idx < n;
+            uint32_t key = 0, val = 0, dg = SEG_BINS;
+            if (valid) { key = kin[idx]; val = vin[idx]; dg = (key >> shift) & (SEG_BINS - 1u); }
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, dg);
+            const uint32_t rank = __popc(peers & lt);
+            if (valid && rank == 0) s_w[warp][dg] = __popc(peers);
+            __syncthreads();
+            {
+                uint32_t run = s_off[tid];
+#pragma unroll
+                for (int w = 0; w < SEG_WARPS; ++w) {
+                    const uint32_t c = s_w[w][tid];
+                    s_w[w][tid] = run;
+                    run += c;
+                }
+                s_off[tid] = run;
+            }
+            __syncthreads();
+            if (valid) {
+                const uint32_t pos = s_w[warp][dg] + rank;
+                kout[pos] = key;
+                vout[pos] = val;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int w = 0; w < SEG_WARPS; ++w) s_w[w][tid] = 0;
+            __syncthreads();
         }
     }
-    keys[i] = (P.key_shift >= 32) ? lk : ((P.rank << P.key_shift) | lk);
-    vals[i] = i;
 }
 
 // Hilbert keys of all real particles of every system (module interface)
@@ -96,8 +189,9 @@ constexpr int RADIX_ROUNDS = 8;
 constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;
 
 __global__ void __launch_bounds__(RADIX_THREADS) k_radix_hist(const uint32_t* keys, uint32_t n, uint32_t shift,
-                                                              uint32_t* hist, uint32_t ntiles)
+                                                              uint32_t* hist, uint32_t ntiles, const uint32_t* enable)
 {
+    if (enable && *enable == 0u) return;
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -114,8 +208,9 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_hist(const uint32_t* ke
 // exclusive scan of hist[0 .. 256*ntiles) by one block of 1024 threads: each
 // warp owns a contiguous chunk, reads it lane-strided (coalesced) once to
 // total it and once more to scan it with warp shuffles and a running carry
-__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t* hist, uint32_t total)
+__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t* hist, uint32_t total, const uint32_t* enable)
 {
+    if (enable && *enable == 0u) return;
     __shared__ uint32_t s_warp[32];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint32_t chunk = (total + nw - 1) / nw;
@@ -154,8 +249,10 @@ __global__ void __launch_bounds__(1024) k_radix_scan(uint32_t* hist, uint32_t to
 
 __global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint32_t* kin, const uint32_t* vin,
                                                                  uint32_t* kout, uint32_t* vout, uint32_t n,
-                                                                 uint32_t shift, const uint32_t* hist, uint32_t ntiles)
+                                                                 uint32_t shift, const uint32_t* hist, uint32_t ntiles,
+                                                                 const uint32_t* enable)
 {
+    if (enable && *enable == 0u) return;
     __shared__ uint32_t s_w[RADIX_THREADS / 32][256];
     __shared__ uint32_t s_base[256];
     __shared__ uint32_t s_goff[256];
@@ -425,22 +522,43 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
 int radix_passes(uint32_t key_bits) { return (int)((key_bits + 7) / 8); }
 
 // sort keys/values of all S slots; returns the buffer index holding the result
-int launch_sort(const Dev& d, uint32_t key_bits, cudaStream_t st)
+// Sort the slot ranges of the systems that rebuild: one launch of per-system
+// block sorts for systems up to SEG_MAX slots, and a multi-block sort over
+// the range of each larger system.  The permutation ends in val[0].
+void launch_sort(const Dev& d, const SortSeg* big, int nbig, uint32_t nsys_grid, cudaStream_t st)
 {
-    const uint32_t n = d.S;
-    const uint32_t ntiles = (n + RADIX_TILE - 1) / RADIX_TILE;
-    k_sort_keys<<<n / 256, 256, 0, st>>>(d, d.key[0], d.val[0]);
-    int cur = 0;
-    const int passes = radix_passes(key_bits);
-    for (int p = 0; p < passes; ++p) {
-        const uint32_t shift = 8u * p;
-        k_radix_hist<<<ntiles, RADIX_THREADS, 0, st>>>(d.key[cur], n, shift, d.hist, ntiles);
-        k_radix_scan<<<1, 1024, 0, st>>>(d.hist, 256u * ntiles);
-        k_radix_scatter<<<ntiles, RADIX_THREADS, 0, st>>>(d.key[cur], d.val[cur], d.key[1 - cur], d.val[1 - cur],
-                                                           n, shift, d.hist, ntiles);
-        cur = 1 - cur;
+    k_segment_sort<<<nsys_grid, SEG_THREADS, 0, st>>>(d);
+    for (int b = 0; b < nbig; ++b) {
+        const SortSeg& g = big[b];
+        const uint32_t n = g.slots;
+        const uint32_t ntiles = (n + RADIX_TILE - 1) / RADIX_TILE;
+        const uint32_t* flag = &d.st[g.sys].rebuild;
+        k_segment_keys<<<(n + 255) / 256, 256, 0, st>>>(d, g.sys);
+        uint32_t* kk[2] = {d.key[0] + g.off, d.key[1] + g.off};
+        uint32_t* vv[2] = {d.val[0] + g.off, d.val[1] + g.off};
+        int passes = radix_passes(3u * g.depth);
+        passes += passes & 1;
+        int cur = 0;
+        for (int p = 0; p < passes; ++p) {
+            const uint32_t shift = 8u * p;
+            k_radix_hist<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], n, shift, d.hist, ntiles, flag);
+            k_radix_scan<<<1, 1024, 0, st>>>(d.hist, 256u * ntiles, flag);
+            k_radix_scatter<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], vv[cur], kk[1 - cur], vv[1 - cur], n, shift,
+                                                               d.hist, ntiles, flag);
+            cur = 1 - cur;
+        }
     }
-    return cur;
+}
+
+int sort_kernel_count(const SortSeg* big, int nbig)
+{
+    int k = 1;
+    for (int b = 0; b < nbig; ++b) {
+        int passes = radix_passes(3u * big[b].depth);
+        passes += passes & 1;
+        k += 1 + 3 * passes;
+    }
+    return k;
 }
 
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st)
@@ -476,10 +594,10 @@ void launch_radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t*
     int cur = 0;
     for (int p = 0; p < radix_passes(key_bits); ++p) {
         const uint32_t shift = 8u * p;
-        k_radix_hist<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], n, shift, hist, ntiles);
-        k_radix_scan<<<1, 1024, 0, st>>>(hist, 256u * ntiles);
+        k_radix_hist<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], n, shift, hist, ntiles, nullptr);
+        k_radix_scan<<<1, 1024, 0, st>>>(hist, 256u * ntiles, nullptr);
         k_radix_scatter<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], vv[cur], kk[1 - cur], vv[1 - cur], n, shift,
-                                                           hist, ntiles);
+                                                           hist, ntiles, nullptr);
         cur = 1 - cur;
     }
     *result_buffer = cur;
