@@ -212,13 +212,26 @@ void Engine::commit()
         shift = std::max(shift, 3 * h.P.depth);
         any_sort_ = any_sort_ || h.P.sort_enable;
     }
-    // each system sorts its own slot range with 3*depth-bit Hilbert keys
+    // each system sorts its own slot range with 3*depth-bit Hilbert keys, in
+    // tiles that never straddle two systems
     key_bits_ = shift;
-    big_.clear();
+    sort_passes_ = radix_passes(key_bits_);
+    sort_passes_ += sort_passes_ & 1;
+    std::vector<uint2> tiles;
+    uint32_t hist_words = 0;
     for (uint32_t s = 0; s < sys_.size(); ++s) {
-        const SysParam& P = sys_[s].P;
-        if (P.sort_enable && P.A > SORT_SEG_MAX) big_.push_back(SortSeg{s, P.off, P.A, P.depth});
+        SysParam& P = sys_[s].P;
+        P.sort_ntiles = (P.A + SORT_TILE - 1) / SORT_TILE;
+        P.sort_hist_off = hist_words;
+        if (!P.sort_enable) continue;
+        hist_words += 256u * P.sort_ntiles;
+        for (uint32_t t = 0; t < P.sort_ntiles; ++t) tiles.push_back(make_uint2(s, P.off + t * SORT_TILE));
     }
+    ntiles_ = (uint32_t)tiles.size();
+    tiles_.alloc(std::max<size_t>(tiles.size(), 1));
+    if (!tiles.empty())
+        HMD_CUDA(cudaMemcpy(tiles_.p, tiles.data(), tiles.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    hist_.alloc(std::max<uint32_t>(hist_words, 1));
     // lanes per particle in the force kernel: enough threads to fill 152 SMs
     // for small engines, fewer lanes (less reduction work) for large ones
     if (lanes_ == 0) lanes_ = S_ <= (1u << 19) ? 8u : 4u;
@@ -232,7 +245,7 @@ void Engine::commit()
     nbr_.alloc((size_t)nbr_cap_ * S); nbr_count_.alloc(S);
     cell_.alloc(std::max<uint32_t>(cell_words, 1)); cell_count_.alloc(total_cells_); cell_sys_.alloc(total_cells_);
     chunk_sys_.alloc(S / CHUNK);
-    key0_.alloc(S); key1_.alloc(S); val0_.alloc(S); val1_.alloc(S); hist_.alloc(radix_hist_words(S_));
+    key0_.alloc(S); key1_.alloc(S); val0_.alloc(S); val1_.alloc(S);
     status_.alloc(1); done_.alloc(1); any_rebuild_.alloc(1);
     dsys_.alloc(sys_.size()); dst_.alloc(sys_.size());
     {
@@ -321,6 +334,7 @@ Dev Engine::dev() const
     d.S = S_; d.nsys = (uint32_t)sys_.size();
     d.status = status_.p; d.done = done_.p; d.any_rebuild = any_rebuild_.p;
     d.key[0] = key0_.p; d.key[1] = key1_.p; d.val[0] = val0_.p; d.val[1] = val1_.p; d.hist = hist_.p;
+    d.tiles = tiles_.p; d.ntiles = ntiles_;
     d.tpos = tpos_.p; d.tvel = tvel_.p; d.timg = timg_.p; d.tid = tid_.p;
     d.partial = partial_.p; d.thermo = thermo_.p;
     return d;
@@ -643,7 +657,7 @@ void Engine::rebuild_chain(cudaStream_t st)
 {
     const Dev d = dev();
     if (any_sort_) {
-        launch_sort(d, big_.data(), (int)big_.size(), d.nsys, st);
+        launch_sort(d, sort_passes_, st);
         launch_rearrange(d, ds(), d.val[0], st);
     }
     launch_binning(d, st);
@@ -889,7 +903,7 @@ void Engine::profile_get(const std::string& phase, double* total_ms, uint64_t* c
 uint32_t Engine::rebuild_kernel_count() const
 {
     // sort keys + (hist, scan, scatter) per pass + rearrange + copy back; cell clear, bin, sort; list build
-    return (any_sort_ ? (uint32_t)sort_kernel_count(big_.data(), (int)big_.size()) + 2u : 0u) + 3u + 1u;
+    return (any_sort_ ? (uint32_t)sort_kernel_count(sort_passes_) + 2u : 0u) + 3u + 1u;
 }
 
 void Engine::integrate()

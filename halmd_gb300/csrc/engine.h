@@ -128,7 +128,9 @@ private:
     uint32_t total_cells_ = 0;
     uint32_t nbr_cap_ = 0;
     uint32_t lanes_ = 0;        // force-kernel lanes per particle (0: choose at commit)
-    std::vector<SortSeg> big_;  // systems sorted by the multi-block radix sort
+    int sort_passes_ = 0;       // radix passes of the segmented sort (even)
+    uint32_t ntiles_ = 0;
+    DevBuf<uint2> tiles_;
     uint32_t key_bits_ = 0;
     bool any_sort_ = false;
     cudaStream_t stream_ = nullptr;

@@ -77,6 +77,8 @@ struct SysParam {
     uint32_t sort_enable;      // Hilbert reorder on rebuild
     uint32_t rank;             // position among systems (sort key prefix)
     float inner[3];            // |r| below this in every dimension: no list pair wraps the box
+    uint32_t sort_hist_off;    // first word of this system's digit histograms
+    uint32_t sort_ntiles;      // sort tiles covering the slot range
 };
 
 // mutable per-system device state
@@ -125,6 +127,8 @@ struct Dev {
     uint32_t* key[2];
     uint32_t* val[2];
     uint32_t* hist;
+    const uint2* tiles;        // (system, first slot) of every sort tile
+    uint32_t ntiles;
     // rearrange temporaries
     float4* tpos;
     float4* tvel;

@@ -17,20 +17,13 @@ void launch_thermo(const Dev& d, cudaStream_t st);
 
 // rebuild (kernels_rebuild.cu)
 int radix_passes(uint32_t key_bits);
-// a system sorted by the multi-block radix sort (larger than one block handles)
-struct SortSeg {
-    uint32_t sys, off, slots, depth;
-};
-constexpr uint32_t SORT_SEG_MAX = 262144;   // systems up to this many slots sort in one block each
-void launch_sort(const Dev& d, const SortSeg* big, int nbig, uint32_t nsys_grid, cudaStream_t st);
-int sort_kernel_count(const SortSeg* big, int nbig);
+constexpr uint32_t SORT_TILE = 2048;   // keys per tile of the segmented radix sort
+void launch_sort(const Dev& d, int passes, cudaStream_t st);
+int sort_kernel_count(int passes);
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st);
 void launch_binning(const Dev& d, cudaStream_t st);
 void launch_neighbour(const Dev& d, cudaStream_t st);
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st);
-void launch_radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t* hist, uint32_t n,
-                             uint32_t key_bits, cudaStream_t st, int* result_buffer);
-uint32_t radix_hist_words(uint32_t n);
 
 // observables (kernels_obs.cu)
 void launch_sample_position(const Dev& d, uint32_t first, uint32_t count, double* out, cudaStream_t st);

@@ -62,110 +62,6 @@ __device__ __forceinline__ uint32_t slot_key(const Dev& d, const SysParam& P, ui
     return hilbert_key(__fdiv_rn(r.x, P.L[0]), __fdiv_rn(r.y, P.L[1]), __fdiv_rn(r.z, P.L[2]), P.depth);
 }
 
-// keys and identity values of one (large) system's slot range
-__global__ void __launch_bounds__(256) k_segment_keys(Dev d, uint32_t s)
-{
-    const SysParam& P = d.sys[s];
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.A || !(P.active && P.sort_enable && d.st[s].rebuild)) return;
-    d.key[0][P.off + t] = slot_key(d, P, P.off + t);
-    d.val[0][P.off + t] = P.off + t;
-}
-
-// ---------------------------------------------------------------------------
-// Per-system sort: one thread block sorts the slot range of one system that
-// rebuilds (stable LSD radix sort, 9-bit digits, an even number of passes so
-// the permutation ends in val[0]).  All systems up to SEG_MAX slots sort in
-// a single launch, each at the cost of its own size.
-// ---------------------------------------------------------------------------
-
-constexpr uint32_t SEG_MAX = SORT_SEG_MAX;
-constexpr int SEG_THREADS = 512;
-constexpr int SEG_WARPS = SEG_THREADS / 32;
-constexpr int SEG_BITS = 9;
-constexpr int SEG_BINS = 1 << SEG_BITS;
-
-__global__ void __launch_bounds__(SEG_THREADS) k_segment_sort(Dev d)
-{
-    const uint32_t s = blockIdx.x;
-    if (s >= d.nsys) return;
-    const SysParam& P = d.sys[s];
-    if (!(P.active && P.sort_enable && d.st[s].rebuild) || P.A > SEG_MAX) return;   // block-uniform
-    __shared__ uint32_t s_w[SEG_WARPS][SEG_BINS];
-    __shared__ uint32_t s_off[SEG_BINS];
-    __shared__ uint32_t s_tot[SEG_WARPS];
-    const uint32_t off = P.off, n = P.A;
-    uint32_t* kb[2] = {d.key[0] + off, d.key[1] + off};
-    uint32_t* vb[2] = {d.val[0] + off, d.val[1] + off};
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, lt = (1u << lane) - 1u;
-    for (uint32_t t = tid; t < n; t += SEG_THREADS) {
-        kb[0][t] = slot_key(d, P, off + t);
-        vb[0][t] = off + t;
-    }
-    for (int w = 0; w < SEG_WARPS; ++w) s_w[w][tid] = 0;
-    const uint32_t bits = 3u * P.depth;
-    uint32_t passes = (bits + SEG_BITS - 1) / SEG_BITS;
-    passes += passes & 1u;
-    for (uint32_t p = 0; p < passes; ++p) {
-        const uint32_t shift = SEG_BITS * p;
-        const uint32_t* kin = kb[p & 1u];
-        const uint32_t* vin = vb[p & 1u];
-        uint32_t* kout = kb[(p + 1) & 1u];
-        uint32_t* vout = vb[(p + 1) & 1u];
-        s_off[tid] = 0;
-        __syncthreads();
-        for (uint32_t t = tid; t < n; t += SEG_THREADS) atomicAdd(&s_off[(kin[t] >> shift) & (SEG_BINS - 1u)], 1u);
-        __syncthreads();
-        // exclusive scan of the SEG_BINS counts (one per thread)
-        {
-            const uint32_t v = s_off[tid];
-            uint32_t incl = v;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                if (lane >= (uint32_t)o) incl += x;
-            }
-            if (lane == 31) s_tot[warp] = incl;
-            __syncthreads();
-            uint32_t before = 0;
-            for (uint32_t w = 0; w < warp; ++w) before += s_tot[w];
-            __syncthreads();
-            s_off[tid] = before + incl - v;
-        }
-        __syncthreads();
-        for (uint32_t base = 0; base < n; base += SEG_THREADS) {
-            const uint32_t idx = base + tid;
-            const bool valid = idx < n;
-            uint32_t key = 0, val = 0, dg = SEG_BINS;
-            if (valid) { key = kin[idx]; val = vin[idx]; dg = (key >> shift) & (SEG_BINS - 1u); }
-            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, dg);
-            const uint32_t rank = __popc(peers & lt);
-            if (valid && rank == 0) s_w[warp][dg] = __popc(peers);
-            __syncthreads();
-            {
-                uint32_t run = s_off[tid];
-#pragma unroll
-                for (int w = 0; w < SEG_WARPS; ++w) {
-                    const uint32_t c = s_w[w][tid];
-                    s_w[w][tid] = run;
-                    run += c;
-                }
-                s_off[tid] = run;
-            }
-            __syncthreads();
-            if (valid) {
-                const uint32_t pos = s_w[warp][dg] + rank;
-                kout[pos] = key;
-                vout[pos] = val;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int w = 0; w < SEG_WARPS; ++w) s_w[w][tid] = 0;
-            __syncthreads();
-        }
-    }
-}
-
 // Hilbert keys of all real particles of every system (module interface)
 __global__ void k_hilbert_keys(Dev d, uint32_t* keys)
 {
@@ -179,38 +75,68 @@ __global__ void k_hilbert_keys(Dev d, uint32_t* keys)
 }
 
 // ---------------------------------------------------------------------------
-// stable LSD radix sort, 8-bit digits (algorithm/gpu/radix_sort_kernel.cu:76-230
-// restated): per-tile digit histograms, one scan, stable scatter with
-// warp-match ranking.  Tiles of 2048 keys (256 threads x 8 rounds).
+// Segmented stable LSD radix sort, 8-bit digits (algorithm/gpu/radix_sort_kernel.cu:76-230
+// restated per system): the slot range of every system is cut into tiles of
+// 2048 keys that never straddle two systems (tile table d.tiles); each pass
+// is one launch over all tiles (digit histograms), one block per system
+// (digit-major exclusive scan of its tiles) and one launch over all tiles
+// (stable scatter with warp-match ranking).  Only systems that rebuild with
+// sorting on do work; passes are even so the permutation ends in val[0].
 // ---------------------------------------------------------------------------
 
 constexpr int RADIX_THREADS = 256;
 constexpr int RADIX_ROUNDS = 8;
 constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;
+static_assert(RADIX_TILE == SORT_TILE, "tile table and kernels disagree");
 
-__global__ void __launch_bounds__(RADIX_THREADS) k_radix_hist(const uint32_t* keys, uint32_t n, uint32_t shift,
-                                                              uint32_t* hist, uint32_t ntiles, const uint32_t* enable)
+__device__ __forceinline__ bool sort_live(const Dev& d, uint32_t s)
 {
-    if (enable && *enable == 0u) return;
+    const SysParam& P = d.sys[s];
+    return P.active && P.sort_enable && d.st[s].rebuild;
+}
+
+// keys (Hilbert code, ghosts last) and identity values of the sorting systems
+__global__ void __launch_bounds__(256) k_seg_keys(Dev d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    if (!sort_live(d, s)) return;
+    d.key[0][i] = slot_key(d, d.sys[s], i);
+    d.val[0][i] = i;
+}
+
+__global__ void __launch_bounds__(RADIX_THREADS) k_seg_hist(Dev d, const uint32_t* keys, uint32_t shift)
+{
+    const uint32_t t = blockIdx.x;
+    if (t >= d.ntiles) return;
+    const uint2 tl = d.tiles[t];
+    if (!sort_live(d, tl.x)) return;   // block-uniform
+    const SysParam& P = d.sys[tl.x];
+    const uint32_t end = min(tl.y + (uint32_t)RADIX_TILE, P.off + P.A);
+    const uint32_t local = (tl.y - P.off) / RADIX_TILE;
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
-    const uint32_t base = blockIdx.x * RADIX_TILE;
 #pragma unroll
     for (int r = 0; r < RADIX_ROUNDS; ++r) {
-        const uint32_t idx = base + r * RADIX_THREADS + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+        const uint32_t idx = tl.y + r * RADIX_THREADS + threadIdx.x;
+        if (idx < end) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
     }
     __syncthreads();
-    hist[threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+    d.hist[P.sort_hist_off + threadIdx.x * P.sort_ntiles + local] = h[threadIdx.x];
 }
 
-// exclusive scan of hist[0 .. 256*ntiles) by one block of 1024 threads: each
-// warp owns a contiguous chunk, reads it lane-strided (coalesced) once to
-// total it and once more to scan it with warp shuffles and a running carry
-__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t* hist, uint32_t total, const uint32_t* enable)
+// exclusive scan of one system's histogram (digit-major over its tiles) by one
+// block of 1024 threads: each warp owns a contiguous chunk, reads it
+// lane-strided (coalesced) once to total it and once more to scan it with
+// warp shuffles and a running carry; offsets come out as absolute slots
+__global__ void __launch_bounds__(1024) k_seg_scan(Dev d)
 {
-    if (enable && *enable == 0u) return;
+    const uint32_t s = blockIdx.x;
+    if (s >= d.nsys || !sort_live(d, s)) return;
+    const SysParam& P = d.sys[s];
+    uint32_t* hist = d.hist + P.sort_hist_off;
+    const uint32_t total = 256u * P.sort_ntiles;
     __shared__ uint32_t s_warp[32];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const uint32_t chunk = (total + nw - 1) / nw;
@@ -226,47 +152,50 @@ __global__ void __launch_bounds__(1024) k_radix_scan(uint32_t* hist, uint32_t to
         uint32_t incl = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= (uint32_t)o) incl += t;
+            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += x;
         }
         if (lane < nw) s_warp[lane] = incl - v;
     }
     __syncthreads();
-    uint32_t carry = s_warp[warp];
+    uint32_t carry = P.off + s_warp[warp];
     for (uint32_t k0 = b; k0 < e; k0 += 32) {
         const uint32_t k = k0 + lane;
         const uint32_t v = (k < e) ? hist[k] : 0u;
         uint32_t incl = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= (uint32_t)o) incl += t;
+            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += x;
         }
         if (k < e) hist[k] = carry + incl - v;
         carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
 }
 
-__global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint32_t* kin, const uint32_t* vin,
-                                                                 uint32_t* kout, uint32_t* vout, uint32_t n,
-                                                                 uint32_t shift, const uint32_t* hist, uint32_t ntiles,
-                                                                 const uint32_t* enable)
+__global__ void __launch_bounds__(RADIX_THREADS) k_seg_scatter(Dev d, const uint32_t* kin, const uint32_t* vin,
+                                                               uint32_t* kout, uint32_t* vout, uint32_t shift)
 {
-    if (enable && *enable == 0u) return;
+    const uint32_t t = blockIdx.x;
+    if (t >= d.ntiles) return;
+    const uint2 tl = d.tiles[t];
+    if (!sort_live(d, tl.x)) return;   // block-uniform
+    const SysParam& P = d.sys[tl.x];
+    const uint32_t end = min(tl.y + (uint32_t)RADIX_TILE, P.off + P.A);
+    const uint32_t local = (tl.y - P.off) / RADIX_TILE;
     __shared__ uint32_t s_w[RADIX_THREADS / 32][256];
     __shared__ uint32_t s_base[256];
     __shared__ uint32_t s_goff[256];
-    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
-    s_base[t] = 0;
-    s_goff[t] = hist[t * ntiles + blockIdx.x];
+    const uint32_t th = threadIdx.x, lane = th & 31u, warp = th >> 5;
+    s_base[th] = 0;
+    s_goff[th] = d.hist[P.sort_hist_off + th * P.sort_ntiles + local];
 #pragma unroll
-    for (int w = 0; w < RADIX_THREADS / 32; ++w) s_w[w][t] = 0;
+    for (int w = 0; w < RADIX_THREADS / 32; ++w) s_w[w][th] = 0;
     __syncthreads();
-    const uint32_t base = blockIdx.x * RADIX_TILE;
     const uint32_t lt = (1u << lane) - 1u;
     for (int r = 0; r < RADIX_ROUNDS; ++r) {
-        const uint32_t idx = base + r * RADIX_THREADS + t;
-        const bool valid = idx < n;
+        const uint32_t idx = tl.y + r * RADIX_THREADS + th;
+        const bool valid = idx < end;
         uint32_t key = 0, val = 0, dg = 256u;
         if (valid) { key = kin[idx]; val = vin[idx]; dg = (key >> shift) & 255u; }
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, dg);
@@ -274,14 +203,14 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint32_t*
         if (valid && rank == 0) s_w[warp][dg] = __popc(peers);
         __syncthreads();
         {
-            uint32_t run = s_base[t];
+            uint32_t run = s_base[th];
 #pragma unroll
             for (int w = 0; w < RADIX_THREADS / 32; ++w) {
-                const uint32_t c = s_w[w][t];
-                s_w[w][t] = run;
+                const uint32_t c = s_w[w][th];
+                s_w[w][th] = run;
                 run += c;
             }
-            s_base[t] = run;
+            s_base[th] = run;
         }
         __syncthreads();
         if (valid) {
@@ -291,7 +220,7 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint32_t*
         }
         __syncthreads();
 #pragma unroll
-        for (int w = 0; w < RADIX_THREADS / 32; ++w) s_w[w][t] = 0;
+        for (int w = 0; w < RADIX_THREADS / 32; ++w) s_w[w][th] = 0;
         __syncthreads();
     }
 }
@@ -521,45 +450,22 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
 
 int radix_passes(uint32_t key_bits) { return (int)((key_bits + 7) / 8); }
 
-// sort keys/values of all S slots; returns the buffer index holding the result
-// Sort the slot ranges of the systems that rebuild: one launch of per-system
-// block sorts for systems up to SEG_MAX slots, and a multi-block sort over
-// the range of each larger system.  The permutation ends in val[0].
-void launch_sort(const Dev& d, const SortSeg* big, int nbig, uint32_t nsys_grid, cudaStream_t st)
+// Sort the slot ranges of the systems that rebuild; `passes` is even, so the
+// permutation ends in val[0]
+void launch_sort(const Dev& d, int passes, cudaStream_t st)
 {
-    k_segment_sort<<<nsys_grid, SEG_THREADS, 0, st>>>(d);
-    for (int b = 0; b < nbig; ++b) {
-        const SortSeg& g = big[b];
-        const uint32_t n = g.slots;
-        const uint32_t ntiles = (n + RADIX_TILE - 1) / RADIX_TILE;
-        const uint32_t* flag = &d.st[g.sys].rebuild;
-        k_segment_keys<<<(n + 255) / 256, 256, 0, st>>>(d, g.sys);
-        uint32_t* kk[2] = {d.key[0] + g.off, d.key[1] + g.off};
-        uint32_t* vv[2] = {d.val[0] + g.off, d.val[1] + g.off};
-        int passes = radix_passes(3u * g.depth);
-        passes += passes & 1;
-        int cur = 0;
-        for (int p = 0; p < passes; ++p) {
-            const uint32_t shift = 8u * p;
-            k_radix_hist<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], n, shift, d.hist, ntiles, flag);
-            k_radix_scan<<<1, 1024, 0, st>>>(d.hist, 256u * ntiles, flag);
-            k_radix_scatter<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], vv[cur], kk[1 - cur], vv[1 - cur], n, shift,
-                                                               d.hist, ntiles, flag);
-            cur = 1 - cur;
-        }
+    k_seg_keys<<<d.S / 256, 256, 0, st>>>(d);
+    for (int p = 0; p < passes; ++p) {
+        const uint32_t shift = 8u * p;
+        const int cur = p & 1;
+        k_seg_hist<<<d.ntiles, RADIX_THREADS, 0, st>>>(d, d.key[cur], shift);
+        k_seg_scan<<<d.nsys, 1024, 0, st>>>(d);
+        k_seg_scatter<<<d.ntiles, RADIX_THREADS, 0, st>>>(d, d.key[cur], d.val[cur], d.key[1 - cur], d.val[1 - cur],
+                                                          shift);
     }
 }
 
-int sort_kernel_count(const SortSeg* big, int nbig)
-{
-    int k = 1;
-    for (int b = 0; b < nbig; ++b) {
-        int passes = radix_passes(3u * big[b].depth);
-        passes += passes & 1;
-        k += 1 + 3 * passes;
-    }
-    return k;
-}
+int sort_kernel_count(int passes) { return 1 + 3 * passes; }
 
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st)
 {
@@ -584,25 +490,5 @@ void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
 {
     k_hilbert_keys<<<(d.S + 255) / 256, 256, 0, st>>>(d, keys);
 }
-
-void launch_radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t* hist, uint32_t n,
-                             uint32_t key_bits, cudaStream_t st, int* result_buffer)
-{
-    const uint32_t ntiles = (n + RADIX_TILE - 1) / RADIX_TILE;
-    uint32_t* kk[2] = {k0, k1};
-    uint32_t* vv[2] = {v0, v1};
-    int cur = 0;
-    for (int p = 0; p < radix_passes(key_bits); ++p) {
-        const uint32_t shift = 8u * p;
-        k_radix_hist<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], n, shift, hist, ntiles, nullptr);
-        k_radix_scan<<<1, 1024, 0, st>>>(hist, 256u * ntiles, nullptr);
-        k_radix_scatter<<<ntiles, RADIX_THREADS, 0, st>>>(kk[cur], vv[cur], kk[1 - cur], vv[1 - cur], n, shift,
-                                                           hist, ntiles, nullptr);
-        cur = 1 - cur;
-    }
-    *result_buffer = cur;
-}
-
-uint32_t radix_hist_words(uint32_t n) { return 256u * ((n + RADIX_TILE - 1) / RADIX_TILE); }
 
 } // namespace hmd
