@@ -198,6 +198,120 @@ def run_reference(args, w):
     print(json.dumps(line))
 
 
+def ensemble_specs(count=256, seed=256):
+    """Replicas of the batched-ensemble workload: N log-uniform in [500, 32000],
+    density uniform in [0.7, 1.2], T uniform in [0.5, 2.0], LJ or KA by a coin
+    flip (KA: 80:20, smooth_r4, Andersen at T; LJ: shifted cut-off, NVE)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(np.floor(np.exp(rng.uniform(np.log(500), np.log(32000)))))
+        rho = float(rng.uniform(0.7, 1.2))
+        T = float(rng.uniform(0.5, 2.0))
+        ka = bool(rng.integers(0, 2))
+        L = (n / rho) ** (1 / 3)
+        m = int(np.ceil(n ** (1 / 3)))
+        g = (np.arange(m) + 0.5) * (L / m) - 0.5 * L
+        sites = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+        r = sites[rng.permutation(len(sites))[:n]] + rng.uniform(-0.02, 0.02, size=(n, 3))
+        v = rng.normal(0, np.sqrt(T), size=(n, 3))
+        v -= v.mean(axis=0)
+        sp = np.zeros(n, dtype=np.uint32)
+        if ka:
+            sp[rng.permutation(n)[: n // 5]] = 1
+            d = dict(epsilon=KA["eps"], sigma=KA["sigma"], r_cut=2.5, truncation="smooth_r4", smoothing=0.005,
+                     skin=0.3, timestep=0.002, integrator="andersen", temperature=T, collision_rate=1.0,
+                     seed=1000 + k)
+        else:
+            d = dict(r_cut=2.5, truncation="shifted", skin=0.3, timestep=0.002)
+        out.append(dict(n=n, L=L, r=r, v=v, sp=sp, desc=d))
+    return out
+
+
+def run_ensemble(args):
+    """ENS-256: all replicas in one engine (one launch per phase, graph-captured
+    step chunks) against looping the one-system path over the same replicas."""
+    import torch
+    import halmd_gb300 as hg
+    from halmd_gb300.tune import autotune_force_lanes
+    specs = ensemble_specs()
+    ntot = sum(s["n"] for s in specs)
+    M = args.md_steps
+
+    def load(eng, k, s):
+        eng.set("species", s["sp"], k)
+        eng.set("position", s["r"], k)
+        eng.set("velocity", s["v"], k)
+
+    batch = hg.Engine("dsfloat")
+    for s in specs:
+        batch.add_system(hg.system_desc(s["n"], s["L"], **s["desc"]))
+    batch.commit()
+    for k, s in enumerate(specs):
+        load(batch, k, s)
+    batch.step(M)
+    lanes, lane_ms = autotune_force_lanes(batch, use_cache=False)
+    for _ in range(args.warmup):
+        batch.step(M)
+    stream = torch.cuda.ExternalStream(batch.stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    chains0 = batch.get_option("rebuild_chains")
+    clocks = ClockSampler(0)
+    total_ms = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.step(M)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    clk = clocks.stop()
+    chains = batch.get_option("rebuild_chains") - chains0
+    inf = batch.info(0)
+    batched = ntot * M * args.steps / (total_ms * 1e-3)
+    # three kernels per step, plus the rebuild chain in every step where any replica rebuilt
+    launches = M * args.steps * 3 + chains * inf.rebuild_kernels
+    batch.close()
+
+    # the plain path: one engine per replica, stepped one after another
+    engines = []
+    for s in specs:
+        e = hg.Engine("dsfloat")
+        e.add_system(hg.system_desc(s["n"], s["L"], **s["desc"]))
+        e.commit()
+        load(e, 0, s)
+        e.step(M)
+        engines.append(e)
+    for e in engines:
+        e.step(M)
+    torch.cuda.synchronize()
+    loop_steps = max(1, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(loop_steps):
+        for e in engines:
+            e.step(M)
+    torch.cuda.synchronize()
+    loop_s = time.perf_counter() - t0
+    looped = ntot * M * loop_steps / loop_s
+    for e in engines:
+        e.close()
+    line = {"metric": "particle-steps/s", "value": batched, "unit": "particle-steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / (M * args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (dsfloat state)",
+            "data": "synthetic",
+            "config": {"workload": "ENS-256", "replicas": len(specs), "particles": ntot,
+                       "md_steps_per_bench_step": M, "force_lanes": lanes,
+                       "autotune_force_ms": {str(k): v for k, v in lane_ms.items()},
+                       "l2": "flushed (256 MB write) between timed bench steps"},
+            "looped_plain_path": {"value": looped, "unit": "particle-steps/s",
+                                  "note": "256 engines of one replica each, hmd_step(%d) in turn" % M},
+            "batch_speedup": batched / looped, "gpu_launches": launches, "clocks": clk}
+    print(json.dumps(line))
+
+
 def run_phases(args, w):
     """Per-phase breakdown of the MD step through the module-level calls."""
     r, v, species, L = initial_state(w)
@@ -240,6 +354,10 @@ def main():
                          "each, no graph) with the per-phase CUDA-event timers, print the breakdown and exit; "
                          "this is the run profilers can attribute kernel by kernel")
     args = ap.parse_args()
+    if args.workload == "ens256":
+        if args.impl == "reference":
+            raise SystemExit("the ensemble workload has no reference arm")
+        return run_ensemble(args)
     w = workload(args.workload)
     if args.phases:
         return run_phases(args, w)

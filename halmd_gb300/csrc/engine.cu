@@ -246,7 +246,7 @@ void Engine::commit()
     cell_.alloc(std::max<uint32_t>(cell_words, 1)); cell_count_.alloc(total_cells_); cell_sys_.alloc(total_cells_);
     chunk_sys_.alloc(S / CHUNK);
     key0_.alloc(S); key1_.alloc(S); val0_.alloc(S); val1_.alloc(S);
-    status_.alloc(1); done_.alloc(1); any_rebuild_.alloc(1);
+    status_.alloc(1); done_.alloc(1); any_rebuild_.alloc(2);   // [0] this step rebuilds, [1] rebuild chains run
     dsys_.alloc(sys_.size()); dst_.alloc(sys_.size());
     {
         size_t np = 0;
@@ -640,6 +640,11 @@ int64_t Engine::get_option(const std::string& name) const
 {
     if (name == "force_lanes") return lanes_;
     if (name == "neighbour_capacity") return nbr_cap_;
+    if (name == "rebuild_chains") {
+        uint32_t v[2];
+        const_cast<Engine*>(this)->download(any_rebuild_, 0, 2, v);
+        return v[1];
+    }
     throw Error(HMD_ERR_INVALID, "unknown option '" + name + "'");
 }
 

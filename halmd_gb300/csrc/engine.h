@@ -161,7 +161,7 @@ private:
     void toc(const char* phase);
     uint32_t rebuild_kernel_count() const;
 
-    static constexpr int CHUNK_STEPS = 50;
+    static constexpr int CHUNK_STEPS = 100;
     static constexpr uint64_t SEGMENT_STEPS = 5000;
     cudaGraphExec_t g_chunk_ = nullptr, g_one_ = nullptr, g_one_aux_ = nullptr;
 };

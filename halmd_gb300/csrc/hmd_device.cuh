@@ -122,7 +122,7 @@ struct Dev {
     uint32_t S, nsys;
     uint32_t* status;          // ST_* bits
     uint32_t* done;            // last-block ticket counter
-    uint32_t* any_rebuild;
+    uint32_t* any_rebuild;      // [0] this step rebuilds, [1] count of steps that ran the rebuild chain
     // sort scratch
     uint32_t* key[2];
     uint32_t* val[2];

@@ -118,7 +118,8 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d, cudaGraphConditionalHa
     any = __syncthreads_or(any);
     if (threadIdx.x == 0) {
         *d.done = 0u;
-        *d.any_rebuild = any ? 1u : 0u;
+        d.any_rebuild[0] = any ? 1u : 0u;
+        d.any_rebuild[1] += any ? 1u : 0u;
         if (use_handle) cudaGraphSetConditional(h, any ? 1u : 0u);
     }
 }

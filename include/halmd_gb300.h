@@ -125,6 +125,7 @@ HMD_API int hmd_engine_commit(hmd_engine* engine);
  *   "force_lanes"   threads per particle in the force kernel: 0 (auto), 1, 2, 4, 8
  *                   (the reference's unroll_force_loop, neighbour.lua.in:98-101, is 32)
  *   "neighbour_capacity" (get only) list slots per particle
+ *   "rebuild_chains"     (get only) steps in which the rebuild chain ran (any system rebuilt)
  */
 HMD_API int hmd_engine_set_option(hmd_engine* engine, const char* name, int64_t value);
 HMD_API int hmd_engine_get_option(hmd_engine* engine, const char* name, int64_t* value);
