@@ -312,6 +312,73 @@ def run_ensemble(args):
     print(json.dumps(line))
 
 
+def serve_jobs(count, steps_scale, rate=50.0, seed=2000):
+    """Served-workload stream: Poisson arrivals at `rate` per second, N
+    log-uniform in [1e3, 2e5], density uniform in [0.8, 1.2], T uniform in
+    [0.5, 1.5], steps log-uniform in [1e3, 1e5] times `steps_scale`, LJ or KA by
+    a coin flip; all drawn from `seed`."""
+    from halmd_gb300.serve import Job
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    jobs = []
+    for k in range(count):
+        t += rng.exponential(1.0 / rate)
+        n = int(np.floor(np.exp(rng.uniform(np.log(1e3), np.log(2e5)))))
+        rho = float(rng.uniform(0.8, 1.2))
+        T = float(rng.uniform(0.5, 1.5))
+        steps = max(1, int(np.exp(rng.uniform(np.log(1e3), np.log(1e5))) * steps_scale))
+        ka = bool(rng.integers(0, 2))
+        L = (n / rho) ** (1 / 3)
+        m = int(np.ceil(n ** (1 / 3)))
+        g = (np.arange(m) + 0.5) * (L / m) - 0.5 * L
+        sites = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+        r = sites[rng.permutation(len(sites))[:n]] + rng.uniform(-0.02, 0.02, size=(n, 3))
+        v = rng.normal(0, np.sqrt(T), size=(n, 3))
+        v -= v.mean(axis=0)
+        sp = np.zeros(n, dtype=np.uint32)
+        if ka:
+            sp[rng.permutation(n)[: n // 5]] = 1
+            d = dict(epsilon=KA["eps"], sigma=KA["sigma"], r_cut=2.5, truncation="smooth_r4", smoothing=0.005,
+                     skin=0.3, timestep=0.002, integrator="andersen", temperature=T, collision_rate=1.0,
+                     seed=5000 + k)
+        else:
+            d = dict(r_cut=2.5, truncation="shifted", skin=0.3, timestep=0.002)
+        jobs.append(Job(k, n, L, d, r, v, sp, steps, arrival=t))
+    return jobs
+
+
+def run_serve(args):
+    """SERVE: continuous batching under an 80% HBM budget against a FIFO run
+    of the one-system path, same job stream."""
+    from halmd_gb300.serve import Server, latency_stats, run_fifo
+    jobs = serve_jobs(args.serve_jobs, args.serve_steps_scale)
+    work = sum(j.work for j in jobs)
+    srv = Server(budget_fraction=0.8, max_slots=args.serve_max_slots, max_jobs=1024, neighbour_capacity=288,
+                 chunk=args.md_steps)
+    clocks = ClockSampler(0)
+    st = srv.run(jobs, realtime=True)
+    clk = clocks.stop()
+    lat = latency_stats(jobs)
+    budget = srv.budget
+    srv.close()
+    fifo_jobs = serve_jobs(args.serve_jobs, args.serve_steps_scale)
+    fst = run_fifo(fifo_jobs)
+    flat = latency_stats(fifo_jobs)
+    line = {"metric": "particle-steps/s", "value": work / st["makespan"], "unit": "particle-steps/s", "n_gpus": 1,
+            "steps": st["chunks"], "warmup": 0, "ms_per_step": 1e3 * st["makespan"] / max(st["chunks"], 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (dsfloat state)",
+            "data": "synthetic",
+            "config": {"workload": "SERVE", "jobs": len(jobs), "arrival_rate_per_s": 50,
+                       "steps_scale": args.serve_steps_scale, "particle_steps": work, "chunk_md_steps": args.md_steps,
+                       "hbm_budget": budget},
+            "latency_s": {"p50": lat["p50"], "p99": lat["p99"], "mean": lat["mean"]},
+            "makespan_s": st["makespan"],
+            "fifo_plain_path": {"value": work / fst["makespan"], "unit": "particle-steps/s",
+                                "latency_s": flat, "makespan_s": fst["makespan"]},
+            "throughput_ratio_vs_fifo": fst["makespan"] / st["makespan"], "clocks": clk}
+    print(json.dumps(line))
+
+
 def run_phases(args, w):
     """Per-phase breakdown of the MD step through the module-level calls."""
     r, v, species, L = initial_state(w)
@@ -353,7 +420,14 @@ def main():
                     help="run N MD steps through the module calls (integrate / force / finalize, one launch "
                          "each, no graph) with the per-phase CUDA-event timers, print the breakdown and exit; "
                          "this is the run profilers can attribute kernel by kernel")
+    ap.add_argument("--serve-jobs", type=int, default=200)
+    ap.add_argument("--serve-steps-scale", type=float, default=0.1)
+    ap.add_argument("--serve-max-slots", type=int, default=1 << 24)
     args = ap.parse_args()
+    if args.workload == "serve":
+        if args.impl == "reference":
+            raise SystemExit("the served workload has no reference arm")
+        return run_serve(args)
     if args.workload == "ens256":
         if args.impl == "reference":
             raise SystemExit("the ensemble workload has no reference arm")

@@ -105,6 +105,10 @@ def load():
         "hmd_engine_add_system": (I, [P, P, P]),
         "hmd_engine_commit": (I, [P]),
         "hmd_engine_stream": (I, [P, P]),
+        "hmd_engine_reserve": (I, [P, U, U, U]),
+        "hmd_engine_remove_system": (I, [P, U]),
+        "hmd_engine_capacity": (I, [P, P]),
+        "hmd_engine_progress": (I, [P, P, P, U]),
         "hmd_engine_set_option": (I, [P, ctypes.c_char_p, ctypes.c_int64]),
         "hmd_engine_get_option": (I, [P, ctypes.c_char_p, P]),
         "hmd_info": (I, [P, U, P]),
@@ -231,6 +235,38 @@ class Engine:
     def commit(self):
         self._check(self._L.hmd_engine_commit(self._h))
         self.committed = True
+
+    def reserve(self, slots, systems, neighbour_capacity=0):
+        self._check(self._L.hmd_engine_reserve(self._h, int(slots), int(systems), int(neighbour_capacity)))
+        self.capacity_mode = True
+
+    def add(self, desc):
+        """Add a system; on a committed engine with reserved capacity it joins
+        between steps and keeps its index until removed."""
+        idx = ctypes.c_uint32()
+        self._check(self._L.hmd_engine_add_system(self._h, ctypes.byref(desc), ctypes.byref(idx)))
+        k = idx.value
+        while len(self.systems) <= k:
+            self.systems.append(None)
+        self.systems[k] = desc
+        return k
+
+    def remove(self, s):
+        self._check(self._L.hmd_engine_remove_system(self._h, int(s)))
+        self.systems[s] = None
+
+    def progress(self, n):
+        step = np.zeros(n, dtype=np.uint64)
+        left = np.zeros(n, dtype=np.uint32)
+        self._check(self._L.hmd_engine_progress(self._h, _ptr(step), _ptr(left), int(n)))
+        return step, left
+
+    def capacity(self):
+        out = np.zeros(8, dtype=np.uint64)
+        self._check(self._L.hmd_engine_capacity(self._h, _ptr(out)))
+        keys = ("slots", "slots_used", "cells", "cells_used", "neighbour_capacity", "systems", "system_table",
+                "bytes_per_slot")
+        return {k: int(v) for k, v in zip(keys, out)}
 
     def set_option(self, name, value):
         self._check(self._L.hmd_engine_set_option(self._h, name.encode(), int(value)))

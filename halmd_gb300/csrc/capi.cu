@@ -117,6 +117,31 @@ int hmd_engine_commit(hmd_engine* h)
     return guard(h, [&] { h->e->commit(); });
 }
 
+int hmd_engine_reserve(hmd_engine* h, uint32_t slots, uint32_t systems, uint32_t neighbour_capacity)
+{
+    ENGINE_OR_FAIL(h);
+    return guard(h, [&] { h->e->reserve(slots, systems, neighbour_capacity); });
+}
+
+int hmd_engine_remove_system(hmd_engine* h, uint32_t sys)
+{
+    ENGINE_OR_FAIL(h);
+    return guard(h, [&] { h->e->remove_system(sys); });
+}
+
+int hmd_engine_capacity(hmd_engine* h, uint64_t* out)
+{
+    ENGINE_OR_FAIL(h);
+    if (!out) return HMD_ERR_INVALID;
+    return guard(h, [&] { h->e->capacity_info(out); });
+}
+
+int hmd_engine_progress(hmd_engine* h, uint64_t* step, uint32_t* steps_left, uint32_t n)
+{
+    ENGINE_OR_FAIL(h);
+    return guard(h, [&] { h->e->progress(step, steps_left, n); });
+}
+
 int hmd_engine_set_option(hmd_engine* h, const char* name, int64_t value)
 {
     ENGINE_OR_FAIL(h);

@@ -17,6 +17,8 @@ void cuda_check(cudaError_t e, const char* what)
 }
 
 static uint32_t round_up(uint32_t x, uint32_t m) { return (x + m - 1) / m * m; }
+static float f32_from_bits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+static uint32_t bits_of(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 
 Engine::Engine(int precision, int device) : precision_(precision), device_(device)
 {
@@ -49,7 +51,7 @@ void Engine::check_committed() const
 void Engine::check_sys(uint32_t s) const
 {
     check_committed();
-    if (s >= sys_.size()) throw Error(HMD_ERR_INVALID, "no such system");
+    if (s >= table_size_ || !sys_[s].used) throw Error(HMD_ERR_INVALID, "no such system");
 }
 
 const SysHost& Engine::system(uint32_t s) const
@@ -72,7 +74,7 @@ static void lj_double(double eps, double sigma2, double rr, double& fval, double
 
 uint32_t Engine::add_system(const hmd_system_desc& d)
 {
-    if (committed_) throw Error(HMD_ERR_STATE, "systems must be added before commit");
+    if (committed_ && !capacity_) throw Error(HMD_ERR_STATE, "systems must be added before commit");
     if (d.nparticle == 0) throw Error(HMD_ERR_INVALID, "nparticle must be positive");
     if (d.nspecies < 1 || d.nspecies > HMD_MAX_SPECIES) throw Error(HMD_ERR_INVALID, "nspecies out of range [1, 4]");
     if (d.truncation < 0 || d.truncation > 3) throw Error(HMD_ERR_INVALID, "unknown truncation");
@@ -91,21 +93,24 @@ uint32_t Engine::add_system(const hmd_system_desc& d)
         if (!(d.box[q] > 0)) throw Error(HMD_ERR_INVALID, "box edges must be positive");
     if (d.integrator == HMD_INTEGRATOR_ANDERSEN && (!(d.temperature >= 0) || !(d.collision_rate >= 0)))
         throw Error(HMD_ERR_INVALID, "bad thermostat parameters");
+    if (committed_) return add_live_system(d);   // joins a running engine with a reserved capacity
     if (sys_.size() >= 65536) throw Error(HMD_ERR_INVALID, "too many systems");
+    if (capacity_ && sys_.size() >= cap_systems_) throw Error(HMD_ERR_NOMEM, "system table full");
     SysHost h;
     std::memset(&h.P, 0, sizeof(h.P));
     h.desc = d;
+    h.used = true;
     sys_.push_back(h);
     return (uint32_t)(sys_.size() - 1);
 }
 
-void Engine::layout_system(SysHost& h, uint32_t rank)
+void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
 {
     const hmd_system_desc& d = h.desc;
     SysParam& P = h.P;
     const uint32_t ns = d.nspecies;
     P.n = d.nparticle;
-    P.A = round_up(std::max<uint32_t>(d.nparticle, 1), SLOT_ALIGN);
+    P.A = round_up(std::max<uint32_t>(d.nparticle, 1), align);
     P.ns = ns;
     P.trunc = (uint32_t)d.truncation;
     P.rank = rank;
@@ -188,45 +193,166 @@ void Engine::layout_system(SysHost& h, uint32_t rank)
     h.nbr_size = std::max<uint32_t>(h.nbr_size, 32);
 }
 
+// ---- layout ---------------------------------------------------------------
+//
+// Fixed engines lay their systems out back to back (slot ranges padded to
+// SLOT_ALIGN).  Engines with a reserved capacity keep slots, cells and cell
+// words in first-fit arenas so systems can join and leave between steps: slot
+// ranges are then SORT_TILE-aligned, free ranges belong to an inert "null
+// system" at the last table index, and every kernel reads all per-system state
+// from device tables, so captured step graphs stay valid while the set of
+// systems changes.
+
+bool Arena::alloc(uint32_t n, uint32_t& at)
+{
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+        if (it->second >= n) {
+            at = it->first;
+            const uint32_t rest = it->second - n;
+            free_.erase(it);
+            if (rest) free_[at + n] = rest;
+            used_ += n;
+            return true;
+        }
+    }
+    return false;
+}
+
+void Arena::release(uint32_t at, uint32_t n)
+{
+    if (n == 0) return;
+    used_ -= n;
+    auto next = free_.lower_bound(at);
+    uint32_t start = at, len = n;
+    if (next != free_.begin()) {
+        auto prev = std::prev(next);
+        if (prev->first + prev->second == at) {
+            start = prev->first;
+            len += prev->second;
+            free_.erase(prev);
+        }
+    }
+    next = free_.lower_bound(at);
+    if (next != free_.end() && next->first == at + n) {
+        len += next->second;
+        free_.erase(next);
+    }
+    free_[start] = len;
+}
+
+void Engine::reserve(uint32_t slots, uint32_t systems, uint32_t neighbour_capacity)
+{
+    if (committed_) throw Error(HMD_ERR_STATE, "capacity must be reserved before commit");
+    if (slots == 0 || systems == 0) throw Error(HMD_ERR_INVALID, "capacity must be positive");
+    capacity_ = true;
+    cap_slots_ = round_up(slots, SORT_TILE);
+    cap_systems_ = systems;
+    cap_nbr_ = neighbour_capacity;
+}
+
+// place system s in the arenas (capacity mode); false if it does not fit
+bool Engine::place(uint32_t s)
+{
+    SysParam& P = sys_[s].P;
+    uint32_t at_slot, at_cell, at_word;
+    if (!slot_arena_.alloc(P.A / SORT_TILE, at_slot)) return false;
+    if (!cell_arena_.alloc(P.ncells, at_cell)) {
+        slot_arena_.release(at_slot, P.A / SORT_TILE);
+        return false;
+    }
+    if (!word_arena_.alloc(P.ncells * P.cell_size / 32, at_word)) {
+        slot_arena_.release(at_slot, P.A / SORT_TILE);
+        cell_arena_.release(at_cell, P.ncells);
+        return false;
+    }
+    P.off = at_slot * SORT_TILE;
+    P.cell_off = at_cell;
+    P.cell_word_off = at_word * 32;
+    P.sort_ntiles = P.A / SORT_TILE;
+    P.sort_hist_off = 256u * at_slot;
+    return true;
+}
+
+void Engine::unplace(uint32_t s)
+{
+    const SysParam& P = sys_[s].P;
+    slot_arena_.release(P.off / SORT_TILE, P.A / SORT_TILE);
+    cell_arena_.release(P.cell_off, P.ncells);
+    word_arena_.release(P.cell_word_off / 32, P.ncells * P.cell_size / 32);
+}
+
 void Engine::commit()
 {
     if (committed_) throw Error(HMD_ERR_STATE, "engine already committed");
-    if (sys_.empty()) throw Error(HMD_ERR_STATE, "no systems");
+    if (sys_.empty() && !capacity_) throw Error(HMD_ERR_STATE, "no systems");
     HMD_CUDA(cudaSetDevice(device_));
-    S_ = 0;
-    total_cells_ = 0;
     uint32_t cell_words = 0;
+    uint32_t hist_words = 0;
+    std::vector<uint2> tiles;
     nbr_cap_ = 0;
-    uint32_t shift = 0;
     any_sort_ = false;
-    for (uint32_t s = 0; s < sys_.size(); ++s) {
-        SysHost& h = sys_[s];
-        layout_system(h, s);
-        h.P.off = S_;
-        S_ += h.P.A;
-        h.P.cell_off = total_cells_;
-        h.P.cell_word_off = cell_words;
-        total_cells_ += h.P.ncells;
-        cell_words += h.P.ncells * h.P.cell_size;
-        nbr_cap_ = std::max(nbr_cap_, round_up(h.nbr_size, 8));
-        shift = std::max(shift, 3 * h.P.depth);
-        any_sort_ = any_sort_ || h.P.sort_enable;
+    uint32_t shift = 0;
+    if (!capacity_) {
+        table_size_ = (uint32_t)sys_.size();
+        null_sys_ = PLACEHOLDER;
+        S_ = 0;
+        total_cells_ = 0;
+        for (uint32_t s = 0; s < sys_.size(); ++s) {
+            SysHost& h = sys_[s];
+            layout_system(h, s, SLOT_ALIGN);
+            h.P.off = S_;
+            S_ += h.P.A;
+            h.P.cell_off = total_cells_;
+            h.P.cell_word_off = cell_words;
+            total_cells_ += h.P.ncells;
+            cell_words += h.P.ncells * h.P.cell_size;
+            nbr_cap_ = std::max(nbr_cap_, round_up(h.nbr_size, 8));
+            shift = std::max(shift, 3 * h.P.depth);
+            any_sort_ = any_sort_ || h.P.sort_enable;
+        }
+        // each system sorts its own slot range with 3*depth-bit Hilbert keys,
+        // in tiles that never straddle two systems
+        for (uint32_t s = 0; s < sys_.size(); ++s) {
+            SysParam& P = sys_[s].P;
+            P.sort_ntiles = (P.A + SORT_TILE - 1) / SORT_TILE;
+            P.sort_hist_off = hist_words;
+            if (!P.sort_enable) continue;
+            hist_words += 256u * P.sort_ntiles;
+            for (uint32_t t = 0; t < P.sort_ntiles; ++t) tiles.push_back(make_uint2(s, P.off + t * SORT_TILE));
+        }
+    } else {
+        table_size_ = cap_systems_ + 1;
+        null_sys_ = cap_systems_;
+        S_ = cap_slots_;
+        // cells: at most one per 8 slots on average, 32-word cells (grown on demand)
+        total_cells_ = std::max<uint32_t>(S_ / 8, 64);
+        cell_words = 64u * total_cells_;
+        slot_arena_.init(S_ / SORT_TILE);
+        cell_arena_.init(total_cells_);
+        word_arena_.init(cell_words / 32);
+        std::vector<SysHost> pre = sys_;
+        sys_.assign(table_size_, SysHost());
+        for (uint32_t s = 0; s < pre.size(); ++s) {
+            sys_[s] = pre[s];
+            layout_system(sys_[s], s, SORT_TILE);
+            if (!place(s)) throw Error(HMD_ERR_NOMEM, "reserved capacity too small for the systems");
+            sys_[s].used = true;
+        }
+        for (auto& h : sys_) nbr_cap_ = std::max(nbr_cap_, h.used ? round_up(h.nbr_size, 8) : 0u);
+        nbr_cap_ = std::max(nbr_cap_, round_up(cap_nbr_, 8));
+        shift = 30;           // any depth up to 10
+        any_sort_ = true;
+        hist_words = 256u * (S_ / SORT_TILE);
+        tiles.resize(S_ / SORT_TILE);
+        for (uint32_t t = 0; t < tiles.size(); ++t) tiles[t] = make_uint2(null_sys_, t * SORT_TILE);
+        for (uint32_t s = 0; s < pre.size(); ++s)
+            for (uint32_t t = 0; t < sys_[s].P.sort_ntiles; ++t)
+                tiles[sys_[s].P.off / SORT_TILE + t] = make_uint2(s, sys_[s].P.off + t * SORT_TILE);
     }
-    // each system sorts its own slot range with 3*depth-bit Hilbert keys, in
-    // tiles that never straddle two systems
+    if (nbr_cap_ == 0) nbr_cap_ = 64;
     key_bits_ = shift;
     sort_passes_ = radix_passes(key_bits_);
     sort_passes_ += sort_passes_ & 1;
-    std::vector<uint2> tiles;
-    uint32_t hist_words = 0;
-    for (uint32_t s = 0; s < sys_.size(); ++s) {
-        SysParam& P = sys_[s].P;
-        P.sort_ntiles = (P.A + SORT_TILE - 1) / SORT_TILE;
-        P.sort_hist_off = hist_words;
-        if (!P.sort_enable) continue;
-        hist_words += 256u * P.sort_ntiles;
-        for (uint32_t t = 0; t < P.sort_ntiles; ++t) tiles.push_back(make_uint2(s, P.off + t * SORT_TILE));
-    }
     ntiles_ = (uint32_t)tiles.size();
     tiles_.alloc(std::max<size_t>(tiles.size(), 1));
     if (!tiles.empty())
@@ -243,81 +369,200 @@ void Engine::commit()
     en_pot_.alloc(S); stress_.alloc(6 * S);
     id_.alloc(S); rid_.alloc(S);
     nbr_.alloc((size_t)nbr_cap_ * S); nbr_count_.alloc(S);
-    cell_.alloc(std::max<uint32_t>(cell_words, 1)); cell_count_.alloc(total_cells_); cell_sys_.alloc(total_cells_);
+    cell_.alloc(std::max<uint32_t>(cell_words, 1));
+    cell_count_.alloc(std::max<uint32_t>(total_cells_, 1));
+    cell_sys_.alloc(std::max<uint32_t>(total_cells_, 1));
     chunk_sys_.alloc(S / CHUNK);
     key0_.alloc(S); key1_.alloc(S); val0_.alloc(S); val1_.alloc(S);
     status_.alloc(1); done_.alloc(1); any_rebuild_.alloc(2);   // [0] this step rebuilds, [1] rebuild chains run
-    dsys_.alloc(sys_.size()); dst_.alloc(sys_.size());
-    {
-        size_t np = 0;
-        for (auto& h : sys_) np += h.pairs.size();
-        dpair_.alloc(np);
-    }
-    partial_.alloc((S / 256) * NTHERMO + 1); thermo_.alloc(sys_.size() * NTHERMO);
+    dsys_.alloc(table_size_); dst_.alloc(table_size_);
+    dpair_.alloc((size_t)table_size_ * MAX_SPECIES * MAX_SPECIES);
+    partial_.alloc((S / 256) * NTHERMO + 1); thermo_.alloc((size_t)table_size_ * NTHERMO);
 
-    // initial contents: ghosts everywhere, real particles at slot = off + tag
-    std::vector<float4> hpos(2 * S), hvel(2 * S, make_float4(0, 0, 0, 0));
-    std::vector<uint32_t> hid(S, PLACEHOLDER), hrid(S, 0), hchunk(S / CHUNK), hcs(total_cells_);
-    float ghost;
+    // everything starts as ghosts owned by the null system (capacity mode)
     {
-        uint32_t g = PLACEHOLDER;
-        std::memcpy(&ghost, &g, 4);
+        std::vector<float4> hpos(S, make_float4(0, 0, 0, f32_from_bits(PLACEHOLDER)));
+        HMD_CUDA(cudaMemcpyAsync(pos_.p, hpos.data(), S * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+        HMD_CUDA(cudaMemcpyAsync(r0_.p, hpos.data(), S * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+        HMD_CUDA(cudaMemsetAsync(pos_.p + S, 0, S * sizeof(float4), stream_));
+        HMD_CUDA(cudaMemsetAsync(vel_.p, 0, vel_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(img_.p, 0, img_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(force_.p, 0, force_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(en_pot_.p, 0, en_pot_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(stress_.p, 0, stress_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(nbr_count_.p, 0, nbr_count_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(cell_count_.p, 0, cell_count_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(status_.p, 0, status_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(done_.p, 0, done_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(any_rebuild_.p, 0, any_rebuild_.bytes(), stream_));
+        HMD_CUDA(cudaMemsetAsync(id_.p, 0xFF, id_.bytes(), stream_));
+        std::vector<uint32_t> iota(S);
+        for (size_t k = 0; k < S; ++k) iota[k] = (uint32_t)k;
+        HMD_CUDA(cudaMemcpyAsync(rid_.p, iota.data(), rid_.bytes(), cudaMemcpyHostToDevice, stream_));
+        const uint32_t owner = capacity_ ? null_sys_ : 0u;
+        std::vector<uint32_t> hchunk(S / CHUNK, owner), hcs(std::max<uint32_t>(total_cells_, 1), owner);
+        HMD_CUDA(cudaMemcpyAsync(chunk_sys_.p, hchunk.data(), chunk_sys_.bytes(), cudaMemcpyHostToDevice, stream_));
+        HMD_CUDA(cudaMemcpyAsync(cell_sys_.p, hcs.data(), cell_sys_.bytes(), cudaMemcpyHostToDevice, stream_));
+        std::vector<SysState> st(table_size_);
+        for (auto& t : st) std::memset(&t, 0, sizeof(t));
+        HMD_CUDA(cudaMemcpyAsync(dst_.p, st.data(), dst_.bytes(), cudaMemcpyHostToDevice, stream_));
+        std::vector<SysParam> P(table_size_);
+        for (auto& p : P) std::memset(&p, 0, sizeof(p));
+        HMD_CUDA(cudaMemcpyAsync(dsys_.p, P.data(), dsys_.bytes(), cudaMemcpyHostToDevice, stream_));
+        sync();
     }
-    for (size_t k = 0; k < 2 * S; ++k) hpos[k] = make_float4(0, 0, 0, k < S ? ghost : 0.0f);
-    for (uint32_t s = 0; s < sys_.size(); ++s) {
-        const SysParam& P = sys_[s].P;
-        for (uint32_t c = P.off / CHUNK; c < (P.off + P.A) / CHUNK; ++c) hchunk[c] = s;
-        for (uint32_t c = P.cell_off; c < P.cell_off + P.ncells; ++c) hcs[c] = s;
-        for (uint32_t t = 0; t < P.A; ++t) {
-            const uint32_t slot = P.off + t;
-            hrid[slot] = slot;
-            if (t < P.n) {
-                hid[slot] = t;
-                float zero = 0.0f;
-                hpos[slot].w = zero;   // species 0
-                hvel[slot].w = 1.0f;   // unit mass (particle.cpp:56-160)
-            }
-        }
-    }
-    HMD_CUDA(cudaMemcpyAsync(pos_.p, hpos.data(), pos_.bytes(), cudaMemcpyHostToDevice, stream_));
-    HMD_CUDA(cudaMemcpyAsync(vel_.p, hvel.data(), vel_.bytes(), cudaMemcpyHostToDevice, stream_));
-    HMD_CUDA(cudaMemcpyAsync(r0_.p, hpos.data(), r0_.bytes(), cudaMemcpyHostToDevice, stream_));
-    HMD_CUDA(cudaMemsetAsync(img_.p, 0, img_.bytes(), stream_));
-    HMD_CUDA(cudaMemsetAsync(force_.p, 0, force_.bytes(), stream_));
-    HMD_CUDA(cudaMemsetAsync(en_pot_.p, 0, en_pot_.bytes(), stream_));
-    HMD_CUDA(cudaMemsetAsync(stress_.p, 0, stress_.bytes(), stream_));
-    HMD_CUDA(cudaMemsetAsync(nbr_count_.p, 0, nbr_count_.bytes(), stream_));
-    HMD_CUDA(cudaMemsetAsync(cell_count_.p, 0, cell_count_.bytes(), stream_));
-    HMD_CUDA(cudaMemsetAsync(status_.p, 0, status_.bytes(), stream_));
-    HMD_CUDA(cudaMemsetAsync(done_.p, 0, done_.bytes(), stream_));
-    HMD_CUDA(cudaMemsetAsync(any_rebuild_.p, 0, any_rebuild_.bytes(), stream_));
-    HMD_CUDA(cudaMemcpyAsync(id_.p, hid.data(), id_.bytes(), cudaMemcpyHostToDevice, stream_));
-    HMD_CUDA(cudaMemcpyAsync(rid_.p, hrid.data(), rid_.bytes(), cudaMemcpyHostToDevice, stream_));
-    HMD_CUDA(cudaMemcpyAsync(chunk_sys_.p, hchunk.data(), chunk_sys_.bytes(), cudaMemcpyHostToDevice, stream_));
-    if (total_cells_) HMD_CUDA(cudaMemcpyAsync(cell_sys_.p, hcs.data(), cell_sys_.bytes(), cudaMemcpyHostToDevice, stream_));
-    std::vector<SysState> st(sys_.size());
-    for (auto& t : st) {
-        std::memset(&t, 0, sizeof(t));
-        t.steps_left = 0xFFFFFFFFu;
-        t.rebuild_request = 1u;
-    }
-    HMD_CUDA(cudaMemcpyAsync(dst_.p, st.data(), dst_.bytes(), cudaMemcpyHostToDevice, stream_));
-    upload_tables();
-    sync();
     committed_ = true;
+    for (uint32_t s = 0; s < table_size_; ++s)
+        if (!capacity_ || sys_[s].used) install(s);
+    sync();
+}
+
+// write one system's slots, maps, tables and state to the device
+void Engine::install(uint32_t s)
+{
+    SysHost& h = sys_[s];
+    h.used = true;
+    SysParam& P = h.P;
+    P.pair_off = s * (uint32_t)(MAX_SPECIES * MAX_SPECIES);
+    P.active = 1;
+    P.key_shift = key_bits_;
+    const size_t S = S_;
+    std::vector<float4> hp(P.A), hv(P.A, make_float4(0, 0, 0, 0));
+    std::vector<uint32_t> ids(P.A), rids(P.A);
+    for (uint32_t t = 0; t < P.A; ++t) {
+        const bool real = t < P.n;
+        hp[t] = make_float4(0, 0, 0, real ? 0.0f : f32_from_bits(PLACEHOLDER));   // species 0
+        hv[t].w = real ? 1.0f : 0.0f;                                           // unit mass (particle.cpp:56-160)
+        ids[t] = real ? t : PLACEHOLDER;
+        rids[t] = P.off + t;
+    }
+    HMD_CUDA(cudaMemcpyAsync(pos_.p + P.off, hp.data(), P.A * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(r0_.p + P.off, hp.data(), P.A * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemsetAsync(pos_.p + S + P.off, 0, P.A * sizeof(float4), stream_));
+    HMD_CUDA(cudaMemcpyAsync(vel_.p + P.off, hv.data(), P.A * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemsetAsync(vel_.p + S + P.off, 0, P.A * sizeof(float4), stream_));
+    HMD_CUDA(cudaMemsetAsync(img_.p + P.off, 0, P.A * sizeof(float4), stream_));
+    HMD_CUDA(cudaMemsetAsync(force_.p + P.off, 0, P.A * sizeof(float4), stream_));
+    HMD_CUDA(cudaMemsetAsync(en_pot_.p + P.off, 0, P.A * sizeof(float), stream_));
+    for (int c = 0; c < 6; ++c) HMD_CUDA(cudaMemsetAsync(stress_.p + c * S + P.off, 0, P.A * sizeof(float), stream_));
+    HMD_CUDA(cudaMemsetAsync(nbr_count_.p + P.off, 0, P.A * sizeof(uint32_t), stream_));
+    HMD_CUDA(cudaMemcpyAsync(id_.p + P.off, ids.data(), P.A * 4, cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(rid_.p + P.off, rids.data(), P.A * 4, cudaMemcpyHostToDevice, stream_));
+    std::vector<uint32_t> own(std::max<uint32_t>(P.A / CHUNK, P.ncells), s);
+    HMD_CUDA(cudaMemcpyAsync(chunk_sys_.p + P.off / CHUNK, own.data(), (P.A / CHUNK) * 4, cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(cell_sys_.p + P.cell_off, own.data(), P.ncells * 4, cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemsetAsync(cell_count_.p + P.cell_off, 0, P.ncells * 4, stream_));
+    if (capacity_) {
+        std::vector<uint2> tl(P.sort_ntiles);
+        for (uint32_t t = 0; t < P.sort_ntiles; ++t) tl[t] = make_uint2(P.sort_enable ? s : null_sys_, P.off + t * SORT_TILE);
+        HMD_CUDA(cudaMemcpyAsync(tiles_.p + P.off / SORT_TILE, tl.data(), tl.size() * sizeof(uint2),
+                                 cudaMemcpyHostToDevice, stream_));
+    }
+    SysState st;
+    std::memset(&st, 0, sizeof(st));
+    st.steps_left = 0xFFFFFFFFu;
+    st.rebuild_request = 1u;
+    HMD_CUDA(cudaMemcpyAsync(dst_.p + s, &st, sizeof(st), cudaMemcpyHostToDevice, stream_));
+    upload_system(s);
+    sync();
+    forces_valid_ = false;
+}
+
+void Engine::upload_system(uint32_t s)
+{
+    const SysHost& h = sys_[s];
+    HMD_CUDA(cudaMemcpyAsync(dsys_.p + s, &h.P, sizeof(SysParam), cudaMemcpyHostToDevice, stream_));
+    if (!h.pairs.empty())
+        HMD_CUDA(cudaMemcpyAsync(dpair_.p + h.P.pair_off, h.pairs.data(), h.pairs.size() * sizeof(PairParam),
+                                 cudaMemcpyHostToDevice, stream_));
+    sync();
 }
 
 void Engine::upload_tables()
 {
-    std::vector<SysParam> P(sys_.size());
-    std::vector<PairParam> pp;
-    for (uint32_t s = 0; s < sys_.size(); ++s) {
-        sys_[s].P.pair_off = (uint32_t)pp.size();
-        P[s] = sys_[s].P;
-        pp.insert(pp.end(), sys_[s].pairs.begin(), sys_[s].pairs.end());
+    for (uint32_t s = 0; s < table_size_; ++s)
+        if (sys_[s].used) upload_system(s);
+}
+
+uint32_t Engine::add_live_system(const hmd_system_desc& d)
+{
+    if (!capacity_) throw Error(HMD_ERR_STATE, "systems join a committed engine only with a reserved capacity");
+    uint32_t s = PLACEHOLDER;
+    for (uint32_t k = 0; k < cap_systems_; ++k)
+        if (!sys_[k].used) { s = k; break; }
+    if (s == PLACEHOLDER) throw Error(HMD_ERR_NOMEM, "system table full");
+    SysHost h;
+    std::memset(&h.P, 0, sizeof(h.P));
+    h.desc = d;
+    sys_[s] = h;
+    layout_system(sys_[s], s, SORT_TILE);
+    if (round_up(sys_[s].nbr_size, 8) > nbr_cap_) {
+        sys_[s] = SysHost();
+        throw Error(HMD_ERR_NOMEM, "system needs more neighbour-list slots than the engine reserved");
     }
-    HMD_CUDA(cudaMemcpyAsync(dsys_.p, P.data(), dsys_.bytes(), cudaMemcpyHostToDevice, stream_));
-    HMD_CUDA(cudaMemcpyAsync(dpair_.p, pp.data(), pp.size() * sizeof(PairParam), cudaMemcpyHostToDevice, stream_));
+    if (!place(s)) {
+        sys_[s] = SysHost();
+        throw Error(HMD_ERR_NOMEM, "no room in the reserved capacity");
+    }
+    install(s);
+    return s;
+}
+
+void Engine::remove_system(uint32_t s)
+{
+    check_sys(s);
+    if (!capacity_) throw Error(HMD_ERR_STATE, "systems leave only engines with a reserved capacity");
+    SysParam P = sys_[s].P;
+    std::vector<float4> ghost(P.A, make_float4(0, 0, 0, f32_from_bits(PLACEHOLDER)));
+    HMD_CUDA(cudaMemcpyAsync(pos_.p + P.off, ghost.data(), P.A * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemsetAsync(id_.p + P.off, 0xFF, P.A * 4, stream_));
+    std::vector<uint32_t> own(std::max<uint32_t>(P.A / CHUNK, P.ncells), null_sys_);
+    HMD_CUDA(cudaMemcpyAsync(chunk_sys_.p + P.off / CHUNK, own.data(), (P.A / CHUNK) * 4, cudaMemcpyHostToDevice, stream_));
+    HMD_CUDA(cudaMemcpyAsync(cell_sys_.p + P.cell_off, own.data(), P.ncells * 4, cudaMemcpyHostToDevice, stream_));
+    std::vector<uint2> tl(P.sort_ntiles);
+    for (uint32_t t = 0; t < P.sort_ntiles; ++t) tl[t] = make_uint2(null_sys_, P.off + t * SORT_TILE);
+    HMD_CUDA(cudaMemcpyAsync(tiles_.p + P.off / SORT_TILE, tl.data(), tl.size() * sizeof(uint2),
+                             cudaMemcpyHostToDevice, stream_));
+    SysParam z;
+    std::memset(&z, 0, sizeof(z));
+    HMD_CUDA(cudaMemcpyAsync(dsys_.p + s, &z, sizeof(z), cudaMemcpyHostToDevice, stream_));
+    SysState st;
+    std::memset(&st, 0, sizeof(st));
+    HMD_CUDA(cudaMemcpyAsync(dst_.p + s, &st, sizeof(st), cudaMemcpyHostToDevice, stream_));
+    sync();
+    unplace(s);
+    sys_[s] = SysHost();
+}
+
+void Engine::capacity_info(uint64_t* out) const
+{
+    out[0] = S_;
+    out[1] = capacity_ ? (uint64_t)slot_arena_.used() * SORT_TILE : S_;
+    out[2] = total_cells_;
+    out[3] = capacity_ ? cell_arena_.used() : total_cells_;
+    out[4] = nbr_cap_;
+    uint32_t n = 0;
+    for (uint32_t s = 0; s < table_size_; ++s) n += sys_[s].used ? 1u : 0u;
+    out[5] = n;
+    out[6] = capacity_ ? cap_systems_ : table_size_;
+    out[7] = bytes_per_slot();
+}
+
+void Engine::progress(uint64_t* step, uint32_t* steps_left, uint32_t n)
+{
+    check_committed();
+    std::vector<SysState> st = read_state();
+    for (uint32_t s = 0; s < n && s < table_size_; ++s) {
+        if (step) step[s] = st[s].step;
+        if (steps_left) steps_left[s] = st[s].steps_left;
+    }
+}
+
+uint64_t Engine::bytes_per_slot() const
+{
+    // device bytes that scale with the slot count
+    return 2 * 16 + 2 * 16 + 16 + 16 + 16 + 2 * 16 + 2 * 16 + 16 + 4 + 4 + 24 + 4 + 4 + 4 + 16 + 4ull * nbr_cap_ +
+           2 * 16 + 2 * 16 + 16 + 16 + 8;
 }
 
 Dev Engine::dev() const
@@ -331,7 +576,7 @@ Dev Engine::dev() const
     d.lanes_log2 = lanes_ == 8 ? 3u : lanes_ == 4 ? 2u : lanes_ == 2 ? 1u : 0u;
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
-    d.S = S_; d.nsys = (uint32_t)sys_.size();
+    d.S = S_; d.nsys = table_size_;
     d.status = status_.p; d.done = done_.p; d.any_rebuild = any_rebuild_.p;
     d.key[0] = key0_.p; d.key[1] = key1_.p; d.val[0] = val0_.p; d.val[1] = val1_.p; d.hist = hist_.p;
     d.tiles = tiles_.p; d.ntiles = ntiles_;
@@ -358,7 +603,7 @@ void Engine::upload(DevBuf<T>& b, size_t first, size_t count, const T* host)
 
 std::vector<SysState> Engine::read_state()
 {
-    std::vector<SysState> st(sys_.size());
+    std::vector<SysState> st(table_size_);
     download(dst_, 0, st.size(), st.data());
     return st;
 }
@@ -372,9 +617,6 @@ std::vector<uint32_t> Engine::slots_of(uint32_t s)
     download(rid_, P.off, P.n, r.data());
     return r;
 }
-
-static float f32_from_bits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
-static uint32_t bits_of(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 
 void Engine::set(uint32_t s, const std::string& name, const void* host, size_t count)
 {
@@ -760,7 +1002,7 @@ void Engine::snapshot()
     const size_t S = S_;
     if (!snap_pos_.p) {
         snap_pos_.alloc(2 * S); snap_vel_.alloc(2 * S); snap_img_.alloc(S); snap_force_.alloc(S);
-        snap_id_.alloc(S); snap_rid_.alloc(S); snap_st_.alloc(sys_.size());
+        snap_id_.alloc(S); snap_rid_.alloc(S); snap_st_.alloc(table_size_);
     }
     HMD_CUDA(cudaMemcpyAsync(snap_pos_.p, pos_.p, pos_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(snap_vel_.p, vel_.p, vel_.bytes(), cudaMemcpyDeviceToDevice, stream_));
@@ -791,20 +1033,41 @@ bool Engine::grow_after_overflow(uint32_t status)
     std::vector<SysState> st = read_state();
     bool changed = false;
     if (status & ST_CELL_OVERFLOW) {
-        uint32_t words = 0;
-        for (uint32_t s = 0; s < sys_.size(); ++s) {
-            SysParam& P = sys_[s].P;
-            if (st[s].max_cell > P.cell_size) {
+        if (!capacity_) {
+            uint32_t words = 0;
+            for (uint32_t s = 0; s < table_size_; ++s) {
+                SysParam& P = sys_[s].P;
+                if (st[s].max_cell > P.cell_size) {
+                    const uint32_t want = round_up((uint32_t)std::ceil(st[s].max_cell * 1.25), 32);
+                    if (want > 256 || want <= P.cell_size) return false;
+                    P.cell_size = want;
+                    changed = true;
+                }
+                P.cell_word_off = words;
+                words += P.ncells * P.cell_size;
+            }
+            cell_.alloc(std::max<uint32_t>(words, 1));
+            upload_tables();
+        } else {
+            // move each crowded system's cell contents to a larger word range
+            for (uint32_t s = 0; s < table_size_; ++s) {
+                SysParam& P = sys_[s].P;
+                if (!sys_[s].used || st[s].max_cell <= P.cell_size) continue;
                 const uint32_t want = round_up((uint32_t)std::ceil(st[s].max_cell * 1.25), 32);
                 if (want > 256 || want <= P.cell_size) return false;
+                word_arena_.release(P.cell_word_off / 32, P.ncells * P.cell_size / 32);
+                uint32_t at;
+                if (!word_arena_.alloc(P.ncells * want / 32, at)) {
+                    word_arena_.alloc(P.ncells * P.cell_size / 32, at);   // the range just freed
+                    P.cell_word_off = at * 32;
+                    return false;
+                }
                 P.cell_size = want;
+                P.cell_word_off = at * 32;
+                upload_system(s);
                 changed = true;
             }
-            P.cell_word_off = words;
-            words += P.ncells * P.cell_size;
         }
-        cell_.alloc(std::max<uint32_t>(words, 1));
-        upload_tables();
     }
     if (status & ST_NBR_OVERFLOW) {
         uint32_t m = 0;

@@ -3,6 +3,7 @@
 // decision, and recovery from capacity overflow.
 #pragma once
 
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -56,7 +57,26 @@ struct SysHost {
     hmd_system_desc desc;
     SysParam P;
     std::vector<PairParam> pairs;
-    uint32_t nbr_size;   // list capacity estimate (from_binning.cpp:96-119)
+    uint32_t nbr_size = 0;   // list capacity estimate (from_binning.cpp:96-119)
+    bool used = false;       // the table entry holds a system
+};
+
+// first-fit allocator of [0, cap) in fixed units (slot tiles, cells, cell words)
+class Arena {
+public:
+    void init(uint32_t cap)
+    {
+        free_.clear();
+        used_ = 0;
+        if (cap) free_[0] = cap;
+    }
+    bool alloc(uint32_t n, uint32_t& at);
+    void release(uint32_t at, uint32_t n);
+    uint32_t used() const { return used_; }
+
+private:
+    std::map<uint32_t, uint32_t> free_;   // start -> length
+    uint32_t used_ = 0;
 };
 
 class Engine {
@@ -65,7 +85,12 @@ public:
     ~Engine();
 
     uint32_t add_system(const hmd_system_desc& desc);
+    void reserve(uint32_t slots, uint32_t systems, uint32_t neighbour_capacity);
     void commit();
+    void remove_system(uint32_t s);
+    void capacity_info(uint64_t* out) const;
+    void progress(uint64_t* step, uint32_t* steps_left, uint32_t n);
+    uint64_t bytes_per_slot() const;
     void set(uint32_t s, const std::string& name, const void* host, size_t count);
     void get(uint32_t s, const std::string& name, void* host, size_t count);
     void get_raw(uint32_t s, const std::string& name, void* host, size_t bytes);
@@ -100,8 +125,13 @@ public:
 private:
     void check_committed() const;
     void check_sys(uint32_t s) const;
-    void layout_system(SysHost& h, uint32_t rank);
+    void layout_system(SysHost& h, uint32_t rank, uint32_t align);
     void upload_tables();
+    void upload_system(uint32_t s);
+    void install(uint32_t s);
+    bool place(uint32_t s);
+    void unplace(uint32_t s);
+    uint32_t add_live_system(const hmd_system_desc& desc);
     void ensure_forces(bool aux);
     void rebuild_chain(cudaStream_t st);
     void build_graphs();
@@ -124,6 +154,11 @@ private:
     bool aux_valid_ = false;
     bool integrated_ = false;   // hmd_integrate since the last force
     std::vector<SysHost> sys_;
+    uint32_t table_size_ = 0;      // entries of the device system tables
+    uint32_t null_sys_ = 0xFFFFFFFFu;   // inert owner of free ranges (capacity mode)
+    bool capacity_ = false;
+    uint32_t cap_slots_ = 0, cap_systems_ = 0, cap_nbr_ = 0;
+    Arena slot_arena_, cell_arena_, word_arena_;
     uint32_t S_ = 0;
     uint32_t total_cells_ = 0;
     uint32_t nbr_cap_ = 0;

@@ -121,6 +121,22 @@ HMD_API int hmd_engine_add_system(hmd_engine* engine, const hmd_system_desc* des
 /* lay out and allocate all device arrays (particle.cpp:56-160 ctor) */
 HMD_API int hmd_engine_commit(hmd_engine* engine);
 /*
+ * Reserve device capacity before commit so that systems can join and leave
+ * the committed engine between steps (continuous batching; no counterpart in
+ * the reference, whose modules are sized once per simulation): `slots`
+ * particle slots, `systems` table entries, `neighbour_capacity` list slots
+ * per particle (0: from the systems present at commit).  After commit,
+ * hmd_engine_add_system places a new system in free capacity
+ * (HMD_ERR_NOMEM when it does not fit) and hmd_engine_remove_system frees one.
+ */
+HMD_API int hmd_engine_reserve(hmd_engine* engine, uint32_t slots, uint32_t systems, uint32_t neighbour_capacity);
+HMD_API int hmd_engine_remove_system(hmd_engine* engine, uint32_t sys);
+/* out[8]: slots total, slots in use, cells total, cells in use, list slots per
+ * particle, systems in use, system table size, device bytes per slot */
+HMD_API int hmd_engine_capacity(hmd_engine* engine, uint64_t* out);
+/* completed steps and steps still to do of the first n table entries (one read) */
+HMD_API int hmd_engine_progress(hmd_engine* engine, uint64_t* step, uint32_t* steps_left, uint32_t n);
+/*
  * Tuning options (autotuned or set by the caller):
  *   "force_lanes"   threads per particle in the force kernel: 0 (auto), 1, 2, 4, 8
  *                   (the reference's unroll_force_loop, neighbour.lua.in:98-101, is 32)
