@@ -137,6 +137,7 @@ def load():
         "hmd_dynamics_finalise": (I, [P]),
         "hmd_dynamics_result": (I, [P, ctypes.c_int32, P, P, P]),
         "hmd_dynamics_shells": (I, [P, ctypes.c_int32, P, P]),
+        "hmd_msd_pair_noalloc": (I, [P, P, U, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -364,4 +364,11 @@ int hmd_dynamics_shells(hmd_dynamics* x, int32_t tcf, uint32_t* nshell, double* 
     return guard(x->owner, [&] { x->d->shells(tcf, nshell, wavenumber); });
 }
 
+int hmd_msd_pair_noalloc(const double* origin, const double* position, uint32_t count, double* out, void* stream)
+{
+    return guard(nullptr, [&] {
+        hmd::msd_pair_noalloc(origin, position, count, out, static_cast<cudaStream_t>(stream));
+    });
+}
+
 } // extern "C"

@@ -33,4 +33,7 @@ void launch_density_modes(const Dev& d, const uint32_t* range, uint32_t nrange, 
                           const uint32_t* blk_begin, uint32_t nblk, const float4* q, uint32_t nq, double* partial,
                           double* out, cudaStream_t st);
 
+// MSD of one sample pair with fixed scratch and no allocation (msd_noalloc.cu)
+void msd_pair_noalloc(const double* origin, const double* position, uint32_t count, double* out, cudaStream_t st);
+
 } // namespace hmd

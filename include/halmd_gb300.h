@@ -252,6 +252,38 @@ HMD_API int hmd_dynamics_finalise(hmd_dynamics* dyn);
 HMD_API int hmd_dynamics_result(hmd_dynamics* dyn, int32_t tcf, double* mean, double* error, uint64_t* count);
 HMD_API int hmd_dynamics_shells(hmd_dynamics* dyn, int32_t tcf, uint32_t* nshell, double* wavenumber);
 
+/* ---- allocation-free MSD of one sample pair ----------------------------- */
+
+/*
+ * No counterpart in the reference: its MSD exists only inside the blocking
+ * scheme (observables/gpu/dynamics/mean_square_displacement.cpp:55-68),
+ * which owns its buffers.  This entry point is for callers that must not
+ * allocate device memory when they sample: cudaMalloc/cudaFree synchronise
+ * the whole device (stalling a simulation whose steps are in flight), and a
+ * server that reserved nearly all of HBM for its engine may have no room
+ * left.  It allocates nothing; its scratch is a fixed array of the library
+ * in device memory (96 KiB per device).
+ *
+ * origin, position: device arrays of count x 3 doubles (unwrapped positions
+ * in the same particle order).  out: device array of 3 doubles, written with
+ * (count, mean, variance) of |position - origin|^2, the triple the dynamics
+ * path accumulates.  stream: a cudaStream_t (NULL for the legacy default
+ * stream); the call enqueues two kernels and returns without synchronising.
+ *
+ * - count above HMD_MSD_NOALLOC_MAX_PARTICLES (2^25) is rejected with
+ *   HMD_ERR_INVALID, as are null, misaligned or non-device pointers.
+ * - The first call on each device looks up the scratch array's address
+ *   (which can load this library's device code there): make that first
+ *   call, on every device used, before any stream capture begins.
+ * - Nothing needs to be zeroed first.
+ * - All calls on one device share the one scratch array: calls that can
+ *   overlap (different streams, or host threads without ordering) race and
+ *   return wrong results.  Serialise them on one stream.
+ */
+#define HMD_MSD_NOALLOC_MAX_PARTICLES (1u << 25)
+HMD_API int hmd_msd_pair_noalloc(const double* origin, const double* position, uint32_t count, double* out,
+                                 void* stream);
+
 #ifdef __cplusplus
 }
 #endif
