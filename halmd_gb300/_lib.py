@@ -121,6 +121,7 @@ def load():
         "hmd_finalize": (I, [P]),
         "hmd_request_rebuild": (I, [P, U]),
         "hmd_set_steps_left": (I, [P, U, U]),
+        "hmd_minimize": (I, [P, U, U, D, D]),
         "hmd_max_displacement": (I, [P, U, P]),
         "hmd_thermo": (I, [P, U, P]),
         "hmd_neighbour_lists": (I, [P, U, P, P, U]),
@@ -332,6 +333,10 @@ class Engine:
 
     def set_steps_left(self, steps, s=0):
         self._check(self._L.hmd_set_steps_left(self._h, s, int(steps) & 0xFFFFFFFF))
+
+    def minimize(self, steps=1000, step_size=1e-3, max_move=0.05, s=0):
+        """Steepest-descent relaxation of system s (positions only)."""
+        self._check(self._L.hmd_minimize(self._h, s, int(steps), float(step_size), float(max_move)))
 
     def max_displacement(self, s=0):
         d = ctypes.c_double()

@@ -228,6 +228,12 @@ int hmd_set_steps_left(hmd_engine* h, uint32_t sys, uint32_t steps)
     return guard(h, [&] { h->e->set_steps_left(sys, steps); });
 }
 
+int hmd_minimize(hmd_engine* h, uint32_t sys, uint32_t steps, double step_size, double max_move)
+{
+    ENGINE_OR_FAIL(h);
+    return guard(h, [&] { h->e->minimize(sys, steps, step_size, max_move); });
+}
+
 int hmd_max_displacement(hmd_engine* h, uint32_t sys, double* displacement)
 {
     ENGINE_OR_FAIL(h);

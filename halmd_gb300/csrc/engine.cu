@@ -898,6 +898,47 @@ void Engine::set_steps_left(uint32_t s, uint32_t steps)
     write_state(st);
 }
 
+// Steepest-descent minimisation of one system's potential energy (set-up
+// of a start configuration from random positions; no counterpart in the
+// reference).  The system runs `steps` steps of the captured step graph
+// with its integrator switched to INTEG_DESCENT; the other systems are held
+// (steps_left = 0) meanwhile.  Velocities are not touched; the step counter
+// is restored afterwards, so minimisation does not count as MD time.
+void Engine::minimize(uint32_t s, uint32_t steps, double step_size, double max_move)
+{
+    check_committed();
+    check_sys(s);
+    if (!(step_size > 0) || !(max_move > 0) || !std::isfinite(step_size) || !std::isfinite(max_move))
+        throw Error(HMD_ERR_INVALID, "minimize: step_size and max_move must be positive");
+    if (steps == 0) return;
+    if (steps == 0xFFFFFFFFu) throw Error(HMD_ERR_INVALID, "minimize: too many steps");
+    SysHost& h = sys_[s];
+    const SysParam saved = h.P;
+    const std::vector<SysState> before = read_state();
+    std::vector<SysState> st = before;
+    for (uint32_t q = 0; q < (uint32_t)st.size(); ++q) st[q].steps_left = (q == s) ? steps : 0u;
+    write_state(st);
+    h.P.integrator = INTEG_DESCENT;
+    h.P.descent_step = (float)step_size;
+    h.P.descent_max = (float)max_move;
+    upload_system(s);
+    auto put_back = [&] {
+        std::vector<SysState> now = read_state();
+        for (uint32_t q = 0; q < (uint32_t)now.size(); ++q) now[q].steps_left = before[q].steps_left;
+        now[s].step = before[s].step;
+        write_state(now);
+        h.P = saved;
+        upload_system(s);
+    };
+    try {
+        step(steps, false);
+    } catch (...) {
+        put_back();
+        throw;
+    }
+    put_back();
+}
+
 // ---- the step --------------------------------------------------------------
 
 void Engine::rebuild_chain(cudaStream_t st)

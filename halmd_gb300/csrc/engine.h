@@ -102,6 +102,7 @@ public:
     void finalize();
     void request_rebuild(uint32_t s);
     void set_steps_left(uint32_t s, uint32_t steps);
+    void minimize(uint32_t s, uint32_t steps, double step_size, double max_move);
     void set_option(const std::string& name, int64_t value);
     int64_t get_option(const std::string& name) const;
     double max_displacement(uint32_t s);

@@ -29,7 +29,8 @@ constexpr int SLOT_ALIGN = 256;   // slots per system are a multiple of this
 constexpr int CHUNK = 64;         // granularity of the slot -> system map
 
 enum Trunc : uint32_t { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3 };
-enum Integrator : uint32_t { INTEG_VERLET = 0, INTEG_ANDERSEN = 1 };
+// INTEG_DESCENT: steepest-descent energy minimisation (positions only)
+enum Integrator : uint32_t { INTEG_VERLET = 0, INTEG_ANDERSEN = 1, INTEG_DESCENT = 2 };
 enum Status : uint32_t {
     ST_CELL_OVERFLOW = 1u,
     ST_NBR_OVERFLOW = 2u,
@@ -79,6 +80,8 @@ struct SysParam {
     float inner[3];            // |r| below this in every dimension: no list pair wraps the box
     uint32_t sort_hist_off;    // first word of this system's digit histograms
     uint32_t sort_ntiles;      // sort tiles covering the slot range
+    float descent_step;        // INTEG_DESCENT: move = descent_step * F ...
+    float descent_max;         // ... capped at this length per particle and step
 };
 
 // mutable per-system device state

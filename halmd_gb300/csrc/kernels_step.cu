@@ -43,6 +43,50 @@ __device__ __forceinline__ void integrate_component(float& rh, float& rl, float&
     im = __fadd_rn(im, k);
 }
 
+// Steepest descent (energy minimisation of a start configuration; no
+// counterpart in the reference): each particle moves by descent_step * F,
+// shortened to descent_max.  A non-finite force (two particles almost on
+// top of each other) moves the particle by descent_max along its infinite
+// components, or not at all when a component is NaN.
+__device__ __forceinline__ float3 descent_move(float4 f, float step, float dmax)
+{
+    float3 g = make_float3(__fmul_rn(f.x, step), __fmul_rn(f.y, step), __fmul_rn(f.z, step));
+    if (isnan(g.x) || isnan(g.y) || isnan(g.z)) return make_float3(0.0f, 0.0f, 0.0f);
+    const bool inf = isinf(g.x) || isinf(g.y) || isinf(g.z);
+    if (inf) {
+        g.x = isinf(g.x) ? copysignf(1.0f, g.x) : 0.0f;
+        g.y = isinf(g.y) ? copysignf(1.0f, g.y) : 0.0f;
+        g.z = isinf(g.z) ? copysignf(1.0f, g.z) : 0.0f;
+    }
+    const float m = fmaxf(fabsf(g.x), fmaxf(fabsf(g.y), fabsf(g.z)));
+    if (m == 0.0f) return g;
+    const float ux = g.x / m, uy = g.y / m, uz = g.z / m;   // scaled: no overflow in the norm
+    const float len = m * sqrtf(ux * ux + uy * uy + uz * uz);
+    if (inf || len > dmax) {
+        const float c = dmax / len;
+        g.x *= c; g.y *= c; g.z *= c;
+    }
+    return g;
+}
+
+template <bool DS>
+__device__ __forceinline__ void descend_component(float& rh, float& rl, float& im, float g, float L, float Linv)
+{
+    float k;
+    if (DS) {
+        float r0, r1;
+        ds_add(r0, r1, rh, rl, g, 0.0f);
+        k = rintf(__fmul_rn(r0, Linv));
+        ds_sub(r0, r1, r0, r1, __fmul_rn(k, L), 0.0f);
+        rh = r0; rl = r1;
+    } else {
+        float r = __fadd_rn(rh, g);
+        k = rintf(__fmul_rn(r, Linv));
+        rh = __fsub_rn(r, __fmul_rn(k, L));
+    }
+    im = __fadd_rn(im, k);
+}
+
 template <bool DS>
 __global__ void __launch_bounds__(256) k_integrate(Dev d, cudaGraphConditionalHandle h, int use_handle)
 {
@@ -60,13 +104,22 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d, cudaGraphConditionalHa
             float4 k = make_float4(0, 0, 0, 0);   // box images crossed in this step
             float4 rl = make_float4(0, 0, 0, 0), vl = make_float4(0, 0, 0, 0);
             if (DS) { rl = d.pos[d.S + i]; vl = d.vel[d.S + i]; }
-            const float m = v.w;
-            integrate_component<DS>(r.x, rl.x, v.x, vl.x, k.x, f.x, m, P.dt, P.dt_half, P.L[0], P.Linv[0]);
-            integrate_component<DS>(r.y, rl.y, v.y, vl.y, k.y, f.y, m, P.dt, P.dt_half, P.L[1], P.Linv[1]);
-            integrate_component<DS>(r.z, rl.z, v.z, vl.z, k.z, f.z, m, P.dt, P.dt_half, P.L[2], P.Linv[2]);
-            d.pos[i] = r;
-            d.vel[i] = v;
-            if (DS) { d.pos[d.S + i] = rl; d.vel[d.S + i] = vl; }
+            if (P.integrator == INTEG_DESCENT) {   // block-uniform
+                const float3 g = descent_move(f, P.descent_step, P.descent_max);
+                descend_component<DS>(r.x, rl.x, k.x, g.x, P.L[0], P.Linv[0]);
+                descend_component<DS>(r.y, rl.y, k.y, g.y, P.L[1], P.Linv[1]);
+                descend_component<DS>(r.z, rl.z, k.z, g.z, P.L[2], P.Linv[2]);
+                d.pos[i] = r;
+                if (DS) d.pos[d.S + i] = rl;
+            } else {
+                const float m = v.w;
+                integrate_component<DS>(r.x, rl.x, v.x, vl.x, k.x, f.x, m, P.dt, P.dt_half, P.L[0], P.Linv[0]);
+                integrate_component<DS>(r.y, rl.y, v.y, vl.y, k.y, f.y, m, P.dt, P.dt_half, P.L[1], P.Linv[1]);
+                integrate_component<DS>(r.z, rl.z, v.z, vl.z, k.z, f.z, m, P.dt, P.dt_half, P.L[2], P.Linv[2]);
+                d.pos[i] = r;
+                d.vel[i] = v;
+                if (DS) { d.pos[d.S + i] = rl; d.vel[d.S + i] = vl; }
+            }
             if (k.x != 0.0f || k.y != 0.0f || k.z != 0.0f) {
                 // image counters are read and written only on a wrap
                 float4 im = d.img[i];
@@ -360,6 +413,29 @@ __device__ __forceinline__ void force_loop_far(const Dev& d, uint32_t i, uint32_
         const PairParam& p = *pp;
         if (!(rr < p.rr_cut)) continue;
         float fval, e;
+        if (WRAP) {
+            // across the box ri - rj is of order L and its rounding error
+            // (up to ulp(L)/2) would dominate the separation error: add the
+            // TwoSum error back (the cut-off decision above keeps the
+            // rounded rr of the list criterion)
+            const float ex = __fadd_rn(dx, two_sum_err(ri.x, -rj.x, sx));
+            const float ey = __fadd_rn(dy, two_sum_err(ri.y, -rj.y, sy));
+            const float ez = __fadd_rn(dz, two_sum_err(ri.z, -rj.z, sz));
+            pair_eval_fast<TR>(p, rr_exact(ex, ey, ez), rri_smooth, fval, e);
+            A.gx = __fmaf_rn(fval, ex, A.gx);
+            A.gy = __fmaf_rn(fval, ey, A.gy);
+            A.gz = __fmaf_rn(fval, ez, A.gz);
+            if (AUX) {
+                A.en += e;
+                A.s0 += fval * ex * ex;
+                A.s1 += fval * ey * ey;
+                A.s2 += fval * ez * ez;
+                A.s3 += fval * ex * ey;
+                A.s4 += fval * ex * ez;
+                A.s5 += fval * ey * ez;
+            }
+            continue;
+        }
         pair_eval_fast<TR>(p, rr, rri_smooth, fval, e);
         A.gx = __fmaf_rn(fval, dx, A.gx);
         A.gy = __fmaf_rn(fval, dy, A.gy);
@@ -498,7 +574,7 @@ __global__ void __launch_bounds__(256) k_finalize(Dev d)
     const uint32_t s = d.chunk_sys[i / CHUNK];
     const SysParam& P = d.sys[s];
     const SysState& st = d.st[s];
-    if (!P.active || !st.live || *d.status != 0u) return;
+    if (!P.active || !st.live || *d.status != 0u || P.integrator == INTEG_DESCENT) return;
     if (species_bits(d.pos[i].w) == PLACEHOLDER) return;
     float4 v = d.vel[i];
     float4 vl = make_float4(0, 0, 0, 0);

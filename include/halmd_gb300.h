@@ -191,6 +191,15 @@ HMD_API int hmd_finalize(hmd_engine* engine);
 HMD_API int hmd_request_rebuild(hmd_engine* engine, uint32_t sys);
 /* steps a system still has to do (serving); ~0u = unbounded */
 HMD_API int hmd_set_steps_left(hmd_engine* engine, uint32_t sys, uint32_t steps);
+/*
+ * Steepest-descent minimisation of one system's potential energy, used to
+ * relax random start positions (no counterpart in the reference, which has
+ * no minimiser).  Each step moves every particle by step_size * F_i, cut to
+ * max_move in length, then recomputes forces (lists rebuilt by the usual
+ * skin rule).  Other systems of the engine do not advance meanwhile;
+ * velocities and the step counter are left as they were.
+ */
+HMD_API int hmd_minimize(hmd_engine* engine, uint32_t sys, uint32_t steps, double step_size, double max_move);
 
 /*
  * Per-phase runtime accumulators (utility/profiler.hpp:56-99, the modules'

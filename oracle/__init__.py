@@ -65,6 +65,7 @@ def lib():
         L.orc_wavevectors.argtypes = [I, P, P, D, I, P, I, P, P]
         L.orc_fcc_lattice.argtypes = [I, D, P]
         L.orc_md_run.argtypes = [I, P, P, P, P, P, P, P, D, D, I, D, D, ctypes.c_uint64, P]
+        L.orc_minimize.argtypes = [I, P, P, P, P, P, D, I, D, D, P]
         _lib = L
     return _lib
 
@@ -293,6 +294,19 @@ def fcc_lattice(ncell, L):
     r = np.zeros((4 * ncell ** 3, 3))
     lib().orc_fcc_lattice(int(ncell), float(L), _p(r))
     return r
+
+
+def minimize(r, species, L, pot, skin, nsteps, step=1e-3, max_move=0.05, image=None):
+    """FP64 steepest descent; returns (r, image, dict(epot, fmax))."""
+    r = np.array(r, dtype=np.float64, copy=True)
+    n = r.shape[0]
+    image = np.zeros((n, 3)) if image is None else np.array(image, dtype=np.float64, copy=True)
+    sp = np.ascontiguousarray(species, dtype=np.uint32)
+    L = np.ascontiguousarray(L, dtype=np.float64)
+    stats = np.zeros(2)
+    lib().orc_minimize(n, _p(r), _p(image), _p(sp), _p(L), pot.ptr, float(skin), int(nsteps), float(step),
+                       float(max_move), _p(stats))
+    return r, image, dict(epot=stats[0], fmax=stats[1])
 
 
 def md_run(r, v, species, mass, L, pot, skin, dt, nsteps, temperature=0.0, coll_rate=0.0, seed=0, image=None):

@@ -1131,3 +1131,56 @@ ORC_API int orc_md_run(int n, double* r, double* v, double* image, const u32* sp
     if (stats) { stats[0] = rebuilds; stats[1] = totals[0]; stats[2] = ek; }
     return 0;
 }
+
+/*
+ * Steepest-descent minimisation in FP64: the restatement of the engine's
+ * minimiser (the reference has none).  Each step moves particle i by
+ * step * F_i, shortened to max_move when longer; a NaN force component
+ * leaves the particle in place, infinite components move it by max_move
+ * along them.  Lists follow the usual skin rule.  stats[0] = potential
+ * energy and stats[1] = max_i |F_i| of the final positions.
+ */
+ORC_API int orc_minimize(int n, double* r, double* image, const u32* sp, const double* L, const orc_pot* p,
+                         double skin, int nsteps, double step, double max_move, double* stats)
+{
+    std::vector<double> f(3 * (size_t)n), r0(r, r + 3 * (size_t)n);
+    half_list hl;
+    double totals[2] = {0, 0};
+    build_half_list(n, r, sp, L, p, skin, hl);
+    force_half(n, r, sp, L, p, hl, 0, nullptr, nullptr, f.data(), nullptr, nullptr, totals);
+    for (int s = 0; s < nsteps; ++s) {
+        double rr_max = 0;
+        for (int i = 0; i < n; ++i) {
+            double g[3];
+            bool nan = false, inf = false;
+            for (int d = 0; d < 3; ++d) {
+                g[d] = f[3 * i + d] * step;
+                nan |= std::isnan(g[d]);
+                inf |= std::isinf(g[d]);
+            }
+            if (nan) continue;
+            if (inf)
+                for (int d = 0; d < 3; ++d) g[d] = std::isinf(g[d]) ? std::copysign(1.0, g[d]) : 0.0;
+            const double len = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+            const double c = (inf || len > max_move) ? max_move / len : 1.0;
+            double dr[3];
+            for (int d = 0; d < 3; ++d) {
+                r[3 * i + d] += c * g[d];
+                image[3 * i + d] += reduce_periodic_d(r[3 * i + d], L[d]);
+                dr[d] = r[3 * i + d] - r0[3 * i + d];
+                reduce_periodic_d(dr[d], L[d]);
+            }
+            rr_max = std::max(rr_max, dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+        }
+        if (std::sqrt(rr_max) > skin / 2) {
+            build_half_list(n, r, sp, L, p, skin, hl);
+            std::copy(r, r + 3 * (size_t)n, r0.begin());
+        }
+        force_half(n, r, sp, L, p, hl, 0, nullptr, nullptr, f.data(), nullptr, nullptr, totals);
+    }
+    double fmax = 0;
+    for (int i = 0; i < n; ++i)
+        fmax = std::max(fmax, std::sqrt(f[3 * i] * f[3 * i] + f[3 * i + 1] * f[3 * i + 1] + f[3 * i + 2] * f[3 * i + 2]));
+    if (stats) { stats[0] = totals[0]; stats[1] = fmax; }
+    return 0;
+}

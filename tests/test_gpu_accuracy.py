@@ -1,0 +1,100 @@
+"""Force accuracy at the benchmark sizes (LJ-1M, KA-64k) against FP64.
+
+Large boxes matter: across the periodic boundary the float difference of two
+positions is of order L, and its rounding error grows with L, so the small
+systems of the other parity tests do not exercise the worst case.
+Metric: max_i |F_i - F64_i| / max(|F64_i|, F_rms) <= 1e-6.
+"""
+import numpy as np
+import pytest
+
+import halmd_gb300 as hg
+import oracle
+from _systems import KA_EPS, KA_SIGMA, fcc, maxwell_boltzmann, rel_force_error
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-6
+
+
+def oracle_forces(eng, species, pot):
+    inf = eng.info()
+    Lf = np.array(inf.box_f32, dtype=np.float32)
+    pos4 = eng.get_raw("position_hi")[eng.get("reverse_id")]
+    r = pos4[:, :3].astype(np.float64)
+    return oracle.forces(r, species, Lf.astype(np.float64), pot, pos4=pos4, Lf=Lf)
+
+
+def check(eng, species, pot, label):
+    eng.force(aux=True)
+    f = eng.get("force")
+    ref = oracle_forces(eng, species, pot)
+    emax, emed = rel_force_error(f, ref["force"])
+    epot = eng.thermo()["epot"]
+    print("%s: force rel err max %.3g median %.3g; epot rel err %.3g"
+          % (label, emax, emed, abs(epot - ref["epot"]) / abs(ref["epot"])))
+    assert emax < FORCE_TOL
+    assert abs(epot - ref["epot"]) < 1e-6 * abs(ref["epot"])
+
+
+def test_lj1m_force_accuracy():
+    r, L = fcc(64, 0.8442, jitter=0.05, seed=9)
+    n = r.shape[0]
+    assert n == 1048576
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, L, r_cut=2.5, truncation="shifted", skin=0.3, timestep=0.002))
+    eng.commit()
+    eng.set("position", r)
+    eng.set("velocity", maxwell_boltzmann(n, 0.722, seed=10))
+    eng.step(300)
+    check(eng, np.zeros(n), oracle.Potential(1.0, 1.0, 2.5, "shifted"), "LJ-1M")
+    eng.close()
+
+
+def test_ka64k_force_accuracy():
+    n, rho = 64000, 1.2
+    L = (n / rho) ** (1 / 3)
+    rng = np.random.default_rng(64)
+    r = rng.uniform(-L / 2, L / 2, size=(n, 3))
+    sp = np.zeros(n, dtype=np.uint32)
+    sp[rng.permutation(n)[: n // 5]] = 1
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, L, epsilon=KA_EPS, sigma=KA_SIGMA, r_cut=2.5, truncation="smooth_r4",
+                                  smoothing=0.005, skin=0.3, timestep=0.002, integrator="andersen",
+                                  temperature=0.7, collision_rate=1.0, seed=3))
+    eng.commit()
+    eng.set("species", sp)
+    eng.set("position", r)
+    eng.minimize(steps=1000, step_size=1e-3, max_move=0.05)
+    eng.set("velocity", maxwell_boltzmann(n, 0.7, seed=65))
+    eng.step(300)
+    pot = oracle.Potential(KA_EPS, KA_SIGMA, 2.5 * np.ones((2, 2)), "smooth_r4", h=0.005)
+    check(eng, sp, pot, "KA-64k")
+    eng.close()
+
+
+def test_lj1m_energy_drift():
+    """NVE energy drift at LJ-1M over 2*10^4 steps, extrapolated linearly to 10^5 steps."""
+    r, L = fcc(64, 0.8442, jitter=0.05, seed=9)
+    n = r.shape[0]
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, L, r_cut=2.5, truncation="shifted", skin=0.3, timestep=0.002))
+    eng.commit()
+    eng.set("position", r)
+    eng.set("velocity", maxwell_boltzmann(n, 0.722, seed=10))
+    eng.step(2000)                       # let the lattice melt a little before measuring
+    t, e = [], []
+    for k in range(21):
+        if k:
+            eng.step(999)
+        eng.step(1, aux_last=True)
+        th = eng.thermo()
+        t.append(k * 1000)
+        e.append(0.5 * th["mv2"] + th["epot"])
+    e = np.array(e)
+    slope = np.polyfit(np.array(t, dtype=float), e, 1)[0]
+    drift = abs(slope) * 1e5 / abs(e[0])
+    fluct = np.std(e) / abs(e[0])
+    print("LJ-1M NVE: E0/n %.6f, drift %.3g per 1e5 steps, fluctuation %.3g" % (e[0] / n, drift, fluct))
+    assert drift < 1e-5
+    eng.close()
