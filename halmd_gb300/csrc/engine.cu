@@ -136,7 +136,9 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
         p.en_cut = (d.truncation == HMD_TRUNC_SHARP) ? 0.0f : (float)ec;
         p.f_cut = (d.truncation == HMD_TRUNC_FORCE_SHIFTED) ? (float)(fc * rc) : 0.0f;
         p.rr_near = (float)(NEAR_SIGMA * NEAR_SIGMA * sigma2);
-        p.pad[0] = p.pad[1] = p.pad[2] = 0.0f;
+        p.sigma2_lo = (float)(sigma2 - (double)p.sigma2);
+        p.c48_lo = (float)(48 * eps / sigma2 - (double)p.c48);
+        p.pad = 0.0f;
         rc_max = std::max(rc_max, rc);
         rcs_max = std::max(rcs_max, rcs);
     }

@@ -47,7 +47,9 @@ struct PairParam {
     float rr_cut_skin; // (float)((r_c + skin)^2)
     float f_cut;       // force_shifted: F_c = fval(r_c) r_c
     float rr_near;     // (float)((NEAR_SIGMA sigma)^2): list pairs closer at build time get the compensated path
-    float pad[3];
+    float sigma2_lo;   // sigma^2 - sigma2 (the rounding error of the float parameter)
+    float c48_lo;      // 48 eps / sigma^2 - c48
+    float pad;
 };
 
 // pairs closer than NEAR_SIGMA sigma at list build time are evaluated with

@@ -226,26 +226,41 @@ __device__ __forceinline__ float fast_err_pos(float a, float b, float s)
 }
 
 // LJ + truncation (lennard_jones_kernel.hpp:44-56, truncations/*_kernel.cuh).
-// Compensated LJ: the squared distance arrives as a (hi, lo) pair, the
-// reciprocal is refined by one Newton step against rr_hi + rr_lo, and fval
-// gets the first-order term d fval / d rri * rri_lo; the steep r^-14 law
-// would otherwise amplify the float rounding of r^2 seven-fold.  The
-// smoothing factors (smooth_r4) and the force shift use approximate
-// reciprocal / square-root intrinsics: their errors scale forces that are
-// already small near r_c.
+// Compensated LJ for close pairs, whose forces can be an order of magnitude
+// above the particle's net force: the squared distance arrives as a (hi, lo)
+// pair, the reciprocal is refined against it, the float parameters sigma^2
+// and 48 eps / sigma^2 carry their rounding errors, and every product of
+// fval = 48 eps/sigma^2 rri^4 (rri^3 - 1/2) keeps its exact residual (FMA),
+// so fval + flo is accurate to first order in the float roundings (the
+// steep r^-14 law would otherwise amplify them seven-fold).  The smoothing
+// factors (smooth_r4) and the force shift use approximate reciprocal /
+// square-root intrinsics: their errors scale forces that are already small
+// near r_c.
 template <int TR>
 __device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rrl, float rri_smooth,
-                                          float& fval, float& en)
+                                          float& fval, float& flo, float& en)
 {
     float y;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(rr));
     const float res = __fmaf_rn(-rrl, y, __fmaf_rn(-rr, y, 1.0f));
     const float ylo = __fmul_rn(y, res);
     const float rri = __fmul_rn(p.sigma2, y);
-    const float rril = __fmaf_rn(p.sigma2, ylo, __fmaf_rn(p.sigma2, y, -rri));
-    const float ri6 = rri * rri * rri;
-    fval = p.c48 * rri * ri6 * (ri6 - 0.5f);
-    fval = __fmaf_rn(p.c48 * ri6 * __fmaf_rn(7.0f, ri6, -2.0f), rril, fval);
+    float rril = __fmaf_rn(p.sigma2, ylo, __fmaf_rn(p.sigma2, y, -rri));
+    rril = __fmaf_rn(p.sigma2_lo, y, rril);
+    const float t1 = __fmul_rn(rri, rri);
+    const float ri6 = __fmul_rn(t1, rri);
+    const float a = __fmul_rn(p.c48, rri);
+    const float b = __fmul_rn(a, ri6);
+    const float u = __fsub_rn(ri6, 0.5f);
+    fval = __fmul_rn(b, u);
+    // residuals: ri6 = rri^3, u = ri6 - 1/2, a = c48 rri, b = a ri6, fval = b u
+    float ri6l = __fmaf_rn(__fmaf_rn(rri, rri, -t1), rri, __fmaf_rn(t1, rri, -ri6));
+    ri6l = __fmaf_rn(__fmul_rn(3.0f, t1), rril, ri6l);
+    const float ul = __fadd_rn(two_sum_err(ri6, -0.5f, u), ri6l);
+    float al = __fmaf_rn(p.c48, rril, __fmaf_rn(p.c48, rri, -a));
+    al = __fmaf_rn(p.c48_lo, rri, al);
+    const float bl = __fmaf_rn(a, ri6l, __fmaf_rn(al, ri6, __fmaf_rn(a, ri6, -b)));
+    flo = __fmaf_rn(b, ul, __fmaf_rn(bl, u, __fmaf_rn(b, u, -fval)));
     en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
     if (TR == TRUNC_SMOOTH_R4) {
         const float rinv = rsqrtf(rr);
@@ -257,6 +272,7 @@ __device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rr
         const float h0 = x4 * x4i;
         const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
         fval = h0 * fval - h1 * (en * rinv);
+        flo = h0 * flo;
         en = h0 * en;
     } else if (TR == TRUNC_FORCE_SHIFTED) {
         const float rinv = rsqrtf(rr);
@@ -353,15 +369,15 @@ __device__ __forceinline__ void force_loop(const Dev& d, uint32_t i, uint32_t q,
         float rrl = __fadd_rn(__fadd_rn(__fmaf_rn(dx, dx, -px), __fmaf_rn(dy, dy, -py)), __fmaf_rn(dz, dz, -pz));
         rrl = __fadd_rn(rrl, __fadd_rn(fast_err_pos(px, py, pxy), fast_err_pos(pxy, pz, rr)));
         rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
-        float fval, e;
-        pair_eval<TR>(p, rr, rrl, rri_smooth, fval, e);
+        float fval, flo, e;
+        pair_eval<TR>(p, rr, rrl, rri_smooth, fval, flo, e);
         const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
         two_sum_acc(A.fx, A.cx, tx);
         two_sum_acc(A.fy, A.cy, ty);
         two_sum_acc(A.fz, A.cz, tz);
-        A.cx = __fmaf_rn(fval, dxl, __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx)));
-        A.cy = __fmaf_rn(fval, dyl, __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty)));
-        A.cz = __fmaf_rn(fval, dzl, __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz)));
+        A.cx = __fmaf_rn(flo, dx, __fmaf_rn(fval, dxl, __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx))));
+        A.cy = __fmaf_rn(flo, dy, __fmaf_rn(fval, dyl, __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty))));
+        A.cz = __fmaf_rn(flo, dz, __fmaf_rn(fval, dzl, __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz))));
         if (AUX) {
             A.en += e;
             A.s0 += fval * dx * dx;
