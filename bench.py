@@ -393,6 +393,8 @@ def run_phases(args, w):
     """Per-phase breakdown of the MD step through the module-level calls."""
     r, v, species, L = initial_state(w)
     eng = make_engine(w, L)
+    if args.force_lanes:
+        eng.set_option("force_lanes", args.force_lanes)
     eng.set("species", species)
     eng.set("position", r)
     if w["nspecies"] == 2:
@@ -434,6 +436,9 @@ def main():
                     help="run N MD steps through the module calls (integrate / force / finalize, one launch "
                          "each, no graph) with the per-phase CUDA-event timers, print the breakdown and exit; "
                          "this is the run profilers can attribute kernel by kernel")
+    ap.add_argument("--force-lanes", type=int, default=0,
+                    help="threads per particle in the force kernel (0: autotune in the bench, engine default "
+                         "in --phases)")
     ap.add_argument("--serve-jobs", type=int, default=200)
     ap.add_argument("--serve-steps-scale", type=float, default=0.1)
     ap.add_argument("--serve-max-slots", type=int, default=1 << 24)
@@ -474,7 +479,11 @@ def main():
     eng.set("velocity", v)
     eng.step(max(1, args.md_steps))   # equilibrate lists / first rebuilds
     from halmd_gb300.tune import autotune_force_lanes
-    lanes, lane_ms = autotune_force_lanes(eng, use_cache=False)
+    if args.force_lanes:
+        eng.set_option("force_lanes", args.force_lanes)
+        lanes, lane_ms = args.force_lanes, {}
+    else:
+        lanes, lane_ms = autotune_force_lanes(eng, use_cache=False)
     stream = torch.cuda.ExternalStream(eng.stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 

@@ -575,7 +575,7 @@ Dev Engine::dev() const
     d.en_pot = en_pot_.p; d.stress = stress_.p; d.id = id_.p; d.rid = rid_.p;
     d.nbr = nbr_.p; d.nbr_count = nbr_count_.p; d.nbr_cap = nbr_cap_;
     d.lanes = lanes_;
-    d.lanes_log2 = lanes_ == 8 ? 3u : lanes_ == 4 ? 2u : lanes_ == 2 ? 1u : 0u;
+    d.lb_log2 = list_block(lanes_) == 8u ? 3u : 2u;
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
     d.S = S_; d.nsys = table_size_;
@@ -1327,8 +1327,8 @@ void Engine::neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint
         const uint32_t k = slot[t] - P.off;
         if ((cnt[k] & 0xFFFFu) + (cnt[k] >> 16) > maxn) throw Error(HMD_ERR_INVALID, "maxn smaller than a neighbour count");
     }
-    // lane-blocked layout: block b holds entries [b*W, b*W + W) of every slot
-    const uint32_t W = lanes_;
+    // blocked layout: block b holds entries [b*W, b*W + W) of every slot
+    const uint32_t W = list_block(lanes_);
     const uint32_t nblk = nbr_cap_ / W;
     std::vector<uint32_t> all((size_t)nbr_cap_ * P.A);
     for (uint32_t b = 0; b < nblk; ++b)

@@ -28,6 +28,10 @@ constexpr int MAX_SPECIES = 4;
 constexpr int SLOT_ALIGN = 256;   // slots per system are a multiple of this
 constexpr int CHUNK = 64;         // granularity of the slot -> system map
 
+// entries per block of the neighbour-list layout for a force kernel with w
+// threads per particle (each thread reads list_block(w) / w entries at once)
+__host__ __device__ constexpr uint32_t list_block(uint32_t w) { return w < 4u ? 4u : w; }
+
 enum Trunc : uint32_t { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3 };
 // INTEG_DESCENT: steepest-descent energy minimisation (positions only)
 enum Integrator : uint32_t { INTEG_VERLET = 0, INTEG_ANDERSEN = 1, INTEG_DESCENT = 2 };
@@ -111,11 +115,11 @@ struct Dev {
     float* stress;             // [6S]
     uint32_t* id;              // [S] tag of the particle within its system
     uint32_t* rid;             // [S] slot of (off + tag)
-    uint32_t* nbr;             // [nbr_cap * S], lane-blocked: entry k of slot i at ((k/lanes)*S + i)*lanes + k%lanes
+    uint32_t* nbr;             // [nbr_cap * S], blocked: entry k of slot i at ((k/LB)*S + i)*LB + k%LB, LB = list_block(lanes)
     uint32_t* nbr_count;       // [S] near count | far count << 16 (near entries from the front, far from the back)
     uint32_t nbr_cap;          // multiple of 8
     uint32_t lanes;            // threads per particle in the force kernel (1, 2, 4, 8)
-    uint32_t lanes_log2;
+    uint32_t lb_log2;          // log2 of the list block width list_block(lanes)
     uint32_t* cell;            // cell contents
     uint32_t* cell_count;      // [total_cells]
     const uint32_t* cell_sys;  // [total_cells] owning system

@@ -354,7 +354,8 @@ __global__ void __launch_bounds__(128) k_cell_sort(Dev d)
 // full Verlet list, one thread per particle: the 27 cells around the
 // particle's cell (each distinct cell once when a dimension has fewer than
 // 3 cells), criterion rr <= (r_c + skin)^2 in float
-// (from_binning_kernel.cu:144-163), transposed layout k*S + i.
+// (from_binning_kernel.cu:144-163), blocked layout (see Dev::nbr): near
+// pairs (closer than NEAR_SIGMA sigma) from the front, far pairs from the back.
 // Also stores r0 = r for the displacement check (max_displacement.cpp:60-72).
 // ---------------------------------------------------------------------------
 
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
         const int loz = nz >= 3 ? -1 : 0, hiz = nz >= 2 ? 1 : 0;
         const uint32_t cs = P.cell_size;
         const uint32_t cap = d.nbr_cap;
-        const uint32_t lw = d.lanes_log2, lmask = d.lanes - 1u;
+        const uint32_t lw = d.lb_log2, lmask = (1u << lw) - 1u;
         const size_t bstride = (size_t)d.S << lw;
         uint32_t* out = d.nbr + ((size_t)i << lw);
         const float* rrcs = s_rrcs + a * P.ns;

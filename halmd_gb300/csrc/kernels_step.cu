@@ -315,155 +315,157 @@ struct ForceAcc {
     float en = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
 };
 
-// W lanes per particle; lane q takes list entries q, q+W, ...  The list is
-// stored lane-blocked: entry k of slot i at ((k/W)*S + i)*W + k%W, so a warp
-// reads 128 contiguous bytes per load.  WRAP = false when no particle of the
-// warp can see a neighbour across the box: then rint(s/L) = 0 for every pair
-// and the minimum-image arithmetic is skipped without changing any result.
 // TR >= ONE_SPECIES: single-species system, the pair table has one entry
 constexpr int ONE_SPECIES = 16;
 
-template <int W, int TRX, bool AUX, bool WRAP>
-__device__ __forceinline__ void force_loop(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
-                                           const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
+// Pair-parameter lookup for a neighbour of species b; false when b is not a
+// species of the system (lists hold real particles only: this keeps the
+// table lookup in bounds)
+template <bool NS1>
+__device__ __forceinline__ bool pair_of(const PairParam* row, const PairParam& p1, uint32_t ns, float w,
+                                        const PairParam*& pp)
 {
-    constexpr bool NS1 = TRX >= ONE_SPECIES;
-    constexpr int TR = TRX & (ONE_SPECIES - 1);
-    const uint32_t* lst = d.nbr + (size_t)i * W + q;
-    const size_t bstride = (size_t)d.S * W;
-    const uint32_t ns = P.ns;
-    const float Lx = P.L[0], Ly = P.L[1], Lz = P.L[2];
-    const float Ix = P.Linv[0], Iy = P.Linv[1], Iz = P.Linv[2];
-    const float rri_smooth = P.rri_smooth;
-    const PairParam* row = spp + a * ns;
-    PairParam p1;
-    if (NS1) p1 = spp[0];
-#pragma unroll 2
-    for (uint32_t k = q; k < cnt; k += W, lst += bstride) {
-        const uint32_t j = __ldg(lst);
-        const float4 rj = __ldg(d.pos + j);
-        const float sx = __fsub_rn(ri.x, rj.x);
-        const float sy = __fsub_rn(ri.y, rj.y);
-        const float sz = __fsub_rn(ri.z, rj.z);
-        const float dx = WRAP ? min_image(sx, Lx, Ix) : sx;
-        const float dy = WRAP ? min_image(sy, Ly, Iy) : sy;
-        const float dz = WRAP ? min_image(sz, Lz, Iz) : sz;
-        const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
-        const float pxy = __fadd_rn(px, py);
-        const float rr = __fadd_rn(pxy, pz);   // == rr_exact(dx, dy, dz)
-        const PairParam* pp;
-        if (NS1) {
-            pp = &p1;
-        } else {
-            const uint32_t b = species_bits(rj.w);
-            if (b >= ns) continue;   // lists hold real particles only; keep the table lookup in bounds
-            pp = row + b;
-        }
-        const PairParam& p = *pp;
-        if (!(rr < p.rr_cut)) continue;
-        // dx - k L is exact (k = 0, or Sterbenz for k = +-1): the difference
-        // error is the TwoSum error of ri - rj
-        const float dxl = two_sum_err(ri.x, -rj.x, sx);
-        const float dyl = two_sum_err(ri.y, -rj.y, sy);
-        const float dzl = two_sum_err(ri.z, -rj.z, sz);
-        float rrl = __fadd_rn(__fadd_rn(__fmaf_rn(dx, dx, -px), __fmaf_rn(dy, dy, -py)), __fmaf_rn(dz, dz, -pz));
-        rrl = __fadd_rn(rrl, __fadd_rn(fast_err_pos(px, py, pxy), fast_err_pos(pxy, pz, rr)));
-        rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
-        float fval, flo, e;
-        pair_eval<TR>(p, rr, rrl, rri_smooth, fval, flo, e);
-        const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
-        two_sum_acc(A.fx, A.cx, tx);
-        two_sum_acc(A.fy, A.cy, ty);
-        two_sum_acc(A.fz, A.cz, tz);
-        A.cx = __fmaf_rn(flo, dx, __fmaf_rn(fval, dxl, __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx))));
-        A.cy = __fmaf_rn(flo, dy, __fmaf_rn(fval, dyl, __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty))));
-        A.cz = __fmaf_rn(flo, dz, __fmaf_rn(fval, dzl, __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz))));
-        if (AUX) {
-            A.en += e;
-            A.s0 += fval * dx * dx;
-            A.s1 += fval * dy * dy;
-            A.s2 += fval * dz * dz;
-            A.s3 += fval * dx * dy;
-            A.s4 += fval * dx * dz;
-            A.s5 += fval * dy * dz;
-        }
+    if (NS1) { pp = &p1; return true; }
+    const uint32_t b = species_bits(w);
+    if (b >= ns) return false;
+    pp = row + b;
+    return true;
+}
+
+// one near pair: compensated separation, squared distance and LJ value;
+// WRAP = false when no particle of the warp can see a neighbour across the
+// box: then rint(s/L) = 0 for every pair and the minimum-image arithmetic is
+// skipped without changing any result
+template <int TR, bool AUX, bool WRAP>
+__device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A)
+{
+    const float sx = __fsub_rn(ri.x, rj.x);
+    const float sy = __fsub_rn(ri.y, rj.y);
+    const float sz = __fsub_rn(ri.z, rj.z);
+    const float dx = WRAP ? min_image(sx, P.L[0], P.Linv[0]) : sx;
+    const float dy = WRAP ? min_image(sy, P.L[1], P.Linv[1]) : sy;
+    const float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
+    const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
+    const float pxy = __fadd_rn(px, py);
+    const float rr = __fadd_rn(pxy, pz);   // == rr_exact(dx, dy, dz)
+    if (!(rr < p.rr_cut)) return;
+    // dx - k L is exact (k = 0, or Sterbenz for k = +-1): the difference
+    // error is the TwoSum error of ri - rj
+    const float dxl = two_sum_err(ri.x, -rj.x, sx);
+    const float dyl = two_sum_err(ri.y, -rj.y, sy);
+    const float dzl = two_sum_err(ri.z, -rj.z, sz);
+    float rrl = __fadd_rn(__fadd_rn(__fmaf_rn(dx, dx, -px), __fmaf_rn(dy, dy, -py)), __fmaf_rn(dz, dz, -pz));
+    rrl = __fadd_rn(rrl, __fadd_rn(fast_err_pos(px, py, pxy), fast_err_pos(pxy, pz, rr)));
+    rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
+    float fval, flo, e;
+    pair_eval<TR>(p, rr, rrl, P.rri_smooth, fval, flo, e);
+    const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
+    two_sum_acc(A.fx, A.cx, tx);
+    two_sum_acc(A.fy, A.cy, ty);
+    two_sum_acc(A.fz, A.cz, tz);
+    A.cx = __fmaf_rn(flo, dx, __fmaf_rn(fval, dxl, __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx))));
+    A.cy = __fmaf_rn(flo, dy, __fmaf_rn(fval, dyl, __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty))));
+    A.cz = __fmaf_rn(flo, dz, __fmaf_rn(fval, dzl, __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz))));
+    if (AUX) {
+        A.en += e;
+        A.s0 += fval * dx * dx;
+        A.s1 += fval * dy * dy;
+        A.s2 += fval * dz * dz;
+        A.s3 += fval * dx * dy;
+        A.s4 += fval * dx * dz;
+        A.s5 += fval * dy * dz;
     }
 }
 
-// far part of the list: entry k at list position cap-1-k (stored from the
-// back), lane q walks its own lane column backwards
-template <int W, int TRX, bool AUX, bool WRAP>
-__device__ __forceinline__ void force_loop_far(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
-                                               const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
+// one far pair: plain FP32 (forces of order eps / sigma or less)
+template <int TR, bool AUX, bool WRAP>
+__device__ __forceinline__ void far_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A)
+{
+    const float sx = __fsub_rn(ri.x, rj.x);
+    const float sy = __fsub_rn(ri.y, rj.y);
+    const float sz = __fsub_rn(ri.z, rj.z);
+    float dx = WRAP ? min_image(sx, P.L[0], P.Linv[0]) : sx;
+    float dy = WRAP ? min_image(sy, P.L[1], P.Linv[1]) : sy;
+    float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
+    float rr = rr_exact(dx, dy, dz);
+    if (!(rr < p.rr_cut)) return;
+    if (WRAP) {
+        // across the box ri - rj is of order L and its rounding error (up to
+        // ulp(L)/2) would dominate the separation error: add the TwoSum error
+        // back (the cut-off decision above keeps the rounded rr of the list
+        // criterion)
+        dx = __fadd_rn(dx, two_sum_err(ri.x, -rj.x, sx));
+        dy = __fadd_rn(dy, two_sum_err(ri.y, -rj.y, sy));
+        dz = __fadd_rn(dz, two_sum_err(ri.z, -rj.z, sz));
+        rr = rr_exact(dx, dy, dz);
+    }
+    float fval, e;
+    pair_eval_fast<TR>(p, rr, P.rri_smooth, fval, e);
+    A.gx = __fmaf_rn(fval, dx, A.gx);
+    A.gy = __fmaf_rn(fval, dy, A.gy);
+    A.gz = __fmaf_rn(fval, dz, A.gz);
+    if (AUX) {
+        A.en += e;
+        A.s0 += fval * dx * dx;
+        A.s1 += fval * dy * dy;
+        A.s2 += fval * dz * dz;
+        A.s3 += fval * dx * dy;
+        A.s4 += fval * dx * dz;
+        A.s5 += fval * dy * dz;
+    }
+}
+
+// E list entries per lane and block, read with one vector load
+template <int E> struct IdxVec;
+template <> struct IdxVec<1> { using T = uint32_t; };
+template <> struct IdxVec<2> { using T = uint2; };
+template <> struct IdxVec<4> { using T = uint4; };
+__device__ __forceinline__ uint32_t idx_at(uint32_t v, int) { return v; }
+__device__ __forceinline__ uint32_t idx_at(uint2 v, int e) { return e == 0 ? v.x : v.y; }
+__device__ __forceinline__ uint32_t idx_at(uint4 v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
+
+// The list is stored in blocks of LB = W * E entries: entry k of slot i at
+// ((k/LB)*S + i)*LB + k%LB, near entries from the front of the list, far
+// entries from its back (entry k of the far part at list position cap-1-k).
+// Lane q of the W lanes of a particle takes the E consecutive entries
+// [q*E, q*E + E) of every block with one E-wide load, so a warp reads
+// contiguous memory and each lane has E independent position gathers in
+// flight.  Entries past the count are never dereferenced (the lane gathers
+// its own position instead).
+template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR>
+__device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
+                                             const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
 {
     constexpr bool NS1 = TRX >= ONE_SPECIES;
     constexpr int TR = TRX & (ONE_SPECIES - 1);
-    const size_t bstride = (size_t)d.S * W;
-    const uint32_t* lst = d.nbr + (size_t)(d.nbr_cap / W - 1) * bstride + (size_t)i * W + (W - 1 - q);
+    constexpr uint32_t LB = W * E;
+    using V = typename IdxVec<E>::T;
+    const size_t bstride = (size_t)d.S;   // in V units: S * LB entries per block row / E
+    const V* lst = reinterpret_cast<const V*>(d.nbr + (size_t)i * LB + q * E);
+    if (FAR) lst += (size_t)(d.nbr_cap / LB - 1) * bstride * W;
+    const ptrdiff_t step = FAR ? -(ptrdiff_t)(bstride * W) : (ptrdiff_t)(bstride * W);
     const uint32_t ns = P.ns;
-    const float Lx = P.L[0], Ly = P.L[1], Lz = P.L[2];
-    const float Ix = P.Linv[0], Iy = P.Linv[1], Iz = P.Linv[2];
-    const float rri_smooth = P.rri_smooth;
     const PairParam* row = spp + a * ns;
     PairParam p1;
     if (NS1) p1 = spp[0];
-#pragma unroll 2
-    for (uint32_t k = q; k < cnt; k += W, lst -= bstride) {
-        const uint32_t j = __ldg(lst);
-        const float4 rj = __ldg(d.pos + j);
-        const float sx = __fsub_rn(ri.x, rj.x);
-        const float sy = __fsub_rn(ri.y, rj.y);
-        const float sz = __fsub_rn(ri.z, rj.z);
-        const float dx = WRAP ? min_image(sx, Lx, Ix) : sx;
-        const float dy = WRAP ? min_image(sy, Ly, Iy) : sy;
-        const float dz = WRAP ? min_image(sz, Lz, Iz) : sz;
-        const float rr = rr_exact(dx, dy, dz);
-        const PairParam* pp;
-        if (NS1) {
-            pp = &p1;
-        } else {
-            const uint32_t b = species_bits(rj.w);
-            if (b >= ns) continue;
-            pp = row + b;
+    const uint32_t nblk = (cnt + LB - 1) / LB;
+    for (uint32_t b = 0; b < nblk; ++b, lst += step) {
+        const V jv = __ldg(lst);
+        float4 rj[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t o = q * E + e;
+            const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
+            rj[e] = __ldg(d.pos + (k < cnt ? idx_at(jv, e) : i));
         }
-        const PairParam& p = *pp;
-        if (!(rr < p.rr_cut)) continue;
-        float fval, e;
-        if (WRAP) {
-            // across the box ri - rj is of order L and its rounding error
-            // (up to ulp(L)/2) would dominate the separation error: add the
-            // TwoSum error back (the cut-off decision above keeps the
-            // rounded rr of the list criterion)
-            const float ex = __fadd_rn(dx, two_sum_err(ri.x, -rj.x, sx));
-            const float ey = __fadd_rn(dy, two_sum_err(ri.y, -rj.y, sy));
-            const float ez = __fadd_rn(dz, two_sum_err(ri.z, -rj.z, sz));
-            pair_eval_fast<TR>(p, rr_exact(ex, ey, ez), rri_smooth, fval, e);
-            A.gx = __fmaf_rn(fval, ex, A.gx);
-            A.gy = __fmaf_rn(fval, ey, A.gy);
-            A.gz = __fmaf_rn(fval, ez, A.gz);
-            if (AUX) {
-                A.en += e;
-                A.s0 += fval * ex * ex;
-                A.s1 += fval * ey * ey;
-                A.s2 += fval * ez * ez;
-                A.s3 += fval * ex * ey;
-                A.s4 += fval * ex * ez;
-                A.s5 += fval * ey * ez;
-            }
-            continue;
-        }
-        pair_eval_fast<TR>(p, rr, rri_smooth, fval, e);
-        A.gx = __fmaf_rn(fval, dx, A.gx);
-        A.gy = __fmaf_rn(fval, dy, A.gy);
-        A.gz = __fmaf_rn(fval, dz, A.gz);
-        if (AUX) {
-            A.en += e;
-            A.s0 += fval * dx * dx;
-            A.s1 += fval * dy * dy;
-            A.s2 += fval * dz * dz;
-            A.s3 += fval * dx * dy;
-            A.s4 += fval * dx * dz;
-            A.s5 += fval * dy * dz;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t o = q * E + e;
+            const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
+            const PairParam* pp;
+            if (k >= cnt || !pair_of<NS1>(row, p1, ns, rj[e].w, pp)) continue;
+            if (FAR) far_pair<TR, AUX, WRAP>(*pp, P, ri, rj[e], A);
+            else near_pair<TR, AUX, WRAP>(*pp, P, ri, rj[e], A);
         }
     }
 }
@@ -473,12 +475,13 @@ __device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_
                                                bool wrap, const SysParam& P, const PairParam* spp, float4 ri,
                                                uint32_t a, ForceAcc& A)
 {
+    constexpr int E = list_block(W) / W;
     if (wrap) {
-        force_loop<W, TR, AUX, true>(d, i, q, nn, P, spp, ri, a, A);
-        force_loop_far<W, TR, AUX, true>(d, i, q, nf, P, spp, ri, a, A);
+        force_blocks<W, E, TR, AUX, true, false>(d, i, q, nn, P, spp, ri, a, A);
+        force_blocks<W, E, TR, AUX, true, true>(d, i, q, nf, P, spp, ri, a, A);
     } else {
-        force_loop<W, TR, AUX, false>(d, i, q, nn, P, spp, ri, a, A);
-        force_loop_far<W, TR, AUX, false>(d, i, q, nf, P, spp, ri, a, A);
+        force_blocks<W, E, TR, AUX, false, false>(d, i, q, nn, P, spp, ri, a, A);
+        force_blocks<W, E, TR, AUX, false, true>(d, i, q, nf, P, spp, ri, a, A);
     }
     // fold the plain far-pair sums into the compensated accumulators
     two_sum_acc(A.fx, A.cx, A.gx);
