@@ -395,6 +395,8 @@ def run_phases(args, w):
     eng = make_engine(w, L)
     if args.force_lanes:
         eng.set_option("force_lanes", args.force_lanes)
+    if args.neighbour_scan:
+        eng.set_option("neighbour_scan", args.neighbour_scan)
     eng.set("species", species)
     eng.set("position", r)
     if w["nspecies"] == 2:
@@ -439,6 +441,8 @@ def main():
     ap.add_argument("--force-lanes", type=int, default=0,
                     help="threads per particle in the force kernel (0: autotune in the bench, engine default "
                          "in --phases)")
+    ap.add_argument("--neighbour-scan", type=int, default=0,
+                    help="list build: 0 auto, 1 per lane, 2 shared per warp")
     ap.add_argument("--serve-jobs", type=int, default=200)
     ap.add_argument("--serve-steps-scale", type=float, default=0.1)
     ap.add_argument("--serve-max-slots", type=int, default=1 << 24)
@@ -470,6 +474,8 @@ def main():
 
     r, v, species, L = initial_state(w, seed=2024 + rank)
     eng = make_engine(w, L, seed=7 + rank)
+    if args.neighbour_scan:
+        eng.set_option("neighbour_scan", args.neighbour_scan)
     n = w["n"]
     eng.set("species", species)
     eng.set("position", r)

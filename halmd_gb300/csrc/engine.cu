@@ -576,6 +576,10 @@ Dev Engine::dev() const
     d.nbr = nbr_.p; d.nbr_count = nbr_count_.p; d.nbr_cap = nbr_cap_;
     d.lanes = lanes_;
     d.lb_log2 = list_block(lanes_) == 8u ? 3u : 2u;
+    // the shared scan does a warp's 32 particles in one serial pass over the
+    // cells around them: it pays off once there are enough warps per SM to
+    // hide that pass's latency (about 2^19 slots on 152 SMs)
+    d.nbr_shared_scan = nbr_scan_ == 2u || (nbr_scan_ == 0u && S_ >= (1u << 19));
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
     d.S = S_; d.nsys = table_size_;
@@ -877,12 +881,20 @@ void Engine::set_option(const std::string& name, int64_t value)
         forces_valid_ = false;
         return;
     }
+    if (name == "neighbour_scan") {
+        if (value < 0 || value > 2) throw Error(HMD_ERR_INVALID, "neighbour_scan must be 0 (auto), 1 (per lane) or 2 (shared)");
+        if (nbr_scan_ == (uint32_t)value) return;
+        nbr_scan_ = (uint32_t)value;
+        if (committed_) destroy_graphs();   // captured launches carry the old setting
+        return;
+    }
     throw Error(HMD_ERR_INVALID, "unknown option '" + name + "'");
 }
 
 int64_t Engine::get_option(const std::string& name) const
 {
     if (name == "force_lanes") return lanes_;
+    if (name == "neighbour_scan") return nbr_scan_;
     if (name == "neighbour_capacity") return nbr_cap_;
     if (name == "rebuild_chains") {
         uint32_t v[2];

@@ -164,6 +164,7 @@ private:
     uint32_t total_cells_ = 0;
     uint32_t nbr_cap_ = 0;
     uint32_t lanes_ = 0;        // force-kernel lanes per particle (0: choose at commit)
+    uint32_t nbr_scan_ = 0;   // list build: 0 auto, 1 per lane, 2 shared scan per warp
     int sort_passes_ = 0;       // radix passes of the segmented sort (even)
     uint32_t ntiles_ = 0;
     DevBuf<uint2> tiles_;

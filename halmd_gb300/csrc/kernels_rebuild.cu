@@ -351,21 +351,163 @@ __global__ void __launch_bounds__(128) k_cell_sort(Dev d)
 }
 
 // ---------------------------------------------------------------------------
-// full Verlet list, one thread per particle: the 27 cells around the
-// particle's cell (each distinct cell once when a dimension has fewer than
-// 3 cells), criterion rr <= (r_c + skin)^2 in float
-// (from_binning_kernel.cu:144-163), blocked layout (see Dev::nbr): near
-// pairs (closer than NEAR_SIGMA sigma) from the front, far pairs from the back.
-// Also stores r0 = r for the displacement check (max_displacement.cpp:60-72).
+// Full Verlet list (from_binning_kernel.cu:144-163): every j != i with
+// rr <= (r_c + skin)^2 in float, minimum image; blocked layout (Dev::nbr),
+// near pairs (closer than NEAR_SIGMA sigma) from the front, far pairs from
+// the back.  Also stores r0 = r for the displacement check
+// (max_displacement.cpp:60-72).
+//
+// Shared scan (Dev::nbr_shared_scan; by default engines of at least 2^19
+// slots): one
+// warp per 32 consecutive slots.  After the Hilbert sort these are
+// spatially compact, so the warp scans the cells around its bounding box
+// once for all 32 particles: lanes load 32 candidates of a cell at a time,
+// drop those farther than r_c + skin from the box, stage the rest in shared
+// memory, and every lane tests every staged candidate against its own
+// particle.  Smaller engines, and warps whose box spans too many cells (an
+// unsorted system, a tiny box), scan per lane instead: the 27 cells around each particle (each
+// distinct cell once when a dimension has fewer than 3 cells).  Both scans
+// test the same float criterion, so the pair sets are identical; entries are
+// appended in cell order and, within a cell, in slot order (deterministic).
 // ---------------------------------------------------------------------------
+
+constexpr uint32_t NBR_CLUSTER_MAX_CELLS = 150;   // larger cell ranges: per-lane scan
+
+struct NbrOut {
+    uint32_t* out;        // this slot's row in the blocked list
+    size_t bstride;       // words between list blocks
+    uint32_t lw, lmask;   // log2 of the block width, width - 1
+    uint32_t cap;
+    uint32_t nn = 0, nf = 0;
+    __device__ __forceinline__ void add(uint32_t j, bool near)
+    {
+        const uint32_t e = near ? nn : cap - 1u - nf;
+        if (nn + nf < cap) out[(e >> lw) * bstride + (e & lmask)] = j;
+        if (near) ++nn; else ++nf;
+    }
+};
+
+template <bool WRAP>
+__device__ __forceinline__ void nbr_test(const SysParam& P, float4 ri, uint32_t i, float4 rj, uint32_t j,
+                                         const float* rrcs, const float* rrnear, NbrOut& o)
+{
+    if (j == i) return;
+    const float sx = __fsub_rn(ri.x, rj.x), sy = __fsub_rn(ri.y, rj.y), sz = __fsub_rn(ri.z, rj.z);
+    // without a wrap every |s| < L/2, where min_image returns s unchanged
+    const float dx = WRAP ? min_image(sx, P.L[0], P.Linv[0]) : sx;
+    const float dy = WRAP ? min_image(sy, P.L[1], P.Linv[1]) : sy;
+    const float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
+    const float rr = rr_exact(dx, dy, dz);
+    const uint32_t b = species_bits(rj.w);
+    if (b < P.ns && rr <= rrcs[b]) o.add(j, rr < rrnear[b]);
+}
+
+// the 27 cells around the particle, for one lane
+__device__ __forceinline__ void lane_scan(const Dev& d, const SysParam& P, float4 ri, uint32_t i, const float* rrcs,
+                                          const float* rrnear, NbrOut& o)
+{
+    int cx, cy, cz;
+    cell_coords(P, ri, cx, cy, cz);
+    const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
+    const int lox = nx >= 3 ? -1 : 0, hix = nx >= 2 ? 1 : 0;
+    const int loy = ny >= 3 ? -1 : 0, hiy = ny >= 2 ? 1 : 0;
+    const int loz = nz >= 3 ? -1 : 0, hiz = nz >= 2 ? 1 : 0;
+    const uint32_t cs = P.cell_size;
+    for (int oz = loz; oz <= hiz; ++oz) {
+        const int z = (cz + oz + nz) % nz;
+        for (int oy = loy; oy <= hiy; ++oy) {
+            const int y = (cy + oy + ny) % ny;
+            for (int ox = lox; ox <= hix; ++ox) {
+                const int x = (cx + ox + nx) % nx;
+                const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
+                // occupied slots of the cell (ascending), four at a time so the
+                // position gathers are independent of one another
+                const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
+                const uint4* cell4 = reinterpret_cast<const uint4*>(d.cell + P.cell_word_off + c * cs);
+                for (uint32_t k = 0; k < nc; k += 4) {
+                    const uint4 jj = __ldg(cell4 + (k >> 2));
+                    const uint32_t jv[4] = {jj.x, jj.y, jj.z, jj.w};
+                    float4 rv[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) rv[u] = (k + u < nc) ? __ldg(d.pos + jv[u]) : make_float4(0, 0, 0, 0);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (k + u < nc) nbr_test<true>(P, ri, i, rv[u], jv[u], rrcs, rrnear, o);
+                }
+            }
+        }
+    }
+}
+
+// the cells around the warp's bounding box [lo, hi] (cell ranges c0 + [0, nc)
+// per dimension, wrapped), for all lanes at once
+template <bool WRAP>
+__device__ __forceinline__ void cluster_scan(const Dev& d, const SysParam& P, float4 ri, uint32_t i, bool real,
+                                             const float* rrcs, const float* rrnear, NbrOut& o, const float* lo,
+                                             const float* hi, const int* c0, const int* ncr, float rcs2,
+                                             float4* s_pos, uint32_t* s_j, uint32_t lane)
+{
+    const float cxb = 0.5f * (lo[0] + hi[0]), cyb = 0.5f * (lo[1] + hi[1]), czb = 0.5f * (lo[2] + hi[2]);
+    const float hxb = 0.5f * (hi[0] - lo[0]), hyb = 0.5f * (hi[1] - lo[1]), hzb = 0.5f * (hi[2] - lo[2]);
+    const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
+    const uint32_t cs = P.cell_size;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    for (int kz = 0; kz < ncr[2]; ++kz) {
+        const int z = (c0[2] + kz) % nz;
+        for (int ky = 0; ky < ncr[1]; ++ky) {
+            const int y = (c0[1] + ky) % ny;
+            for (int kx = 0; kx < ncr[0]; ++kx) {
+                const int x = (c0[0] + kx) % nx;
+                const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
+                const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
+                const uint32_t* cell = d.cell + P.cell_word_off + c * cs;
+                for (uint32_t k = 0; k < nc; k += 32) {
+                    const bool have = k + lane < nc;
+                    const uint32_t j = have ? __ldg(cell + k + lane) : 0u;
+                    const float4 rj = have ? __ldg(d.pos + j) : make_float4(0, 0, 0, 0);
+                    bool keep = false;
+                    if (have) {
+                        // distance from the candidate to the bounding box
+                        float ex = __fsub_rn(rj.x, cxb), ey = __fsub_rn(rj.y, cyb), ez = __fsub_rn(rj.z, czb);
+                        if (WRAP) {
+                            ex = min_image(ex, P.L[0], P.Linv[0]);
+                            ey = min_image(ey, P.L[1], P.Linv[1]);
+                            ez = min_image(ez, P.L[2], P.Linv[2]);
+                        }
+                        const float qx = fmaxf(fabsf(ex) - hxb, 0.0f);
+                        const float qy = fmaxf(fabsf(ey) - hyb, 0.0f);
+                        const float qz = fmaxf(fabsf(ez) - hzb, 0.0f);
+                        keep = qx * qx + qy * qy + qz * qz <= rcs2;
+                    }
+                    const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, keep);
+                    if (keep) {
+                        const uint32_t at = __popc(ballot & lt_mask);
+                        s_pos[at] = rj;
+                        s_j[at] = j;
+                    }
+                    __syncwarp();
+                    const uint32_t nk = __popc(ballot);
+                    if (real) {
+#pragma unroll 4
+                        for (uint32_t u = 0; u < nk; ++u) nbr_test<WRAP>(P, ri, i, s_pos[u], s_j[u], rrcs, rrnear, o);
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+    }
+}
 
 __global__ void __launch_bounds__(128) k_neighbour(Dev d)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t s = d.chunk_sys[i / CHUNK];
     const SysParam& P = d.sys[s];
     __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
     __shared__ float s_rrnear[MAX_SPECIES * MAX_SPECIES];
+    __shared__ float4 s_pos[4][32];
+    __shared__ uint32_t s_j[4][32];
     if (threadIdx.x < P.ns * P.ns) {
         s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
         s_rrnear[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_near;
@@ -374,72 +516,76 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
     if (!(P.active && d.st[s].rebuild)) return;   // block-uniform
     const float4 ri = d.pos[i];
     const uint32_t a = species_bits(ri.w);
-    uint32_t count = 0;
-    uint32_t nn = 0, nf = 0;   // near entries from the front, far entries from the back
-    if (a != PLACEHOLDER) {
-        d.r0[i] = ri;
-        int cx, cy, cz;
-        cell_coords(P, ri, cx, cy, cz);
-        const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
-        const int lox = nx >= 3 ? -1 : 0, hix = nx >= 2 ? 1 : 0;
-        const int loy = ny >= 3 ? -1 : 0, hiy = ny >= 2 ? 1 : 0;
-        const int loz = nz >= 3 ? -1 : 0, hiz = nz >= 2 ? 1 : 0;
-        const uint32_t cs = P.cell_size;
-        const uint32_t cap = d.nbr_cap;
-        const uint32_t lw = d.lb_log2, lmask = (1u << lw) - 1u;
-        const size_t bstride = (size_t)d.S << lw;
-        uint32_t* out = d.nbr + ((size_t)i << lw);
-        const float* rrcs = s_rrcs + a * P.ns;
-        const float* rrnear = s_rrnear + a * P.ns;
-        for (int oz = loz; oz <= hiz; ++oz) {
-            const int z = (cz + oz + nz) % nz;
-            for (int oy = loy; oy <= hiy; ++oy) {
-                const int y = (cy + oy + ny) % ny;
-                for (int ox = lox; ox <= hix; ++ox) {
-                    const int x = (cx + ox + nx) % nx;
-                    const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
-                    // occupied slots of the cell (ascending); read four at a time
-                    // so the position gathers are independent of one another
-                    const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
-                    const uint4* cell4 = reinterpret_cast<const uint4*>(d.cell + P.cell_word_off + c * cs);
-                    for (uint32_t k = 0; k < nc; k += 4) {
-                        const uint4 jj = __ldg(cell4 + (k >> 2));
-                        const uint32_t jv[4] = {jj.x, jj.y, jj.z, jj.w};
-                        float4 rv[4];
+    const bool real = a != PLACEHOLDER;
+    NbrOut o;
+    o.lw = d.lb_log2;
+    o.lmask = (1u << o.lw) - 1u;
+    o.bstride = (size_t)d.S << o.lw;
+    o.out = d.nbr + ((size_t)i << o.lw);
+    o.cap = d.nbr_cap;
+    const float* rrcs = s_rrcs + (real ? a : 0u) * P.ns;
+    const float* rrnear = s_rrnear + (real ? a : 0u) * P.ns;
+    if (real) d.r0[i] = ri;
+    // bounding box of the warp's real particles
+    float lo[3] = {real ? ri.x : INFINITY, real ? ri.y : INFINITY, real ? ri.z : INFINITY};
+    float hi[3] = {real ? ri.x : -INFINITY, real ? ri.y : -INFINITY, real ? ri.z : -INFINITY};
 #pragma unroll
-                        for (int u = 0; u < 4; ++u)
-                            rv[u] = (k + u < nc) ? __ldg(d.pos + jv[u]) : make_float4(0, 0, 0, 0);
+    for (int q = 0; q < 3; ++q) {
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const uint32_t j = jv[u];
-                            if (k + u >= nc || j == i) continue;
-                            const float4 rj = rv[u];
-                            const float dx = min_image(__fsub_rn(ri.x, rj.x), P.L[0], P.Linv[0]);
-                            const float dy = min_image(__fsub_rn(ri.y, rj.y), P.L[1], P.Linv[1]);
-                            const float dz = min_image(__fsub_rn(ri.z, rj.z), P.L[2], P.Linv[2]);
-                            const float rr = rr_exact(dx, dy, dz);
-                            const uint32_t b = species_bits(rj.w);
-                            if (b < P.ns && rr <= rrcs[b]) {
-                                const bool near = rr < rrnear[b];
-                                const uint32_t e = near ? nn : cap - 1u - nf;
-                                if (nn + nf < cap) out[(e >> lw) * bstride + (e & lmask)] = j;
-                                if (near) ++nn; else ++nf;
-                            }
-                        }
-                    }
-                }
-            }
+        for (int w = 16; w > 0; w >>= 1) {
+            lo[q] = fminf(lo[q], __shfl_xor_sync(0xFFFFFFFFu, lo[q], w));
+            hi[q] = fmaxf(hi[q], __shfl_xor_sync(0xFFFFFFFFu, hi[q], w));
         }
-        count = nn + nf;
-        const uint32_t sn = min(nn, cap);
-        const uint32_t sf = min(nf, cap - sn);   // stored regions never overlap
+    }
+    if (__any_sync(0xFFFFFFFFu, real)) {
+        float rcs2 = 0.0f;
+        for (uint32_t q = 0; q < P.ns * P.ns; ++q) rcs2 = fmaxf(rcs2, s_rrcs[q]);
+        const float rcs = sqrtf(rcs2) * (1.0f + 1e-4f);   // margin: a superset of the cells is harmless
+        // cell range per dimension, with the binning's own float formula (monotonic in x)
+        int c0[3], ncr[3];
+        bool wrap = false;
+        uint32_t ncells = 1;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int n = P.ncell[q];
+            float ul = __fadd_rn(__fdiv_rn(__fsub_rn(lo[q], rcs), P.cell_len[q]), (float)n);
+            float uh = __fadd_rn(__fdiv_rn(__fadd_rn(hi[q], rcs), P.cell_len[q]), (float)n);
+            // positions lie in [-L/2, L/2]: u in [n/2 - 1, 3n/2 + 1]; the clamp only
+            // guards the integer conversion against non-finite positions
+            ul = fminf(fmaxf(ul, 0.0f), 4.0f * n);
+            uh = fminf(fmaxf(uh, 0.0f), 4.0f * n);
+            const int a0 = (int)floorf(ul), a1 = (int)floorf(uh);
+            if (!(a1 >= a0) || a1 - a0 + 1 >= n) { c0[q] = 0; ncr[q] = n; }
+            else { c0[q] = a0 % n; ncr[q] = a1 - a0 + 1; }
+            ncells *= (uint32_t)ncr[q];
+            const float half = 0.5f * P.L[q];
+            // no pair of the scan reaches |s| >= L/2 and no cell range crosses the box
+            wrap |= !(__fsub_rn(lo[q], rcs) > -half && __fadd_rn(hi[q], rcs) < half &&
+                      (hi[q] - lo[q]) + 2.0f * rcs < 0.49f * P.L[q]);
+        }
+        if (d.nbr_shared_scan && ncells <= NBR_CLUSTER_MAX_CELLS) {
+            if (wrap)
+                cluster_scan<true>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos[warp],
+                                   s_j[warp], lane);
+            else
+                cluster_scan<false>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos[warp],
+                                    s_j[warp], lane);
+        } else if (real) {
+            lane_scan(d, P, ri, i, rrcs, rrnear, o);
+        }
+    }
+    uint32_t count = 0;
+    if (real) {
+        count = o.nn + o.nf;
+        const uint32_t sn = min(o.nn, o.cap);
+        const uint32_t sf = min(o.nf, o.cap - sn);   // stored regions never overlap
         d.nbr_count[i] = sn | (sf << 16);
     }
     // warp-aggregated maximum and overflow flag (all lanes of the warp are here)
     uint32_t m = count;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
-    if ((threadIdx.x & 31u) == 0) {
+    for (int w = 16; w > 0; w >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, w));
+    if (lane == 0) {
         if (m > 0) atomicMax(&d.st[s].max_nbr, m);
         if (m > d.nbr_cap) atomicOr(d.status, ST_NBR_OVERFLOW);
     }

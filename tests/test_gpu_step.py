@@ -117,12 +117,28 @@ def test_ka_smooth_r4_force_parity():
     eng.close()
 
 
-@pytest.mark.parametrize("make", ["lj", "ka"])
-def test_neighbour_lists_bit_exact(make):
+@pytest.mark.parametrize("scan", [1, 2])
+@pytest.mark.parametrize("make", ["lj", "ka", "lj_large", "ka_large", "lj_unsorted"])
+def test_neighbour_lists_bit_exact(make, scan):
+    # both list-build scans (per lane, shared per warp) on small boxes (3 cells
+    # per dimension: every warp wraps), large boxes (interior warps scan
+    # without minimum image) and an unsorted system (warps too spread out for
+    # the shared scan: it falls back to the per-lane scan)
     if make == "lj":
         eng, r, v, L = lj_engine()
+    elif make == "lj_large":
+        eng, r, v, L = lj_engine(ncell=16)
+    elif make == "lj_unsorted":
+        eng, r, v, L = lj_engine(ncell=12, sort=0)
+        perm = np.random.default_rng(3).permutation(r.shape[0])   # slots in random spatial order
+        eng.set("position", r[perm])
+        eng.set("velocity", v[perm])
+    elif make == "ka_large":
+        eng, r, v, sp, L = ka_engine(ncell=14)
     else:
         eng, r, v, sp, L = ka_engine()
+    eng.set_option("neighbour_scan", scan)
+    eng.request_rebuild()
     eng.force()
     inf = eng.info()
     ns = inf.nspecies
