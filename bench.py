@@ -133,6 +133,19 @@ class ClockSampler:
                 "samples": len(rows), "reasons": sorted(reasons)}
 
 
+def dram_traffic(workload):
+    """DRAM bytes per force launch from the committed ncu capture of this workload, or None."""
+    path = os.path.join(REPO, "profiles", "dram_traffic.json")
+    try:
+        with open(path) as fh:
+            rec = json.load(fh).get(workload)
+    except (OSError, ValueError):
+        return None, None
+    if not rec:
+        return None, None
+    return float(rec["dram_bytes_per_launch"]), rec["from"]
+
+
 def peaks():
     try:
         with open(MEASURED) as fh:
@@ -560,6 +573,7 @@ def main():
     bytes_per_launch = n * (16 + 4 * K_l + 16)
     achieved = bytes_per_launch / (f_ms / f_cnt * 1e-3) / 1e9
     peak, peak_kind = peaks()
+    traffic_bytes, traffic_from = dram_traffic(w["name"])
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -580,7 +594,8 @@ def main():
                             "hmd_get(position, velocity)" % M},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": "k_force",
+                         "frac": achieved / peak, "traffic": traffic_bytes, "traffic_unit": "bytes per launch",
+                         "traffic_from": traffic_from, "kernel": "k_force",
                          "peak_source": peak_kind,
                          "bytes_per_launch": bytes_per_launch, "mean_list_length": K_l,
                          "force_ms": f_ms / f_cnt},
