@@ -176,7 +176,7 @@ def system_desc(nparticle, box, epsilon=1.0, sigma=1.0, r_cut=2.5, truncation="s
     def mat(x):
         m = np.asarray(x, dtype=np.float64)
         if m.size == 1:
-            m = np.full((ns, ns), float(m))
+            m = np.full((ns, ns), float(m.reshape(-1)[0]))
         return m.reshape(ns, ns)
     eps, sig, rc = mat(epsilon), mat(sigma), mat(r_cut)
     d.nparticle = int(nparticle)

@@ -1,0 +1,461 @@
+"""Module-style front end with the names, keyword arguments and defaults of the
+reference's Lua API for the MD step, over the engine's C ABI.
+
+    from halmd_gb300 import halmd
+    box = halmd.mdsim.box(length=[L, L, L])
+    particle = halmd.mdsim.particle(dimension=3, particles=n, species=2)
+    particle.data["species"] = species
+    particle.data["position"] = r
+    potential = halmd.mdsim.potentials.pair.lennard_jones(
+        epsilon=[[1, 1.5], [1.5, 0.5]], sigma=[[1, 0.8], [0.8, 0.88]]).truncate("smooth_r4", cutoff=2.5, h=0.005)
+    force = halmd.mdsim.forces.pair(box=box, particle=particle, potential=potential, neighbour={"skin": 0.3})
+    integrator = halmd.mdsim.integrators.verlet_nvt_andersen(
+        box=box, particle=particle, timestep=0.002, temperature=0.7, rate=1)
+    thermo = halmd.observables.thermodynamics(box=box, group=particle)
+    halmd.observables.sampler.run(1000)
+    print(thermo.potential_energy(), thermo.temperature())
+
+Lua tables become Python keywords, or a dict with the same keys.  A
+positional first entry, as in `truncate({"smooth_r4", cutoff = 2.5, h = 0.005})`,
+becomes the first positional argument.  The modules mirror:
+
+    lua/halmd/mdsim/box.lua.in                 box{length | edges}
+    lua/halmd/mdsim/particle.lua.in:63-68      particle{dimension, particles, species=1, precision, label="all"}
+    lua/halmd/mdsim/potentials/pair/lennard_jones.lua.in:56-60
+                                               lennard_jones{epsilon=1, sigma=1, species}
+    .../adapters/truncate.lua.in:287-305       :truncate{kind="shifted", cutoff, h}
+    lua/halmd/mdsim/neighbour.lua.in:88-102    neighbour{skin=0.5, occupancy, disable_sorting}
+    lua/halmd/mdsim/forces/pair.lua.in:36-40   forces.pair{box, particle, potential, neighbour}
+    lua/halmd/mdsim/integrators/verlet.lua.in:57-59, verlet_nvt_andersen.lua.in:52-56
+    lua/halmd/observables/thermodynamics.lua.in:60-130 (formulas)
+    lua/halmd/observables/sampler.lua.in        sampler.run(steps), sampler.on_sample(fn, every)
+    lua/halmd/observables/dynamics/*.lua.in     blocking_scheme, mean_square_displacement,
+                                               intermediate_scattering_function
+
+All modules of one script share one engine, committed when the simulation
+first needs the device (the first `sampler.run` or read of device data).
+Several `particle` instances become independent systems of that engine and
+advance together.  `reset()` starts a new script.
+"""
+import numpy as np
+
+from ._lib import Dynamics, Engine, system_desc
+
+
+def _args(args, kw):
+    out = dict(args or {})
+    out.update(kw)
+    return out
+
+
+class _Script:
+    """The modules of one script and the engine they share."""
+
+    def __init__(self):
+        self.particles = []
+        self.engine = None
+        self.observers = []          # (every, fn) called after steps that are multiples of every
+        self.blocking = []
+        self.step = 0
+
+    def committed(self):
+        return self.engine is not None
+
+    def commit(self):
+        if self.engine is not None:
+            return self.engine
+        if not self.particles:
+            raise RuntimeError("no particle instance")
+        precisions = {p.precision for p in self.particles}
+        if len(precisions) != 1:
+            raise ValueError("all particle instances of a script share one precision")
+        eng = Engine("dsfloat" if precisions.pop() == "double-single" else "float")
+        for p in self.particles:
+            p._index = eng.add_system(p._desc())
+        eng.commit()
+        for p in self.particles:
+            for name in ("species", "mass", "position", "image", "velocity"):
+                if name in p._pending:
+                    eng.set(name, p._pending[name], p._index)
+            p._pending.clear()
+        self.engine = eng
+        for b in self.blocking:
+            b._attach()
+        return eng
+
+
+_script = _Script()
+
+
+def reset():
+    """Forget every module; the next ones form a new script (a new engine)."""
+    global _script
+    if _script.engine is not None:
+        for b in _script.blocking:
+            b._close()
+        _script.engine.close()
+    _script = _Script()
+
+
+class _Namespace:
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+# ---- mdsim ------------------------------------------------------------------
+
+class box:
+    """halmd.mdsim.box{length = {Lx, Ly, Lz}} (or diagonal `edges`)."""
+
+    def __init__(self, args=None, **kw):
+        a = _args(args, kw)
+        if "length" in a:
+            self.length = [float(x) for x in a["length"]]
+        elif "edges" in a:
+            e = np.asarray(a["edges"], dtype=float)
+            if np.count_nonzero(e - np.diag(np.diagonal(e))):
+                raise ValueError("only cuboid boxes are supported")
+            self.length = list(np.diagonal(e))
+        else:
+            raise ValueError("box: missing argument 'length' or 'edges'")
+        if len(self.length) != 3:
+            raise ValueError("box: 3 edge lengths expected")
+
+    @property
+    def volume(self):
+        return float(np.prod(self.length))
+
+
+class _Data:
+    def __init__(self, particle):
+        self._p = particle
+
+    def __getitem__(self, name):
+        return self._p.get(name)
+
+    def __setitem__(self, name, value):
+        self._p.set(name, value)
+
+    def __getattr__(self, name):
+        return self._p.get(name)
+
+
+class particle:
+    """halmd.mdsim.particle{dimension, particles, species = 1, precision, label = "all"}."""
+
+    def __init__(self, args=None, **kw):
+        a = _args(args, kw)
+        if int(a.get("dimension", 3)) != 3:
+            raise ValueError("unsupported space dimension: '%d'" % int(a["dimension"]))
+        self.nparticle = int(a["particles"])
+        self.nspecies = int(a.get("species", 1))
+        self.precision = a.get("precision", "double-single")
+        if self.precision not in ("double-single", "single"):
+            raise ValueError("unsupported floating-point precision: '%s'" % self.precision)
+        self.label = a.get("label", "all")
+        self.memory = "gpu"
+        self.data = _Data(self)
+        self._pending = {}
+        self._index = None
+        self._box = self._potential = self._neighbour = self._integrator = None
+        _script.particles.append(self)
+
+    def set(self, name, value):
+        value = np.asarray(value)
+        if _script.committed():
+            _script.engine.set(name, value, self._index)
+        else:
+            self._pending[name] = value
+
+    def get(self, name):
+        if not _script.committed() and name in self._pending:
+            return self._pending[name]
+        return _script.commit().get(name, self._index)
+
+    def _desc(self):
+        if self._box is None or self._potential is None or self._integrator is None:
+            raise RuntimeError("particle '%s' needs a box, a pair force and an integrator" % self.label)
+        pot, nb, integ = self._potential, self._neighbour or {}, self._integrator
+        kw = dict(epsilon=pot.epsilon, sigma=pot.sigma, r_cut=pot.cutoff, truncation=pot.kind,
+                  skin=nb.get("skin", 0.5), timestep=integ.timestep, integrator=integ.kind,
+                  sort=not nb.get("disable_sorting", False))
+        if pot.kind == "smooth_r4":
+            kw["smoothing"] = pot.h
+        if nb.get("occupancy") is not None:
+            kw["neighbour_occupancy"] = nb["occupancy"]
+        if integ.kind == "andersen":
+            kw.update(temperature=integ.temperature, collision_rate=integ.rate, seed=integ.seed)
+        return system_desc(self.nparticle, self._box.length, nspecies=self.nspecies, **kw)
+
+
+class _Potential:
+    def __init__(self, epsilon, sigma, species):
+        self.epsilon, self.sigma, self.species = epsilon, sigma, species
+        self.kind, self.cutoff, self.h = None, None, None
+
+    def truncate(self, args=None, **kw):
+        """:truncate{kind = "shifted", cutoff, h} (truncate.lua.in:287-305)."""
+        if isinstance(args, str):
+            args = {1: args}
+        a = _args(args, kw)
+        if "cutoff" not in a:
+            raise ValueError("missing keyword argument 'cutoff'")
+        kind = a.get(1, a.get("kind", "shifted"))
+        if kind not in ("sharp", "shifted", "smooth_r4", "force_shifted"):
+            raise ValueError("invalid truncation type '%s'" % kind)
+        out = _Potential(self.epsilon, self.sigma, self.species)
+        out.kind, out.cutoff = kind, a["cutoff"]
+        if kind == "smooth_r4":
+            if "h" not in a:
+                raise ValueError("missing keyword argument 'h'")
+            out.h = float(a["h"])
+        return out
+
+    @property
+    def r_cut(self):
+        return self.cutoff
+
+
+def lennard_jones(args=None, **kw):
+    """halmd.mdsim.potentials.pair.lennard_jones{epsilon = 1, sigma = 1, species}."""
+    a = _args(args, kw)
+    eps = np.atleast_2d(np.asarray(a.get("epsilon", 1.0), dtype=float))
+    sig = np.atleast_2d(np.asarray(a.get("sigma", 1.0), dtype=float))
+    species = int(a.get("species", max(eps.shape[0], sig.shape[0])))
+    return _Potential(eps, sig, species)
+
+
+def neighbour(args=None, **kw):
+    """halmd.mdsim.neighbour{skin = 0.5, occupancy, disable_sorting = false} (as keyword table)."""
+    return _args(args, kw)
+
+
+def pair(args=None, **kw):
+    """halmd.mdsim.forces.pair{box, particle, potential, neighbour}."""
+    a = _args(args, kw)
+    pot = a["potential"]
+    if pot.kind is None:
+        raise ValueError("untruncated pair potentials (pair_full) are not on this path: call :truncate")
+    parts = a["particle"] if isinstance(a["particle"], (list, tuple)) else [a["particle"]]
+    if len(parts) != 1:
+        raise ValueError("forces between two particle instances are not supported")
+    p = parts[0]
+    p._box, p._potential, p._neighbour = a["box"], pot, dict(a.get("neighbour") or {})
+    return _Namespace(particle=p, potential=pot)
+
+
+class _Integrator:
+    def __init__(self, kind, a):
+        if "timestep" not in a:
+            raise ValueError("missing keyword argument 'timestep'")
+        self.kind = kind
+        self.timestep = float(a["timestep"])
+        self.particle = a["particle"]
+        a["particle"]._box = a.get("box", a["particle"]._box)
+        a["particle"]._integrator = self
+        if kind == "andersen":
+            self.temperature = float(a["temperature"])
+            self.rate = float(a["rate"])
+            self.seed = int(a.get("seed", 0))
+
+
+def verlet(args=None, **kw):
+    """halmd.mdsim.integrators.verlet{box, particle, timestep}."""
+    return _Integrator("verlet", _args(args, kw))
+
+
+def verlet_nvt_andersen(args=None, **kw):
+    """halmd.mdsim.integrators.verlet_nvt_andersen{box, particle, timestep, temperature, rate}."""
+    return _Integrator("andersen", _args(args, kw))
+
+
+mdsim = _Namespace(
+    box=box, particle=particle, neighbour=neighbour,
+    potentials=_Namespace(pair=_Namespace(lennard_jones=lennard_jones)),
+    forces=_Namespace(pair=pair),
+    integrators=_Namespace(verlet=verlet, verlet_nvt_andersen=verlet_nvt_andersen),
+)
+
+
+# ---- observables -------------------------------------------------------------
+
+class thermodynamics:
+    """halmd.observables.thermodynamics{box, group}: per-particle means from the
+    FP64 device reductions (observables/thermodynamics.lua.in:60-130)."""
+
+    def __init__(self, args=None, **kw):
+        a = _args(args, kw)
+        self.box = a["box"]
+        self.group = a["group"]
+
+    def _sums(self):
+        eng = _script.commit()
+        return eng.thermo(self.group._index)
+
+    def particle_number(self):
+        return self.group.nparticle
+
+    def volume(self):
+        return self.box.volume
+
+    def density(self):
+        return self.group.nparticle / self.box.volume
+
+    def kinetic_energy(self):
+        return 0.5 * self._sums()["mv2"] / self.group.nparticle
+
+    def potential_energy(self):
+        return self._sums()["epot"] / self.group.nparticle
+
+    def internal_energy(self):
+        t = self._sums()
+        return (0.5 * t["mv2"] + t["epot"]) / self.group.nparticle
+
+    def temperature(self):
+        return 2.0 * self.kinetic_energy() / 3.0
+
+    def virial(self):
+        return self._sums()["virial"] / self.group.nparticle
+
+    def pressure(self):
+        t = self._sums()
+        n = self.group.nparticle
+        return n / self.box.volume * ((t["mv2"] / n) / 3.0 + (t["virial"] / n) / 3.0)
+
+    def center_of_mass_velocity(self):
+        t = self._sums()
+        return t["momentum"] / t["mass"]
+
+    def mean_mass(self):
+        return self._sums()["mass"] / self.group.nparticle
+
+
+class _Sampler:
+    """halmd.observables.sampler: run(steps) and on_sample(fn, every, start)."""
+
+    def on_sample(self, fn, every=1, start=0):
+        _script.observers.append((int(every), int(start), fn))
+
+    def run(self, steps):
+        eng = _script.commit()
+        steps = int(steps)
+        if _script.step == 0 and not getattr(_script, "started", False):
+            # the initial state is a sample too (sampler.lua.in: setup, then sample)
+            _script.started = True
+            eng.force(aux=True)
+            for every, start, fn in _script.observers:
+                if every and start == 0:
+                    fn()
+        stops = {steps}
+        for every, start, _ in _script.observers:
+            k = _script.step + ((start - _script.step) % every if every else 0)
+            while k <= _script.step + steps and every:
+                if k > _script.step:
+                    stops.add(k - _script.step)
+                k += every
+        for b in _script.blocking:
+            stops.update(b._stops(_script.step, steps))
+        done = 0
+        for stop in sorted(stops):
+            if stop > done:
+                eng.step(stop - done, aux_last=True)
+                done = stop
+            now = _script.step + done
+            for every, start, fn in _script.observers:
+                if every and now >= start and (now - start) % every == 0:
+                    fn()
+            for b in _script.blocking:
+                b._sample(now)
+        _script.step += steps
+
+
+sampler = _Sampler()
+
+
+class mean_square_displacement:
+    """halmd.observables.dynamics.mean_square_displacement{particle (group)}."""
+
+    def __init__(self, args=None, **kw):
+        a = _args(args, kw)
+        self.group = a.get("group", a.get("particle"))
+        self.first, self.last = int(a.get("first", 0)), int(a.get("last", self.group.nparticle))
+
+
+class intermediate_scattering_function:
+    """halmd.observables.dynamics.intermediate_scattering_function{particle, wavenumber,
+    tolerance, max_count, norm}: shells of reciprocal-lattice vectors (wavevector.cpp:40-160)."""
+
+    def __init__(self, args=None, **kw):
+        a = _args(args, kw)
+        self.group = a.get("group", a.get("particle"))
+        self.wavenumber = [float(k) for k in np.atleast_1d(a["wavenumber"])]
+        self.tolerance = float(a.get("tolerance", 0.01))
+        self.max_count = int(a.get("max_count", 7))
+        self.norm = float(a.get("norm", self.group.nparticle))
+        self.first, self.last = int(a.get("first", 0)), int(a.get("last", self.group.nparticle))
+
+
+class blocking_scheme:
+    """halmd.observables.dynamics.blocking_scheme{max_lag, every, size = 10, shift, separation,
+    correlations} (blocking_scheme.lua.in:83-93 defaults: shift = floor(sqrt(size)),
+    separation = size); `every` is the sampling interval in steps."""
+
+    def __init__(self, args=None, **kw):
+        a = _args(args, kw)
+        self.max_lag = float(a["max_lag"])
+        self.every = int(a.get("every", 1))
+        self.size = int(a.get("size", 10))
+        self.shift = int(a.get("shift", int(np.floor(np.sqrt(self.size)))))
+        self.separation = int(a.get("separation", self.size))
+        self.correlations = list(a.get("correlations", []))
+        groups = {id(c.group) for c in self.correlations}
+        if len(groups) != 1:
+            raise ValueError("blocking_scheme: correlations of one particle instance expected")
+        self.group = self.correlations[0].group
+        self._dyn = None
+        self._tcf = []
+        _script.blocking.append(self)
+        if _script.committed():
+            self._attach()
+
+    def _attach(self):
+        eng = _script.engine
+        dt = self.group._integrator.timestep
+        self._dyn = Dynamics(eng, self.max_lag, self.every * dt, block_size=self.size, shift=self.shift,
+                             separation=self.separation, s=self.group._index)
+        for c in self.correlations:
+            if isinstance(c, mean_square_displacement):
+                self._tcf.append(self._dyn.add_msd(c.first, c.last))
+            else:
+                self._tcf.append(self._dyn.add_isf(c.wavenumber, tolerance=c.tolerance, max_count=c.max_count,
+                                                   first=c.first, last=c.last, norm=c.norm))
+        self._dyn.sample()
+
+    def _stops(self, step0, steps):
+        k = ((step0 // self.every) + 1) * self.every
+        return {s - step0 for s in range(k, step0 + steps + 1, self.every)}
+
+    def _sample(self, now):
+        if self._dyn is not None and now % self.every == 0:
+            self._dyn.sample()
+
+    def finalise(self):
+        self._dyn.finalise()
+
+    def time(self):
+        return self._dyn.time()
+
+    def result(self, k):
+        """(mean, error, count) arrays [levels, size, shells] of correlation k."""
+        return self._dyn.result(self._tcf[k])
+
+    def _close(self):
+        if self._dyn is not None:
+            self._dyn.close()
+
+
+observables = _Namespace(
+    thermodynamics=thermodynamics, sampler=sampler,
+    dynamics=_Namespace(blocking_scheme=blocking_scheme, mean_square_displacement=mean_square_displacement,
+                        intermediate_scattering_function=intermediate_scattering_function),
+)

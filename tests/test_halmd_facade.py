@@ -1,0 +1,73 @@
+"""The module-style front end maps the Lua API's names and defaults onto the
+system description (no GPU: only the library's descriptor initialiser runs)."""
+import numpy as np
+import pytest
+
+from halmd_gb300 import _lib
+
+
+@pytest.fixture
+def halmd():
+    import os
+    if not os.path.exists(_lib.LIB_PATH):
+        from halmd_gb300 import build
+        build.build()
+    from halmd_gb300 import halmd as h
+    h.reset()
+    yield h
+    h.reset()
+
+
+def ka_script(halmd, n=1000, L=9.4):
+    box = halmd.mdsim.box(length=[L, L, L])
+    particle = halmd.mdsim.particle(dimension=3, particles=n, species=2)
+    pot = halmd.mdsim.potentials.pair.lennard_jones(epsilon=[[1, 1.5], [1.5, 0.5]], sigma=[[1, 0.8], [0.8, 0.88]])
+    pot = pot.truncate({1: "smooth_r4", "cutoff": 2.5, "h": 0.005})
+    halmd.mdsim.forces.pair(box=box, particle=particle, potential=pot, neighbour={"skin": 0.3})
+    halmd.mdsim.integrators.verlet_nvt_andersen(box=box, particle=particle, timestep=0.002, temperature=0.7, rate=1.0)
+    return particle
+
+
+def test_description_follows_the_modules(halmd):
+    d = ka_script(halmd)._desc()
+    assert d.nparticle == 1000 and d.nspecies == 2
+    assert list(d.box) == [9.4, 9.4, 9.4]
+    assert d.truncation == _lib.TRUNCATION["smooth_r4"] and d.smoothing == 0.005
+    assert [d.epsilon[k] for k in range(4)] == [1, 1.5, 1.5, 0.5]
+    assert [d.sigma[k] for k in range(4)] == [1, 0.8, 0.8, 0.88]
+    assert [d.r_cut[k] for k in range(4)] == [2.5] * 4        # in units of sigma_ab, as the Lua cutoff
+    assert d.skin == 0.3 and d.timestep == 0.002
+    assert d.integrator == _lib.INTEGRATOR["andersen"] and d.temperature == 0.7 and d.collision_rate == 1.0
+    assert d.sort == 1
+
+
+def test_lua_defaults(halmd):
+    box = halmd.mdsim.box({"length": [10, 10, 10]})
+    p = halmd.mdsim.particle({"particles": 100})
+    assert p.nspecies == 1 and p.precision == "double-single" and p.label == "all"
+    pot = halmd.mdsim.potentials.pair.lennard_jones().truncate(cutoff=2.5)
+    assert pot.kind == "shifted"                                  # truncate.lua.in:289
+    assert np.all(pot.epsilon == 1) and np.all(pot.sigma == 1)
+    halmd.mdsim.forces.pair(box=box, particle=p, potential=pot)
+    halmd.mdsim.integrators.verlet(box=box, particle=p, timestep=0.001)
+    d = p._desc()
+    assert d.skin == 0.5                                          # neighbour.lua.in:162
+    assert d.neighbour_occupancy == 0.4 and d.cell_occupancy == 0.5
+    assert d.integrator == _lib.INTEGRATOR["verlet"]
+
+
+def test_argument_errors(halmd):
+    with pytest.raises(ValueError):
+        halmd.mdsim.particle(dimension=2, particles=10)
+    with pytest.raises(ValueError):
+        halmd.mdsim.potentials.pair.lennard_jones().truncate("shifted")        # no cutoff
+    with pytest.raises(ValueError):
+        halmd.mdsim.potentials.pair.lennard_jones().truncate("cubic", cutoff=2.5)
+    with pytest.raises(ValueError):
+        halmd.mdsim.potentials.pair.lennard_jones().truncate("smooth_r4", cutoff=2.5)  # no h
+    box = halmd.mdsim.box(length=[5, 5, 5])
+    p = halmd.mdsim.particle(particles=10)
+    with pytest.raises(ValueError):
+        halmd.mdsim.forces.pair(box=box, particle=p, potential=halmd.mdsim.potentials.pair.lennard_jones())
+    with pytest.raises(RuntimeError):
+        p._desc()                                                  # no force / integrator yet
