@@ -895,6 +895,7 @@ int64_t Engine::get_option(const std::string& name) const
 {
     if (name == "force_lanes") return lanes_;
     if (name == "neighbour_scan") return nbr_scan_;
+    if (name == "step_kernels") return (int64_t)step_kernels_;
     if (name == "neighbour_capacity") return nbr_cap_;
     if (name == "rebuild_chains") {
         uint32_t v[2];
@@ -998,10 +999,14 @@ cudaGraphExec_t Engine::capture(int nsteps, bool aux_last)
     HMD_CUDA(cudaGraphCreate(&g, 0));
     HMD_CUDA(cudaStreamBeginCaptureToGraph(stream_, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     try {
+        // step k: [integrate k] -> IF(rebuild k) -> force k -> [finalize k + integrate k+1];
+        // the fused kernel sets the conditional of step k+1, so the handles exist up front
+        std::vector<cudaGraphConditionalHandle> hs(nsteps);
+        for (int k = 0; k < nsteps; ++k)
+            HMD_CUDA(cudaGraphConditionalHandleCreate(&hs[k], g, 0, cudaGraphCondAssignDefault));
+        launch_integrate(d, ds(), hs[0], true, stream_);
         for (int k = 0; k < nsteps; ++k) {
-            cudaGraphConditionalHandle h;
-            HMD_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
-            launch_integrate(d, ds(), h, true, stream_);
+            const cudaGraphConditionalHandle h = hs[k];
             cudaStreamCaptureStatus cs;
             cudaGraph_t cg;
             const cudaGraphNode_t* deps = nullptr;
@@ -1020,7 +1025,8 @@ cudaGraphExec_t Engine::capture(int nsteps, bool aux_last)
             cudaGraph_t body_out;
             HMD_CUDA(cudaStreamEndCapture(side_, &body_out));
             launch_force(d, aux_last && k == nsteps - 1, stream_);
-            launch_finalize(d, ds(), stream_);
+            if (k + 1 < nsteps) launch_finalize_integrate(d, ds(), hs[k + 1], stream_);
+            else launch_finalize(d, ds(), stream_);
         }
     } catch (...) {
         cudaGraph_t tmp;
@@ -1039,15 +1045,17 @@ cudaGraphExec_t Engine::capture(int nsteps, bool aux_last)
 void Engine::destroy_graphs()
 {
     if (g_chunk_) cudaGraphExecDestroy(g_chunk_);
+    if (g_short_) cudaGraphExecDestroy(g_short_);
     if (g_one_) cudaGraphExecDestroy(g_one_);
     if (g_one_aux_) cudaGraphExecDestroy(g_one_aux_);
-    g_chunk_ = g_one_ = g_one_aux_ = nullptr;
+    g_chunk_ = g_short_ = g_one_ = g_one_aux_ = nullptr;
 }
 
 void Engine::build_graphs()
 {
     destroy_graphs();
     g_chunk_ = capture(CHUNK_STEPS, false);
+    g_short_ = capture(SHORT_STEPS, false);
     g_one_ = capture(1, false);
     g_one_aux_ = capture(1, true);
 }
@@ -1142,17 +1150,27 @@ bool Engine::grow_after_overflow(uint32_t status)
 void Engine::run_steps(uint64_t nsteps, bool aux_last)
 {
     if (!g_chunk_) build_graphs();
+    // a captured chunk of n steps launches 2n + 1 step kernels (integrate, n
+    // forces, n - 1 fused finalize + integrate, finalize), plus the
+    // conditional rebuild chains
     uint64_t left = nsteps;
     while (left > 0) {
         if (left >= (uint64_t)CHUNK_STEPS && !(aux_last && left == (uint64_t)CHUNK_STEPS)) {
             HMD_CUDA(cudaGraphLaunch(g_chunk_, stream_));
             left -= CHUNK_STEPS;
+            step_kernels_ += 2 * CHUNK_STEPS + 1;
+        } else if (left >= (uint64_t)SHORT_STEPS && !(aux_last && left == (uint64_t)SHORT_STEPS)) {
+            HMD_CUDA(cudaGraphLaunch(g_short_, stream_));
+            left -= SHORT_STEPS;
+            step_kernels_ += 2 * SHORT_STEPS + 1;
         } else if (left == 1 && aux_last) {
             HMD_CUDA(cudaGraphLaunch(g_one_aux_, stream_));
             left -= 1;
+            step_kernels_ += 3;
         } else {
             HMD_CUDA(cudaGraphLaunch(g_one_, stream_));
             left -= 1;
+            step_kernels_ += 3;
         }
     }
 }

@@ -199,8 +199,10 @@ private:
     uint32_t rebuild_kernel_count() const;
 
     static constexpr int CHUNK_STEPS = 100;
+    static constexpr int SHORT_STEPS = 10;       // chunk for the remainder below CHUNK_STEPS
     static constexpr uint64_t SEGMENT_STEPS = 5000;
-    cudaGraphExec_t g_chunk_ = nullptr, g_one_ = nullptr, g_one_aux_ = nullptr;
+    cudaGraphExec_t g_chunk_ = nullptr, g_short_ = nullptr, g_one_ = nullptr, g_one_aux_ = nullptr;
+    uint64_t step_kernels_ = 0;                  // kernels of the step graphs launched (rebuild chains not counted)
 };
 
 } // namespace hmd

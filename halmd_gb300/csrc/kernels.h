@@ -13,6 +13,8 @@ void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool 
 void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st);
 void launch_force(const Dev& d, bool aux, cudaStream_t st);
 void launch_finalize(const Dev& d, bool ds, cudaStream_t st);
+// finalize of step k fused with the integrate of step k + 1 (captured chunks)
+void launch_finalize_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, cudaStream_t st);
 void launch_thermo(const Dev& d, cudaStream_t st);
 
 // rebuild (kernels_rebuild.cu)

@@ -87,15 +87,99 @@ __device__ __forceinline__ void descend_component(float& rh, float& rl, float& i
     im = __fadd_rn(im, k);
 }
 
+// ---------------------------------------------------------------------------
+// finalize: second half-kick (verlet_kernel.cu:78-98) or Andersen
+// (per-particle collisions with the heat bath, host convention
+// mdsim/host/integrators/verlet_nvt_andersen.cpp:111-137; Philox4x32-10
+// streams keyed by (seed, particle tag, step) so results do not depend on
+// particle order or on which other systems share the launch)
+// ---------------------------------------------------------------------------
+
 template <bool DS>
+__device__ __forceinline__ void half_kick(float& vh, float& vl, float f, float m, float dt_half)
+{
+    const float a = __fdiv_rn(__fmul_rn(f, dt_half), m);
+    if (DS) {
+        float v0, v1;
+        ds_add(v0, v1, vh, vl, a, 0.0f);
+        vh = v0; vl = v1;
+    } else {
+        vh = __fadd_rn(vh, a);
+    }
+}
+
+// the second half of step st.step of slot i, on velocities held in registers
+template <bool DS>
+__device__ __forceinline__ void finalize_slot(const Dev& d, const SysParam& P, const SysState& st, uint32_t i,
+                                              float4& v, float4& vl, float4 f)
+{
+    if (P.integrator == INTEG_ANDERSEN) {
+        const unsigned long long step = st.step - 1ull;
+        const uint4 ctr = make_uint4(d.id[i], (uint32_t)step, (uint32_t)(step >> 32), 0x414E4452u);
+        const uint4 u = philox4x32_10(ctr, P.seed_lo, P.seed_hi);
+        if (u.x < P.coll_threshold) {
+            const uint4 w = philox4x32_10(make_uint4(ctr.x, ctr.y, ctr.z, 0x414E4453u), P.seed_lo, P.seed_hi);
+            const float rad0 = sqrtf(-2.0f * logf(u01(w.x)));
+            const float rad1 = sqrtf(-2.0f * logf(u01(w.z)));
+            float sn0, cs0, sn1, cs1;
+            sincospif(2.0f * u01(w.y), &sn0, &cs0);
+            sincospif(2.0f * u01(w.w), &sn1, &cs1);
+            v.x = P.sqrt_T * rad0 * cs0;
+            v.y = P.sqrt_T * rad0 * sn0;
+            v.z = P.sqrt_T * rad1 * cs1;
+            vl = make_float4(0, 0, 0, vl.w);
+            return;
+        }
+    }
+    half_kick<DS>(v.x, vl.x, f.x, v.w, P.dt_half);
+    half_kick<DS>(v.y, vl.y, f.y, v.w, P.dt_half);
+    half_kick<DS>(v.z, vl.z, f.z, v.w, P.dt_half);
+}
+
+template <bool DS>
+__global__ void __launch_bounds__(256) k_finalize(Dev d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    const SysState& st = d.st[s];
+    if (!P.active || !st.live || *d.status != 0u || P.integrator == INTEG_DESCENT) return;
+    if (species_bits(d.pos[i].w) == PLACEHOLDER) return;
+    float4 v = d.vel[i];
+    float4 vl = make_float4(0, 0, 0, 0);
+    if (DS) vl = d.vel[d.S + i];
+    finalize_slot<DS>(d, P, st, i, v, vl, d.force[i]);
+    d.vel[i] = v;
+    if (DS) d.vel[d.S + i] = vl;
+}
+
+// FIN: the finalize of the previous step (its force is in d.force) runs
+// first, on the same registers: one pass over the phase space per step
+// inside a captured chunk.  The per-system flags it reads (live,
+// steps_left) are read before any block arrives at the decision that
+// updates them, so both halves see the state of their own step.
+template <bool DS, bool FIN>
 __global__ void __launch_bounds__(256) k_integrate(Dev d, cudaGraphConditionalHandle h, int use_handle)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t s = d.chunk_sys[i / CHUNK];
     const SysParam& P = d.sys[s];
     SysState& st = d.st[s];
-    const bool live = P.active && st.steps_left != 0u && (*d.status == 0u);
+    const bool clean = *d.status == 0u;
+    const bool live = P.active && st.steps_left != 0u && clean;
+    const bool fin = FIN && P.active && st.live && clean && P.integrator != INTEG_DESCENT;
     float rr = 0.0f;
+    if (fin && !live) {
+        // the system finished with the previous step: its last half-kick only
+        if (species_bits(d.pos[i].w) != PLACEHOLDER) {
+            float4 v = d.vel[i];
+            float4 vl = make_float4(0, 0, 0, 0);
+            if (DS) vl = d.vel[d.S + i];
+            finalize_slot<DS>(d, P, st, i, v, vl, d.force[i]);
+            d.vel[i] = v;
+            if (DS) d.vel[d.S + i] = vl;
+        }
+    }
     if (live) {
         float4 r = d.pos[i];
         if (species_bits(r.w) != PLACEHOLDER) {
@@ -104,6 +188,7 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d, cudaGraphConditionalHa
             float4 k = make_float4(0, 0, 0, 0);   // box images crossed in this step
             float4 rl = make_float4(0, 0, 0, 0), vl = make_float4(0, 0, 0, 0);
             if (DS) { rl = d.pos[d.S + i]; vl = d.vel[d.S + i]; }
+            if (fin) finalize_slot<DS>(d, P, st, i, v, vl, f);
             if (P.integrator == INTEG_DESCENT) {   // block-uniform
                 const float3 g = descent_move(f, P.descent_step, P.descent_max);
                 descend_component<DS>(r.x, rl.x, k.x, g.x, P.L[0], P.Linv[0]);
@@ -566,66 +651,6 @@ __global__ void __launch_bounds__(128) k_force(Dev d)
 }
 
 // ---------------------------------------------------------------------------
-// finalize: second half-kick (verlet_kernel.cu:78-98) or Andersen
-// (per-particle collisions with the heat bath, host convention
-// mdsim/host/integrators/verlet_nvt_andersen.cpp:111-137; Philox4x32-10
-// streams keyed by (seed, particle tag, step) so results do not depend on
-// particle order or on which other systems share the launch)
-// ---------------------------------------------------------------------------
-
-template <bool DS>
-__device__ __forceinline__ void half_kick(float& vh, float& vl, float f, float m, float dt_half)
-{
-    const float a = __fdiv_rn(__fmul_rn(f, dt_half), m);
-    if (DS) {
-        float v0, v1;
-        ds_add(v0, v1, vh, vl, a, 0.0f);
-        vh = v0; vl = v1;
-    } else {
-        vh = __fadd_rn(vh, a);
-    }
-}
-
-template <bool DS>
-__global__ void __launch_bounds__(256) k_finalize(Dev d)
-{
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t s = d.chunk_sys[i / CHUNK];
-    const SysParam& P = d.sys[s];
-    const SysState& st = d.st[s];
-    if (!P.active || !st.live || *d.status != 0u || P.integrator == INTEG_DESCENT) return;
-    if (species_bits(d.pos[i].w) == PLACEHOLDER) return;
-    float4 v = d.vel[i];
-    float4 vl = make_float4(0, 0, 0, 0);
-    if (DS) vl = d.vel[d.S + i];
-    const float4 f = d.force[i];
-    if (P.integrator == INTEG_ANDERSEN) {
-        const unsigned long long step = st.step - 1ull;
-        const uint4 ctr = make_uint4(d.id[i], (uint32_t)step, (uint32_t)(step >> 32), 0x414E4452u);
-        const uint4 u = philox4x32_10(ctr, P.seed_lo, P.seed_hi);
-        if (u.x < P.coll_threshold) {
-            const uint4 w = philox4x32_10(make_uint4(ctr.x, ctr.y, ctr.z, 0x414E4453u), P.seed_lo, P.seed_hi);
-            const float rad0 = sqrtf(-2.0f * logf(u01(w.x)));
-            const float rad1 = sqrtf(-2.0f * logf(u01(w.z)));
-            float sn0, cs0, sn1, cs1;
-            sincospif(2.0f * u01(w.y), &sn0, &cs0);
-            sincospif(2.0f * u01(w.w), &sn1, &cs1);
-            v.x = P.sqrt_T * rad0 * cs0;
-            v.y = P.sqrt_T * rad0 * sn0;
-            v.z = P.sqrt_T * rad1 * cs1;
-            d.vel[i] = v;
-            if (DS) d.vel[d.S + i] = make_float4(0, 0, 0, vl.w);
-            return;
-        }
-    }
-    half_kick<DS>(v.x, vl.x, f.x, v.w, P.dt_half);
-    half_kick<DS>(v.y, vl.y, f.y, v.w, P.dt_half);
-    half_kick<DS>(v.z, vl.z, f.z, v.w, P.dt_half);
-    d.vel[i] = v;
-    if (DS) d.vel[d.S + i] = vl;
-}
-
-// ---------------------------------------------------------------------------
 // FP64 reductions (observables/gpu/thermodynamics_kernel.cu:35-106 and
 // algorithm/gpu/reduce_kernel.cuh:126): per-block partial sums, then a
 // fixed-order per-system reduction (deterministic, no double atomics).
@@ -701,8 +726,15 @@ __global__ void __launch_bounds__(256) k_thermo_reduce(Dev d)
 void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool use_handle, cudaStream_t st)
 {
     const unsigned grid = d.S / 256;
-    if (ds) k_integrate<true><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
-    else k_integrate<false><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
+    if (ds) k_integrate<true, false><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
+    else k_integrate<false, false><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
+}
+
+void launch_finalize_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, cudaStream_t st)
+{
+    const unsigned grid = d.S / 256;
+    if (ds) k_integrate<true, true><<<grid, 256, 0, st>>>(d, h, 1);
+    else k_integrate<false, true><<<grid, 256, 0, st>>>(d, h, 1);
 }
 
 void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st)

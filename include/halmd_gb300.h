@@ -145,6 +145,8 @@ HMD_API int hmd_engine_progress(hmd_engine* engine, uint64_t* step, uint32_t* st
  *                   particles once); all give the same lists
  *   "neighbour_capacity" (get only) list slots per particle
  *   "rebuild_chains"     (get only) steps in which the rebuild chain ran (any system rebuilt)
+ *   "step_kernels"       (get only) kernels of the captured step graphs launched so far
+ *                        (rebuild chains not included: rebuild_chains x hmd_system_info.rebuild_kernels)
  */
 HMD_API int hmd_engine_set_option(hmd_engine* engine, const char* name, int64_t value);
 HMD_API int hmd_engine_get_option(hmd_engine* engine, const char* name, int64_t* value);
