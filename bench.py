@@ -408,6 +408,7 @@ def run_phases(args, w):
     eng = make_engine(w, L)
     if args.force_lanes:
         eng.set_option("force_lanes", args.force_lanes)
+        eng.set_option("list_block", args.list_block)
     if args.neighbour_scan:
         eng.set_option("neighbour_scan", args.neighbour_scan)
     eng.set("species", species)
@@ -426,7 +427,8 @@ def run_phases(args, w):
         eng.finalize()
     inf1 = eng.info()
     out = {"workload": w["name"], "n": w["n"], "md_steps": args.phases,
-           "rebuilds": int(inf1.rebuilds - inf0.rebuilds), "force_lanes": eng.get_option("force_lanes")}
+           "rebuilds": int(inf1.rebuilds - inf0.rebuilds), "force_lanes": eng.get_option("force_lanes"),
+           "list_block": eng.get_option("list_block")}
     for ph in ("integrate", "rebuild", "force", "finalize"):
         ms, cnt = eng.profile_get(ph)
         out[ph + "_ms_per_call"] = ms / max(cnt, 1)
@@ -454,6 +456,8 @@ def main():
     ap.add_argument("--force-lanes", type=int, default=0,
                     help="threads per particle in the force kernel (0: autotune in the bench, engine default "
                          "in --phases)")
+    ap.add_argument("--list-block", type=int, default=0, help="list block width (0 auto, 4, 8) with --force-lanes")
+    ap.add_argument("--fuse-steps", type=int, default=1, help="1: fused finalize + integrate in chunks")
     ap.add_argument("--neighbour-scan", type=int, default=0,
                     help="list build: 0 auto, 1 per lane, 2 shared per warp")
     ap.add_argument("--serve-jobs", type=int, default=200)
@@ -487,6 +491,7 @@ def main():
 
     r, v, species, L = initial_state(w, seed=2024 + rank)
     eng = make_engine(w, L, seed=7 + rank)
+    eng.set_option("fuse_steps", args.fuse_steps)
     if args.neighbour_scan:
         eng.set_option("neighbour_scan", args.neighbour_scan)
     n = w["n"]
@@ -500,6 +505,7 @@ def main():
     from halmd_gb300.tune import autotune_force_lanes
     if args.force_lanes:
         eng.set_option("force_lanes", args.force_lanes)
+        eng.set_option("list_block", args.list_block)
         lanes, lane_ms = args.force_lanes, {}
     else:
         lanes, lane_ms = autotune_force_lanes(eng, use_cache=False)
@@ -588,7 +594,8 @@ def main():
                        "md_steps_per_bench_step": M, "truncation": w["trunc"], "skin": w["skin"],
                        "precision": "dsfloat", "l2": "flushed (256 MB write) between timed bench steps",
                        "rebuilds_in_timed_region": rebuilds, "parallelism": "replicas" if world > 1 else "single",
-                       "force_lanes": lanes, "autotune_force_ms": {str(k): v for k, v in lane_ms.items()}},
+                       "force_lanes": lanes, "list_block": eng.get_option("list_block"),
+                       "autotune_force_ms": {str(k): v for k, v in lane_ms.items()}},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "note": "per bench step: hmd_set(position, velocity) + hmd_step(%d) + "

@@ -575,7 +575,7 @@ Dev Engine::dev() const
     d.en_pot = en_pot_.p; d.stress = stress_.p; d.id = id_.p; d.rid = rid_.p;
     d.nbr = nbr_.p; d.nbr_count = nbr_count_.p; d.nbr_cap = nbr_cap_;
     d.lanes = lanes_;
-    d.lb_log2 = list_block(lanes_) == 8u ? 3u : 2u;
+    d.lb_log2 = block() == 8u ? 3u : 2u;
     // the shared scan does a warp's 32 particles in one serial pass over the
     // cells around them: it pays off once there are enough warps per SM to
     // hide that pass's latency (about 2^19 slots on 152 SMs)
@@ -862,6 +862,16 @@ void Engine::request_rebuild(uint32_t s)
     forces_valid_ = false;
 }
 
+// list block width: the option when it fits the lane count (1 lane: 4;
+// 8 lanes: 8; 2 or 4 lanes: 4 or 8), else the default for the lanes
+uint32_t Engine::block() const
+{
+    const uint32_t w = lanes_ ? lanes_ : 4u;
+    if (lb_ == 8u && (w == 2u || w == 4u)) return 8u;
+    if (lb_ == 4u && w <= 4u) return 4u;
+    return list_block(w);
+}
+
 void Engine::set_option(const std::string& name, int64_t value)
 {
     if (name == "force_lanes") {
@@ -881,6 +891,26 @@ void Engine::set_option(const std::string& name, int64_t value)
         forces_valid_ = false;
         return;
     }
+    if (name == "list_block") {
+        if (value != 0 && value != 4 && value != 8) throw Error(HMD_ERR_INVALID, "list_block must be 0 (auto), 4 or 8");
+        if ((uint32_t)value == lb_) return;
+        lb_ = (uint32_t)value;
+        if (committed_) {   // the list layout changes: rebuild every list before the next force
+            destroy_graphs();
+            std::vector<SysState> st = read_state();
+            for (auto& t : st) t.rebuild_request = 1u;
+            write_state(st);
+            forces_valid_ = false;
+        }
+        return;
+    }
+    if (name == "fuse_steps") {
+        const bool f = value != 0;
+        if (f == fuse_) return;
+        fuse_ = f;
+        if (committed_) destroy_graphs();
+        return;
+    }
     if (name == "neighbour_scan") {
         if (value < 0 || value > 2) throw Error(HMD_ERR_INVALID, "neighbour_scan must be 0 (auto), 1 (per lane) or 2 (shared)");
         if (nbr_scan_ == (uint32_t)value) return;
@@ -894,8 +924,10 @@ void Engine::set_option(const std::string& name, int64_t value)
 int64_t Engine::get_option(const std::string& name) const
 {
     if (name == "force_lanes") return lanes_;
+    if (name == "list_block") return block();
     if (name == "neighbour_scan") return nbr_scan_;
     if (name == "step_kernels") return (int64_t)step_kernels_;
+    if (name == "fuse_steps") return fuse_ ? 1 : 0;
     if (name == "neighbour_capacity") return nbr_cap_;
     if (name == "rebuild_chains") {
         uint32_t v[2];
@@ -1025,8 +1057,12 @@ cudaGraphExec_t Engine::capture(int nsteps, bool aux_last)
             cudaGraph_t body_out;
             HMD_CUDA(cudaStreamEndCapture(side_, &body_out));
             launch_force(d, aux_last && k == nsteps - 1, stream_);
-            if (k + 1 < nsteps) launch_finalize_integrate(d, ds(), hs[k + 1], stream_);
-            else launch_finalize(d, ds(), stream_);
+            if (k + 1 < nsteps && fuse_) {
+                launch_finalize_integrate(d, ds(), hs[k + 1], stream_);
+            } else {
+                launch_finalize(d, ds(), stream_);
+                if (k + 1 < nsteps) launch_integrate(d, ds(), hs[k + 1], true, stream_);
+            }
         }
     } catch (...) {
         cudaGraph_t tmp;
@@ -1158,11 +1194,11 @@ void Engine::run_steps(uint64_t nsteps, bool aux_last)
         if (left >= (uint64_t)CHUNK_STEPS && !(aux_last && left == (uint64_t)CHUNK_STEPS)) {
             HMD_CUDA(cudaGraphLaunch(g_chunk_, stream_));
             left -= CHUNK_STEPS;
-            step_kernels_ += 2 * CHUNK_STEPS + 1;
+            step_kernels_ += fuse_ ? 2 * CHUNK_STEPS + 1 : 3 * CHUNK_STEPS;
         } else if (left >= (uint64_t)SHORT_STEPS && !(aux_last && left == (uint64_t)SHORT_STEPS)) {
             HMD_CUDA(cudaGraphLaunch(g_short_, stream_));
             left -= SHORT_STEPS;
-            step_kernels_ += 2 * SHORT_STEPS + 1;
+            step_kernels_ += fuse_ ? 2 * SHORT_STEPS + 1 : 3 * SHORT_STEPS;
         } else if (left == 1 && aux_last) {
             HMD_CUDA(cudaGraphLaunch(g_one_aux_, stream_));
             left -= 1;
@@ -1358,7 +1394,7 @@ void Engine::neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint
         if ((cnt[k] & 0xFFFFu) + (cnt[k] >> 16) > maxn) throw Error(HMD_ERR_INVALID, "maxn smaller than a neighbour count");
     }
     // blocked layout: block b holds entries [b*W, b*W + W) of every slot
-    const uint32_t W = list_block(lanes_);
+    const uint32_t W = block();
     const uint32_t nblk = nbr_cap_ / W;
     std::vector<uint32_t> all((size_t)nbr_cap_ * P.A);
     for (uint32_t b = 0; b < nblk; ++b)

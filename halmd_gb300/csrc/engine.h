@@ -103,6 +103,7 @@ public:
     void request_rebuild(uint32_t s);
     void set_steps_left(uint32_t s, uint32_t steps);
     void minimize(uint32_t s, uint32_t steps, double step_size, double max_move);
+    uint32_t block() const;
     void set_option(const std::string& name, int64_t value);
     int64_t get_option(const std::string& name) const;
     double max_displacement(uint32_t s);
@@ -164,6 +165,7 @@ private:
     uint32_t total_cells_ = 0;
     uint32_t nbr_cap_ = 0;
     uint32_t lanes_ = 0;        // force-kernel lanes per particle (0: choose at commit)
+    uint32_t lb_ = 0;          // list block width option (0 auto, 4, 8)
     uint32_t nbr_scan_ = 0;   // list build: 0 auto, 1 per lane, 2 shared scan per warp
     int sort_passes_ = 0;       // radix passes of the segmented sort (even)
     uint32_t ntiles_ = 0;
@@ -202,6 +204,7 @@ private:
     static constexpr int SHORT_STEPS = 10;       // chunk for the remainder below CHUNK_STEPS
     static constexpr uint64_t SEGMENT_STEPS = 5000;
     cudaGraphExec_t g_chunk_ = nullptr, g_short_ = nullptr, g_one_ = nullptr, g_one_aux_ = nullptr;
+    bool fuse_ = true;                           // captured chunks fuse finalize k with integrate k+1
     uint64_t step_kernels_ = 0;                  // kernels of the step graphs launched (rebuild chains not counted)
 };
 

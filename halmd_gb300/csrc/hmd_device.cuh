@@ -28,8 +28,9 @@ constexpr int MAX_SPECIES = 4;
 constexpr int SLOT_ALIGN = 256;   // slots per system are a multiple of this
 constexpr int CHUNK = 64;         // granularity of the slot -> system map
 
-// entries per block of the neighbour-list layout for a force kernel with w
-// threads per particle (each thread reads list_block(w) / w entries at once)
+// default entries per block of the neighbour-list layout for a force kernel
+// with w threads per particle (each thread reads block / w entries at once;
+// the engine also accepts 8 for w = 2 and w = 4)
 __host__ __device__ constexpr uint32_t list_block(uint32_t w) { return w < 4u ? 4u : w; }
 
 enum Trunc : uint32_t { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3 };
@@ -115,11 +116,11 @@ struct Dev {
     float* stress;             // [6S]
     uint32_t* id;              // [S] tag of the particle within its system
     uint32_t* rid;             // [S] slot of (off + tag)
-    uint32_t* nbr;             // [nbr_cap * S], blocked: entry k of slot i at ((k/LB)*S + i)*LB + k%LB, LB = list_block(lanes)
+    uint32_t* nbr;             // [nbr_cap * S], blocked: entry k of slot i at ((k/LB)*S + i)*LB + k%LB, LB = 1 << lb_log2
     uint32_t* nbr_count;       // [S] near count | far count << 16 (near entries from the front, far from the back)
     uint32_t nbr_cap;          // multiple of 8
     uint32_t lanes;            // threads per particle in the force kernel (1, 2, 4, 8)
-    uint32_t lb_log2;          // log2 of the list block width list_block(lanes)
+    uint32_t lb_log2;          // log2 of the list block width LB (4 or 8)
     uint32_t nbr_shared_scan;  // 1: list build scans the cells once per warp (see k_neighbour)
     uint32_t* cell;            // cell contents
     uint32_t* cell_count;      // [total_cells]

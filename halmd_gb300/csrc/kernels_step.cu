@@ -23,7 +23,8 @@ template <bool DS>
 __device__ __forceinline__ void integrate_component(float& rh, float& rl, float& vh, float& vl, float& im,
                                                     float f, float m, float dt, float dt_half, float L, float Linv)
 {
-    float a = __fdiv_rn(__fmul_rn(f, dt_half), m);
+    float a = __fmul_rn(f, dt_half);
+    if (m != 1.0f) a = __fdiv_rn(a, m);   // x / 1 == x exactly: skip the division for unit masses
     float k;
     if (DS) {
         float v0, v1, d0, d1, r0, r1;
@@ -98,7 +99,8 @@ __device__ __forceinline__ void descend_component(float& rh, float& rl, float& i
 template <bool DS>
 __device__ __forceinline__ void half_kick(float& vh, float& vl, float f, float m, float dt_half)
 {
-    const float a = __fdiv_rn(__fmul_rn(f, dt_half), m);
+    float a = __fmul_rn(f, dt_half);
+    if (m != 1.0f) a = __fdiv_rn(a, m);
     if (DS) {
         float v0, v1;
         ds_add(v0, v1, vh, vl, a, 0.0f);
@@ -555,12 +557,11 @@ __device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t 
     }
 }
 
-template <int W, int TR, bool AUX>
+template <int W, int E, int TR, bool AUX>
 __device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf,
                                                bool wrap, const SysParam& P, const PairParam* spp, float4 ri,
                                                uint32_t a, ForceAcc& A)
 {
-    constexpr int E = list_block(W) / W;
     if (wrap) {
         force_blocks<W, E, TR, AUX, true, false>(d, i, q, nn, P, spp, ri, a, A);
         force_blocks<W, E, TR, AUX, true, true>(d, i, q, nf, P, spp, ri, a, A);
@@ -596,7 +597,7 @@ __device__ __forceinline__ float lane_sum(float v)
     return v;
 }
 
-template <int W, bool AUX>
+template <int W, int E, bool AUX>
 __global__ void __launch_bounds__(128) k_force(Dev d)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -620,11 +621,11 @@ __global__ void __launch_bounds__(128) k_force(Dev d)
         switch (P.trunc) {
         case TRUNC_SHARP:
         case TRUNC_SHIFTED:
-            if (P.ns == 1) force_dispatch<W, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
-            else force_dispatch<W, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
+            if (P.ns == 1) force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
+            else force_dispatch<W, E, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
             break;
-        case TRUNC_SMOOTH_R4: force_dispatch<W, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
-        default: force_dispatch<W, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
+        case TRUNC_SMOOTH_R4: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
+        default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
         }
     }
     lane_merge<W>(A.fx, A.cx);
@@ -742,21 +743,25 @@ void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st)
     k_mark<<<(d.nsys + 255) / 256, 256, 0, st>>>(d, rebuild_all ? 1 : 0);
 }
 
-template <int W>
+template <int W, int E>
 static void launch_force_w(const Dev& d, bool aux, cudaStream_t st)
 {
     const unsigned grid = (unsigned)((size_t)d.S * W / 128);
-    if (aux) k_force<W, true><<<grid, 128, 0, st>>>(d);
-    else k_force<W, false><<<grid, 128, 0, st>>>(d);
+    if (aux) k_force<W, E, true><<<grid, 128, 0, st>>>(d);
+    else k_force<W, E, false><<<grid, 128, 0, st>>>(d);
 }
 
+// (lanes, list block) shapes the engine accepts: E = block / lanes entries per load
 void launch_force(const Dev& d, bool aux, cudaStream_t st)
 {
-    switch (d.lanes) {
-    case 1: launch_force_w<1>(d, aux, st); break;
-    case 2: launch_force_w<2>(d, aux, st); break;
-    case 4: launch_force_w<4>(d, aux, st); break;
-    default: launch_force_w<8>(d, aux, st); break;
+    const uint32_t lb = 1u << d.lb_log2;
+    switch (d.lanes * 16u + lb) {
+    case 1 * 16 + 4: launch_force_w<1, 4>(d, aux, st); break;
+    case 2 * 16 + 4: launch_force_w<2, 2>(d, aux, st); break;
+    case 2 * 16 + 8: launch_force_w<2, 4>(d, aux, st); break;
+    case 4 * 16 + 4: launch_force_w<4, 1>(d, aux, st); break;
+    case 4 * 16 + 8: launch_force_w<4, 2>(d, aux, st); break;
+    default: launch_force_w<8, 1>(d, aux, st); break;
     }
 }
 

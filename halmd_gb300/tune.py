@@ -1,7 +1,8 @@
 """Autotuner for the engine's launch shapes.
 
 Picks the force kernel's lanes per particle (1, 2, 4 or 8 threads share one
-particle's neighbour list) by timing the force kernel on the engine's own
+particle's neighbour list) and the list block width (entries one thread
+reads with one load = block / lanes) by timing the force kernel on the engine's own
 systems with CUDA events (the engine's per-phase profiler).  Results are
 cached as JSON keyed by (GPU name, slots bucket, mean list length bucket)
 so a later engine of similar size reuses the choice without timing.
@@ -11,7 +12,7 @@ import math
 import os
 
 CACHE = os.environ.get("HMD_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "halmd_gb300_tune.json"))
-CHOICES = (1, 2, 4, 8)
+CHOICES = ((1, 4), (2, 4), (2, 8), (4, 4), (4, 8), (8, 8))   # (lanes, list block)
 
 
 def _gpu_name():
@@ -46,29 +47,34 @@ def _store(db):
 
 
 def autotune_force_lanes(engine, repeats=10, use_cache=True):
-    """Time the force kernel for every lane count; keep the fastest.
+    """Time the force kernel for every (lanes, list block) shape; keep the fastest.
 
-    Returns (lanes, {lanes: ms per launch}).  The engine must be committed and
-    hold a representative state (positions set)."""
+    Returns (lanes, {"lanes/block": ms per launch}) and leaves the engine on
+    the fastest shape.  The engine must be committed and hold a representative
+    state (positions set)."""
     key = _key(engine)
     db = _load() if use_cache else {}
-    if use_cache and key in db:
+    if use_cache and key in db and "block" in db[key]:
         engine.set_option("force_lanes", db[key]["lanes"])
+        engine.set_option("list_block", db[key]["block"])
         return db[key]["lanes"], db[key]["ms"]
     timings = {}
-    for w in CHOICES:
+    for w, b in CHOICES:
         engine.set_option("force_lanes", w)
+        engine.set_option("list_block", b)
         engine.force()            # rebuilds the lists in this layout
         engine.profile(True)
         for _ in range(repeats):
             engine.force()
         ms, n = engine.profile_get("force")
         engine.profile(False)
-        timings[w] = ms / max(n, 1)
+        timings[(w, b)] = ms / max(n, 1)
     best = min(timings, key=timings.get)
-    engine.set_option("force_lanes", best)
+    engine.set_option("force_lanes", best[0])
+    engine.set_option("list_block", best[1])
     engine.force()
+    out = {"%d/%d" % k: v for k, v in timings.items()}
     if use_cache:
-        db[key] = {"lanes": best, "ms": {str(k): v for k, v in timings.items()}}
+        db[key] = {"lanes": best[0], "block": best[1], "ms": out}
         _store(db)
-    return best, timings
+    return best[0], out

@@ -145,6 +145,10 @@ HMD_API int hmd_engine_progress(hmd_engine* engine, uint64_t* step, uint32_t* st
  *                   particles once); all give the same lists
  *   "neighbour_capacity" (get only) list slots per particle
  *   "rebuild_chains"     (get only) steps in which the rebuild chain ran (any system rebuilt)
+ *   "list_block"    0 (auto), 4 or 8: entries per block of the list layout; each force thread
+ *                   reads list_block / force_lanes entries with one load (2 or 4 lanes: 4 or 8)
+ *   "fuse_steps"    1 (default): captured chunks run the finalize of step k and the integrate of
+ *                   step k+1 as one kernel; 0: separate kernels (same results)
  *   "step_kernels"       (get only) kernels of the captured step graphs launched so far
  *                        (rebuild chains not included: rebuild_chains x hmd_system_info.rebuild_kernels)
  */

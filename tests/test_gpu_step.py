@@ -81,10 +81,12 @@ def test_lj_force_parity(precision):
     eng.close()
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
-def test_force_lanes_agree(lanes):
+@pytest.mark.parametrize("lanes,block", [(1, 4), (2, 4), (2, 8), (4, 4), (4, 8), (8, 8)])
+def test_force_lanes_agree(lanes, block):
     eng, r, v, L = lj_engine(ncell=7)
     eng.set_option("force_lanes", lanes)
+    eng.set_option("list_block", block)
+    assert eng.get_option("list_block") == block
     eng.force()
     assert eng.get_option("force_lanes") == lanes
     f = eng.get("force")
