@@ -552,7 +552,6 @@ def main():
     h2d = d2h = 0
     pos = eng.get("position")
     vel = eng.get("velocity")
-    A = inf1.slots
     for _ in range(max(1, args.steps // 2)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -563,10 +562,11 @@ def main():
         vel = eng.get("velocity")
         e2e_ms += 1e3 * (time.perf_counter() - t0)
     e2e_steps = M * max(1, args.steps // 2)
-    # bytes the API moves per call: set(position) 3 float4[A] up, set(velocity) 2 up (each after a read-back
-    # of the same arrays); get(position) 3 down, get(velocity) 2 down; reverse ids 4 B/particle per call
-    h2d = (3 + 2) * 16 * A
-    d2h = (3 + 2) * 16 * A + (3 + 2) * 16 * A + 4 * 4 * n
+    # bytes the API moves per bench step: set(position) and set(velocity) copy 3 n doubles each up,
+    # get(position) and get(velocity) 3 n doubles each down (converted on the device); the rebuild request
+    # after set(position) reads and writes the per-system state table
+    h2d = 2 * 24 * n + 48 * len(eng.systems)
+    d2h = 2 * 24 * n + 48 * len(eng.systems)
     e2e_value = world * n * e2e_steps / (e2e_ms * 1e-3)
 
     # dominant kernel: the pair force, timed alone with events on the engine stream

@@ -354,7 +354,6 @@ void Engine::commit()
     if (nbr_cap_ == 0) nbr_cap_ = 64;
     key_bits_ = shift;
     sort_passes_ = radix_passes(key_bits_);
-    sort_passes_ += sort_passes_ & 1;
     ntiles_ = (uint32_t)tiles.size();
     tiles_.alloc(std::max<size_t>(tiles.size(), 1));
     if (!tiles.empty())
@@ -624,60 +623,41 @@ std::vector<uint32_t> Engine::slots_of(uint32_t s)
     return r;
 }
 
+// staging buffer of the device-side set / get conversions (grows on demand)
+void Engine::stage(size_t doubles)
+{
+    if (io_.n < doubles) io_.alloc(doubles);
+}
+
 void Engine::set(uint32_t s, const std::string& name, const void* host, size_t count)
 {
     check_sys(s);
     const SysParam& P = sys_[s].P;
     const uint32_t n = P.n;
-    const size_t S = S_;
-    std::vector<uint32_t> slot = slots_of(s);
     auto need = [&](size_t k) {
         if (count != k) throw Error(HMD_ERR_INVALID, "array '" + name + "' needs " + std::to_string(k) + " elements");
     };
-    if (name == "position") {
+    if (name == "position" || name == "velocity") {
+        // one copy into the staging buffer, then the conversion on the device
         need(3 * (size_t)n);
         const double* x = static_cast<const double*>(host);
-        std::vector<float4> hi(P.A), lo(P.A), im(P.A);
-        download(pos_, P.off, P.A, hi.data());
-        download(pos_, S + P.off, P.A, lo.data());
-        download(img_, P.off, P.A, im.data());
-        for (uint32_t t = 0; t < n; ++t) {
-            const uint32_t k = slot[t] - P.off;
-            float* h = &hi[k].x;
-            float* l = &lo[k].x;
-            float* g = &im[k].x;
-            for (int q = 0; q < 3; ++q) {
-                const double L = (double)P.L[q];
-                const double w = std::rint(x[3 * t + q] / L);
-                const double xr = x[3 * t + q] - w * L;
-                h[q] = (float)xr;
-                l[q] = ds() ? (float)(xr - (double)h[q]) : 0.0f;
-                g[q] = (float)((double)g[q] + w);
-            }
+        if (name == "position")
+            for (size_t k = 0; k < 3 * (size_t)n; ++k)
+                if (!std::isfinite(x[k])) throw Error(HMD_ERR_INVALID, "positions must be finite");
+        stage(3 * (size_t)n);
+        HMD_CUDA(cudaMemcpyAsync(io_.p, x, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        launch_set_vector(dev(), s, n, name == "position" ? 0 : 1, ds(), io_.p, stream_);
+        HMD_CUDA(cudaGetLastError());
+        sync();
+        if (name == "position") {
+            forces_valid_ = false;
+            request_rebuild(s);
         }
-        upload(pos_, P.off, P.A, hi.data());
-        upload(pos_, S + P.off, P.A, lo.data());
-        upload(img_, P.off, P.A, im.data());
-        forces_valid_ = false;
-        request_rebuild(s);
-    } else if (name == "velocity") {
-        need(3 * (size_t)n);
-        const double* x = static_cast<const double*>(host);
-        std::vector<float4> hi(P.A), lo(P.A);
-        download(vel_, P.off, P.A, hi.data());
-        download(vel_, S + P.off, P.A, lo.data());
-        for (uint32_t t = 0; t < n; ++t) {
-            const uint32_t k = slot[t] - P.off;
-            float* h = &hi[k].x;
-            float* l = &lo[k].x;
-            for (int q = 0; q < 3; ++q) {
-                h[q] = (float)x[3 * t + q];
-                l[q] = ds() ? (float)(x[3 * t + q] - (double)h[q]) : 0.0f;
-            }
-        }
-        upload(vel_, P.off, P.A, hi.data());
-        upload(vel_, S + P.off, P.A, lo.data());
-    } else if (name == "mass") {
+        return;
+    }
+    const size_t S = S_;
+    std::vector<uint32_t> slot = slots_of(s);
+    if (name == "mass") {
         need(n);
         const double* x = static_cast<const double*>(host);
         std::vector<float4> hi(P.A);
@@ -723,6 +703,17 @@ void Engine::get(uint32_t s, const std::string& name, void* host, size_t count)
     auto need = [&](size_t k) {
         if (count != k) throw Error(HMD_ERR_INVALID, "array '" + name + "' needs " + std::to_string(k) + " elements");
     };
+    static const char* const vec_names[] = {"position", "unwrapped_position", "velocity", "force", "image"};
+    for (int w = 0; w < 5; ++w) {
+        if (name != vec_names[w]) continue;
+        need(3 * (size_t)n);
+        stage(3 * (size_t)n);
+        launch_get_vector(dev(), s, n, w, io_.p, stream_);
+        HMD_CUDA(cudaGetLastError());
+        HMD_CUDA(cudaMemcpyAsync(host, io_.p, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+        sync();
+        return;
+    }
     if (name == "id") {
         need(P.A);
         download(id_, P.off, P.A, static_cast<uint32_t*>(host));
@@ -993,7 +984,7 @@ void Engine::rebuild_chain(cudaStream_t st)
     const Dev d = dev();
     if (any_sort_) {
         launch_sort(d, sort_passes_, st);
-        launch_rearrange(d, ds(), d.val[0], st);
+        launch_rearrange(d, ds(), d.val[sort_passes_ & 1], st);   // pass p writes val[1 - p % 2]
     }
     launch_binning(d, st);
     launch_neighbour(d, st);

@@ -104,6 +104,7 @@ public:
     void set_steps_left(uint32_t s, uint32_t steps);
     void minimize(uint32_t s, uint32_t steps, double step_size, double max_move);
     uint32_t block() const;
+    void stage(size_t doubles);
     void set_option(const std::string& name, int64_t value);
     int64_t get_option(const std::string& name) const;
     double max_displacement(uint32_t s);
@@ -183,6 +184,7 @@ private:
     DevBuf<SysState> dst_;
     DevBuf<PairParam> dpair_;
     DevBuf<double> partial_, thermo_;
+    DevBuf<double> io_;                          // staging of tag-ordered set / get arrays
     // overflow snapshot
     DevBuf<float4> snap_pos_, snap_vel_, snap_img_, snap_force_;
     DevBuf<uint32_t> snap_id_, snap_rid_;

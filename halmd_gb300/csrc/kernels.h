@@ -35,6 +35,12 @@ void launch_density_modes(const Dev& d, const uint32_t* range, uint32_t nrange, 
                           const uint32_t* blk_begin, uint32_t nblk, const float4* q, uint32_t nq, double* partial,
                           double* out, cudaStream_t st);
 
+// phase-space transfer in tag order (kernels_io.cu): set what = 0 position,
+// 1 velocity; get what = 0 position, 1 unwrapped position, 2 velocity,
+// 3 force, 4 image (arrays of 3 n doubles on the device)
+void launch_set_vector(const Dev& d, uint32_t s, uint32_t n, int what, bool ds, const double* in, cudaStream_t st);
+void launch_get_vector(const Dev& d, uint32_t s, uint32_t n, int what, double* out, cudaStream_t st);
+
 // MSD of one sample pair with fixed scratch and no allocation (msd_noalloc.cu)
 void msd_pair_noalloc(const double* origin, const double* position, uint32_t count, double* out, cudaStream_t st);
 

@@ -81,7 +81,7 @@ __global__ void k_hilbert_keys(Dev d, uint32_t* keys)
 // is one launch over all tiles (digit histograms), one block per system
 // (digit-major exclusive scan of its tiles) and one launch over all tiles
 // (stable scatter with warp-match ranking).  Only systems that rebuild with
-// sorting on do work; passes are even so the permutation ends in val[0].
+// sorting on do work; the permutation ends in val[passes % 2].
 // ---------------------------------------------------------------------------
 
 constexpr int RADIX_THREADS = 256;
@@ -597,8 +597,8 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
 
 int radix_passes(uint32_t key_bits) { return (int)((key_bits + 7) / 8); }
 
-// Sort the slot ranges of the systems that rebuild; `passes` is even, so the
-// permutation ends in val[0]
+// Sort the slot ranges of the systems that rebuild; the permutation ends in
+// val[passes % 2]
 void launch_sort(const Dev& d, int passes, cudaStream_t st)
 {
     k_seg_keys<<<d.S / 256, 256, 0, st>>>(d);
