@@ -445,7 +445,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="ka64k")
     ap.add_argument("--md-steps", type=int, default=100, help="MD steps per bench step")
-    ap.add_argument("--ref-steps", type=int, default=2, help="MD steps per bench step of the reference arm")
+    ap.add_argument("--ref-steps", type=int, default=20, help="MD steps per bench step of the reference arm")
     ap.add_argument("--ref-relax", type=int, default=100,
                     help="steepest-descent steps of the reference arm's KA start (CPU)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
