@@ -578,8 +578,8 @@ Dev Engine::dev() const
     // the shared scan does a warp's 32 particles in one serial pass over the
     // cells around them: it pays off once there are enough warps per SM to
     // hide that pass's latency (about 2^19 slots on 152 SMs); smaller engines
-    // give each particle a warp of its own
-    d.nbr_scan = nbr_scan_ ? nbr_scan_ : (S_ >= (1u << 19) ? 2u : 3u);
+    // scan per lane (a warp per particle measured slower at every size)
+    d.nbr_scan = nbr_scan_ ? nbr_scan_ : (S_ >= (1u << 19) ? 2u : 1u);
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
     d.S = S_; d.nsys = table_size_;
@@ -904,8 +904,8 @@ void Engine::set_option(const std::string& name, int64_t value)
         return;
     }
     if (name == "neighbour_scan") {
-        if (value < 0 || value > 3)
-            throw Error(HMD_ERR_INVALID, "neighbour_scan must be 0 (auto), 1 (per lane), 2 (shared per warp) or 3 (warp per particle)");
+        if (value < 0 || value > 2)
+            throw Error(HMD_ERR_INVALID, "neighbour_scan must be 0 (auto), 1 (per lane) or 2 (shared per warp)");
         if (nbr_scan_ == (uint32_t)value) return;
         nbr_scan_ = (uint32_t)value;
         if (committed_) destroy_graphs();   // captured launches carry the old setting

@@ -628,115 +628,9 @@ void launch_binning(const Dev& d, cudaStream_t st)
     k_cell_sort<<<(d.total_cells + 3) / 4, 128, 0, st>>>(d);
 }
 
-// ---------------------------------------------------------------------------
-// One warp per particle (Dev::nbr_scan = 3; by default engines below 2^19
-// slots, where a thread or a warp per 32 particles leaves most of the GPU
-// idle): the 27 cells around the particle (each distinct cell once when a
-// dimension has fewer than 3 cells), lane t takes entry t of a cell, and the
-// hits of a round are appended in lane order (near from the front of the
-// list, far from its back) with one ballot each: the entries come out in
-// cell order and, within a cell, in slot order.
-// ---------------------------------------------------------------------------
-
-constexpr uint32_t NBR_WARP_BLOCK = 256;   // eight particles per block
-
-__global__ void __launch_bounds__(NBR_WARP_BLOCK) k_neighbour_warp(Dev d)
-{
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t i = blockIdx.x * (NBR_WARP_BLOCK / 32) + warp;
-    const uint32_t s = d.chunk_sys[(blockIdx.x * (NBR_WARP_BLOCK / 32)) / CHUNK];
-    const SysParam& P = d.sys[s];
-    __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
-    __shared__ float s_rrnear[MAX_SPECIES * MAX_SPECIES];
-    __shared__ uint32_t s_max[NBR_WARP_BLOCK / 32];
-    if (threadIdx.x < P.ns * P.ns) {
-        s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
-        s_rrnear[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_near;
-    }
-    __syncthreads();
-    if (!(P.active && d.st[s].rebuild)) return;   // block-uniform (eight slots of one system)
-    const float4 ri = d.pos[i];
-    const uint32_t a = species_bits(ri.w);
-    uint32_t count = 0;
-    if (a != PLACEHOLDER) {                       // warp-uniform
-        if (lane == 0) d.r0[i] = ri;
-        const float* rrcs = s_rrcs + a * P.ns;
-        const float* rrnear = s_rrnear + a * P.ns;
-        // an inner particle sees no neighbour across the box: |s| < L/2 for every
-        // pair it accepts, where the minimum image leaves s unchanged
-        const bool wrap = !(fabsf(ri.x) < P.inner[0] && fabsf(ri.y) < P.inner[1] && fabsf(ri.z) < P.inner[2]);
-        const uint32_t lw = d.lb_log2, lmask = (1u << lw) - 1u;
-        const size_t bstride = (size_t)d.S << lw;
-        uint32_t* out = d.nbr + ((size_t)i << lw);
-        const uint32_t cap = d.nbr_cap;
-        const uint32_t lt = (1u << lane) - 1u;
-        uint32_t nn = 0, nf = 0;
-        int cx, cy, cz;
-        cell_coords(P, ri, cx, cy, cz);
-        const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
-        const int lox = nx >= 3 ? -1 : 0, hix = nx >= 2 ? 1 : 0;
-        const int loy = ny >= 3 ? -1 : 0, hiy = ny >= 2 ? 1 : 0;
-        const int loz = nz >= 3 ? -1 : 0, hiz = nz >= 2 ? 1 : 0;
-        const uint32_t cs = P.cell_size;
-        for (int oz = loz; oz <= hiz; ++oz) {
-            const int z = (cz + oz + nz) % nz;
-            for (int oy = loy; oy <= hiy; ++oy) {
-                const int y = (cy + oy + ny) % ny;
-                for (int ox = lox; ox <= hix; ++ox) {
-                    const int x = (cx + ox + nx) % nx;
-                    const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
-                    const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
-                    const uint32_t* cell = d.cell + P.cell_word_off + c * cs;
-                    for (uint32_t k = 0; k < nc; k += 32) {
-                        bool hit = false, near = false;
-                        uint32_t j = 0;
-                        if (k + lane < nc) {
-                            j = __ldg(cell + k + lane);
-                            const float4 rj = __ldg(d.pos + j);
-                            const float sx = __fsub_rn(ri.x, rj.x), sy = __fsub_rn(ri.y, rj.y), sz = __fsub_rn(ri.z, rj.z);
-                            const float dx = wrap ? min_image(sx, P.L[0], P.Linv[0]) : sx;
-                            const float dy = wrap ? min_image(sy, P.L[1], P.Linv[1]) : sy;
-                            const float dz = wrap ? min_image(sz, P.L[2], P.Linv[2]) : sz;
-                            const float rr = rr_exact(dx, dy, dz);
-                            const uint32_t b = species_bits(rj.w);
-                            hit = j != i && b < P.ns && rr <= rrcs[b];
-                            near = hit && rr < rrnear[b];
-                        }
-                        const uint32_t bn = __ballot_sync(0xFFFFFFFFu, near);
-                        const uint32_t bf = __ballot_sync(0xFFFFFFFFu, hit && !near);
-                        // stored while fewer than cap entries precede it (as the per-lane append)
-                        if (hit && nn + nf + __popc((bn | bf) & lt) < cap) {
-                            const uint32_t e = near ? nn + __popc(bn & lt) : cap - 1u - (nf + __popc(bf & lt));
-                            out[(e >> lw) * bstride + (e & lmask)] = j;
-                        }
-                        nn += __popc(bn);
-                        nf += __popc(bf);
-                    }
-                }
-            }
-        }
-        count = nn + nf;
-        if (lane == 0) {
-            const uint32_t sn = min(nn, cap);
-            const uint32_t sf = min(nf, cap - sn);   // stored regions never overlap
-            d.nbr_count[i] = sn | (sf << 16);
-        }
-    }
-    // block-aggregated maximum and overflow flag
-    if (lane == 0) s_max[warp] = count;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t m = 0;
-        for (uint32_t w = 0; w < NBR_WARP_BLOCK / 32; ++w) m = max(m, s_max[w]);
-        if (m > 0) atomicMax(&d.st[s].max_nbr, m);
-        if (m > d.nbr_cap) atomicOr(d.status, ST_NBR_OVERFLOW);
-    }
-}
-
 void launch_neighbour(const Dev& d, cudaStream_t st)
 {
-    if (d.nbr_scan == 3u) k_neighbour_warp<<<d.S / (NBR_WARP_BLOCK / 32), NBR_WARP_BLOCK, 0, st>>>(d);
-    else k_neighbour<<<d.S / 128, 128, 0, st>>>(d);
+    k_neighbour<<<d.S / 128, 128, 0, st>>>(d);
 }
 
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
