@@ -274,6 +274,24 @@ def run_ensemble(args):
         load(batch, k, s)
     batch.step(M)
     lanes, lane_ms = autotune_force_lanes(batch, use_cache=False)
+    if args.phases:
+        # module-path breakdown of the batched step (one launch per phase for all replicas)
+        chains0 = batch.get_option("rebuild_chains")
+        batch.profile(True)
+        for _ in range(args.phases):
+            batch.integrate()
+            batch.force()
+            batch.finalize()
+        out = {"workload": "ENS-256", "particles": ntot, "md_steps": args.phases, "force_lanes": lanes,
+               "list_block": batch.get_option("list_block"),
+               "rebuild_chains": batch.get_option("rebuild_chains") - chains0}
+        for ph in ("integrate", "rebuild", "force", "finalize"):
+            ms, cnt = batch.profile_get(ph)
+            out[ph + "_ms_per_call"] = ms / max(cnt, 1)
+            out[ph + "_ms_per_step"] = ms / max(args.phases, 1)
+        print(json.dumps(out))
+        batch.close()
+        return
     for _ in range(args.warmup):
         batch.step(M)
     stream = torch.cuda.ExternalStream(batch.stream)

@@ -575,11 +575,7 @@ Dev Engine::dev() const
     d.nbr = nbr_.p; d.nbr_count = nbr_count_.p; d.nbr_cap = nbr_cap_;
     d.lanes = lanes_;
     d.lb_log2 = block() == 8u ? 3u : 2u;
-    // the shared scan does a warp's 32 particles in one serial pass over the
-    // cells around them: it pays off once there are enough warps per SM to
-    // hide that pass's latency (about 2^19 slots on 152 SMs); smaller engines
-    // scan per lane (a warp per particle measured slower at every size)
-    d.nbr_scan = nbr_scan_ ? nbr_scan_ : (S_ >= (1u << 19) ? 2u : 1u);
+    d.nbr_scan = nbr_scan_;   // 0: each system by its own size (k_neighbour)
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
     d.S = S_; d.nsys = table_size_;

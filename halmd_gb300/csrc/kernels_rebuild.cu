@@ -357,14 +357,14 @@ __global__ void __launch_bounds__(128) k_cell_sort(Dev d)
 // the back.  Also stores r0 = r for the displacement check
 // (max_displacement.cpp:60-72).
 //
-// Shared scan (Dev::nbr_scan = 2; by default engines of at least 2^19
-// slots): one
+// Shared scan (Dev::nbr_scan = 2; by default systems of at least
+// NBR_SHARED_MIN_N particles): one
 // warp per 32 consecutive slots.  After the Hilbert sort these are
 // spatially compact, so the warp scans the cells around its bounding box
 // once for all 32 particles: lanes load 32 candidates of a cell at a time,
 // drop those farther than r_c + skin from the box, stage the rest in shared
 // memory, and every lane tests every staged candidate against its own
-// particle.  Smaller engines, and warps whose box spans too many cells (an
+// particle.  Smaller systems, and warps whose box spans too many cells (an
 // unsorted system, a tiny box), scan per lane instead: the 27 cells around each particle (each
 // distinct cell once when a dimension has fewer than 3 cells).  Both scans
 // test the same float criterion, so the pair sets are identical; entries are
@@ -372,6 +372,10 @@ __global__ void __launch_bounds__(128) k_cell_sort(Dev d)
 // ---------------------------------------------------------------------------
 
 constexpr uint32_t NBR_CLUSTER_MAX_CELLS = 150;   // larger cell ranges: per-lane scan
+// The shared scan does a warp's 32 particles in one serial pass over the cells
+// around them; it pays off once a rebuild has enough warps per SM to hide that
+// pass's latency (measured: 1M particles 1.8x faster, 64k particles 1.4x slower)
+constexpr uint32_t NBR_SHARED_MIN_N = 1u << 18;
 
 struct NbrOut {
     uint32_t* out;        // this slot's row in the blocked list
@@ -420,18 +424,20 @@ __device__ __forceinline__ void lane_scan(const Dev& d, const SysParam& P, float
             for (int ox = lox; ox <= hix; ++ox) {
                 const int x = (cx + ox + nx) % nx;
                 const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
-                // occupied slots of the cell (ascending), four at a time so the
-                // position gathers are independent of one another
+                // occupied slots of the cell (ascending), eight at a time so the
+                // position gathers are independent of one another (cells hold a
+                // multiple of 32 words: the second load stays inside the cell)
                 const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
                 const uint4* cell4 = reinterpret_cast<const uint4*>(d.cell + P.cell_word_off + c * cs);
-                for (uint32_t k = 0; k < nc; k += 4) {
-                    const uint4 jj = __ldg(cell4 + (k >> 2));
-                    const uint32_t jv[4] = {jj.x, jj.y, jj.z, jj.w};
-                    float4 rv[4];
+                for (uint32_t k = 0; k < nc; k += 8) {
+                    const uint4 j0 = __ldg(cell4 + (k >> 2));
+                    const uint4 j1 = __ldg(cell4 + (k >> 2) + 1);
+                    const uint32_t jv[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
+                    float4 rv[8];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) rv[u] = (k + u < nc) ? __ldg(d.pos + jv[u]) : make_float4(0, 0, 0, 0);
+                    for (int u = 0; u < 8; ++u) rv[u] = (k + u < nc) ? __ldg(d.pos + jv[u]) : make_float4(0, 0, 0, 0);
 #pragma unroll
-                    for (int u = 0; u < 4; ++u)
+                    for (int u = 0; u < 8; ++u)
                         if (k + u < nc) nbr_test<true>(P, ri, i, rv[u], jv[u], rrcs, rrnear, o);
                 }
             }
@@ -563,7 +569,11 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
             wrap |= !(__fsub_rn(lo[q], rcs) > -half && __fadd_rn(hi[q], rcs) < half &&
                       (hi[q] - lo[q]) + 2.0f * rcs < 0.49f * P.L[q]);
         }
-        if (d.nbr_scan == 2u && ncells <= NBR_CLUSTER_MAX_CELLS) {
+        // by default a system of at least NBR_SHARED_MIN_N particles uses the shared
+        // scan: a decision of the system alone, so its lists (and their order) do
+        // not depend on the other systems of the engine
+        const bool shared = d.nbr_scan == 2u || (d.nbr_scan == 0u && P.n >= NBR_SHARED_MIN_N);
+        if (shared && ncells <= NBR_CLUSTER_MAX_CELLS) {
             if (wrap)
                 cluster_scan<true>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos[warp],
                                    s_j[warp], lane);
