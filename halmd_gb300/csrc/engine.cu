@@ -900,9 +900,8 @@ void Engine::set_option(const std::string& name, int64_t value)
         return;
     }
     if (name == "neighbour_scan") {
-        if (value < 0 || value > 3)
-            throw Error(HMD_ERR_INVALID,
-                        "neighbour_scan must be 0 (auto), 1 (per lane), 2 (shared per warp) or 3 (four lanes per particle)");
+        if (value < 0 || value > 2)
+            throw Error(HMD_ERR_INVALID, "neighbour_scan must be 0 (auto), 1 (per lane) or 2 (shared per warp)");
         if (nbr_scan_ == (uint32_t)value) return;
         nbr_scan_ = (uint32_t)value;
         if (committed_) destroy_graphs();   // captured launches carry the old setting
@@ -986,20 +985,7 @@ void Engine::rebuild_chain(cudaStream_t st)
         launch_rearrange(d, ds(), d.val[sort_passes_ & 1], st);   // pass p writes val[1 - p % 2]
     }
     launch_binning(d, st);
-    uint32_t lo, hi;
-    system_size_range(lo, hi);
-    launch_neighbour(d, lo, hi, st);
-}
-
-// smallest and largest system (which list-build scans a chain launches); an
-// engine with reserved capacity takes any size later, so it launches both
-void Engine::system_size_range(uint32_t& lo, uint32_t& hi) const
-{
-    lo = 0xFFFFFFFFu;
-    hi = 0u;
-    for (const auto& h : sys_)
-        if (h.used) { lo = std::min(lo, h.P.n); hi = std::max(hi, h.P.n); }
-    if (capacity_ || lo > hi) { lo = 0u; hi = 0xFFFFFFFFu; }
+    launch_neighbour(d, st);
 }
 
 void Engine::ensure_forces(bool aux)
@@ -1283,10 +1269,7 @@ void Engine::profile_get(const std::string& phase, double* total_ms, uint64_t* c
 uint32_t Engine::rebuild_kernel_count() const
 {
     // sort keys + (hist, scan, scatter) per pass + rearrange + copy back; cell clear, bin, sort; list build
-    uint32_t lo, hi;
-    system_size_range(lo, hi);
-    return (any_sort_ ? (uint32_t)sort_kernel_count(sort_passes_) + 2u : 0u) + 3u +
-           (uint32_t)neighbour_kernel_count(dev(), lo, hi);
+    return (any_sort_ ? (uint32_t)sort_kernel_count(sort_passes_) + 2u : 0u) + 3u + 1u;
 }
 
 void Engine::integrate()

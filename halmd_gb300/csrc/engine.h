@@ -105,7 +105,6 @@ public:
     void minimize(uint32_t s, uint32_t steps, double step_size, double max_move);
     uint32_t block() const;
     void stage(size_t doubles);
-    void system_size_range(uint32_t& lo, uint32_t& hi) const;
     void set_option(const std::string& name, int64_t value);
     int64_t get_option(const std::string& name) const;
     double max_displacement(uint32_t s);

@@ -24,10 +24,7 @@ void launch_sort(const Dev& d, int passes, cudaStream_t st);
 int sort_kernel_count(int passes);
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st);
 void launch_binning(const Dev& d, cudaStream_t st);
-// list build over all systems that rebuild; min_n / max_n: smallest and largest
-// system of the engine (which scans to launch)
-void launch_neighbour(const Dev& d, uint32_t min_n, uint32_t max_n, cudaStream_t st);
-int neighbour_kernel_count(const Dev& d, uint32_t min_n, uint32_t max_n);
+void launch_neighbour(const Dev& d, cudaStream_t st);
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st);
 
 // observables (kernels_obs.cu)

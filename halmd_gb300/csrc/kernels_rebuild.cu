@@ -364,8 +364,8 @@ __global__ void __launch_bounds__(128) k_cell_sort(Dev d)
 // once for all 32 particles: lanes load 32 candidates of a cell at a time,
 // drop those farther than r_c + skin from the box, stage the rest in shared
 // memory, and every lane tests every staged candidate against its own
-// particle.  Warps whose box spans too many cells (an unsorted system, a
-// tiny box) scan per lane instead; smaller systems use the quad scan below: the 27 cells around each particle (each
+// particle.  Smaller systems, and warps whose box spans too many cells (an
+// unsorted system, a tiny box), scan per lane instead: the 27 cells around each particle (each
 // distinct cell once when a dimension has fewer than 3 cells).  Both scans
 // test the same float criterion, so the pair sets are identical; entries are
 // appended in cell order and, within a cell, in slot order (deterministic).
@@ -520,7 +520,6 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
     }
     __syncthreads();
     if (!(P.active && d.st[s].rebuild)) return;   // block-uniform
-    if (d.nbr_scan == 3u || (d.nbr_scan == 0u && P.n < NBR_SHARED_MIN_N)) return;   // the quad scan's system
     const float4 ri = d.pos[i];
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;
@@ -639,156 +638,9 @@ void launch_binning(const Dev& d, cudaStream_t st)
     k_cell_sort<<<(d.total_cells + 3) / 4, 128, 0, st>>>(d);
 }
 
-// ---------------------------------------------------------------------------
-// Quad scan (Dev::nbr_scan = 3; by default systems below NBR_SHARED_MIN_N
-// particles): four lanes per particle walk the same 27 cells as the per-lane
-// scan, lane q taking entries q and q + 4 of every eight of a cell, and the
-// hits of each round are appended in entry order with ballots over the four
-// lanes.  The list is the per-lane scan's, entry for entry, with a quarter of
-// the serial work per thread: small systems fill the GPU.
-// ---------------------------------------------------------------------------
-
-template <bool WRAP>
-__device__ __forceinline__ void quad_test(const SysParam& P, float4 ri, uint32_t i, uint32_t j, float4 rj, bool have,
-                                          const float* rrcs, const float* rrnear, bool& hit, bool& near)
+void launch_neighbour(const Dev& d, cudaStream_t st)
 {
-    hit = near = false;
-    if (!have || j == i) return;
-    const float sx = __fsub_rn(ri.x, rj.x), sy = __fsub_rn(ri.y, rj.y), sz = __fsub_rn(ri.z, rj.z);
-    // an inner particle accepts no pair across the box: there |s| < L/2, where
-    // the minimum image leaves s unchanged
-    const float dx = WRAP ? min_image(sx, P.L[0], P.Linv[0]) : sx;
-    const float dy = WRAP ? min_image(sy, P.L[1], P.Linv[1]) : sy;
-    const float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
-    const float rr = rr_exact(dx, dy, dz);
-    const uint32_t b = species_bits(rj.w);
-    hit = b < P.ns && rr <= rrcs[b];
-    near = hit && rr < rrnear[b];
-}
-
-template <bool WRAP>
-__device__ __forceinline__ void quad_scan(const Dev& d, const SysParam& P, float4 ri, uint32_t i, uint32_t q,
-                                          uint32_t grp, const float* rrcs, const float* rrnear, NbrOut& o)
-{
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t below = grp & ((1u << lane) - 1u);   // the group's lanes before this one
-    int cx, cy, cz;
-    cell_coords(P, ri, cx, cy, cz);
-    const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
-    const int lox = nx >= 3 ? -1 : 0, hix = nx >= 2 ? 1 : 0;
-    const int loy = ny >= 3 ? -1 : 0, hiy = ny >= 2 ? 1 : 0;
-    const int loz = nz >= 3 ? -1 : 0, hiz = nz >= 2 ? 1 : 0;
-    const uint32_t cs = P.cell_size;
-    for (int oz = loz; oz <= hiz; ++oz) {
-        const int z = (cz + oz + nz) % nz;
-        for (int oy = loy; oy <= hiy; ++oy) {
-            const int y = (cy + oy + ny) % ny;
-            for (int ox = lox; ox <= hix; ++ox) {
-                const int x = (cx + ox + nx) % nx;
-                const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
-                const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
-                const uint32_t* cell = d.cell + P.cell_word_off + c * cs;
-                for (uint32_t k = 0; k < nc; k += 8) {
-                    // entries k + q and k + 4 + q (cells hold a multiple of 32 words)
-                    const bool h0 = k + q < nc, h1 = k + 4 + q < nc;
-                    const uint32_t j0 = __ldg(cell + k + q), j1 = __ldg(cell + k + 4 + q);
-                    const float4 r0 = h0 ? __ldg(d.pos + j0) : make_float4(0, 0, 0, 0);
-                    const float4 r1 = h1 ? __ldg(d.pos + j1) : make_float4(0, 0, 0, 0);
-                    bool hit0, near0, hit1, near1;
-                    quad_test<WRAP>(P, ri, i, j0, r0, h0, rrcs, rrnear, hit0, near0);
-                    quad_test<WRAP>(P, ri, i, j1, r1, h1, rrcs, rrnear, hit1, near1);
-                    const uint32_t bn0 = __ballot_sync(grp, near0) & grp, bf0 = __ballot_sync(grp, hit0 && !near0) & grp;
-                    const uint32_t bn1 = __ballot_sync(grp, near1) & grp, bf1 = __ballot_sync(grp, hit1 && !near1) & grp;
-                    const uint32_t nn0 = o.nn, nf0 = o.nf;
-                    if (hit0) {
-                        const uint32_t before = nn0 + nf0 + __popc((bn0 | bf0) & below);
-                        if (before < o.cap) {
-                            const uint32_t e = near0 ? nn0 + __popc(bn0 & below) : o.cap - 1u - (nf0 + __popc(bf0 & below));
-                            o.out[(e >> o.lw) * o.bstride + (e & o.lmask)] = j0;
-                        }
-                    }
-                    const uint32_t nn1 = nn0 + __popc(bn0), nf1 = nf0 + __popc(bf0);
-                    if (hit1) {
-                        const uint32_t before = nn1 + nf1 + __popc((bn1 | bf1) & below);
-                        if (before < o.cap) {
-                            const uint32_t e = near1 ? nn1 + __popc(bn1 & below) : o.cap - 1u - (nf1 + __popc(bf1 & below));
-                            o.out[(e >> o.lw) * o.bstride + (e & o.lmask)] = j1;
-                        }
-                    }
-                    o.nn = nn1 + __popc(bn1);
-                    o.nf = nf1 + __popc(bf1);
-                }
-            }
-        }
-    }
-}
-
-__global__ void __launch_bounds__(128) k_neighbour_quad(Dev d)
-{
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t i = t >> 2, q = t & 3u;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t s = d.chunk_sys[(blockIdx.x * (blockDim.x / 4)) / CHUNK];
-    const SysParam& P = d.sys[s];
-    __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
-    __shared__ float s_rrnear[MAX_SPECIES * MAX_SPECIES];
-    if (threadIdx.x < P.ns * P.ns) {
-        s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
-        s_rrnear[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_near;
-    }
-    __syncthreads();
-    if (!(P.active && d.st[s].rebuild)) return;   // block-uniform (32 slots of one system)
-    if (!(d.nbr_scan == 3u || (d.nbr_scan == 0u && P.n < NBR_SHARED_MIN_N))) return;   // another scan's system
-    const float4 ri = d.pos[i];
-    const uint32_t a = species_bits(ri.w);
-    const bool real = a != PLACEHOLDER;            // uniform over the particle's four lanes
-    const uint32_t grp = 0xFu << (lane & ~3u);
-    NbrOut o;
-    o.lw = d.lb_log2;
-    o.lmask = (1u << o.lw) - 1u;
-    o.bstride = (size_t)d.S << o.lw;
-    o.out = d.nbr + ((size_t)i << o.lw);
-    o.cap = d.nbr_cap;
-    if (real) {
-        if (q == 0) d.r0[i] = ri;
-        const float* rrcs = s_rrcs + a * P.ns;
-        const float* rrnear = s_rrnear + a * P.ns;
-        const bool inner = fabsf(ri.x) < P.inner[0] && fabsf(ri.y) < P.inner[1] && fabsf(ri.z) < P.inner[2];
-        if (inner) quad_scan<false>(d, P, ri, i, q, grp, rrcs, rrnear, o);
-        else quad_scan<true>(d, P, ri, i, q, grp, rrcs, rrnear, o);
-    }
-    uint32_t count = 0;
-    if (real) {
-        count = o.nn + o.nf;
-        if (q == 0) {
-            const uint32_t sn = min(o.nn, o.cap);
-            const uint32_t sf = min(o.nf, o.cap - sn);   // stored regions never overlap
-            d.nbr_count[i] = sn | (sf << 16);
-        }
-    }
-    uint32_t m = count;
-#pragma unroll
-    for (int w = 16; w > 0; w >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, w));
-    if (lane == 0) {
-        if (m > 0) atomicMax(&d.st[s].max_nbr, m);
-        if (m > d.nbr_cap) atomicOr(d.status, ST_NBR_OVERFLOW);
-    }
-}
-
-// the quad scan serves the systems below NBR_SHARED_MIN_N (or all, when
-// chosen), k_neighbour the rest; each returns early for the other's systems
-bool neighbour_quad(const Dev& d, uint32_t min_n) { return d.nbr_scan == 3u || (d.nbr_scan == 0u && min_n < NBR_SHARED_MIN_N); }
-bool neighbour_lane(const Dev& d, uint32_t max_n) { return d.nbr_scan == 1u || d.nbr_scan == 2u || (d.nbr_scan == 0u && max_n >= NBR_SHARED_MIN_N); }
-
-void launch_neighbour(const Dev& d, uint32_t min_n, uint32_t max_n, cudaStream_t st)
-{
-    if (neighbour_quad(d, min_n)) k_neighbour_quad<<<d.S / 32, 128, 0, st>>>(d);
-    if (neighbour_lane(d, max_n)) k_neighbour<<<d.S / 128, 128, 0, st>>>(d);
-}
-
-int neighbour_kernel_count(const Dev& d, uint32_t min_n, uint32_t max_n)
-{
-    return (neighbour_quad(d, min_n) ? 1 : 0) + (neighbour_lane(d, max_n) ? 1 : 0);
+    k_neighbour<<<d.S / 128, 128, 0, st>>>(d);
 }
 
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
