@@ -391,25 +391,35 @@ struct NbrOut {
     }
 };
 
+// box and species count in registers: the list stores of the scan loops
+// could alias SysParam in global memory and would force a reload per pair
+struct NbrBox {
+    float L[3], Linv[3];
+    uint32_t ns;
+    __device__ __forceinline__ explicit NbrBox(const SysParam& P)
+        : L{P.L[0], P.L[1], P.L[2]}, Linv{P.Linv[0], P.Linv[1], P.Linv[2]}, ns(P.ns) {}
+};
+
 template <bool WRAP>
-__device__ __forceinline__ void nbr_test(const SysParam& P, float4 ri, uint32_t i, float4 rj, uint32_t j,
+__device__ __forceinline__ void nbr_test(const NbrBox& B, float4 ri, uint32_t i, float4 rj, uint32_t j,
                                          const float* rrcs, const float* rrnear, NbrOut& o)
 {
     if (j == i) return;
     const float sx = __fsub_rn(ri.x, rj.x), sy = __fsub_rn(ri.y, rj.y), sz = __fsub_rn(ri.z, rj.z);
     // without a wrap every |s| < L/2, where min_image returns s unchanged
-    const float dx = WRAP ? min_image(sx, P.L[0], P.Linv[0]) : sx;
-    const float dy = WRAP ? min_image(sy, P.L[1], P.Linv[1]) : sy;
-    const float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
+    const float dx = WRAP ? min_image(sx, B.L[0], B.Linv[0]) : sx;
+    const float dy = WRAP ? min_image(sy, B.L[1], B.Linv[1]) : sy;
+    const float dz = WRAP ? min_image(sz, B.L[2], B.Linv[2]) : sz;
     const float rr = rr_exact(dx, dy, dz);
     const uint32_t b = species_bits(rj.w);
-    if (b < P.ns && rr <= rrcs[b]) o.add(j, rr < rrnear[b]);
+    if (b < B.ns && rr <= rrcs[b]) o.add(j, rr < rrnear[b]);
 }
 
 // the 27 cells around the particle, for one lane
 __device__ __forceinline__ void lane_scan(const Dev& d, const SysParam& P, float4 ri, uint32_t i, const float* rrcs,
                                           const float* rrnear, NbrOut& o)
 {
+    const NbrBox B(P);
     int cx, cy, cz;
     cell_coords(P, ri, cx, cy, cz);
     const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
@@ -424,21 +434,19 @@ __device__ __forceinline__ void lane_scan(const Dev& d, const SysParam& P, float
             for (int ox = lox; ox <= hix; ++ox) {
                 const int x = (cx + ox + nx) % nx;
                 const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
-                // occupied slots of the cell (ascending), eight at a time so the
-                // position gathers are independent of one another (cells hold a
-                // multiple of 32 words: the second load stays inside the cell)
+                // occupied slots of the cell (ascending), four at a time so the
+                // position gathers are independent of one another
                 const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
                 const uint4* cell4 = reinterpret_cast<const uint4*>(d.cell + P.cell_word_off + c * cs);
-                for (uint32_t k = 0; k < nc; k += 8) {
-                    const uint4 j0 = __ldg(cell4 + (k >> 2));
-                    const uint4 j1 = __ldg(cell4 + (k >> 2) + 1);
-                    const uint32_t jv[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
-                    float4 rv[8];
+                for (uint32_t k = 0; k < nc; k += 4) {
+                    const uint4 jj = __ldg(cell4 + (k >> 2));
+                    const uint32_t jv[4] = {jj.x, jj.y, jj.z, jj.w};
+                    float4 rv[4];
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) rv[u] = (k + u < nc) ? __ldg(d.pos + jv[u]) : make_float4(0, 0, 0, 0);
+                    for (int u = 0; u < 4; ++u) rv[u] = (k + u < nc) ? __ldg(d.pos + jv[u]) : make_float4(0, 0, 0, 0);
 #pragma unroll
-                    for (int u = 0; u < 8; ++u)
-                        if (k + u < nc) nbr_test<true>(P, ri, i, rv[u], jv[u], rrcs, rrnear, o);
+                    for (int u = 0; u < 4; ++u)
+                        if (k + u < nc) nbr_test<true>(B, ri, i, rv[u], jv[u], rrcs, rrnear, o);
                 }
             }
         }
@@ -453,6 +461,7 @@ __device__ __forceinline__ void cluster_scan(const Dev& d, const SysParam& P, fl
                                              const float* hi, const int* c0, const int* ncr, float rcs2,
                                              float4* s_pos, uint32_t* s_j, uint32_t lane)
 {
+    const NbrBox B(P);
     const float cxb = 0.5f * (lo[0] + hi[0]), cyb = 0.5f * (lo[1] + hi[1]), czb = 0.5f * (lo[2] + hi[2]);
     const float hxb = 0.5f * (hi[0] - lo[0]), hyb = 0.5f * (hi[1] - lo[1]), hzb = 0.5f * (hi[2] - lo[2]);
     const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
@@ -476,9 +485,9 @@ __device__ __forceinline__ void cluster_scan(const Dev& d, const SysParam& P, fl
                         // distance from the candidate to the bounding box
                         float ex = __fsub_rn(rj.x, cxb), ey = __fsub_rn(rj.y, cyb), ez = __fsub_rn(rj.z, czb);
                         if (WRAP) {
-                            ex = min_image(ex, P.L[0], P.Linv[0]);
-                            ey = min_image(ey, P.L[1], P.Linv[1]);
-                            ez = min_image(ez, P.L[2], P.Linv[2]);
+                            ex = min_image(ex, B.L[0], B.Linv[0]);
+                            ey = min_image(ey, B.L[1], B.Linv[1]);
+                            ez = min_image(ez, B.L[2], B.Linv[2]);
                         }
                         const float qx = fmaxf(fabsf(ex) - hxb, 0.0f);
                         const float qy = fmaxf(fabsf(ey) - hyb, 0.0f);
@@ -495,7 +504,7 @@ __device__ __forceinline__ void cluster_scan(const Dev& d, const SysParam& P, fl
                     const uint32_t nk = __popc(ballot);
                     if (real) {
 #pragma unroll 4
-                        for (uint32_t u = 0; u < nk; ++u) nbr_test<WRAP>(P, ri, i, s_pos[u], s_j[u], rrcs, rrnear, o);
+                        for (uint32_t u = 0; u < nk; ++u) nbr_test<WRAP>(B, ri, i, s_pos[u], s_j[u], rrcs, rrnear, o);
                     }
                     __syncwarp();
                 }
