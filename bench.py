@@ -256,8 +256,17 @@ def run_ensemble(args):
     step chunks) against looping the one-system path over the same replicas."""
     import torch
     import halmd_gb300 as hg
+    from halmd_gb300.shard import combine, partition, rank_env
     from halmd_gb300.tune import autotune_force_lanes
+    rank, world, local = rank_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     specs = ensemble_specs()
+    count = len(specs)
+    # replicas only: each rank takes a share of the replicas (bin-packed by size)
+    specs = [specs[k] for k in partition([s["n"] for s in specs], world)[rank]]
     ntot = sum(s["n"] for s in specs)
     M = args.md_steps
 
@@ -312,7 +321,9 @@ def run_ensemble(args):
     clk = clocks.stop()
     chains = batch.get_option("rebuild_chains") - chains0
     inf = batch.info(0)
-    batched = ntot * M * args.steps / (total_ms * 1e-3)
+    work_all, ms_all = combine(ntot * M * args.steps, total_ms, device="cuda")
+    batched = work_all / (ms_all * 1e-3)
+    ntot_all = combine(ntot, 0.0, device="cuda")[0]
     # step-graph kernels, plus the rebuild chain in every step where any replica rebuilt
     launches = (batch.get_option("step_kernels") - kernels0) + chains * inf.rebuild_kernels
     batch.close()
@@ -336,14 +347,20 @@ def run_ensemble(args):
             e.step(M)
     torch.cuda.synchronize()
     loop_s = time.perf_counter() - t0
-    looped = ntot * M * loop_steps / loop_s
+    lwork, lms = combine(ntot * M * loop_steps, 1e3 * loop_s, device="cuda")
+    looped = lwork / (lms * 1e-3)
     for e in engines:
         e.close()
-    line = {"metric": "particle-steps/s", "value": batched, "unit": "particle-steps/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / (M * args.steps),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (dsfloat state)",
-            "data": "synthetic",
-            "config": {"workload": "ENS-256", "replicas": len(specs), "particles": ntot,
+    if world > 1:
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    line = {"metric": "particle-steps/s", "value": batched, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_all / (M * args.steps),
+            "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None,
+            "dtype": "f32 (dsfloat state)", "data": "synthetic",
+            "config": {"workload": "ENS-256", "replicas": count, "particles": int(ntot_all),
+                       "parallelism": "replicas bin-packed over %d GPUs" % world if world > 1 else "single",
                        "md_steps_per_bench_step": M, "force_lanes": lanes,
                        "autotune_force_ms": {str(k): v for k, v in lane_ms.items()},
                        "l2": "flushed (256 MB write) between timed bench steps"},
@@ -391,25 +408,62 @@ def serve_jobs(count, steps_scale, rate=50.0, seed=2000):
 def run_serve(args):
     """SERVE: continuous batching under an 80% HBM budget against a FIFO run
     of the one-system path, same job stream."""
-    from halmd_gb300.serve import Server, latency_stats, run_fifo
-    jobs = serve_jobs(args.serve_jobs, args.serve_steps_scale)
+    import torch
+    from halmd_gb300.serve import Server, run_fifo
+    from halmd_gb300.shard import combine, partition, rank_env
+    rank, world, local = rank_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def my_jobs():
+        # replicas only: each rank serves a share of the stream (bin-packed by work)
+        all_jobs = serve_jobs(args.serve_jobs, args.serve_steps_scale)
+        return [all_jobs[k] for k in partition([j.work for j in all_jobs], world)[rank]]
+
+    def gather_latency(js):
+        lat = [j.completed - j.arrival for j in js]
+        if dist is None:
+            return lat
+        out = [None] * world
+        dist.all_gather_object(out, lat)
+        return [x for part in out for x in part]
+
+    def pct(lat):
+        a = np.array(lat)
+        return {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99)), "mean": float(a.mean())}
+
+    jobs = my_jobs()
     work = sum(j.work for j in jobs)
     srv = Server(budget_fraction=0.8, max_slots=args.serve_max_slots, max_jobs=1024, neighbour_capacity=288,
                  chunk=args.md_steps)
     clocks = ClockSampler(0)
     st = srv.run(jobs, realtime=True)
     clk = clocks.stop()
-    lat = latency_stats(jobs)
+    lat = pct(gather_latency(jobs))
     budget = srv.budget
     srv.close()
-    fifo_jobs = serve_jobs(args.serve_jobs, args.serve_steps_scale)
+    work, makespan = combine(work, st["makespan"], device="cuda")
+    chunks = int(combine(st["chunks"], 0.0, device="cuda")[0])
+    fifo_jobs = my_jobs()
     fst = run_fifo(fifo_jobs)
-    flat = latency_stats(fifo_jobs)
-    line = {"metric": "particle-steps/s", "value": work / st["makespan"], "unit": "particle-steps/s", "n_gpus": 1,
+    flat = pct(gather_latency(fifo_jobs))
+    fmakespan = combine(0.0, fst["makespan"], device="cuda")[1]
+    njobs = int(combine(len(jobs), 0.0, device="cuda")[0])
+    if dist is not None:
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    st = {"makespan": makespan, "chunks": chunks}
+    fst = {"makespan": fmakespan}
+    line = {"metric": "particle-steps/s", "value": work / st["makespan"], "unit": "particle-steps/s", "n_gpus": world,
             "steps": st["chunks"], "warmup": 0, "ms_per_step": 1e3 * st["makespan"] / max(st["chunks"], 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (dsfloat state)",
             "data": "synthetic",
-            "config": {"workload": "SERVE", "jobs": len(jobs), "arrival_rate_per_s": 50,
+            "config": {"workload": "SERVE", "jobs": njobs, "arrival_rate_per_s": 50,
+                       "parallelism": "jobs bin-packed over %d GPUs" % world if world > 1 else "single",
                        "steps_scale": args.serve_steps_scale, "particle_steps": work, "chunk_md_steps": args.md_steps,
                        "hbm_budget": budget},
             "latency_s": {"p50": lat["p50"], "p99": lat["p99"], "mean": lat["mean"]},
