@@ -113,7 +113,6 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
     P.A = round_up(std::max<uint32_t>(d.nparticle, 1), align);
     P.ns = ns;
     P.trunc = (uint32_t)d.truncation;
-    P.rank = rank;
     P.active = 1;
     P.sort_enable = d.sort ? 1u : 0u;
     P.integrator = (uint32_t)d.integrator;
@@ -359,10 +358,15 @@ void Engine::commit()
     if (!tiles.empty())
         HMD_CUDA(cudaMemcpy(tiles_.p, tiles.data(), tiles.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     hist_.alloc(std::max<uint32_t>(hist_words, 1));
-    // lanes per particle in the force kernel: enough threads to fill 152 SMs
-    // for small engines, fewer lanes (less reduction work) for large ones
-    if (lanes_ == 0) lanes_ = S_ <= (1u << 19) ? 8u : 4u;
-    for (auto& h : sys_) h.P.key_shift = shift;
+    // force-kernel shape when not set (the autotuner refines it): small
+    // engines need several lanes per particle to fill 152 SMs (measured best
+    // at 64k particles: 4 lanes, 2 entries per load); large ones one lane
+    // with 4 entries per load (measured best at 1M)
+    if (lanes_ == 0) {
+        const bool small = S_ <= (1u << 19);
+        lanes_ = small ? 4u : 1u;
+        if (lb_ == 0 && small) lb_ = 8u;
+    }
 
     const size_t S = S_;
     pos_.alloc(2 * S); vel_.alloc(2 * S); img_.alloc(S); force_.alloc(S); r0_.alloc(S);
@@ -426,7 +430,6 @@ void Engine::install(uint32_t s)
     SysParam& P = h.P;
     P.pair_off = s * (uint32_t)(MAX_SPECIES * MAX_SPECIES);
     P.active = 1;
-    P.key_shift = key_bits_;
     const size_t S = S_;
     std::vector<float4> hp(P.A), hv(P.A, make_float4(0, 0, 0, 0));
     std::vector<uint32_t> ids(P.A), rids(P.A);

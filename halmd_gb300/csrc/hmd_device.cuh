@@ -76,14 +76,12 @@ struct SysParam {
     float dt, dt_half;
     float rr_half_skin;        // (skin/2)^2 rebuild threshold on squared displacement
     uint32_t depth;            // Hilbert recursion depth
-    uint32_t key_shift;        // sort key = (rank << key_shift) | local key
     uint32_t integrator;
     float sqrt_T;
     uint32_t coll_threshold;   // collision iff philox word < threshold
     uint32_t seed_lo, seed_hi;
     uint32_t active;           // 0: all slots are ghosts, kernels skip
     uint32_t sort_enable;      // Hilbert reorder on rebuild
-    uint32_t rank;             // position among systems (sort key prefix)
     float inner[3];            // |r| below this in every dimension: no list pair wraps the box
     uint32_t sort_hist_off;    // first word of this system's digit histograms
     uint32_t sort_ntiles;      // sort tiles covering the slot range
