@@ -153,6 +153,14 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
     }
     P.seed_lo = (uint32_t)d.seed;
     P.seed_hi = (uint32_t)(d.seed >> 32);
+    {
+        // a near pair (closer than NEAR_SIGMA sigma at the build) is within
+        // NEAR_SIGMA sigma + skin at force time in every coordinate; from twice
+        // that distance to zero on, a coordinate and its partner's differ exactly
+        double near_max = 0;
+        for (uint32_t ab = 0; ab < ns * ns; ++ab) near_max = std::max(near_max, NEAR_SIGMA * d.sigma[ab] + d.skin);
+        P.exact_min = (float)(2.0 * near_max * (1.0 + 1e-6));
+    }
     for (int q = 0; q < 3; ++q) {
         // a list pair is within r_c + skin of each other at force time (each
         // particle moved < skin/2 since the build); particles farther than

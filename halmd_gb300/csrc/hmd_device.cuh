@@ -85,6 +85,7 @@ struct SysParam {
     float inner[3];            // |r| below this in every dimension: no list pair wraps the box
     uint32_t sort_hist_off;    // first word of this system's digit histograms
     uint32_t sort_ntiles;      // sort tiles covering the slot range
+    float exact_min;           // |coordinate| from which near-pair differences are exact (k_force)
     float descent_step;        // INTEG_DESCENT: move = descent_step * F ...
     float descent_max;         // ... capped at this length per particle and step
 };
@@ -153,10 +154,13 @@ constexpr int NTHERMO = 14;    // see k_thermo_partial
 __device__ __forceinline__ uint32_t species_bits(float w) { return __float_as_uint(w); }
 
 // minimum image: k = rint(dr / L) via dr * (1/L); dr - k L (box_kernel.cuh:37-47)
+// dr - rint(dr / L) L for dr = ri - rj of two in-box positions: |dr| <= L,
+// so k is -1, 0 or 1, k L is exact, and the fused form rounds once exactly
+// like dr - fl(k L)
 __device__ __forceinline__ float min_image(float dr, float L, float Linv)
 {
-    float k = rintf(__fmul_rn(dr, Linv));
-    return __fsub_rn(dr, __fmul_rn(k, L));
+    const float k = rintf(__fmul_rn(dr, Linv));
+    return __fmaf_rn(-k, L, dr);
 }
 
 __device__ __forceinline__ float rr_exact(float dx, float dy, float dz)

@@ -423,7 +423,12 @@ __device__ __forceinline__ bool pair_of(const PairParam* row, const PairParam& p
 // WRAP = false when no particle of the warp can see a neighbour across the
 // box: then rint(s/L) = 0 for every pair and the minimum-image arithmetic is
 // skipped without changing any result
-template <int TR, bool AUX, bool WRAP>
+// EXACT: every coordinate of every particle of the warp is at least
+// SysParam::exact_min from zero, so each near partner (closer than that half
+// distance per coordinate) has the same sign and lies within a factor of two:
+// ri - rj is exact (Sterbenz) and its TwoSum error is zero, so the
+// error terms are dropped without changing any bit of the result
+template <int TR, bool AUX, bool WRAP, bool EXACT>
 __device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A)
 {
     const float sx = __fsub_rn(ri.x, rj.x);
@@ -438,21 +443,32 @@ __device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P,
     if (!(rr < p.rr_cut)) return;
     // dx - k L is exact (k = 0, or Sterbenz for k = +-1): the difference
     // error is the TwoSum error of ri - rj
-    const float dxl = two_sum_err(ri.x, -rj.x, sx);
-    const float dyl = two_sum_err(ri.y, -rj.y, sy);
-    const float dzl = two_sum_err(ri.z, -rj.z, sz);
+    float dxl = 0.0f, dyl = 0.0f, dzl = 0.0f;
+    if (!EXACT) {
+        dxl = two_sum_err(ri.x, -rj.x, sx);
+        dyl = two_sum_err(ri.y, -rj.y, sy);
+        dzl = two_sum_err(ri.z, -rj.z, sz);
+    }
     float rrl = __fadd_rn(__fadd_rn(__fmaf_rn(dx, dx, -px), __fmaf_rn(dy, dy, -py)), __fmaf_rn(dz, dz, -pz));
     rrl = __fadd_rn(rrl, __fadd_rn(fast_err_pos(px, py, pxy), fast_err_pos(pxy, pz, rr)));
-    rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
+    if (!EXACT) rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
     float fval, flo, e;
     pair_eval<TR>(p, rr, rrl, P.rri_smooth, fval, flo, e);
     const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
     two_sum_acc(A.fx, A.cx, tx);
     two_sum_acc(A.fy, A.cy, ty);
     two_sum_acc(A.fz, A.cz, tz);
-    A.cx = __fmaf_rn(flo, dx, __fmaf_rn(fval, dxl, __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx))));
-    A.cy = __fmaf_rn(flo, dy, __fmaf_rn(fval, dyl, __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty))));
-    A.cz = __fmaf_rn(flo, dz, __fmaf_rn(fval, dzl, __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz))));
+    float cx = __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx));
+    float cy = __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty));
+    float cz = __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz));
+    if (!EXACT) {
+        cx = __fmaf_rn(fval, dxl, cx);
+        cy = __fmaf_rn(fval, dyl, cy);
+        cz = __fmaf_rn(fval, dzl, cz);
+    }
+    A.cx = __fmaf_rn(flo, dx, cx);
+    A.cy = __fmaf_rn(flo, dy, cy);
+    A.cz = __fmaf_rn(flo, dz, cz);
     if (AUX) {
         A.en += e;
         A.s0 += fval * dx * dx;
@@ -519,7 +535,7 @@ __device__ __forceinline__ uint32_t idx_at(uint4 v, int e) { return e == 0 ? v.x
 // contiguous memory and each lane has E independent position gathers in
 // flight.  Entries past the count are never dereferenced (the lane gathers
 // its own position instead).
-template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR>
+template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool EXACT = false>
 __device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
                                              const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
 {
@@ -552,21 +568,22 @@ __device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t 
             const PairParam* pp;
             if (k >= cnt || !pair_of<NS1>(row, p1, ns, rj[e].w, pp)) continue;
             if (FAR) far_pair<TR, AUX, WRAP>(*pp, P, ri, rj[e], A);
-            else near_pair<TR, AUX, WRAP>(*pp, P, ri, rj[e], A);
+            else near_pair<TR, AUX, WRAP, EXACT>(*pp, P, ri, rj[e], A);
         }
     }
 }
 
 template <int W, int E, int TR, bool AUX>
 __device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf,
-                                               bool wrap, const SysParam& P, const PairParam* spp, float4 ri,
-                                               uint32_t a, ForceAcc& A)
+                                               bool wrap, bool exact, const SysParam& P, const PairParam* spp,
+                                               float4 ri, uint32_t a, ForceAcc& A)
 {
     if (wrap) {
         force_blocks<W, E, TR, AUX, true, false>(d, i, q, nn, P, spp, ri, a, A);
         force_blocks<W, E, TR, AUX, true, true>(d, i, q, nf, P, spp, ri, a, A);
     } else {
-        force_blocks<W, E, TR, AUX, false, false>(d, i, q, nn, P, spp, ri, a, A);
+        if (exact) force_blocks<W, E, TR, AUX, false, false, true>(d, i, q, nn, P, spp, ri, a, A);
+        else force_blocks<W, E, TR, AUX, false, false>(d, i, q, nn, P, spp, ri, a, A);
         force_blocks<W, E, TR, AUX, false, true>(d, i, q, nf, P, spp, ri, a, A);
     }
     // fold the plain far-pair sums into the compensated accumulators
@@ -616,16 +633,19 @@ __global__ void __launch_bounds__(128) k_force(Dev d)
     const uint32_t nn = packed & 0xFFFFu, nf = packed >> 16;   // near / far list parts
     const bool inner = !real || (fabsf(ri.x) < P.inner[0] && fabsf(ri.y) < P.inner[1] && fabsf(ri.z) < P.inner[2]);
     const bool wrap = __any_sync(0xFFFFFFFFu, !inner);
+    const bool far_from_zero = !real || (fabsf(ri.x) >= P.exact_min && fabsf(ri.y) >= P.exact_min &&
+                                         fabsf(ri.z) >= P.exact_min);
+    const bool exact = __all_sync(0xFFFFFFFFu, far_from_zero);
     ForceAcc A;
     if (real) {
         switch (P.trunc) {
         case TRUNC_SHARP:
         case TRUNC_SHIFTED:
-            if (P.ns == 1) force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
-            else force_dispatch<W, E, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
+            if (P.ns == 1) force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+            else force_dispatch<W, E, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
             break;
-        case TRUNC_SMOOTH_R4: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
-        default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
+        case TRUNC_SMOOTH_R4: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
+        default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
         }
     }
     lane_merge<W>(A.fx, A.cx);
