@@ -81,6 +81,31 @@ def test_lj_force_parity(precision):
     eng.close()
 
 
+@pytest.mark.parametrize("trunc", ["sharp", "force_shifted", "smooth_r4"])
+def test_truncation_parity(trunc):
+    # the truncations of truncations/*_kernel.cuh on one species (shifted: above)
+    kw = dict(smoothing=0.005) if trunc == "smooth_r4" else {}
+    r, v, L = lj_system(ncell=6)
+    n = r.shape[0]
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, L, r_cut=2.5, truncation=trunc, skin=0.3, timestep=0.005, **kw))
+    eng.commit()
+    eng.set("position", r)
+    eng.set("velocity", v)
+    eng.step(20)
+    eng.force(aux=True)
+    f = eng.get("force")
+    pot = oracle.Potential(1.0, 1.0, 2.5, trunc, h=0.005) if trunc == "smooth_r4" else oracle.Potential(1.0, 1.0, 2.5, trunc)
+    ref, _ = oracle_forces(eng, np.zeros(n), pot)
+    emax, emed = rel_force_error(f, ref["force"])
+    print("%s force rel err max %.3g median %.3g" % (trunc, emax, emed))
+    assert emax < FORCE_TOL
+    en = eng.get("potential_energy")
+    assert abs(en.sum() - ref["epot"]) < 1e-6 * abs(ref["epot"])
+    np.testing.assert_allclose(en, ref["en_pot"], rtol=1e-5, atol=1e-5)
+    eng.close()
+
+
 @pytest.mark.parametrize("lanes,block", [(1, 4), (2, 4), (2, 8), (4, 4), (4, 8), (8, 8)])
 def test_force_lanes_agree(lanes, block):
     eng, r, v, L = lj_engine(ncell=7)
