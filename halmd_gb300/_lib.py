@@ -133,6 +133,8 @@ def load():
         "hmd_dynamics_levels": (I, [P, P, P]),
         "hmd_dynamics_time": (I, [P, P]),
         "hmd_dynamics_add_msd": (I, [P, U, U, P]),
+        "hmd_dynamics_add_mqd": (I, [P, U, U, P]),
+        "hmd_dynamics_add_vacf": (I, [P, U, U, P]),
         "hmd_dynamics_add_isf": (I, [P, P, U, D, U, U, U, D, P]),
         "hmd_dynamics_sample": (I, [P]),
         "hmd_dynamics_finalise": (I, [P]),
@@ -409,8 +411,17 @@ class Dynamics:
         return t
 
     def add_msd(self, first, last):
+        return self._add_particle_tcf(self._L.hmd_dynamics_add_msd, first, last)
+
+    def add_mqd(self, first, last):
+        return self._add_particle_tcf(self._L.hmd_dynamics_add_mqd, first, last)
+
+    def add_vacf(self, first, last):
+        return self._add_particle_tcf(self._L.hmd_dynamics_add_vacf, first, last)
+
+    def _add_particle_tcf(self, fn, first, last):
         k = ctypes.c_int32()
-        self._check(self._L.hmd_dynamics_add_msd(self._h, int(first), int(last), ctypes.byref(k)))
+        self._check(fn(self._h, int(first), int(last), ctypes.byref(k)))
         self.shells[k.value] = 1
         return k.value
 

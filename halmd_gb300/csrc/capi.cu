@@ -335,6 +335,24 @@ int hmd_dynamics_add_msd(hmd_dynamics* x, uint32_t first, uint32_t last, int32_t
     });
 }
 
+int hmd_dynamics_add_mqd(hmd_dynamics* x, uint32_t first, uint32_t last, int32_t* tcf)
+{
+    DYN_OR_FAIL(x);
+    return guard(x->owner, [&] {
+        int32_t k = x->d->add_mqd(first, last);
+        if (tcf) *tcf = k;
+    });
+}
+
+int hmd_dynamics_add_vacf(hmd_dynamics* x, uint32_t first, uint32_t last, int32_t* tcf)
+{
+    DYN_OR_FAIL(x);
+    return guard(x->owner, [&] {
+        int32_t k = x->d->add_vacf(first, last);
+        if (tcf) *tcf = k;
+    });
+}
+
 int hmd_dynamics_add_isf(hmd_dynamics* x, const double* wavenumber, uint32_t nk, double tolerance, uint32_t max_count,
                          uint32_t first, uint32_t last, double norm, int32_t* tcf)
 {

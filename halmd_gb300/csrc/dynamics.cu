@@ -86,13 +86,14 @@ void Dynamics::setup_blocks(Tcf& t, uint32_t begin, uint32_t end, uint32_t chunk
     }
 }
 
-int32_t Dynamics::add_msd(uint32_t first, uint32_t last)
+// MSD (kind 0), MQD (2) or VACF (3) of the particles with tag in [first, last)
+int32_t Dynamics::add_particle_tcf(int kind, uint32_t first, uint32_t last)
 {
     if (started_) throw Error(HMD_ERR_STATE, "correlations must be added before the first sample");
     const SysHost& h = e_.system(sys_);
     if (first >= last || last > h.P.n) throw Error(HMD_ERR_INVALID, "bad particle range");
     auto t = std::make_unique<Tcf>();
-    t->kind = 0;
+    t->kind = kind;
     t->first = first;
     t->last = last;
     t->nshell = 1;
@@ -186,12 +187,21 @@ std::shared_ptr<Dynamics::Sample> Dynamics::acquire(uint64_t step)
     s->step = step;
     const Dev d = e_.dev();
     const SysParam& P = e_.system(sys_).P;
-    bool need_pos = false;
-    for (auto& t : tcf_) need_pos = need_pos || t->kind == 0;
+    bool need_pos = false, need_vel = false;
+    for (auto& t : tcf_) {
+        need_pos = need_pos || t->kind == 0 || t->kind == 2;
+        need_vel = need_vel || t->kind == 3;
+    }
     if (need_pos) {
         s->pos = std::make_shared<PosSample>();
         s->pos->r.alloc(3 * (size_t)P.n);
         launch_sample_position(d, P.off, P.A, s->pos->r.p, e_.stream());
+        HMD_CUDA(cudaGetLastError());
+    }
+    if (need_vel) {
+        s->vel = std::make_shared<PosSample>();
+        s->vel->r.alloc(3 * (size_t)P.n);
+        launch_sample_velocity(d, P.off, P.A, s->vel->r.p, e_.stream());
         HMD_CUDA(cudaGetLastError());
     }
     for (auto& t : tcf_) {
@@ -229,9 +239,10 @@ void Dynamics::finalise()
 
 void Dynamics::correlate(Tcf& t, const Sample& a, const Sample& b, Accum* out)
 {
-    if (t.kind == 0) {
-        launch_msd(a.pos->r.p, b.pos->r.p, t.range.p, 1, t.blk_range.p, t.blk_begin.p, t.nblk, t.partial.p, t.out.p,
-                   e_.stream());
+    if (t.kind != 1) {
+        const bool vel = t.kind == 3;
+        launch_tcf(t.kind, vel ? a.vel->r.p : a.pos->r.p, vel ? b.vel->r.p : b.pos->r.p, t.range.p, 1, t.blk_range.p,
+                   t.blk_begin.p, t.nblk, t.partial.p, t.out.p, e_.stream());
         HMD_CUDA(cudaGetLastError());
         double r[3];
         HMD_CUDA(cudaMemcpyAsync(r, t.out.p, 24, cudaMemcpyDeviceToHost, e_.stream()));

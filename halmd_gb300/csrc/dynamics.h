@@ -1,9 +1,11 @@
-// dynamics.h — blocking scheme and time-correlation functions (MSD, ISF)
-// over one system of an engine.
+// dynamics.h — blocking scheme and time-correlation functions (MSD, MQD,
+// VACF, ISF) over one system of an engine.
 //   blocking scheme   observables/dynamics/blocking_scheme.cpp:35-200,
 //                     observables/samples/blocking_scheme.hpp:74-189
 //   correlation       observables/dynamics/correlation.hpp:208-224
 //   MSD               observables/gpu/dynamics/mean_square_displacement.cpp:55-68
+//   MQD               observables/dynamics/mean_quartic_displacement.hpp:34-41
+//   VACF              observables/dynamics/velocity_autocorrelation.hpp:34-38
 //   ISF               observables/dynamics/intermediate_scattering_function.hpp:89-113
 //   wavevectors       observables/utility/wavevector.cpp:40-160,
 //                     algorithm/host/pick_lattice_points.hpp:74-160
@@ -30,7 +32,9 @@ public:
     uint32_t levels() const { return (uint32_t)interval_.size(); }
     uint32_t block_size() const { return block_size_; }
     void time(double* out) const;
-    int32_t add_msd(uint32_t first, uint32_t last);
+    int32_t add_msd(uint32_t first, uint32_t last) { return add_particle_tcf(0, first, last); }
+    int32_t add_mqd(uint32_t first, uint32_t last) { return add_particle_tcf(2, first, last); }
+    int32_t add_vacf(uint32_t first, uint32_t last) { return add_particle_tcf(3, first, last); }
     int32_t add_isf(const double* wavenumber, uint32_t nk, double tolerance, uint32_t max_count, uint32_t first,
                     uint32_t last, double norm);
     void sample();
@@ -48,10 +52,11 @@ private:
     struct Sample {
         uint64_t step = 0;
         std::shared_ptr<PosSample> pos;
+        std::shared_ptr<PosSample> vel;          // velocities, tag order, 3n (VACF)
         std::vector<std::shared_ptr<Rho>> rho;   // per ISF
     };
     struct Tcf {
-        int kind = 0;            // 0: MSD, 1: ISF
+        int kind = 0;            // 0: MSD, 1: ISF, 2: MQD, 3: VACF
         uint32_t first = 0, last = 0;
         double norm = 1;
         int isf = -1;            // index into Sample::rho
@@ -67,6 +72,7 @@ private:
         DevBuf<double> partial, out;
     };
 
+    int32_t add_particle_tcf(int kind, uint32_t first, uint32_t last);
     uint64_t current_step();
     std::shared_ptr<Sample> acquire(uint64_t step);
     void process(uint32_t level);

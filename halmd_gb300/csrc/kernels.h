@@ -31,6 +31,11 @@ void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st);
 void launch_sample_position(const Dev& d, uint32_t first, uint32_t count, double* out, cudaStream_t st);
 void launch_msd(const double* r1, const double* r2, const uint32_t* range, uint32_t nrange, const uint32_t* blk_range,
                 const uint32_t* blk_begin, uint32_t nblk, double* partial, double* out, cudaStream_t st);
+// kind 0 MSD, 2 MQD, 3 VACF (r1, r2: velocity samples) over particle ranges
+void launch_tcf(int kind, const double* r1, const double* r2, const uint32_t* range, uint32_t nrange,
+                const uint32_t* blk_range, const uint32_t* blk_begin, uint32_t nblk, double* partial, double* out,
+                cudaStream_t st);
+void launch_sample_velocity(const Dev& d, uint32_t first, uint32_t count, double* out, cudaStream_t st);
 void launch_density_modes(const Dev& d, const uint32_t* range, uint32_t nrange, const uint32_t* blk_range,
                           const uint32_t* blk_begin, uint32_t nblk, const float4* q, uint32_t nq, double* partial,
                           double* out, cudaStream_t st);

@@ -1,7 +1,8 @@
-// kernels_obs.cu — observables on the device: unwrapped positions in tag
-// order (observables/gpu/phase_space_kernel.cu:39-64), mean-square
-// displacement of two samples with an FP64 Welford accumulator per particle
-// range (observables/gpu/dynamics/mean_square_displacement.cpp:55-68,
+// kernels_obs.cu — observables on the device: unwrapped positions and
+// velocities in tag order (observables/gpu/phase_space_kernel.cu:39-64),
+// mean-square / mean-quartic displacement and velocity autocorrelation of
+// two samples with an FP64 Welford accumulator per particle range
+// (observables/gpu/dynamics/mean_square_displacement.cpp:55-68,
 // numeric/accumulator.hpp:83-119), and density modes rho(q) = Σ exp(i q·r)
 // (observables/gpu/density_mode_kernel.cu:46-108) summed in FP64.
 #include "hmd_device.cuh"
@@ -41,6 +42,36 @@ __device__ __forceinline__ void acc_merge(double& n, double& m, double& v, doubl
 
 constexpr uint32_t MSD_CHUNK = 8192;
 
+// velocities in tag order: out[tag * 3 + c] = hi + lo
+__global__ void __launch_bounds__(256) k_sample_velocity(Dev d, uint32_t first, double* out)
+{
+    const uint32_t i = first + blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = d.chunk_sys[i / CHUNK];
+    const SysParam& P = d.sys[s];
+    if (!P.active || species_bits(d.pos[i].w) == PLACEHOLDER) return;
+    const float4 v = d.vel[i];
+    const float4 vl = d.vel[d.S + i];
+    double* o = out + (size_t)d.id[i] * 3;
+    o[0] = (double)v.x + (double)vl.x;
+    o[1] = (double)v.y + (double)vl.y;
+    o[2] = (double)v.z + (double)vl.z;
+}
+
+// per-particle value of a correlation of two samples: KIND 0 |r2 - r1|^2
+// (MSD), 2 |r2 - r1|^4 (MQD, mean_quartic_displacement.hpp:34-41),
+// 3 r1 . r2 (VACF on velocity samples, velocity_autocorrelation.hpp:34-38)
+template <int KIND>
+__device__ __forceinline__ double tcf_value(const double* r1, const double* r2, size_t k)
+{
+    if (KIND == 3) return r1[3 * k] * r2[3 * k] + r1[3 * k + 1] * r2[3 * k + 1] + r1[3 * k + 2] * r2[3 * k + 2];
+    const double dx = r2[3 * k] - r1[3 * k];
+    const double dy = r2[3 * k + 1] - r1[3 * k + 1];
+    const double dz = r2[3 * k + 2] - r1[3 * k + 2];
+    const double x = dx * dx + dy * dy + dz * dz;
+    return KIND == 2 ? x * x : x;
+}
+
+template <int KIND>
 __global__ void __launch_bounds__(256) k_msd_partial(const double* r1, const double* r2, const uint32_t* range,
                                                      const uint32_t* blk_range, const uint32_t* blk_begin,
                                                      double* partial)
@@ -51,10 +82,7 @@ __global__ void __launch_bounds__(256) k_msd_partial(const double* r1, const dou
     const uint32_t end = min(beg + MSD_CHUNK, range[2 * rg + 1]);
     double n = 0, m = 0, v = 0;
     for (uint32_t k = beg + threadIdx.x; k < end; k += blockDim.x) {
-        const double dx = r2[3 * (size_t)k] - r1[3 * (size_t)k];
-        const double dy = r2[3 * (size_t)k + 1] - r1[3 * (size_t)k + 1];
-        const double dz = r2[3 * (size_t)k + 2] - r1[3 * (size_t)k + 2];
-        const double x = dx * dx + dy * dy + dz * dz;
+        const double x = tcf_value<KIND>(r1, r2, k);
         const double t = x - m;
         n += 1;
         m += t / n;
@@ -149,11 +177,27 @@ void launch_sample_position(const Dev& d, uint32_t first, uint32_t count, double
     k_sample_position<<<count / 256, 256, 0, st>>>(d, first, out);
 }
 
+void launch_sample_velocity(const Dev& d, uint32_t first, uint32_t count, double* out, cudaStream_t st)
+{
+    k_sample_velocity<<<count / 256, 256, 0, st>>>(d, first, out);
+}
+
+void launch_tcf(int kind, const double* r1, const double* r2, const uint32_t* range, uint32_t nrange,
+                const uint32_t* blk_range, const uint32_t* blk_begin, uint32_t nblk, double* partial, double* out,
+                cudaStream_t st)
+{
+    if (nblk > 0) {
+        if (kind == 2) k_msd_partial<2><<<nblk, 256, 0, st>>>(r1, r2, range, blk_range, blk_begin, partial);
+        else if (kind == 3) k_msd_partial<3><<<nblk, 256, 0, st>>>(r1, r2, range, blk_range, blk_begin, partial);
+        else k_msd_partial<0><<<nblk, 256, 0, st>>>(r1, r2, range, blk_range, blk_begin, partial);
+    }
+    k_msd_reduce<<<(nrange + 127) / 128, 128, 0, st>>>(blk_range, nblk, partial, nrange, out);
+}
+
 void launch_msd(const double* r1, const double* r2, const uint32_t* range, uint32_t nrange, const uint32_t* blk_range,
                 const uint32_t* blk_begin, uint32_t nblk, double* partial, double* out, cudaStream_t st)
 {
-    if (nblk > 0) k_msd_partial<<<nblk, 256, 0, st>>>(r1, r2, range, blk_range, blk_begin, partial);
-    k_msd_reduce<<<(nrange + 127) / 128, 128, 0, st>>>(blk_range, nblk, partial, nrange, out);
+    launch_tcf(0, r1, r2, range, nrange, blk_range, blk_begin, nblk, partial, out, st);
 }
 
 void launch_density_modes(const Dev& d, const uint32_t* range, uint32_t nrange, const uint32_t* blk_range,

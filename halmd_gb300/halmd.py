@@ -30,6 +30,7 @@ becomes the first positional argument.  The modules mirror:
     lua/halmd/observables/thermodynamics.lua.in:60-130 (formulas)
     lua/halmd/observables/sampler.lua.in        sampler.run(steps), sampler.on_sample(fn, every)
     lua/halmd/observables/dynamics/*.lua.in     blocking_scheme, mean_square_displacement,
+                                               mean_quartic_displacement, velocity_autocorrelation,
                                                intermediate_scattering_function
 
 All modules of one script share one engine, committed when the simulation
@@ -381,6 +382,14 @@ class mean_square_displacement:
         self.first, self.last = int(a.get("first", 0)), int(a.get("last", self.group.nparticle))
 
 
+class mean_quartic_displacement(mean_square_displacement):
+    """halmd.observables.dynamics.mean_quartic_displacement{particle (group)}."""
+
+
+class velocity_autocorrelation(mean_square_displacement):
+    """halmd.observables.dynamics.velocity_autocorrelation{particle (group)}."""
+
+
 class intermediate_scattering_function:
     """halmd.observables.dynamics.intermediate_scattering_function{particle, wavenumber,
     tolerance, max_count, norm}: shells of reciprocal-lattice vectors (wavevector.cpp:40-160)."""
@@ -424,7 +433,11 @@ class blocking_scheme:
         self._dyn = Dynamics(eng, self.max_lag, self.every * dt, block_size=self.size, shift=self.shift,
                              separation=self.separation, s=self.group._index)
         for c in self.correlations:
-            if isinstance(c, mean_square_displacement):
+            if isinstance(c, mean_quartic_displacement):
+                self._tcf.append(self._dyn.add_mqd(c.first, c.last))
+            elif isinstance(c, velocity_autocorrelation):
+                self._tcf.append(self._dyn.add_vacf(c.first, c.last))
+            elif isinstance(c, mean_square_displacement):
                 self._tcf.append(self._dyn.add_msd(c.first, c.last))
             else:
                 self._tcf.append(self._dyn.add_isf(c.wavenumber, tolerance=c.tolerance, max_count=c.max_count,
@@ -457,5 +470,7 @@ class blocking_scheme:
 observables = _Namespace(
     thermodynamics=thermodynamics, sampler=sampler,
     dynamics=_Namespace(blocking_scheme=blocking_scheme, mean_square_displacement=mean_square_displacement,
+                        mean_quartic_displacement=mean_quartic_displacement,
+                        velocity_autocorrelation=velocity_autocorrelation,
                         intermediate_scattering_function=intermediate_scattering_function),
 )

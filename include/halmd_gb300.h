@@ -255,6 +255,10 @@ HMD_API int hmd_dynamics_levels(hmd_dynamics* dyn, uint32_t* levels, uint32_t* b
 HMD_API int hmd_dynamics_time(hmd_dynamics* dyn, double* time);
 /* MSD of the particles with tag in [first, last) (id_range particle group) */
 HMD_API int hmd_dynamics_add_msd(hmd_dynamics* dyn, uint32_t first, uint32_t last, int32_t* tcf);
+/* mean quartic displacement (mean_quartic_displacement.hpp:34-41) and velocity
+ * autocorrelation (velocity_autocorrelation.hpp:34-38) of the same groups */
+HMD_API int hmd_dynamics_add_mqd(hmd_dynamics* dyn, uint32_t first, uint32_t last, int32_t* tcf);
+HMD_API int hmd_dynamics_add_vacf(hmd_dynamics* dyn, uint32_t first, uint32_t last, int32_t* tcf);
 /*
  * ISF of a particle group at the given wavenumbers (wavevector.cpp:40-160:
  * shells of reciprocal-lattice vectors within tolerance, <= max_count each),

@@ -66,6 +66,7 @@ def lib():
         L.orc_fcc_lattice.argtypes = [I, D, P]
         L.orc_md_run.argtypes = [I, P, P, P, P, P, P, P, D, D, I, D, D, ctypes.c_uint64, P]
         L.orc_minimize.argtypes = [I, P, P, P, P, P, D, I, D, D, P]
+        L.orc_tcf.argtypes = [I, I, I, P, P, P]
         _lib = L
     return _lib
 
@@ -258,6 +259,16 @@ def msd(r1, r2, first=0, last=None):
     last = r1.shape[0] if last is None else last
     out = np.zeros(3)
     lib().orc_msd(int(first), int(last), _p(r1), _p(r2), _p(out))
+    return dict(count=out[0], mean=out[1], variance=out[2])
+
+
+def tcf(kind, a, b, first=0, last=None):
+    """kind "msd", "mqd" (|b - a|^4) or "vacf" (a . b) over particles [first, last)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    last = a.shape[0] if last is None else last
+    out = np.zeros(3)
+    lib().orc_tcf({"msd": 0, "mqd": 2, "vacf": 3}[kind], int(first), int(last), _p(a), _p(b), _p(out))
     return dict(count=out[0], mean=out[1], variance=out[2])
 
 

@@ -883,6 +883,31 @@ ORC_API void orc_msd(int first, int last, const double* r1, const double* r2, do
 }
 
 /*
+ * mean quartic displacement (observables/dynamics/mean_quartic_displacement.hpp:34-41):
+ * |r2 - r1|^4, and velocity autocorrelation
+ * (observables/dynamics/velocity_autocorrelation.hpp:34-38): v1 . v2, both
+ * accumulated like the MSD.  kind 0: MSD, 2: MQD, 3: VACF.
+ */
+ORC_API void orc_tcf(int kind, int first, int last, const double* a, const double* b, double* out)
+{
+    orc_acc acc = {0, 0, 0};
+    for (int i = first; i < last; ++i) {
+        double x = 0;
+        if (kind == 3) {
+            for (int d = 0; d < 3; ++d) x += a[3 * i + d] * b[3 * i + d];
+        } else {
+            for (int d = 0; d < 3; ++d) {
+                const double dx = b[3 * i + d] - a[3 * i + d];
+                x += dx * dx;
+            }
+            if (kind == 2) x = x * x;
+        }
+        acc_add(acc, x);
+    }
+    out[0] = acc.n; out[1] = acc.m; out[2] = acc.n > 0 ? acc.v / acc.n : 0;
+}
+
+/*
  * density modes ρ(q) = Σ_j exp(i q·r_j) over particles [first,last) with the
  * reference's sign convention (imaginary part negated, density_mode.cpp:128).
  * q·r is evaluated in float as (qx*x + qy*y) + qz*z (the GPU's rounding); the

@@ -93,3 +93,54 @@ def test_msd_isf_blocking_scheme():
     assert msd_mean[0, 1, 0] < msd_mean[0, block - 1, 0]
     dyn.close()
     eng.close()
+
+
+def test_mqd_vacf_blocking_scheme():
+    """Mean quartic displacement and velocity autocorrelation against the
+    FP64 oracle on the same samples (mean_quartic_displacement.hpp:34-41,
+    velocity_autocorrelation.hpp:34-38)."""
+    r, v, L = lj_system(ncell=5, T=1.2)
+    n = r.shape[0]
+    dt = 0.005
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, L, r_cut=2.5, truncation="shifted", skin=0.3, timestep=dt))
+    eng.commit()
+    eng.set("position", r)
+    eng.set("velocity", v)
+    block, shift, sep = 4, 2, 4
+    max_lag, res = 40 * dt, dt
+    dyn = hg.Dynamics(eng, max_lag, res, block_size=block, shift=shift, separation=sep)
+    k_mqd = dyn.add_mqd(0, n)
+    k_vacf = dyn.add_vacf(n // 3, n)
+    bs = BlockingScheme(dt, max_lag, res, block, shift, sep)
+
+    def tcf_fn(kind, key, first, last):
+        def fn(a, b):
+            o = oracle.tcf(kind, a[key], b[key], first, last)
+            return [(o["count"], o["mean"], o["variance"] * o["count"])]
+        return fn
+
+    bs.add(tcf_fn("mqd", "r", 0, n))
+    bs.add(tcf_fn("vacf", "v", n // 3, n))
+    for step in range(0, 61):
+        if step > 0:
+            eng.step(1)
+        dyn.sample()
+        bs.sample(step, lambda: {"r": eng.get("unwrapped_position"), "v": eng.get("velocity")})
+    dyn.finalise()
+    bs.finalise()
+    for tcf, k in ((k_mqd, 0), (k_vacf, 1)):
+        mean, err, cnt = dyn.result(tcf)
+        ref = bs.mean_error_count(k)
+        for lv in range(dyn.levels):
+            for j in range(dyn.block_size):
+                m, e, c = ref[lv][j][0]
+                assert cnt[lv, j, 0] == c
+                if c > 0:
+                    assert abs(mean[lv, j, 0] - m) <= 1e-12 * max(abs(m), 1e-300) + 1e-18
+                    assert abs(err[lv, j, 0] - e) <= 1e-9 * max(abs(e), 1e-300) + 1e-15
+    # VACF at lag 0 is the mean v^2 of the group: positive and decaying
+    vmean, _, _ = dyn.result(k_vacf)
+    assert vmean[0, 0, 0] > 0 and vmean[0, 0, 0] > vmean[0, block - 1, 0]
+    dyn.close()
+    eng.close()
