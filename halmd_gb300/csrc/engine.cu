@@ -290,6 +290,14 @@ void Engine::unplace(uint32_t s)
     word_arena_.release(P.cell_word_off / 32, P.ncells * P.cell_size / 32);
 }
 
+// kind of pair interaction of a system (kernels.h ForceKind; the device
+// counterpart is force_kind_of in force.cuh)
+static int force_kind(const SysParam& P)
+{
+    if (P.trunc == TRUNC_SHARP || P.trunc == TRUNC_SHIFTED) return P.ns == 1 ? FK_LJ1 : FK_SHIFTED;
+    return P.trunc == TRUNC_SMOOTH_R4 ? FK_SMOOTH : FK_FSHIFT;
+}
+
 void Engine::commit()
 {
     if (committed_) throw Error(HMD_ERR_STATE, "engine already committed");
@@ -301,6 +309,7 @@ void Engine::commit()
     nbr_cap_ = 0;
     any_sort_ = false;
     uint32_t shift = 0;
+    force_kinds_ = 0;
     if (!capacity_) {
         table_size_ = (uint32_t)sys_.size();
         null_sys_ = PLACEHOLDER;
@@ -318,6 +327,7 @@ void Engine::commit()
             nbr_cap_ = std::max(nbr_cap_, round_up(h.nbr_size, 8));
             shift = std::max(shift, 3 * h.P.depth);
             any_sort_ = any_sort_ || h.P.sort_enable;
+            force_kinds_ |= 1u << force_kind(h.P);
         }
         // each system sorts its own slot range with 3*depth-bit Hilbert keys,
         // in tiles that never straddle two systems
@@ -587,6 +597,7 @@ Dev Engine::dev() const
     d.lanes = lanes_;
     d.lb_log2 = block() == 8u ? 3u : 2u;
     d.nbr_scan = nbr_scan_;   // 0: each system by its own size (k_neighbour)
+    d.force_kinds = force_kinds_;
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
     d.S = S_; d.nsys = table_size_;

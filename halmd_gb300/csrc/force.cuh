@@ -1,0 +1,795 @@
+// force.cuh — truncated Lennard-Jones pair force from the neighbour list
+// (mdsim/gpu/forces/pair_trunc_kernel.cuh, potentials/pair/lennard_jones_kernel.hpp,
+// truncations/*_kernel.cuh).  The kernel is a template over the kind of pair
+// interaction; kernels_force_*.cu compile one kind each, so every kind gets
+// its own register allocation, and kernels_step.cu launches the kinds an
+// engine holds.
+#pragma once
+
+#include "hmd_device.cuh"
+#include "kernels.h"
+
+namespace hmd {
+
+// Resident blocks of 128 threads per SM that the register allocation aims
+// for: 7 (72 registers a thread).  The kernel is bound by the latency of the
+// list stream and the position gathers; at LJ-1M (one lane, four entries per
+// load) it measured 173 us with 7 blocks and the list prefetch below, 183-192
+// us with 8 blocks (64 registers, more spills) or without the prefetch, and
+// 211-286 us with 5 or 6 blocks and no spills.
+#ifndef HMD_FORCE_MINB
+#define HMD_FORCE_MINB 7
+#endif
+// 1: load a lane's next list block one iteration ahead (force_blocks2)
+#ifndef HMD_FORCE_PREFETCH
+#define HMD_FORCE_PREFETCH 1
+#endif
+
+// ---------------------------------------------------------------------------
+// pair force (mdsim/gpu/forces/pair_trunc_kernel.cuh:165-255)
+//   F_i = Σ_j fval(r_ij²) r_ij over list entries with r_ij² < r_c²;
+//   aux: E_i = ½ Σ U, stress_i = ½ Σ fval r⊗r (full list, weight ½,
+//   pair_trunc.hpp:291-294).
+// FP32 math; each force component is accumulated with Knuth's TwoSum and
+// a running compensation term, so the per-particle sum is as accurate as a
+// double-single accumulator (the reference uses dsfloat, :194).
+// The within-range test uses the same rounded squared distance as the list
+// build, so the pair set is reproducible on the CPU.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float x)
+{
+    const float t = __fadd_rn(s, x);
+    const float z = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z));
+    s = t;
+    c = __fadd_rn(c, e);
+}
+
+// error of s = fl(a + b) (Knuth TwoSum)
+__device__ __forceinline__ float two_sum_err(float a, float b, float s)
+{
+    const float bp = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// error of s = fl(a + b) for a, b >= 0 (Dekker's Fast2Sum on the ordered pair)
+__device__ __forceinline__ float fast_err_pos(float a, float b, float s)
+{
+    return __fsub_rn(fminf(a, b), __fsub_rn(s, fmaxf(a, b)));
+}
+
+// LJ + truncation (lennard_jones_kernel.hpp:44-56, truncations/*_kernel.cuh).
+// Compensated LJ for close pairs, whose forces can be an order of magnitude
+// above the particle's net force: the squared distance arrives as a (hi, lo)
+// pair, the reciprocal is refined against it, the float parameters sigma^2
+// and 48 eps / sigma^2 carry their rounding errors, and every product of
+// fval = 48 eps/sigma^2 rri^4 (rri^3 - 1/2) keeps its exact residual (FMA),
+// so fval + flo is accurate to first order in the float roundings (the
+// steep r^-14 law would otherwise amplify them seven-fold).  The smoothing
+// factors (smooth_r4) and the force shift use approximate reciprocal /
+// square-root intrinsics: their errors scale forces that are already small
+// near r_c.
+template <int TR>
+__device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rrl, float rri_smooth,
+                                          float& fval, float& flo, float& en)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(rr));
+    const float res = __fmaf_rn(-rrl, y, __fmaf_rn(-rr, y, 1.0f));
+    const float ylo = __fmul_rn(y, res);
+    const float rri = __fmul_rn(p.sigma2, y);
+    float rril = __fmaf_rn(p.sigma2, ylo, __fmaf_rn(p.sigma2, y, -rri));
+    rril = __fmaf_rn(p.sigma2_lo, y, rril);
+    const float t1 = __fmul_rn(rri, rri);
+    const float ri6 = __fmul_rn(t1, rri);
+    const float a = __fmul_rn(p.c48, rri);
+    const float b = __fmul_rn(a, ri6);
+    const float u = __fsub_rn(ri6, 0.5f);
+    fval = __fmul_rn(b, u);
+    // residuals: ri6 = rri^3, u = ri6 - 1/2, a = c48 rri, b = a ri6, fval = b u
+    float ri6l = __fmaf_rn(__fmaf_rn(rri, rri, -t1), rri, __fmaf_rn(t1, rri, -ri6));
+    ri6l = __fmaf_rn(__fmul_rn(3.0f, t1), rril, ri6l);
+    const float ul = __fadd_rn(two_sum_err(ri6, -0.5f, u), ri6l);
+    float al = __fmaf_rn(p.c48, rril, __fmaf_rn(p.c48, rri, -a));
+    al = __fmaf_rn(p.c48_lo, rri, al);
+    const float bl = __fmaf_rn(a, ri6l, __fmaf_rn(al, ri6, __fmaf_rn(a, ri6, -b)));
+    flo = __fmaf_rn(b, ul, __fmaf_rn(bl, u, __fmaf_rn(b, u, -fval)));
+    en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
+    if (TR == TRUNC_SMOOTH_R4) {
+        const float rinv = rsqrtf(rr);
+        const float r = rr * rinv;
+        const float dr = r - p.r_cut;
+        const float x2 = dr * dr * rri_smooth;
+        const float x4 = x2 * x2;
+        const float x4i = __fdividef(1.0f, 1.0f + x4);
+        const float h0 = x4 * x4i;
+        const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
+        fval = h0 * fval - h1 * (en * rinv);
+        flo = h0 * flo;
+        en = h0 * en;
+    } else if (TR == TRUNC_FORCE_SHIFTED) {
+        const float rinv = rsqrtf(rr);
+        fval = fval - p.f_cut * rinv;
+        en = en + (rr * rinv - p.r_cut) * p.f_cut;
+    }
+}
+
+// plain FP32 evaluation for pairs that were farther than NEAR_SIGMA sigma at
+// list build time (forces of order eps / sigma or less)
+template <int TR>
+__device__ __forceinline__ void pair_eval_fast(const PairParam& p, float rr, float rri_smooth, float& fval, float& en)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(rr));
+    const float rri = p.sigma2 * y;
+    const float ri6 = rri * rri * rri;
+    fval = p.c48 * rri * ri6 * (ri6 - 0.5f);
+    en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
+    if (TR == TRUNC_SMOOTH_R4) {
+        const float rinv = rsqrtf(rr);
+        const float dr = rr * rinv - p.r_cut;
+        const float x2 = dr * dr * rri_smooth;
+        const float x4 = x2 * x2;
+        const float x4i = __fdividef(1.0f, 1.0f + x4);
+        const float h0 = x4 * x4i;
+        const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
+        fval = h0 * fval - h1 * (en * rinv);
+        en = h0 * en;
+    } else if (TR == TRUNC_FORCE_SHIFTED) {
+        const float rinv = rsqrtf(rr);
+        fval = fval - p.f_cut * rinv;
+        en = en + (rr * rinv - p.r_cut) * p.f_cut;
+    }
+}
+
+struct ForceAcc {
+    float fx = 0, fy = 0, fz = 0, cx = 0, cy = 0, cz = 0;   // compensated (near pairs)
+    float gx = 0, gy = 0, gz = 0;                           // plain sums (far pairs)
+    float en = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
+};
+
+// TR >= ONE_SPECIES: single-species system, the pair table has one entry
+constexpr int ONE_SPECIES = 16;
+
+// Pair-parameter lookup for a neighbour of species b; false when b is not a
+// species of the system (lists hold real particles only: this keeps the
+// table lookup in bounds)
+template <bool NS1>
+__device__ __forceinline__ bool pair_of(const PairParam* row, const PairParam& p1, uint32_t ns, float w,
+                                        const PairParam*& pp)
+{
+    if (NS1) { pp = &p1; return true; }
+    const uint32_t b = species_bits(w);
+    if (b >= ns) return false;
+    pp = row + b;
+    return true;
+}
+
+// one near pair: compensated separation, squared distance and LJ value;
+// WRAP = false when no particle of the warp can see a neighbour across the
+// box: then rint(s/L) = 0 for every pair and the minimum-image arithmetic is
+// skipped without changing any result
+// EXACT: every coordinate of every particle of the warp is at least
+// SysParam::exact_min from zero, so each near partner (closer than that half
+// distance per coordinate) has the same sign and lies within a factor of two:
+// ri - rj is exact (Sterbenz) and its TwoSum error is zero, so the
+// error terms are dropped without changing any bit of the result
+template <int TR, bool AUX, bool WRAP, bool EXACT>
+__device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A)
+{
+    const float sx = __fsub_rn(ri.x, rj.x);
+    const float sy = __fsub_rn(ri.y, rj.y);
+    const float sz = __fsub_rn(ri.z, rj.z);
+    const float dx = WRAP ? min_image(sx, P.L[0], P.Linv[0]) : sx;
+    const float dy = WRAP ? min_image(sy, P.L[1], P.Linv[1]) : sy;
+    const float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
+    const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
+    const float pxy = __fadd_rn(px, py);
+    const float rr = __fadd_rn(pxy, pz);   // == rr_exact(dx, dy, dz)
+    if (!(rr < p.rr_cut)) return;
+    // dx - k L is exact (k = 0, or Sterbenz for k = +-1): the difference
+    // error is the TwoSum error of ri - rj
+    float dxl = 0.0f, dyl = 0.0f, dzl = 0.0f;
+    if (!EXACT) {
+        dxl = two_sum_err(ri.x, -rj.x, sx);
+        dyl = two_sum_err(ri.y, -rj.y, sy);
+        dzl = two_sum_err(ri.z, -rj.z, sz);
+    }
+    float rrl = __fadd_rn(__fadd_rn(__fmaf_rn(dx, dx, -px), __fmaf_rn(dy, dy, -py)), __fmaf_rn(dz, dz, -pz));
+    rrl = __fadd_rn(rrl, __fadd_rn(fast_err_pos(px, py, pxy), fast_err_pos(pxy, pz, rr)));
+    if (!EXACT) rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
+    float fval, flo, e;
+    pair_eval<TR>(p, rr, rrl, P.rri_smooth, fval, flo, e);
+    const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
+    two_sum_acc(A.fx, A.cx, tx);
+    two_sum_acc(A.fy, A.cy, ty);
+    two_sum_acc(A.fz, A.cz, tz);
+    float cx = __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx));
+    float cy = __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty));
+    float cz = __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz));
+    if (!EXACT) {
+        cx = __fmaf_rn(fval, dxl, cx);
+        cy = __fmaf_rn(fval, dyl, cy);
+        cz = __fmaf_rn(fval, dzl, cz);
+    }
+    A.cx = __fmaf_rn(flo, dx, cx);
+    A.cy = __fmaf_rn(flo, dy, cy);
+    A.cz = __fmaf_rn(flo, dz, cz);
+    if (AUX) {
+        A.en += e;
+        A.s0 += fval * dx * dx;
+        A.s1 += fval * dy * dy;
+        A.s2 += fval * dz * dz;
+        A.s3 += fval * dx * dy;
+        A.s4 += fval * dx * dz;
+        A.s5 += fval * dy * dz;
+    }
+}
+
+// one far pair: plain FP32 (forces of order eps / sigma or less)
+template <int TR, bool AUX, bool WRAP>
+__device__ __forceinline__ void far_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A)
+{
+    const float sx = __fsub_rn(ri.x, rj.x);
+    const float sy = __fsub_rn(ri.y, rj.y);
+    const float sz = __fsub_rn(ri.z, rj.z);
+    float dx = WRAP ? min_image(sx, P.L[0], P.Linv[0]) : sx;
+    float dy = WRAP ? min_image(sy, P.L[1], P.Linv[1]) : sy;
+    float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
+    float rr = rr_exact(dx, dy, dz);
+    if (!(rr < p.rr_cut)) return;
+    if (WRAP) {
+        // across the box ri - rj is of order L and its rounding error (up to
+        // ulp(L)/2) would dominate the separation error: add the TwoSum error
+        // back (the cut-off decision above keeps the rounded rr of the list
+        // criterion)
+        dx = __fadd_rn(dx, two_sum_err(ri.x, -rj.x, sx));
+        dy = __fadd_rn(dy, two_sum_err(ri.y, -rj.y, sy));
+        dz = __fadd_rn(dz, two_sum_err(ri.z, -rj.z, sz));
+        rr = rr_exact(dx, dy, dz);
+    }
+    float fval, e;
+    pair_eval_fast<TR>(p, rr, P.rri_smooth, fval, e);
+    A.gx = __fmaf_rn(fval, dx, A.gx);
+    A.gy = __fmaf_rn(fval, dy, A.gy);
+    A.gz = __fmaf_rn(fval, dz, A.gz);
+    if (AUX) {
+        A.en += e;
+        A.s0 += fval * dx * dx;
+        A.s1 += fval * dy * dy;
+        A.s2 += fval * dz * dz;
+        A.s3 += fval * dx * dy;
+        A.s4 += fval * dx * dz;
+        A.s5 += fval * dy * dz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Two list entries per instruction.  The SMs of this GPU issue FP32 add,
+// multiply and FMA on register pairs (f32x2): entries e and e+1 of a lane's
+// list load are evaluated together, lane .x of every float2 holding entry e
+// and lane .y entry e+1.  Each lane of an f32x2 operation rounds exactly as
+// the scalar operation, so a pair's force value equals that of the scalar
+// path above bit for bit; the per-particle sums run as two interleaved
+// accumulators (even and odd entries) that are merged at the end.  The
+// evaluation is branch-free: entries past the count, pairs outside r_c and
+// neighbours of no species of the system are masked by selecting zero for
+// their force value (the lane still evaluates them, as the warp would).
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 sel2(bool ka, bool kb, float2 v)
+{
+    return make_float2(ka ? v.x : 0.0f, kb ? v.y : 0.0f);
+}
+
+// error of s = fl(a - b) per lane (Knuth TwoSum of a and -b), a shared
+__device__ __forceinline__ float2 diff_err2(float a, float bA, float bB, float2 s)
+{
+    const float2 bp = sub2(s, bc2(a));
+    const float2 e1 = sub2(bc2(a), sub2(s, bp));
+    return add2(e1, f2(__fsub_rn(-bA, bp.x), __fsub_rn(-bB, bp.y)));
+}
+
+__device__ __forceinline__ float2 two_sum_err2(float2 a, float2 b, float2 s)
+{
+    const float2 bp = sub2(s, a);
+    return add2(sub2(a, sub2(s, bp)), sub2(b, bp));
+}
+
+__device__ __forceinline__ float2 fast_err_pos2(float2 a, float2 b, float2 s)
+{
+    const float2 mn = f2(fminf(a.x, b.x), fminf(a.y, b.y));
+    const float2 mx = f2(fmaxf(a.x, b.x), fmaxf(a.y, b.y));
+    return sub2(mn, sub2(s, mx));
+}
+
+__device__ __forceinline__ void two_sum_acc2(float2& s, float2& c, float2 x)
+{
+    const float2 t = add2(s, x);
+    const float2 z = sub2(t, s);
+    const float2 e = add2(sub2(s, sub2(t, z)), sub2(x, z));
+    s = t;
+    c = add2(c, e);
+}
+
+__device__ __forceinline__ float2 min_image2(float2 s, float L, float Linv)
+{
+    const float2 q = mul2(s, bc2(Linv));
+    return fma2(f2(-rintf(q.x), -rintf(q.y)), bc2(L), s);
+}
+
+// the parameters of two pairs, lane by lane
+struct PP2 {
+    float2 eps4, c48, sigma2, rr_cut, en_cut, r_cut, f_cut, sigma2_lo, c48_lo;
+};
+
+__device__ __forceinline__ PP2 pack_params(const PairParam& a, const PairParam& b)
+{
+    PP2 p;
+    p.eps4 = f2(a.eps4, b.eps4);
+    p.c48 = f2(a.c48, b.c48);
+    p.sigma2 = f2(a.sigma2, b.sigma2);
+    p.rr_cut = f2(a.rr_cut, b.rr_cut);
+    p.en_cut = f2(a.en_cut, b.en_cut);
+    p.r_cut = f2(a.r_cut, b.r_cut);
+    p.f_cut = f2(a.f_cut, b.f_cut);
+    p.sigma2_lo = f2(a.sigma2_lo, b.sigma2_lo);
+    p.c48_lo = f2(a.c48_lo, b.c48_lo);
+    return p;
+}
+
+struct ForceAcc2 {
+    float2 fx = {0, 0}, fy = {0, 0}, fz = {0, 0}, cx = {0, 0}, cy = {0, 0}, cz = {0, 0};
+    float2 gx = {0, 0}, gy = {0, 0}, gz = {0, 0};
+    float2 en = {0, 0}, s0 = {0, 0}, s1 = {0, 0}, s2 = {0, 0}, s3 = {0, 0}, s4 = {0, 0}, s5 = {0, 0};
+};
+
+// energy (needed by smooth_r4 and the aux sums) and the truncation factors
+// of the force value, as in pair_eval / pair_eval_fast
+template <int TR, bool NEAR>
+__device__ __forceinline__ void truncate2(const PP2& p, float2 rr, float2 ri6, float rri_smooth, float2& fval,
+                                          float2& flo, float2& en)
+{
+    en = sub2(mul2(mul2(p.eps4, ri6), sub2(ri6, bc2(1.0f))), p.en_cut);
+    if (TR == TRUNC_SMOOTH_R4) {
+        const float2 rinv = f2(rsqrtf(rr.x), rsqrtf(rr.y));
+        const float2 dr = sub2(mul2(rr, rinv), p.r_cut);
+        const float2 x2 = mul2(mul2(dr, dr), bc2(rri_smooth));
+        const float2 x4 = mul2(x2, x2);
+        const float2 den = add2(bc2(1.0f), x4);
+        const float2 x4i = f2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
+        const float2 h0 = mul2(x4, x4i);
+        const float2 h1 = mul2(mul2(mul2(bc2(4.0f * rri_smooth), dr), x2), mul2(x4i, x4i));
+        fval = fma2(h0, fval, neg2(mul2(h1, mul2(en, rinv))));
+        if (NEAR) flo = mul2(h0, flo);
+        en = mul2(h0, en);
+    } else if (TR == TRUNC_FORCE_SHIFTED) {
+        const float2 rinv = f2(rsqrtf(rr.x), rsqrtf(rr.y));
+        fval = fma2(neg2(p.f_cut), rinv, fval);
+        en = fma2(sub2(mul2(rr, rinv), p.r_cut), p.f_cut, en);
+    }
+}
+
+// compensated LJ of two close pairs (pair_eval, lane by lane)
+template <int TR>
+__device__ __forceinline__ void pair_eval2(const PP2& p, float2 rr, float2 rrl, float rri_smooth, float2& fval,
+                                           float2& flo, float2& en)
+{
+    float ya, yb;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ya) : "f"(rr.x));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yb) : "f"(rr.y));
+    const float2 y = f2(ya, yb);
+    const float2 res = fma2(neg2(rrl), y, fma2(neg2(rr), y, bc2(1.0f)));
+    const float2 ylo = mul2(y, res);
+    const float2 rri = mul2(p.sigma2, y);
+    float2 rril = fma2(p.sigma2, ylo, fma2(p.sigma2, y, neg2(rri)));
+    rril = fma2(p.sigma2_lo, y, rril);
+    const float2 t1 = mul2(rri, rri);
+    const float2 ri6 = mul2(t1, rri);
+    const float2 a = mul2(p.c48, rri);
+    const float2 b = mul2(a, ri6);
+    const float2 u = sub2(ri6, bc2(0.5f));
+    fval = mul2(b, u);
+    float2 ri6l = fma2(fma2(rri, rri, neg2(t1)), rri, fma2(t1, rri, neg2(ri6)));
+    ri6l = fma2(mul2(bc2(3.0f), t1), rril, ri6l);
+    const float2 ul = add2(two_sum_err2(ri6, bc2(-0.5f), u), ri6l);
+    float2 al = fma2(p.c48, rril, fma2(p.c48, rri, neg2(a)));
+    al = fma2(p.c48_lo, rri, al);
+    const float2 bl = fma2(a, ri6l, fma2(al, ri6, fma2(a, ri6, neg2(b))));
+    flo = fma2(b, ul, fma2(bl, u, fma2(b, u, neg2(fval))));
+    truncate2<TR, true>(p, rr, ri6, rri_smooth, fval, flo, en);
+}
+
+template <bool AUX>
+__device__ __forceinline__ void aux_acc2(ForceAcc2& A, float2 fval, float2 en, float2 dx, float2 dy, float2 dz)
+{
+    if (AUX) {
+        A.en = add2(A.en, en);
+        const float2 fx = mul2(fval, dx), fy = mul2(fval, dy);
+        A.s0 = fma2(fx, dx, A.s0);
+        A.s1 = fma2(fy, dy, A.s1);
+        A.s2 = fma2(mul2(fval, dz), dz, A.s2);
+        A.s3 = fma2(fx, dy, A.s3);
+        A.s4 = fma2(fx, dz, A.s4);
+        A.s5 = fma2(fy, dz, A.s5);
+    }
+}
+
+// two near pairs (near_pair, lane by lane); va / vb: the entry is a real
+// neighbour of a species of the system
+template <int TR, bool AUX, bool WRAP, bool EXACT>
+__device__ __forceinline__ void near_pair2(const PP2& p, const SysParam& P, float4 ri, float4 ra, float4 rb,
+                                           bool va, bool vb, ForceAcc2& A)
+{
+    const float2 sx = f2(__fsub_rn(ri.x, ra.x), __fsub_rn(ri.x, rb.x));
+    const float2 sy = f2(__fsub_rn(ri.y, ra.y), __fsub_rn(ri.y, rb.y));
+    const float2 sz = f2(__fsub_rn(ri.z, ra.z), __fsub_rn(ri.z, rb.z));
+    const float2 dx = WRAP ? min_image2(sx, P.L[0], P.Linv[0]) : sx;
+    const float2 dy = WRAP ? min_image2(sy, P.L[1], P.Linv[1]) : sy;
+    const float2 dz = WRAP ? min_image2(sz, P.L[2], P.Linv[2]) : sz;
+    const float2 px = mul2(dx, dx), py = mul2(dy, dy), pz = mul2(dz, dz);
+    const float2 pxy = add2(px, py);
+    const float2 rr = add2(pxy, pz);   // == rr_exact(dx, dy, dz) per lane
+    const bool ka = va && rr.x < p.rr_cut.x;
+    const bool kb = vb && rr.y < p.rr_cut.y;
+    float2 dxl = bc2(0.0f), dyl = bc2(0.0f), dzl = bc2(0.0f);
+    if (!EXACT) {
+        dxl = diff_err2(ri.x, ra.x, rb.x, sx);
+        dyl = diff_err2(ri.y, ra.y, rb.y, sy);
+        dzl = diff_err2(ri.z, ra.z, rb.z, sz);
+    }
+    float2 rrl = add2(add2(fma2(dx, dx, neg2(px)), fma2(dy, dy, neg2(py))), fma2(dz, dz, neg2(pz)));
+    rrl = add2(rrl, add2(fast_err_pos2(px, py, pxy), fast_err_pos2(pxy, pz, rr)));
+    if (!EXACT) rrl = fma2(bc2(2.0f), fma2(dx, dxl, fma2(dy, dyl, mul2(dz, dzl))), rrl);
+    float2 fval, flo, e;
+    pair_eval2<TR>(p, rr, rrl, P.rri_smooth, fval, flo, e);
+    fval = sel2(ka, kb, fval);
+    flo = sel2(ka, kb, flo);
+    const float2 tx = mul2(fval, dx), ty = mul2(fval, dy), tz = mul2(fval, dz);
+    two_sum_acc2(A.fx, A.cx, tx);
+    two_sum_acc2(A.fy, A.cy, ty);
+    two_sum_acc2(A.fz, A.cz, tz);
+    float2 cx = add2(A.cx, fma2(fval, dx, neg2(tx)));
+    float2 cy = add2(A.cy, fma2(fval, dy, neg2(ty)));
+    float2 cz = add2(A.cz, fma2(fval, dz, neg2(tz)));
+    if (!EXACT) {
+        cx = fma2(fval, dxl, cx);
+        cy = fma2(fval, dyl, cy);
+        cz = fma2(fval, dzl, cz);
+    }
+    A.cx = fma2(flo, dx, cx);
+    A.cy = fma2(flo, dy, cy);
+    A.cz = fma2(flo, dz, cz);
+    aux_acc2<AUX>(A, fval, sel2(ka, kb, e), dx, dy, dz);
+}
+
+// two far pairs (far_pair, lane by lane)
+template <int TR, bool AUX, bool WRAP>
+__device__ __forceinline__ void far_pair2(const PP2& p, const SysParam& P, float4 ri, float4 ra, float4 rb,
+                                          bool va, bool vb, ForceAcc2& A)
+{
+    const float2 sx = f2(__fsub_rn(ri.x, ra.x), __fsub_rn(ri.x, rb.x));
+    const float2 sy = f2(__fsub_rn(ri.y, ra.y), __fsub_rn(ri.y, rb.y));
+    const float2 sz = f2(__fsub_rn(ri.z, ra.z), __fsub_rn(ri.z, rb.z));
+    float2 dx = WRAP ? min_image2(sx, P.L[0], P.Linv[0]) : sx;
+    float2 dy = WRAP ? min_image2(sy, P.L[1], P.Linv[1]) : sy;
+    float2 dz = WRAP ? min_image2(sz, P.L[2], P.Linv[2]) : sz;
+    float2 rr = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
+    const bool ka = va && rr.x < p.rr_cut.x;
+    const bool kb = vb && rr.y < p.rr_cut.y;
+    if (WRAP) {
+        // across the box: add the separation's rounding error back (far_pair)
+        dx = add2(dx, diff_err2(ri.x, ra.x, rb.x, sx));
+        dy = add2(dy, diff_err2(ri.y, ra.y, rb.y, sy));
+        dz = add2(dz, diff_err2(ri.z, ra.z, rb.z, sz));
+        rr = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
+    }
+    float ya, yb;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ya) : "f"(rr.x));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yb) : "f"(rr.y));
+    const float2 rri = mul2(p.sigma2, f2(ya, yb));
+    const float2 ri6 = mul2(mul2(rri, rri), rri);
+    float2 fval = mul2(mul2(mul2(p.c48, rri), ri6), sub2(ri6, bc2(0.5f)));
+    float2 flo, e = bc2(0.0f);
+    if (AUX || TR == TRUNC_SMOOTH_R4 || TR == TRUNC_FORCE_SHIFTED)
+        truncate2<TR, false>(p, rr, ri6, P.rri_smooth, fval, flo, e);
+    fval = sel2(ka, kb, fval);
+    A.gx = fma2(fval, dx, A.gx);
+    A.gy = fma2(fval, dy, A.gy);
+    A.gz = fma2(fval, dz, A.gz);
+    aux_acc2<AUX>(A, fval, sel2(ka, kb, e), dx, dy, dz);
+}
+
+// merge the even and odd accumulators into one
+template <bool AUX>
+__device__ __forceinline__ void fold_lanes2(const ForceAcc2& B, ForceAcc& A)
+{
+    A.fx = B.fx.x; A.fy = B.fy.x; A.fz = B.fz.x;
+    A.cx = __fadd_rn(B.cx.x, B.cx.y);
+    A.cy = __fadd_rn(B.cy.x, B.cy.y);
+    A.cz = __fadd_rn(B.cz.x, B.cz.y);
+    two_sum_acc(A.fx, A.cx, B.fx.y);
+    two_sum_acc(A.fy, A.cy, B.fy.y);
+    two_sum_acc(A.fz, A.cz, B.fz.y);
+    A.gx = __fadd_rn(B.gx.x, B.gx.y);
+    A.gy = __fadd_rn(B.gy.x, B.gy.y);
+    A.gz = __fadd_rn(B.gz.x, B.gz.y);
+    if (AUX) {
+        A.en = B.en.x + B.en.y;
+        A.s0 = B.s0.x + B.s0.y; A.s1 = B.s1.x + B.s1.y; A.s2 = B.s2.x + B.s2.y;
+        A.s3 = B.s3.x + B.s3.y; A.s4 = B.s4.x + B.s4.y; A.s5 = B.s5.x + B.s5.y;
+    }
+}
+
+// E list entries per lane and block, read with one vector load
+template <int E> struct IdxVec;
+template <> struct IdxVec<1> { using T = uint32_t; };
+template <> struct IdxVec<2> { using T = uint2; };
+template <> struct IdxVec<4> { using T = uint4; };
+__device__ __forceinline__ uint32_t idx_at(uint32_t v, int) { return v; }
+__device__ __forceinline__ uint32_t idx_at(uint2 v, int e) { return e == 0 ? v.x : v.y; }
+__device__ __forceinline__ uint32_t idx_at(uint4 v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
+
+// The list is stored in blocks of LB = W * E entries: entry k of slot i at
+// ((k/LB)*S + i)*LB + k%LB, near entries from the front of the list, far
+// entries from its back (entry k of the far part at list position cap-1-k).
+// Lane q of the W lanes of a particle takes the E consecutive entries
+// [q*E, q*E + E) of every block with one E-wide load, so a warp reads
+// contiguous memory and each lane has E independent position gathers in
+// flight.  Entries past the count are never dereferenced (the lane gathers
+// its own position instead).
+template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool EXACT = false>
+__device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
+                                             const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
+{
+    constexpr bool NS1 = TRX >= ONE_SPECIES;
+    constexpr int TR = TRX & (ONE_SPECIES - 1);
+    constexpr uint32_t LB = W * E;
+    using V = typename IdxVec<E>::T;
+    const size_t bstride = (size_t)d.S;   // in V units: S * LB entries per block row / E
+    const V* lst = reinterpret_cast<const V*>(d.nbr + (size_t)i * LB + q * E);
+    if (FAR) lst += (size_t)(d.nbr_cap / LB - 1) * bstride * W;
+    const ptrdiff_t step = FAR ? -(ptrdiff_t)(bstride * W) : (ptrdiff_t)(bstride * W);
+    const uint32_t ns = P.ns;
+    const PairParam* row = spp + a * ns;
+    PairParam p1;
+    if (NS1) p1 = spp[0];
+    const uint32_t nblk = (cnt + LB - 1) / LB;
+    for (uint32_t b = 0; b < nblk; ++b, lst += step) {
+        const V jv = __ldg(lst);
+        float4 rj[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t o = q * E + e;
+            const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
+            rj[e] = __ldg(d.pos + (k < cnt ? idx_at(jv, e) : i));
+        }
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t o = q * E + e;
+            const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
+            const PairParam* pp;
+            if (k >= cnt || !pair_of<NS1>(row, p1, ns, rj[e].w, pp)) continue;
+            if (FAR) far_pair<TR, AUX, WRAP>(*pp, P, ri, rj[e], A);
+            else near_pair<TR, AUX, WRAP, EXACT>(*pp, P, ri, rj[e], A);
+        }
+    }
+}
+
+// force_blocks with the E entries of a load taken two at a time (E even)
+template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool EXACT = false>
+__device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
+                                              const PairParam* spp, float4 ri, uint32_t a, ForceAcc2& A)
+{
+    static_assert(E % 2 == 0, "entries are taken in pairs");
+    constexpr bool NS1 = TRX >= ONE_SPECIES;
+    constexpr int TR = TRX & (ONE_SPECIES - 1);
+    constexpr uint32_t LB = W * E;
+    using V = typename IdxVec<E>::T;
+    const size_t bstride = (size_t)d.S;
+    const V* lst = reinterpret_cast<const V*>(d.nbr + (size_t)i * LB + q * E);
+    if (FAR) lst += (size_t)(d.nbr_cap / LB - 1) * bstride * W;
+    const ptrdiff_t step = FAR ? -(ptrdiff_t)(bstride * W) : (ptrdiff_t)(bstride * W);
+    const uint32_t ns = P.ns;
+    const PairParam* row = spp + a * ns;
+    PP2 p1;
+    if (NS1) p1 = pack_params(spp[0], spp[0]);
+    const uint32_t nblk = (cnt + LB - 1) / LB;
+    V jv;
+    if (HMD_FORCE_PREFETCH && nblk > 0) jv = __ldg(lst);
+    for (uint32_t b = 0; b < nblk; ++b, lst += step) {
+        // the list stream comes from HBM: the next block's indices are
+        // loaded one iteration ahead of their gathers
+        V jn;
+        if (HMD_FORCE_PREFETCH) {
+            jn = jv;
+            if (b + 1 < nblk) jn = __ldg(lst + step);
+        } else {
+            jv = __ldg(lst);
+        }
+        float4 rj[E];
+        bool in[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t o = q * E + e;
+            const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
+            in[e] = k < cnt;
+            rj[e] = __ldg(d.pos + (in[e] ? idx_at(jv, e) : i));
+        }
+#pragma unroll
+        for (int e = 0; e < E; e += 2) {
+            PP2 pp;
+            bool va = in[e], vb = in[e + 1];
+            if (NS1) {
+                pp = p1;
+            } else {
+                // a neighbour of no species of the system (lists hold real
+                // particles only) reads row entry 0 and is masked
+                const uint32_t ba = species_bits(rj[e].w), bb = species_bits(rj[e + 1].w);
+                va = va && ba < ns;
+                vb = vb && bb < ns;
+                pp = pack_params(row[ba < ns ? ba : 0u], row[bb < ns ? bb : 0u]);
+            }
+            if (FAR) far_pair2<TR, AUX, WRAP>(pp, P, ri, rj[e], rj[e + 1], va, vb, A);
+            else near_pair2<TR, AUX, WRAP, EXACT>(pp, P, ri, rj[e], rj[e + 1], va, vb, A);
+        }
+        if (HMD_FORCE_PREFETCH) jv = jn;
+    }
+}
+
+template <int W, int E, int TR, bool AUX>
+__device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf,
+                                               bool wrap, bool exact, const SysParam& P, const PairParam* spp,
+                                               float4 ri, uint32_t a, ForceAcc& A)
+{
+    if constexpr (E % 2 == 0) {
+        ForceAcc2 B;
+        if (wrap) {
+            force_blocks2<W, E, TR, AUX, true, false>(d, i, q, nn, P, spp, ri, a, B);
+            force_blocks2<W, E, TR, AUX, true, true>(d, i, q, nf, P, spp, ri, a, B);
+        } else {
+            if (exact) force_blocks2<W, E, TR, AUX, false, false, true>(d, i, q, nn, P, spp, ri, a, B);
+            else force_blocks2<W, E, TR, AUX, false, false>(d, i, q, nn, P, spp, ri, a, B);
+            force_blocks2<W, E, TR, AUX, false, true>(d, i, q, nf, P, spp, ri, a, B);
+        }
+        fold_lanes2<AUX>(B, A);
+    } else if (wrap) {
+        force_blocks<W, E, TR, AUX, true, false>(d, i, q, nn, P, spp, ri, a, A);
+        force_blocks<W, E, TR, AUX, true, true>(d, i, q, nf, P, spp, ri, a, A);
+    } else {
+        if (exact) force_blocks<W, E, TR, AUX, false, false, true>(d, i, q, nn, P, spp, ri, a, A);
+        else force_blocks<W, E, TR, AUX, false, false>(d, i, q, nn, P, spp, ri, a, A);
+        force_blocks<W, E, TR, AUX, false, true>(d, i, q, nf, P, spp, ri, a, A);
+    }
+    // fold the plain far-pair sums into the compensated accumulators
+    two_sum_acc(A.fx, A.cx, A.gx);
+    two_sum_acc(A.fy, A.cy, A.gy);
+    two_sum_acc(A.fz, A.cz, A.gz);
+}
+
+// merge the compensated sums of the W lanes of a particle (fixed tree: deterministic)
+template <int W>
+__device__ __forceinline__ void lane_merge(float& s, float& c)
+{
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xFFFFFFFFu, s, o, W);
+        const float c2 = __shfl_xor_sync(0xFFFFFFFFu, c, o, W);
+        const float t = __fadd_rn(s, s2);
+        c = __fadd_rn(__fadd_rn(c, c2), two_sum_err(s, s2, t));
+        s = t;
+    }
+}
+
+template <int W>
+__device__ __forceinline__ float lane_sum(float v)
+{
+#pragma unroll
+    for (int o = W / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o, W);
+    return v;
+}
+
+// kind of pair interaction of a system (FK_*), the template selector of k_force
+__device__ __forceinline__ int force_kind_of(const SysParam& P)
+{
+    if (P.trunc == TRUNC_SHARP || P.trunc == TRUNC_SHIFTED) return P.ns == 1 ? FK_LJ1 : FK_SHIFTED;
+    return P.trunc == TRUNC_SMOOTH_R4 ? FK_SMOOTH : FK_FSHIFT;
+}
+
+template <int W, int E, int KIND, bool AUX>
+__global__ void __launch_bounds__(128, HMD_FORCE_MINB) k_force(Dev d)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = t / W, q = t % W;
+    const uint32_t s = d.chunk_sys[(blockIdx.x * (blockDim.x / W)) / CHUNK];
+    const SysParam& P = d.sys[s];
+    __shared__ PairParam spp[MAX_SPECIES * MAX_SPECIES];
+    const uint32_t np = P.ns * P.ns;
+    if (threadIdx.x < np) spp[threadIdx.x] = d.pair[P.pair_off + threadIdx.x];
+    __syncthreads();
+    if (!P.active || !d.st[s].live || *d.status != 0u) return;   // block-uniform
+    if (KIND != FK_GENERIC && force_kind_of(P) != KIND) return;      // another kind's launch
+    const float4 ri = d.pos[i];
+    const uint32_t a = species_bits(ri.w);
+    const bool real = a != PLACEHOLDER;
+    const uint32_t packed = real ? d.nbr_count[i] : 0u;
+    const uint32_t nn = packed & 0xFFFFu, nf = packed >> 16;   // near / far list parts
+    const bool inner = !real || (fabsf(ri.x) < P.inner[0] && fabsf(ri.y) < P.inner[1] && fabsf(ri.z) < P.inner[2]);
+    const bool wrap = __any_sync(0xFFFFFFFFu, !inner);
+    const bool far_from_zero = !real || (fabsf(ri.x) >= P.exact_min && fabsf(ri.y) >= P.exact_min &&
+                                         fabsf(ri.z) >= P.exact_min);
+    const bool exact = __all_sync(0xFFFFFFFFu, far_from_zero);
+    ForceAcc A;
+    if (real) {
+        if constexpr (KIND == FK_LJ1) {
+            force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+        } else if constexpr (KIND == FK_SHIFTED) {
+            force_dispatch<W, E, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+        } else if constexpr (KIND == FK_SMOOTH) {
+            force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+        } else if constexpr (KIND == FK_FSHIFT) {
+            force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+        } else {
+            switch (force_kind_of(P)) {
+            case FK_LJ1: force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
+            case FK_SHIFTED: force_dispatch<W, E, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
+            case FK_SMOOTH: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
+            default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
+            }
+        }
+    }
+    lane_merge<W>(A.fx, A.cx);
+    lane_merge<W>(A.fy, A.cy);
+    lane_merge<W>(A.fz, A.cz);
+    if (AUX) {
+        A.en = lane_sum<W>(A.en);
+        A.s0 = lane_sum<W>(A.s0); A.s1 = lane_sum<W>(A.s1); A.s2 = lane_sum<W>(A.s2);
+        A.s3 = lane_sum<W>(A.s3); A.s4 = lane_sum<W>(A.s4); A.s5 = lane_sum<W>(A.s5);
+    }
+    if (!real || q != 0) return;
+    d.force[i] = make_float4(A.fx + A.cx, A.fy + A.cy, A.fz + A.cz, 0.0f);
+    if (AUX) {
+        const size_t stride = d.S;
+        d.en_pot[i] = 0.5f * A.en;
+        float* sp = d.stress + i;
+        sp[0 * stride] = 0.5f * A.s0;
+        sp[1 * stride] = 0.5f * A.s1;
+        sp[2 * stride] = 0.5f * A.s2;
+        sp[3 * stride] = 0.5f * A.s3;
+        sp[4 * stride] = 0.5f * A.s4;
+        sp[5 * stride] = 0.5f * A.s5;
+    }
+}
+
+template <int W, int E, int KIND>
+static void launch_force_shape(const Dev& d, bool aux, cudaStream_t st)
+{
+    const unsigned grid = (unsigned)((size_t)d.S * W / 128);
+    if (aux) k_force<W, E, KIND, true><<<grid, 128, 0, st>>>(d);
+    else k_force<W, E, KIND, false><<<grid, 128, 0, st>>>(d);
+}
+
+// (lanes, list block) shapes the engine accepts: E = block / lanes entries per load
+template <int KIND>
+void launch_force_kind(const Dev& d, bool aux, cudaStream_t st)
+{
+    const uint32_t lb = 1u << d.lb_log2;
+    switch (d.lanes * 16u + lb) {
+    case 1 * 16 + 4: launch_force_shape<1, 4, KIND>(d, aux, st); break;
+    case 2 * 16 + 4: launch_force_shape<2, 2, KIND>(d, aux, st); break;
+    case 2 * 16 + 8: launch_force_shape<2, 4, KIND>(d, aux, st); break;
+    case 4 * 16 + 4: launch_force_shape<4, 1, KIND>(d, aux, st); break;
+    case 4 * 16 + 8: launch_force_shape<4, 2, KIND>(d, aux, st); break;
+    default: launch_force_shape<8, 1, KIND>(d, aux, st); break;
+    }
+}
+
+} // namespace hmd

@@ -121,6 +121,7 @@ struct Dev {
     uint32_t lanes;            // threads per particle in the force kernel (1, 2, 4, 8)
     uint32_t lb_log2;          // log2 of the list block width LB (4 or 8)
     uint32_t nbr_scan;         // list build: 0 by system size, 1 per lane, 2 shared per warp of 32 particles
+    uint32_t force_kinds;      // bit k: a system of force kind k (kernels.h ForceKind); 0: unknown, one kernel for all
     uint32_t* cell;            // cell contents
     uint32_t* cell_count;      // [total_cells]
     const uint32_t* cell_sys;  // [total_cells] owning system

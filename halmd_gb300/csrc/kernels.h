@@ -8,9 +8,17 @@ namespace hmd {
 
 struct Dev;
 
+// kinds of pair interaction, one pair-force kernel each (force.cuh):
+// FK_LJ1 one species with a sharp or shifted truncation, FK_SHIFTED several
+// species with a sharp or shifted truncation, FK_SMOOTH smooth_r4, FK_FSHIFT
+// force_shifted; FK_GENERIC handles every kind in one kernel
+enum ForceKind : int { FK_GENERIC = 0, FK_LJ1 = 1, FK_SHIFTED = 2, FK_SMOOTH = 3, FK_FSHIFT = 4 };
+template <int KIND> void launch_force_kind(const Dev& d, bool aux, cudaStream_t st);
+
 // step (kernels_step.cu)
 void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool use_handle, cudaStream_t st);
 void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st);
+// the force kernels of the kinds in Dev::force_kinds (all kinds in one when 0)
 void launch_force(const Dev& d, bool aux, cudaStream_t st);
 void launch_finalize(const Dev& d, bool ds, cudaStream_t st);
 // finalize of step k fused with the integrate of step k + 1 (captured chunks)

@@ -1,6 +1,7 @@
 // kernels_step.cu — per-step kernels: velocity-Verlet integrate (fused with the
-// maximum-displacement reduction and the rebuild decision), truncated LJ pair
-// force from the neighbour list, Verlet / Andersen finalize, FP64 reductions.
+// maximum-displacement reduction and the rebuild decision), Verlet / Andersen
+// finalize, FP64 reductions, and the dispatch of the pair-force kernels
+// (force.cuh, compiled per interaction kind in kernels_force_*.cu).
 //
 // Every kernel runs over all slots of all systems of an engine; a block never
 // straddles two systems (blocks of <= 256 threads, systems padded to 256
@@ -279,399 +280,6 @@ __global__ void k_mark(Dev d, int rebuild_all)
 }
 
 // ---------------------------------------------------------------------------
-// pair force (mdsim/gpu/forces/pair_trunc_kernel.cuh:165-255)
-//   F_i = Σ_j fval(r_ij²) r_ij over list entries with r_ij² < r_c²;
-//   aux: E_i = ½ Σ U, stress_i = ½ Σ fval r⊗r (full list, weight ½,
-//   pair_trunc.hpp:291-294).
-// FP32 math; each force component is accumulated with Knuth's TwoSum and
-// a running compensation term, so the per-particle sum is as accurate as a
-// double-single accumulator (the reference uses dsfloat, :194).
-// The within-range test uses the same rounded squared distance as the list
-// build, so the pair set is reproducible on the CPU.
-// ---------------------------------------------------------------------------
-
-__device__ __forceinline__ void two_sum_acc(float& s, float& c, float x)
-{
-    const float t = __fadd_rn(s, x);
-    const float z = __fsub_rn(t, s);
-    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z));
-    s = t;
-    c = __fadd_rn(c, e);
-}
-
-// error of s = fl(a + b) (Knuth TwoSum)
-__device__ __forceinline__ float two_sum_err(float a, float b, float s)
-{
-    const float bp = __fsub_rn(s, a);
-    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
-}
-
-// error of s = fl(a + b) for a, b >= 0 (Dekker's Fast2Sum on the ordered pair)
-__device__ __forceinline__ float fast_err_pos(float a, float b, float s)
-{
-    return __fsub_rn(fminf(a, b), __fsub_rn(s, fmaxf(a, b)));
-}
-
-// LJ + truncation (lennard_jones_kernel.hpp:44-56, truncations/*_kernel.cuh).
-// Compensated LJ for close pairs, whose forces can be an order of magnitude
-// above the particle's net force: the squared distance arrives as a (hi, lo)
-// pair, the reciprocal is refined against it, the float parameters sigma^2
-// and 48 eps / sigma^2 carry their rounding errors, and every product of
-// fval = 48 eps/sigma^2 rri^4 (rri^3 - 1/2) keeps its exact residual (FMA),
-// so fval + flo is accurate to first order in the float roundings (the
-// steep r^-14 law would otherwise amplify them seven-fold).  The smoothing
-// factors (smooth_r4) and the force shift use approximate reciprocal /
-// square-root intrinsics: their errors scale forces that are already small
-// near r_c.
-template <int TR>
-__device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rrl, float rri_smooth,
-                                          float& fval, float& flo, float& en)
-{
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(rr));
-    const float res = __fmaf_rn(-rrl, y, __fmaf_rn(-rr, y, 1.0f));
-    const float ylo = __fmul_rn(y, res);
-    const float rri = __fmul_rn(p.sigma2, y);
-    float rril = __fmaf_rn(p.sigma2, ylo, __fmaf_rn(p.sigma2, y, -rri));
-    rril = __fmaf_rn(p.sigma2_lo, y, rril);
-    const float t1 = __fmul_rn(rri, rri);
-    const float ri6 = __fmul_rn(t1, rri);
-    const float a = __fmul_rn(p.c48, rri);
-    const float b = __fmul_rn(a, ri6);
-    const float u = __fsub_rn(ri6, 0.5f);
-    fval = __fmul_rn(b, u);
-    // residuals: ri6 = rri^3, u = ri6 - 1/2, a = c48 rri, b = a ri6, fval = b u
-    float ri6l = __fmaf_rn(__fmaf_rn(rri, rri, -t1), rri, __fmaf_rn(t1, rri, -ri6));
-    ri6l = __fmaf_rn(__fmul_rn(3.0f, t1), rril, ri6l);
-    const float ul = __fadd_rn(two_sum_err(ri6, -0.5f, u), ri6l);
-    float al = __fmaf_rn(p.c48, rril, __fmaf_rn(p.c48, rri, -a));
-    al = __fmaf_rn(p.c48_lo, rri, al);
-    const float bl = __fmaf_rn(a, ri6l, __fmaf_rn(al, ri6, __fmaf_rn(a, ri6, -b)));
-    flo = __fmaf_rn(b, ul, __fmaf_rn(bl, u, __fmaf_rn(b, u, -fval)));
-    en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
-    if (TR == TRUNC_SMOOTH_R4) {
-        const float rinv = rsqrtf(rr);
-        const float r = rr * rinv;
-        const float dr = r - p.r_cut;
-        const float x2 = dr * dr * rri_smooth;
-        const float x4 = x2 * x2;
-        const float x4i = __fdividef(1.0f, 1.0f + x4);
-        const float h0 = x4 * x4i;
-        const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
-        fval = h0 * fval - h1 * (en * rinv);
-        flo = h0 * flo;
-        en = h0 * en;
-    } else if (TR == TRUNC_FORCE_SHIFTED) {
-        const float rinv = rsqrtf(rr);
-        fval = fval - p.f_cut * rinv;
-        en = en + (rr * rinv - p.r_cut) * p.f_cut;
-    }
-}
-
-// plain FP32 evaluation for pairs that were farther than NEAR_SIGMA sigma at
-// list build time (forces of order eps / sigma or less)
-template <int TR>
-__device__ __forceinline__ void pair_eval_fast(const PairParam& p, float rr, float rri_smooth, float& fval, float& en)
-{
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(rr));
-    const float rri = p.sigma2 * y;
-    const float ri6 = rri * rri * rri;
-    fval = p.c48 * rri * ri6 * (ri6 - 0.5f);
-    en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
-    if (TR == TRUNC_SMOOTH_R4) {
-        const float rinv = rsqrtf(rr);
-        const float dr = rr * rinv - p.r_cut;
-        const float x2 = dr * dr * rri_smooth;
-        const float x4 = x2 * x2;
-        const float x4i = __fdividef(1.0f, 1.0f + x4);
-        const float h0 = x4 * x4i;
-        const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
-        fval = h0 * fval - h1 * (en * rinv);
-        en = h0 * en;
-    } else if (TR == TRUNC_FORCE_SHIFTED) {
-        const float rinv = rsqrtf(rr);
-        fval = fval - p.f_cut * rinv;
-        en = en + (rr * rinv - p.r_cut) * p.f_cut;
-    }
-}
-
-struct ForceAcc {
-    float fx = 0, fy = 0, fz = 0, cx = 0, cy = 0, cz = 0;   // compensated (near pairs)
-    float gx = 0, gy = 0, gz = 0;                           // plain sums (far pairs)
-    float en = 0, s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0;
-};
-
-// TR >= ONE_SPECIES: single-species system, the pair table has one entry
-constexpr int ONE_SPECIES = 16;
-
-// Pair-parameter lookup for a neighbour of species b; false when b is not a
-// species of the system (lists hold real particles only: this keeps the
-// table lookup in bounds)
-template <bool NS1>
-__device__ __forceinline__ bool pair_of(const PairParam* row, const PairParam& p1, uint32_t ns, float w,
-                                        const PairParam*& pp)
-{
-    if (NS1) { pp = &p1; return true; }
-    const uint32_t b = species_bits(w);
-    if (b >= ns) return false;
-    pp = row + b;
-    return true;
-}
-
-// one near pair: compensated separation, squared distance and LJ value;
-// WRAP = false when no particle of the warp can see a neighbour across the
-// box: then rint(s/L) = 0 for every pair and the minimum-image arithmetic is
-// skipped without changing any result
-// EXACT: every coordinate of every particle of the warp is at least
-// SysParam::exact_min from zero, so each near partner (closer than that half
-// distance per coordinate) has the same sign and lies within a factor of two:
-// ri - rj is exact (Sterbenz) and its TwoSum error is zero, so the
-// error terms are dropped without changing any bit of the result
-template <int TR, bool AUX, bool WRAP, bool EXACT>
-__device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A)
-{
-    const float sx = __fsub_rn(ri.x, rj.x);
-    const float sy = __fsub_rn(ri.y, rj.y);
-    const float sz = __fsub_rn(ri.z, rj.z);
-    const float dx = WRAP ? min_image(sx, P.L[0], P.Linv[0]) : sx;
-    const float dy = WRAP ? min_image(sy, P.L[1], P.Linv[1]) : sy;
-    const float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
-    const float px = __fmul_rn(dx, dx), py = __fmul_rn(dy, dy), pz = __fmul_rn(dz, dz);
-    const float pxy = __fadd_rn(px, py);
-    const float rr = __fadd_rn(pxy, pz);   // == rr_exact(dx, dy, dz)
-    if (!(rr < p.rr_cut)) return;
-    // dx - k L is exact (k = 0, or Sterbenz for k = +-1): the difference
-    // error is the TwoSum error of ri - rj
-    float dxl = 0.0f, dyl = 0.0f, dzl = 0.0f;
-    if (!EXACT) {
-        dxl = two_sum_err(ri.x, -rj.x, sx);
-        dyl = two_sum_err(ri.y, -rj.y, sy);
-        dzl = two_sum_err(ri.z, -rj.z, sz);
-    }
-    float rrl = __fadd_rn(__fadd_rn(__fmaf_rn(dx, dx, -px), __fmaf_rn(dy, dy, -py)), __fmaf_rn(dz, dz, -pz));
-    rrl = __fadd_rn(rrl, __fadd_rn(fast_err_pos(px, py, pxy), fast_err_pos(pxy, pz, rr)));
-    if (!EXACT) rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
-    float fval, flo, e;
-    pair_eval<TR>(p, rr, rrl, P.rri_smooth, fval, flo, e);
-    const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
-    two_sum_acc(A.fx, A.cx, tx);
-    two_sum_acc(A.fy, A.cy, ty);
-    two_sum_acc(A.fz, A.cz, tz);
-    float cx = __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx));
-    float cy = __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty));
-    float cz = __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz));
-    if (!EXACT) {
-        cx = __fmaf_rn(fval, dxl, cx);
-        cy = __fmaf_rn(fval, dyl, cy);
-        cz = __fmaf_rn(fval, dzl, cz);
-    }
-    A.cx = __fmaf_rn(flo, dx, cx);
-    A.cy = __fmaf_rn(flo, dy, cy);
-    A.cz = __fmaf_rn(flo, dz, cz);
-    if (AUX) {
-        A.en += e;
-        A.s0 += fval * dx * dx;
-        A.s1 += fval * dy * dy;
-        A.s2 += fval * dz * dz;
-        A.s3 += fval * dx * dy;
-        A.s4 += fval * dx * dz;
-        A.s5 += fval * dy * dz;
-    }
-}
-
-// one far pair: plain FP32 (forces of order eps / sigma or less)
-template <int TR, bool AUX, bool WRAP>
-__device__ __forceinline__ void far_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A)
-{
-    const float sx = __fsub_rn(ri.x, rj.x);
-    const float sy = __fsub_rn(ri.y, rj.y);
-    const float sz = __fsub_rn(ri.z, rj.z);
-    float dx = WRAP ? min_image(sx, P.L[0], P.Linv[0]) : sx;
-    float dy = WRAP ? min_image(sy, P.L[1], P.Linv[1]) : sy;
-    float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
-    float rr = rr_exact(dx, dy, dz);
-    if (!(rr < p.rr_cut)) return;
-    if (WRAP) {
-        // across the box ri - rj is of order L and its rounding error (up to
-        // ulp(L)/2) would dominate the separation error: add the TwoSum error
-        // back (the cut-off decision above keeps the rounded rr of the list
-        // criterion)
-        dx = __fadd_rn(dx, two_sum_err(ri.x, -rj.x, sx));
-        dy = __fadd_rn(dy, two_sum_err(ri.y, -rj.y, sy));
-        dz = __fadd_rn(dz, two_sum_err(ri.z, -rj.z, sz));
-        rr = rr_exact(dx, dy, dz);
-    }
-    float fval, e;
-    pair_eval_fast<TR>(p, rr, P.rri_smooth, fval, e);
-    A.gx = __fmaf_rn(fval, dx, A.gx);
-    A.gy = __fmaf_rn(fval, dy, A.gy);
-    A.gz = __fmaf_rn(fval, dz, A.gz);
-    if (AUX) {
-        A.en += e;
-        A.s0 += fval * dx * dx;
-        A.s1 += fval * dy * dy;
-        A.s2 += fval * dz * dz;
-        A.s3 += fval * dx * dy;
-        A.s4 += fval * dx * dz;
-        A.s5 += fval * dy * dz;
-    }
-}
-
-// E list entries per lane and block, read with one vector load
-template <int E> struct IdxVec;
-template <> struct IdxVec<1> { using T = uint32_t; };
-template <> struct IdxVec<2> { using T = uint2; };
-template <> struct IdxVec<4> { using T = uint4; };
-__device__ __forceinline__ uint32_t idx_at(uint32_t v, int) { return v; }
-__device__ __forceinline__ uint32_t idx_at(uint2 v, int e) { return e == 0 ? v.x : v.y; }
-__device__ __forceinline__ uint32_t idx_at(uint4 v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
-
-// The list is stored in blocks of LB = W * E entries: entry k of slot i at
-// ((k/LB)*S + i)*LB + k%LB, near entries from the front of the list, far
-// entries from its back (entry k of the far part at list position cap-1-k).
-// Lane q of the W lanes of a particle takes the E consecutive entries
-// [q*E, q*E + E) of every block with one E-wide load, so a warp reads
-// contiguous memory and each lane has E independent position gathers in
-// flight.  Entries past the count are never dereferenced (the lane gathers
-// its own position instead).
-template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool EXACT = false>
-__device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
-                                             const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
-{
-    constexpr bool NS1 = TRX >= ONE_SPECIES;
-    constexpr int TR = TRX & (ONE_SPECIES - 1);
-    constexpr uint32_t LB = W * E;
-    using V = typename IdxVec<E>::T;
-    const size_t bstride = (size_t)d.S;   // in V units: S * LB entries per block row / E
-    const V* lst = reinterpret_cast<const V*>(d.nbr + (size_t)i * LB + q * E);
-    if (FAR) lst += (size_t)(d.nbr_cap / LB - 1) * bstride * W;
-    const ptrdiff_t step = FAR ? -(ptrdiff_t)(bstride * W) : (ptrdiff_t)(bstride * W);
-    const uint32_t ns = P.ns;
-    const PairParam* row = spp + a * ns;
-    PairParam p1;
-    if (NS1) p1 = spp[0];
-    const uint32_t nblk = (cnt + LB - 1) / LB;
-    for (uint32_t b = 0; b < nblk; ++b, lst += step) {
-        const V jv = __ldg(lst);
-        float4 rj[E];
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const uint32_t o = q * E + e;
-            const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
-            rj[e] = __ldg(d.pos + (k < cnt ? idx_at(jv, e) : i));
-        }
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const uint32_t o = q * E + e;
-            const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
-            const PairParam* pp;
-            if (k >= cnt || !pair_of<NS1>(row, p1, ns, rj[e].w, pp)) continue;
-            if (FAR) far_pair<TR, AUX, WRAP>(*pp, P, ri, rj[e], A);
-            else near_pair<TR, AUX, WRAP, EXACT>(*pp, P, ri, rj[e], A);
-        }
-    }
-}
-
-template <int W, int E, int TR, bool AUX>
-__device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf,
-                                               bool wrap, bool exact, const SysParam& P, const PairParam* spp,
-                                               float4 ri, uint32_t a, ForceAcc& A)
-{
-    if (wrap) {
-        force_blocks<W, E, TR, AUX, true, false>(d, i, q, nn, P, spp, ri, a, A);
-        force_blocks<W, E, TR, AUX, true, true>(d, i, q, nf, P, spp, ri, a, A);
-    } else {
-        if (exact) force_blocks<W, E, TR, AUX, false, false, true>(d, i, q, nn, P, spp, ri, a, A);
-        else force_blocks<W, E, TR, AUX, false, false>(d, i, q, nn, P, spp, ri, a, A);
-        force_blocks<W, E, TR, AUX, false, true>(d, i, q, nf, P, spp, ri, a, A);
-    }
-    // fold the plain far-pair sums into the compensated accumulators
-    two_sum_acc(A.fx, A.cx, A.gx);
-    two_sum_acc(A.fy, A.cy, A.gy);
-    two_sum_acc(A.fz, A.cz, A.gz);
-}
-
-// merge the compensated sums of the W lanes of a particle (fixed tree: deterministic)
-template <int W>
-__device__ __forceinline__ void lane_merge(float& s, float& c)
-{
-#pragma unroll
-    for (int o = W / 2; o > 0; o >>= 1) {
-        const float s2 = __shfl_xor_sync(0xFFFFFFFFu, s, o, W);
-        const float c2 = __shfl_xor_sync(0xFFFFFFFFu, c, o, W);
-        const float t = __fadd_rn(s, s2);
-        c = __fadd_rn(__fadd_rn(c, c2), two_sum_err(s, s2, t));
-        s = t;
-    }
-}
-
-template <int W>
-__device__ __forceinline__ float lane_sum(float v)
-{
-#pragma unroll
-    for (int o = W / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o, W);
-    return v;
-}
-
-template <int W, int E, bool AUX>
-__global__ void __launch_bounds__(128) k_force(Dev d)
-{
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t i = t / W, q = t % W;
-    const uint32_t s = d.chunk_sys[(blockIdx.x * (blockDim.x / W)) / CHUNK];
-    const SysParam& P = d.sys[s];
-    __shared__ PairParam spp[MAX_SPECIES * MAX_SPECIES];
-    const uint32_t np = P.ns * P.ns;
-    if (threadIdx.x < np) spp[threadIdx.x] = d.pair[P.pair_off + threadIdx.x];
-    __syncthreads();
-    if (!P.active || !d.st[s].live || *d.status != 0u) return;   // block-uniform
-    const float4 ri = d.pos[i];
-    const uint32_t a = species_bits(ri.w);
-    const bool real = a != PLACEHOLDER;
-    const uint32_t packed = real ? d.nbr_count[i] : 0u;
-    const uint32_t nn = packed & 0xFFFFu, nf = packed >> 16;   // near / far list parts
-    const bool inner = !real || (fabsf(ri.x) < P.inner[0] && fabsf(ri.y) < P.inner[1] && fabsf(ri.z) < P.inner[2]);
-    const bool wrap = __any_sync(0xFFFFFFFFu, !inner);
-    const bool far_from_zero = !real || (fabsf(ri.x) >= P.exact_min && fabsf(ri.y) >= P.exact_min &&
-                                         fabsf(ri.z) >= P.exact_min);
-    const bool exact = __all_sync(0xFFFFFFFFu, far_from_zero);
-    ForceAcc A;
-    if (real) {
-        switch (P.trunc) {
-        case TRUNC_SHARP:
-        case TRUNC_SHIFTED:
-            if (P.ns == 1) force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
-            else force_dispatch<W, E, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
-            break;
-        case TRUNC_SMOOTH_R4: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
-        default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
-        }
-    }
-    lane_merge<W>(A.fx, A.cx);
-    lane_merge<W>(A.fy, A.cy);
-    lane_merge<W>(A.fz, A.cz);
-    if (AUX) {
-        A.en = lane_sum<W>(A.en);
-        A.s0 = lane_sum<W>(A.s0); A.s1 = lane_sum<W>(A.s1); A.s2 = lane_sum<W>(A.s2);
-        A.s3 = lane_sum<W>(A.s3); A.s4 = lane_sum<W>(A.s4); A.s5 = lane_sum<W>(A.s5);
-    }
-    if (!real || q != 0) return;
-    d.force[i] = make_float4(A.fx + A.cx, A.fy + A.cy, A.fz + A.cz, 0.0f);
-    if (AUX) {
-        const size_t stride = d.S;
-        d.en_pot[i] = 0.5f * A.en;
-        float* sp = d.stress + i;
-        sp[0 * stride] = 0.5f * A.s0;
-        sp[1 * stride] = 0.5f * A.s1;
-        sp[2 * stride] = 0.5f * A.s2;
-        sp[3 * stride] = 0.5f * A.s3;
-        sp[4 * stride] = 0.5f * A.s4;
-        sp[5 * stride] = 0.5f * A.s5;
-    }
-}
-
-// ---------------------------------------------------------------------------
 // FP64 reductions (observables/gpu/thermodynamics_kernel.cu:35-106 and
 // algorithm/gpu/reduce_kernel.cuh:126): per-block partial sums, then a
 // fixed-order per-system reduction (deterministic, no double atomics).
@@ -763,26 +371,19 @@ void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st)
     k_mark<<<(d.nsys + 255) / 256, 256, 0, st>>>(d, rebuild_all ? 1 : 0);
 }
 
-template <int W, int E>
-static void launch_force_w(const Dev& d, bool aux, cudaStream_t st)
-{
-    const unsigned grid = (unsigned)((size_t)d.S * W / 128);
-    if (aux) k_force<W, E, true><<<grid, 128, 0, st>>>(d);
-    else k_force<W, E, false><<<grid, 128, 0, st>>>(d);
-}
-
-// (lanes, list block) shapes the engine accepts: E = block / lanes entries per load
+// one launch per kind of pair interaction present in the engine (each
+// kernel skips the blocks of the other kinds); kinds 0: every kind in one
+// kernel (engines whose systems change after commit)
 void launch_force(const Dev& d, bool aux, cudaStream_t st)
 {
-    const uint32_t lb = 1u << d.lb_log2;
-    switch (d.lanes * 16u + lb) {
-    case 1 * 16 + 4: launch_force_w<1, 4>(d, aux, st); break;
-    case 2 * 16 + 4: launch_force_w<2, 2>(d, aux, st); break;
-    case 2 * 16 + 8: launch_force_w<2, 4>(d, aux, st); break;
-    case 4 * 16 + 4: launch_force_w<4, 1>(d, aux, st); break;
-    case 4 * 16 + 8: launch_force_w<4, 2>(d, aux, st); break;
-    default: launch_force_w<8, 1>(d, aux, st); break;
+    if (d.force_kinds == 0u) {
+        launch_force_kind<FK_GENERIC>(d, aux, st);
+        return;
     }
+    if (d.force_kinds & (1u << FK_LJ1)) launch_force_kind<FK_LJ1>(d, aux, st);
+    if (d.force_kinds & (1u << FK_SHIFTED)) launch_force_kind<FK_SHIFTED>(d, aux, st);
+    if (d.force_kinds & (1u << FK_SMOOTH)) launch_force_kind<FK_SMOOTH>(d, aux, st);
+    if (d.force_kinds & (1u << FK_FSHIFT)) launch_force_kind<FK_FSHIFT>(d, aux, st);
 }
 
 void launch_finalize(const Dev& d, bool ds, cudaStream_t st)
