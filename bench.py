@@ -94,22 +94,83 @@ def make_engine(w, L, seed=7):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """SM clocks and throttle reasons sampled during the timed region.
 
+    Reads NVML through ctypes every 5 ms in a thread (the timed regions of
+    the small workloads last well under a second); falls back to
+    `nvidia-smi -lms 50` where NVML cannot be loaded.  Only reads settings.
+    """
+
+    # nvmlClocksEventReasons bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x40: "sw_thermal_slowdown", 0x80: "hw_thermal_slowdown"}
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device=0):
+        import threading
+        self.rows = []          # (sm_mhz, reason bits)
+        self.max_mhz = None
         self.p = None
+        self.thread = None
+        self.stop_flag = threading.Event()
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        index = int(vis.split(",")[device]) if vis and vis.split(",")[device].strip().isdigit() else device
+        if self._nvml_start(index):
+            first = threading.Event()
+            self.thread = threading.Thread(target=self._poll, args=(first,), daemon=True)
+            self.thread.start()
+            first.wait(2.0)
+            return
         try:
-            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + self.Q,
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.p.stdout.readline()   # started: the first sample precedes the timed region
         except OSError:
             self.p = None
 
+    def _nvml_start(self, index):
+        import ctypes
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return False
+            h = ctypes.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(h)) != 0:
+                return False
+            mx = ctypes.c_uint()
+            if lib.nvmlDeviceGetMaxClockInfo(h, ctypes.c_int(1), ctypes.byref(mx)) != 0:   # NVML_CLOCK_SM
+                return False
+            self.max_mhz = float(mx.value)
+            self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            self.lib, self.h = lib, h
+            return True
+        except (OSError, AttributeError):
+            return False
+
+    def _poll(self, first):
+        import ctypes
+        mhz, bits = ctypes.c_uint(), ctypes.c_ulonglong()
+        while True:
+            if self.lib.nvmlDeviceGetClockInfo(self.h, ctypes.c_int(1), ctypes.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.h, ctypes.byref(bits)) == 0:
+                self.rows.append((float(mhz.value), int(bits.value)))
+            first.set()
+            if self.stop_flag.wait(0.005):
+                return
+
     def stop(self):
+        if self.thread is not None:
+            self.stop_flag.set()
+            self.thread.join()
+            self.lib.nvmlShutdown()
+            if not self.rows:
+                return None
+            reasons = sorted({name for _, b in self.rows for bit, name in self.REASONS.items() if b & bit})
+            return {"sm_mhz": float(np.median([r[0] for r in self.rows])), "sm_max_mhz": self.max_mhz,
+                    "samples": len(self.rows), "reasons": reasons, "source": "nvml, 5 ms"}
         if self.p is None:
             return None
         self.p.terminate()
@@ -130,7 +191,7 @@ class ClockSampler:
                 if r[3 + k].lower() == "active":
                     reasons.add(name)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": float(rows[0][1]),
-                "samples": len(rows), "reasons": sorted(reasons)}
+                "samples": len(rows), "reasons": sorted(reasons), "source": "nvidia-smi, 50 ms"}
 
 
 def dram_traffic(workload):
