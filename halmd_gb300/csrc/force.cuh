@@ -278,13 +278,6 @@ __device__ __forceinline__ void far_pair(const PairParam& p, const SysParam& P, 
 // their force value (the lane still evaluates them, as the warp would).
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
-__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 sel2(bool ka, bool kb, float2 v)
 {
     return make_float2(ka ? v.x : 0.0f, kb ? v.y : 0.0f);
@@ -318,12 +311,6 @@ __device__ __forceinline__ void two_sum_acc2(float2& s, float2& c, float2 x)
     const float2 e = add2(sub2(s, sub2(t, z)), sub2(x, z));
     s = t;
     c = add2(c, e);
-}
-
-__device__ __forceinline__ float2 min_image2(float2 s, float L, float Linv)
-{
-    const float2 q = mul2(s, bc2(Linv));
-    return fma2(f2(-rintf(q.x), -rintf(q.y)), bc2(L), s);
 }
 
 // the parameters of two pairs, lane by lane

@@ -169,6 +169,30 @@ __device__ __forceinline__ float rr_exact(float dx, float dy, float dz)
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
+// ---- FP32x2: two values per instruction, each half rounded as the scalar
+// operation (__fadd_rn, __fmul_rn, __fmaf_rn) -------------------------------
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+// min_image of each half
+__device__ __forceinline__ float2 min_image2(float2 s, float L, float Linv)
+{
+    const float2 q = mul2(s, bc2(Linv));
+    return fma2(f2(-rintf(q.x), -rintf(q.y)), bc2(L), s);
+}
+
+// rr_exact of each half
+__device__ __forceinline__ float2 rr_exact2(float2 dx, float2 dy, float2 dz)
+{
+    return add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
+}
+
 // ---- double-single arithmetic: Knuth TwoSum / Dekker split (DSFUN) --------
 
 __device__ __forceinline__ void ds_add(float& c0, float& c1, float a0, float a1, float b0, float b1)
