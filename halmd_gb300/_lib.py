@@ -18,6 +18,7 @@ HMD_OK = 0
 PRECISION = {"float": 0, "single": 0, "dsfloat": 1, "double-single": 1}
 TRUNCATION = {"sharp": 0, "shifted": 1, "smooth_r4": 2, "force_shifted": 3}
 INTEGRATOR = {"verlet": 0, "verlet_nvt_andersen": 1, "andersen": 1}
+POTENTIAL = {"lennard_jones": 0, "mie": 1, "morse": 2, "power_law": 3}
 MAX_SPECIES = 4
 NTHERMO = 14
 PLACEHOLDER = 0xFFFFFFFF
@@ -50,6 +51,12 @@ class SystemDesc(ctypes.Structure):
         ("collision_rate", ctypes.c_double),
         ("seed", ctypes.c_uint64),
         ("sort", ctypes.c_int32),
+        ("potential", ctypes.c_int32),
+        ("index_repulsion", ctypes.c_uint32 * 16),
+        ("index_attraction", ctypes.c_uint32 * 16),
+        ("index", ctypes.c_uint32 * 16),
+        ("r_min", ctypes.c_double * 16),
+        ("distortion", ctypes.c_double * 16),
     ]
 
 
@@ -168,8 +175,14 @@ def check(rc, handle=None):
 
 def system_desc(nparticle, box, epsilon=1.0, sigma=1.0, r_cut=2.5, truncation="shifted", smoothing=0.005,
                 skin=0.5, cell_occupancy=0.5, neighbour_occupancy=0.4, timestep=0.001, integrator="verlet",
-                temperature=1.0, collision_rate=0.0, seed=0, sort=True, nspecies=None):
-    """Build an hmd_system_desc from keyword arguments (Lua module names)."""
+                temperature=1.0, collision_rate=0.0, seed=0, sort=True, nspecies=None, potential="lennard_jones",
+                index_repulsion=12, index_attraction=6, index=12, r_min=None, distortion=1.0):
+    """Build an hmd_system_desc from keyword arguments (Lua module names).
+
+    potential: lennard_jones (epsilon, sigma), mie (index_repulsion m,
+    index_attraction n: even, m > n), morse (r_min, required; distortion B),
+    power_law (index n); every truncation applies to each.
+    """
     L = load()
     d = SystemDesc()
     L.hmd_system_desc_init(ctypes.byref(d))
@@ -202,6 +215,19 @@ def system_desc(nparticle, box, epsilon=1.0, sigma=1.0, r_cut=2.5, truncation="s
     d.collision_rate = collision_rate
     d.seed = int(seed)
     d.sort = 1 if sort else 0
+    d.potential = POTENTIAL[potential]
+    if potential == "morse" and r_min is None:
+        raise ValueError("morse needs r_min")
+    m_rep, m_att, m_idx = mat(index_repulsion), mat(index_attraction), mat(index)
+    m_rmin, m_dist = mat(0.0 if r_min is None else r_min), mat(distortion)
+    for a in range(ns):
+        for c in range(ns):
+            k = a * ns + c
+            d.index_repulsion[k] = int(m_rep[a, c])
+            d.index_attraction[k] = int(m_att[a, c])
+            d.index[k] = int(m_idx[a, c])
+            d.r_min[k] = m_rmin[a, c]
+            d.distortion[k] = m_dist[a, c]
     return d
 
 

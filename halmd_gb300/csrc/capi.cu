@@ -67,6 +67,14 @@ void hmd_system_desc_init(hmd_system_desc* d)
     d->collision_rate = 0.0;
     d->seed = 0;
     d->sort = 1;
+    d->potential = HMD_POTENTIAL_LENNARD_JONES;
+    for (int k = 0; k < HMD_MAX_SPECIES * HMD_MAX_SPECIES; ++k) {
+        d->index_repulsion[k] = 12;
+        d->index_attraction[k] = 6;
+        d->index[k] = 12;
+        d->r_min[k] = 0.0;
+        d->distortion[k] = 1.0;
+    }
 }
 
 int hmd_last_error(const hmd_engine* h, char* buf, size_t size)

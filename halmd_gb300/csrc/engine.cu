@@ -72,6 +72,62 @@ static void lj_double(double eps, double sigma2, double rr, double& fval, double
     en = 4 * eps_r6i * (r6i - 1);
 }
 
+// Mie prefactor C(m, n) = m / (m - n) (m / n)^(n / (m - n)) (mdsim/host/potentials/pair/mie.cpp:85-92)
+static double mie_prefactor(double m, double n) { return m / (m - n) * std::pow(m / n, n / (m - n)); }
+
+// integer power by repeated multiplication (numeric/pow.hpp)
+static double ipow(double x, unsigned n)
+{
+    double y = 1;
+    for (; n; n >>= 1, x *= x)
+        if (n & 1) y *= x;
+    return y;
+}
+
+// the bare pair potential in double for species pair ab: -U'(r)/r and U(r)
+// (host potentials lennard_jones.hpp:56-66, mie.hpp:63-73, morse.hpp:64-77,
+// power_law.hpp:129-148), for the truncation constants at r_c
+static void pot_double(const hmd_system_desc& d, uint32_t ab, double rr, double& fval, double& en)
+{
+    const double eps = d.epsilon[ab], sigma = d.sigma[ab], sigma2 = sigma * sigma;
+    switch (d.potential) {
+    case HMD_POTENTIAL_MIE: {
+        const unsigned m2 = d.index_repulsion[ab] / 2, n2 = d.index_attraction[ab] / 2;
+        const double epsC = eps * mie_prefactor(d.index_repulsion[ab], d.index_attraction[ab]);
+        const double rri = sigma2 / rr;
+        const double rni = ipow(rri, n2);
+        const double rmni = ipow(rri, m2 - n2);
+        const double eps_rni = epsC * rni;
+        fval = 2 * rri * eps_rni * (m2 * rmni - n2) / sigma2;
+        en = eps_rni * (rmni - 1);
+        return;
+    }
+    case HMD_POTENTIAL_MORSE: {
+        const double B = d.distortion[ab];
+        const double r_sigma_B = std::sqrt(rr) / sigma / B;
+        const double dr = d.r_min[ab] / sigma / B - r_sigma_B;
+        const double A = 2 * B * B - 1;
+        const double exp_dr = std::exp(dr), exp_A_dr = std::exp(A * dr);
+        const double eps_exp_dr = eps * exp_dr / A;
+        fval = (A + 1) * eps_exp_dr * (exp_A_dr - 1) * r_sigma_B / rr;
+        en = eps_exp_dr * (exp_A_dr - A - 1);
+        return;
+    }
+    case HMD_POTENTIAL_POWER_LAW: {
+        const unsigned n = d.index[ab];
+        const double rri = sigma2 / rr;
+        double rni = ipow(rri, n / 2);
+        if (n % 2) rni *= std::sqrt(rri);
+        const double eps_rni = eps * rni;
+        fval = n * eps_rni / rr;
+        en = eps_rni;
+        return;
+    }
+    default:
+        lj_double(eps, sigma2, rr, fval, en);
+    }
+}
+
 uint32_t Engine::add_system(const hmd_system_desc& d)
 {
     if (committed_ && !capacity_) throw Error(HMD_ERR_STATE, "systems must be added before commit");
@@ -85,9 +141,23 @@ uint32_t Engine::add_system(const hmd_system_desc& d)
     if (!(d.cell_occupancy > 0) || !(d.neighbour_occupancy > 0)) throw Error(HMD_ERR_INVALID, "occupancy must be positive");
     if (d.truncation == HMD_TRUNC_SMOOTH_R4 && !(d.smoothing > 0)) throw Error(HMD_ERR_INVALID, "smooth_r4 needs h > 0");
     const uint32_t ns = d.nspecies;
+    if (d.potential < HMD_POTENTIAL_LENNARD_JONES || d.potential > HMD_POTENTIAL_POWER_LAW)
+        throw Error(HMD_ERR_INVALID, "unknown potential");
     for (uint32_t ab = 0; ab < ns * ns; ++ab) {
         if (!(d.sigma[ab] > 0) || !(d.r_cut[ab] > 0) || !(d.epsilon[ab] >= 0))
             throw Error(HMD_ERR_INVALID, "bad potential parameters");
+        if (d.potential == HMD_POTENTIAL_MIE) {
+            const uint32_t m = d.index_repulsion[ab], n = d.index_attraction[ab];
+            // mdsim/host/potentials/pair/mie.cpp:72-83
+            if ((m & 1u) || (n & 1u)) throw Error(HMD_ERR_STATE, "power law indices of potential must be even");
+            if (m <= n) throw Error(HMD_ERR_STATE, "repulsive part of potential must be stronger than attraction");
+            if (n == 0 || m > 96) throw Error(HMD_ERR_INVALID, "mie indices out of range [2, 96]");
+        }
+        if (d.potential == HMD_POTENTIAL_MORSE && (!(d.r_min[ab] > 0) || !(d.distortion[ab] > 0) ||
+                                                   2 * d.distortion[ab] * d.distortion[ab] - 1 == 0))
+            throw Error(HMD_ERR_INVALID, "morse needs r_min > 0 and a distortion B > 0 with 2 B^2 != 1");
+        if (d.potential == HMD_POTENTIAL_POWER_LAW && (d.index[ab] < 1 || d.index[ab] > 96))
+            throw Error(HMD_ERR_INVALID, "power_law index out of range [1, 96]");
     }
     for (int q = 0; q < 3; ++q)
         if (!(d.box[q] > 0)) throw Error(HMD_ERR_INVALID, "box edges must be positive");
@@ -113,6 +183,7 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
     P.A = round_up(std::max<uint32_t>(d.nparticle, 1), align);
     P.ns = ns;
     P.trunc = (uint32_t)d.truncation;
+    P.pot = (uint32_t)d.potential;
     P.active = 1;
     P.sort_enable = d.sort ? 1u : 0u;
     P.integrator = (uint32_t)d.integrator;
@@ -124,7 +195,7 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
         const double rc = sigma * d.r_cut[ab];
         const double rcs = rc + d.skin;
         double fc, ec;
-        lj_double(eps, sigma2, rc * rc, fc, ec);
+        pot_double(d, ab, rc * rc, fc, ec);
         PairParam& p = h.pairs[ab];
         p.eps4 = (float)(4 * eps);
         p.c48 = (float)(48 * eps / sigma2);
@@ -137,6 +208,24 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
         p.rr_near = (float)(NEAR_SIGMA * NEAR_SIGMA * sigma2);
         p.sigma2_lo = (float)(sigma2 - (double)p.sigma2);
         p.c48_lo = (float)(48 * eps / sigma2 - (double)p.c48);
+        p.q0 = p.q1 = p.q2 = p.q3 = 0.0f;
+        if (d.potential == HMD_POTENTIAL_MIE) {
+            p.q0 = (float)(eps * mie_prefactor(d.index_repulsion[ab], d.index_attraction[ab]));
+            p.q1 = (float)(2 / sigma2);
+            p.q2 = (float)(d.index_repulsion[ab] / 2);
+            p.q3 = (float)(d.index_attraction[ab] / 2);
+        } else if (d.potential == HMD_POTENTIAL_MORSE) {
+            const double B = d.distortion[ab], A = 2 * B * B - 1;
+            p.q0 = (float)(eps / A);
+            p.q1 = (float)A;
+            p.q2 = (float)(1 / (sigma * B));
+            p.q3 = (float)(d.r_min[ab] / (sigma * B));
+        } else if (d.potential == HMD_POTENTIAL_POWER_LAW) {
+            p.q0 = (float)eps;
+            p.q1 = (float)d.index[ab];
+            p.q2 = (float)(d.index[ab] / 2);
+            p.q3 = (float)(d.index[ab] % 2);
+        }
         p.pad = 0.0f;
         rc_max = std::max(rc_max, rc);
         rcs_max = std::max(rcs_max, rcs);
@@ -294,6 +383,7 @@ void Engine::unplace(uint32_t s)
 // counterpart is force_kind_of in force.cuh)
 static int force_kind(const SysParam& P)
 {
+    if (P.pot != POT_LJ) return FK_POT;
     if (P.trunc == TRUNC_SHARP || P.trunc == TRUNC_SHIFTED) return P.ns == 1 ? FK_LJ1 : FK_SHIFTED;
     return P.trunc == TRUNC_SMOOTH_R4 ? FK_SMOOTH : FK_FSHIFT;
 }

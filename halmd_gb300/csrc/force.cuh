@@ -662,6 +662,193 @@ __device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_
     two_sum_acc(A.fz, A.cz, A.gz);
 }
 
+// ---------------------------------------------------------------------------
+// The other pair potentials (mie, morse, power_law) with any truncation.
+// The geometry runs two entries per FP32x2 instruction as above; each half
+// then evaluates the potential in scalar FP32 (per-pair exponents), the
+// reference's GPU formulas (mie_kernel.hpp, morse_kernel.hpp,
+// power_law_kernel.hpp) with the parameter products precomputed on the host.
+// Near pairs carry the separation's rounding error and are accumulated with
+// compensation, far pairs with plain FMAs.
+// ---------------------------------------------------------------------------
+
+// integer power by repeated squaring, exponent per pair (numeric/pow.hpp)
+__device__ __forceinline__ float ipowf(float x, uint32_t n)
+{
+    float y = 1.0f;
+    for (; n; n >>= 1, x *= x)
+        if (n & 1u) y *= x;
+    return y;
+}
+
+// bare -U'(r)/r and U(r); PairParam::q0..q3 as documented there
+template <int POT>
+__device__ __forceinline__ void pot_eval(const PairParam& p, float rr, float& fval, float& en)
+{
+    if (POT == POT_MIE) {
+        const float rri = __fdiv_rn(p.sigma2, rr);
+        const uint32_t m2 = (uint32_t)p.q2, n2 = (uint32_t)p.q3;
+        const float rni = ipowf(rri, n2);
+        const float rmni = (m2 - n2 == n2) ? rni : ipowf(rri, m2 - n2);
+        const float eps_rni = p.q0 * rni;
+        fval = p.q1 * rri * eps_rni * (p.q2 * rmni - p.q3);
+        en = eps_rni * (rmni - 1.0f);
+    } else if (POT == POT_MORSE) {
+        const float r_sigma_B = sqrtf(rr) * p.q2;
+        const float dr = p.q3 - r_sigma_B;
+        const float e = expf(dr);
+        const float eA = (p.q1 == 1.0f) ? e : expf(p.q1 * dr);
+        const float eps_e = p.q0 * e;
+        fval = __fdiv_rn((p.q1 + 1.0f) * eps_e * (eA - 1.0f) * r_sigma_B, rr);
+        en = eps_e * (eA - p.q1 - 1.0f);
+    } else {
+        const float rri = __fdiv_rn(p.sigma2, rr);
+        float rni = ipowf(rri, (uint32_t)p.q2);
+        if (p.q3 != 0.0f) rni *= sqrtf(rri);
+        const float eps_rni = p.q0 * rni;
+        fval = __fdiv_rn(p.q1 * eps_rni, rr);
+        en = eps_rni;
+    }
+}
+
+// truncations/{sharp,shifted,smooth_r4,force_shifted}_kernel.cuh on a bare
+// (fval, en); en_cut = 0 for sharp.  rrl: the rounding residual of rr.  The
+// smooth_r4 factors vary on the scale h near r_c, so r - r_c is formed from
+// the correctly rounded root plus the residual's first-order term (r and r_c
+// are within a factor two there: the difference is exact)
+__device__ __forceinline__ void truncate_any(const PairParam& p, uint32_t trunc, float rr, float rrl, float rri_smooth,
+                                             float& fval, float& en)
+{
+    en -= p.en_cut;
+    if (trunc == TRUNC_SMOOTH_R4) {
+        const float r = sqrtf(rr);
+        const float rinv = __fdiv_rn(1.0f, r);
+        const float dr = __fmaf_rn(0.5f * rrl, rinv, __fsub_rn(r, p.r_cut));
+        const float x2 = dr * dr * rri_smooth;
+        const float x4 = x2 * x2;
+        const float x4i = __fdiv_rn(1.0f, 1.0f + x4);
+        const float h0 = x4 * x4i;
+        const float h1 = 4.0f * dr * rri_smooth * x2 * x4i * x4i;
+        fval = h0 * fval - h1 * (en * rinv);
+        en = h0 * en;
+    } else if (trunc == TRUNC_FORCE_SHIFTED) {
+        const float rinv = rsqrtf(rr);
+        fval = fval - p.f_cut * rinv;
+        en = en + (rr * rinv - p.r_cut) * p.f_cut;
+    }
+}
+
+template <int POT, bool AUX, bool WRAP, bool NEAR>
+__device__ __forceinline__ void pot_pair2(const PairParam& pa, const PairParam& pb, const SysParam& P, float4 ri,
+                                          float4 ra, float4 rb, bool va, bool vb, ForceAcc2& A)
+{
+    const float2 sx = f2(__fsub_rn(ri.x, ra.x), __fsub_rn(ri.x, rb.x));
+    const float2 sy = f2(__fsub_rn(ri.y, ra.y), __fsub_rn(ri.y, rb.y));
+    const float2 sz = f2(__fsub_rn(ri.z, ra.z), __fsub_rn(ri.z, rb.z));
+    float2 dx = WRAP ? min_image2(sx, P.L[0], P.Linv[0]) : sx;
+    float2 dy = WRAP ? min_image2(sy, P.L[1], P.Linv[1]) : sy;
+    float2 dz = WRAP ? min_image2(sz, P.L[2], P.Linv[2]) : sz;
+    float2 rr = rr_exact2(dx, dy, dz);
+    const bool ka = va && rr.x < pa.rr_cut;
+    const bool kb = vb && rr.y < pb.rr_cut;
+    const bool smooth = P.trunc == TRUNC_SMOOTH_R4;   // block-uniform
+    float2 rrl = bc2(0.0f);
+    if (WRAP || NEAR || smooth) {
+        // the separation's rounding error back in (the cut-off decision above
+        // keeps the rounded squared distance of the list criterion)
+        dx = add2(dx, diff_err2(ri.x, ra.x, rb.x, sx));
+        dy = add2(dy, diff_err2(ri.y, ra.y, rb.y, sy));
+        dz = add2(dz, diff_err2(ri.z, ra.z, rb.z, sz));
+        const float2 px = mul2(dx, dx), py = mul2(dy, dy), pz = mul2(dz, dz);
+        const float2 pxy = add2(px, py);
+        rr = add2(pxy, pz);
+        if (smooth) {
+            rrl = add2(add2(fma2(dx, dx, neg2(px)), fma2(dy, dy, neg2(py))), fma2(dz, dz, neg2(pz)));
+            rrl = add2(rrl, add2(two_sum_err2(px, py, pxy), two_sum_err2(pxy, pz, rr)));
+        }
+    }
+    float fa, ea, fb, eb;
+    pot_eval<POT>(pa, rr.x, fa, ea);
+    pot_eval<POT>(pb, rr.y, fb, eb);
+    truncate_any(pa, P.trunc, rr.x, rrl.x, P.rri_smooth, fa, ea);
+    truncate_any(pb, P.trunc, rr.y, rrl.y, P.rri_smooth, fb, eb);
+    const float2 fval = sel2(ka, kb, f2(fa, fb));
+    if (NEAR) {
+        const float2 tx = mul2(fval, dx), ty = mul2(fval, dy), tz = mul2(fval, dz);
+        two_sum_acc2(A.fx, A.cx, tx);
+        two_sum_acc2(A.fy, A.cy, ty);
+        two_sum_acc2(A.fz, A.cz, tz);
+        A.cx = add2(A.cx, fma2(fval, dx, neg2(tx)));
+        A.cy = add2(A.cy, fma2(fval, dy, neg2(ty)));
+        A.cz = add2(A.cz, fma2(fval, dz, neg2(tz)));
+    } else {
+        A.gx = fma2(fval, dx, A.gx);
+        A.gy = fma2(fval, dy, A.gy);
+        A.gz = fma2(fval, dz, A.gz);
+    }
+    aux_acc2<AUX>(A, fval, sel2(ka, kb, f2(ea, eb)), dx, dy, dz);
+}
+
+// force_blocks2 for the other potentials; an odd E pairs the last entry of
+// a load with a masked copy of the particle itself
+template <int W, int E, int POT, bool AUX, bool WRAP, bool FAR>
+__device__ __forceinline__ void force_blocks_pot(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt,
+                                                 const SysParam& P, const PairParam* spp, float4 ri, uint32_t a,
+                                                 ForceAcc2& A)
+{
+    constexpr uint32_t LB = W * E;
+    using V = typename IdxVec<E>::T;
+    const size_t bstride = (size_t)d.S;
+    const V* lst = reinterpret_cast<const V*>(d.nbr + (size_t)i * LB + q * E);
+    if (FAR) lst += (size_t)(d.nbr_cap / LB - 1) * bstride * W;
+    const ptrdiff_t step = FAR ? -(ptrdiff_t)(bstride * W) : (ptrdiff_t)(bstride * W);
+    const uint32_t ns = P.ns;
+    const PairParam* row = spp + a * ns;
+    const uint32_t nblk = (cnt + LB - 1) / LB;
+    for (uint32_t b = 0; b < nblk; ++b, lst += step) {
+        const V jv = __ldg(lst);
+        float4 rj[E];
+        bool in[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t o = q * E + e;
+            const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
+            in[e] = k < cnt;
+            rj[e] = __ldg(d.pos + (in[e] ? idx_at(jv, e) : i));
+        }
+#pragma unroll
+        for (int e = 0; e < E; e += 2) {
+            const bool two = e + 1 < E;
+            const float4 ra = rj[e], rb = two ? rj[e + 1 < E ? e + 1 : e] : ri;
+            const uint32_t ba = species_bits(ra.w), bb = species_bits(rb.w);
+            const bool va = in[e] && ba < ns;
+            const bool vb = two && in[e + 1 < E ? e + 1 : e] && bb < ns;
+            const PairParam& pa = row[ba < ns ? ba : 0u];
+            const PairParam& pb = row[vb ? bb : 0u];
+            pot_pair2<POT, AUX, WRAP, !FAR>(pa, pb, P, ri, ra, rb, va, vb, A);
+        }
+    }
+}
+
+template <int W, int E, int POT, bool AUX>
+__device__ __forceinline__ void force_dispatch_pot(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf,
+                                                   bool wrap, const SysParam& P, const PairParam* spp, float4 ri,
+                                                   uint32_t a, ForceAcc& A)
+{
+    ForceAcc2 B;
+    if (wrap) {
+        force_blocks_pot<W, E, POT, AUX, true, false>(d, i, q, nn, P, spp, ri, a, B);
+        force_blocks_pot<W, E, POT, AUX, true, true>(d, i, q, nf, P, spp, ri, a, B);
+    } else {
+        force_blocks_pot<W, E, POT, AUX, false, false>(d, i, q, nn, P, spp, ri, a, B);
+        force_blocks_pot<W, E, POT, AUX, false, true>(d, i, q, nf, P, spp, ri, a, B);
+    }
+    fold_lanes2<AUX>(B, A);
+    two_sum_acc(A.fx, A.cx, A.gx);
+    two_sum_acc(A.fy, A.cy, A.gy);
+    two_sum_acc(A.fz, A.cz, A.gz);
+}
+
 // merge the compensated sums of the W lanes of a particle (fixed tree: deterministic)
 template <int W>
 __device__ __forceinline__ void lane_merge(float& s, float& c)
@@ -687,8 +874,20 @@ __device__ __forceinline__ float lane_sum(float v)
 // kind of pair interaction of a system (FK_*), the template selector of k_force
 __device__ __forceinline__ int force_kind_of(const SysParam& P)
 {
+    if (P.pot != POT_LJ) return FK_POT;
     if (P.trunc == TRUNC_SHARP || P.trunc == TRUNC_SHIFTED) return P.ns == 1 ? FK_LJ1 : FK_SHIFTED;
     return P.trunc == TRUNC_SMOOTH_R4 ? FK_SMOOTH : FK_FSHIFT;
+}
+
+template <int W, int E, bool AUX>
+__device__ __forceinline__ void force_pot(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf, bool wrap,
+                                          const SysParam& P, const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
+{
+    switch (P.pot) {
+    case POT_MIE: force_dispatch_pot<W, E, POT_MIE, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
+    case POT_MORSE: force_dispatch_pot<W, E, POT_MORSE, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
+    default: force_dispatch_pot<W, E, POT_POWER_LAW, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
+    }
 }
 
 template <int W, int E, int KIND, bool AUX>
@@ -724,11 +923,14 @@ __global__ void __launch_bounds__(128, HMD_FORCE_MINB) k_force(Dev d)
             force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
         } else if constexpr (KIND == FK_FSHIFT) {
             force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+        } else if constexpr (KIND == FK_POT) {
+            force_pot<W, E, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
         } else {
             switch (force_kind_of(P)) {
             case FK_LJ1: force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
             case FK_SHIFTED: force_dispatch<W, E, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
             case FK_SMOOTH: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
+            case FK_POT: force_pot<W, E, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
             default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
             }
         }

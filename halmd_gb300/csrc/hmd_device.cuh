@@ -34,6 +34,7 @@ constexpr int CHUNK = 64;         // granularity of the slot -> system map
 __host__ __device__ constexpr uint32_t list_block(uint32_t w) { return w < 4u ? 4u : w; }
 
 enum Trunc : uint32_t { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3 };
+enum Pot : uint32_t { POT_LJ = 0, POT_MIE = 1, POT_MORSE = 2, POT_POWER_LAW = 3 };
 // INTEG_DESCENT: steepest-descent energy minimisation (positions only)
 enum Integrator : uint32_t { INTEG_VERLET = 0, INTEG_ANDERSEN = 1, INTEG_DESCENT = 2 };
 enum Status : uint32_t {
@@ -54,6 +55,11 @@ struct PairParam {
     float rr_near;     // (float)((NEAR_SIGMA sigma)^2): list pairs closer at build time get the compensated path
     float sigma2_lo;   // sigma^2 - sigma2 (the rounding error of the float parameter)
     float c48_lo;      // 48 eps / sigma^2 - c48
+    // parameters of the other potentials (SysParam::pot):
+    //   mie:       q0 = eps C(m, n), q1 = 2 / sigma^2, q2 = m/2, q3 = n/2 (integers as float)
+    //   morse:     q0 = eps / A, q1 = A = 2 B^2 - 1, q2 = 1 / (sigma B), q3 = r_min / (sigma B)
+    //   power_law: q0 = eps, q1 = n, q2 = n/2 (integer as float), q3 = 1 for odd n else 0
+    float q0, q1, q2, q3;
     float pad;
 };
 
@@ -88,6 +94,7 @@ struct SysParam {
     float exact_min;           // |coordinate| from which near-pair differences are exact (k_force)
     float descent_step;        // INTEG_DESCENT: move = descent_step * F ...
     float descent_max;         // ... capped at this length per particle and step
+    uint32_t pot;              // pair potential (Pot)
 };
 
 // mutable per-system device state

@@ -11,8 +11,9 @@ struct Dev;
 // kinds of pair interaction, one pair-force kernel each (force.cuh):
 // FK_LJ1 one species with a sharp or shifted truncation, FK_SHIFTED several
 // species with a sharp or shifted truncation, FK_SMOOTH smooth_r4, FK_FSHIFT
-// force_shifted; FK_GENERIC handles every kind in one kernel
-enum ForceKind : int { FK_GENERIC = 0, FK_LJ1 = 1, FK_SHIFTED = 2, FK_SMOOTH = 3, FK_FSHIFT = 4 };
+// force_shifted, FK_POT the other pair potentials (mie, morse, power_law) with
+// any truncation; FK_GENERIC handles every kind in one kernel
+enum ForceKind : int { FK_GENERIC = 0, FK_LJ1 = 1, FK_SHIFTED = 2, FK_SMOOTH = 3, FK_FSHIFT = 4, FK_POT = 5 };
 template <int KIND> void launch_force_kind(const Dev& d, bool aux, cudaStream_t st);
 
 // step (kernels_step.cu)

@@ -384,6 +384,7 @@ void launch_force(const Dev& d, bool aux, cudaStream_t st)
     if (d.force_kinds & (1u << FK_SHIFTED)) launch_force_kind<FK_SHIFTED>(d, aux, st);
     if (d.force_kinds & (1u << FK_SMOOTH)) launch_force_kind<FK_SMOOTH>(d, aux, st);
     if (d.force_kinds & (1u << FK_FSHIFT)) launch_force_kind<FK_FSHIFT>(d, aux, st);
+    if (d.force_kinds & (1u << FK_POT)) launch_force_kind<FK_POT>(d, aux, st);
 }
 
 void launch_finalize(const Dev& d, bool ds, cudaStream_t st)

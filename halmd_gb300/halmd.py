@@ -179,7 +179,7 @@ class particle:
         pot, nb, integ = self._potential, self._neighbour or {}, self._integrator
         kw = dict(epsilon=pot.epsilon, sigma=pot.sigma, r_cut=pot.cutoff, truncation=pot.kind,
                   skin=nb.get("skin", 0.5), timestep=integ.timestep, integrator=integ.kind,
-                  sort=not nb.get("disable_sorting", False))
+                  sort=not nb.get("disable_sorting", False), potential=pot.potential, **pot.params)
         if pot.kind == "smooth_r4":
             kw["smoothing"] = pot.h
         if nb.get("occupancy") is not None:
@@ -190,8 +190,9 @@ class particle:
 
 
 class _Potential:
-    def __init__(self, epsilon, sigma, species):
+    def __init__(self, epsilon, sigma, species, potential="lennard_jones", params=None):
         self.epsilon, self.sigma, self.species = epsilon, sigma, species
+        self.potential, self.params = potential, dict(params or {})
         self.kind, self.cutoff, self.h = None, None, None
 
     def truncate(self, args=None, **kw):
@@ -204,7 +205,7 @@ class _Potential:
         kind = a.get(1, a.get("kind", "shifted"))
         if kind not in ("sharp", "shifted", "smooth_r4", "force_shifted"):
             raise ValueError("invalid truncation type '%s'" % kind)
-        out = _Potential(self.epsilon, self.sigma, self.species)
+        out = _Potential(self.epsilon, self.sigma, self.species, self.potential, self.params)
         out.kind, out.cutoff = kind, a["cutoff"]
         if kind == "smooth_r4":
             if "h" not in a:
@@ -224,6 +225,44 @@ def lennard_jones(args=None, **kw):
     sig = np.atleast_2d(np.asarray(a.get("sigma", 1.0), dtype=float))
     species = int(a.get("species", max(eps.shape[0], sig.shape[0])))
     return _Potential(eps, sig, species)
+
+
+def _species(a, *mats):
+    return int(a.get("species", max(np.atleast_2d(np.asarray(m)).shape[0] for m in mats)))
+
+
+def mie(args=None, **kw):
+    """halmd.mdsim.potentials.pair.mie{epsilon = 1, sigma = 1, index_repulsion, index_attraction, species}
+    (mie.lua.in:66-72; both indices even, repulsion > attraction)."""
+    a = _args(args, kw)
+    for k in ("index_repulsion", "index_attraction"):
+        if k not in a:
+            raise ValueError("missing keyword argument '%s'" % k)
+    eps = np.atleast_2d(np.asarray(a.get("epsilon", 1.0), dtype=float))
+    sig = np.atleast_2d(np.asarray(a.get("sigma", 1.0), dtype=float))
+    params = dict(index_repulsion=a["index_repulsion"], index_attraction=a["index_attraction"])
+    return _Potential(eps, sig, _species(a, eps, sig), "mie", params)
+
+
+def morse(args=None, **kw):
+    """halmd.mdsim.potentials.pair.morse{epsilon = 1, sigma = 1, r_min (or minimum), distortion = 1, species}
+    (morse.lua.in:75-81, 168-185)."""
+    a = _args(args, kw)
+    r_min = a.get("r_min", a.get("minimum"))
+    if r_min is None:
+        raise ValueError("missing keyword argument 'r_min'")
+    eps = np.atleast_2d(np.asarray(a.get("epsilon", 1.0), dtype=float))
+    sig = np.atleast_2d(np.asarray(a.get("sigma", 1.0), dtype=float))
+    params = dict(r_min=r_min, distortion=a.get("distortion", 1.0))
+    return _Potential(eps, sig, _species(a, eps, sig), "morse", params)
+
+
+def power_law(args=None, **kw):
+    """halmd.mdsim.potentials.pair.power_law{epsilon = 1, sigma = 1, index = 12, species} (power_law.lua.in:56-61)."""
+    a = _args(args, kw)
+    eps = np.atleast_2d(np.asarray(a.get("epsilon", 1.0), dtype=float))
+    sig = np.atleast_2d(np.asarray(a.get("sigma", 1.0), dtype=float))
+    return _Potential(eps, sig, _species(a, eps, sig), "power_law", dict(index=a.get("index", 12)))
 
 
 def neighbour(args=None, **kw):
@@ -272,7 +311,7 @@ def verlet_nvt_andersen(args=None, **kw):
 
 mdsim = _Namespace(
     box=box, particle=particle, neighbour=neighbour,
-    potentials=_Namespace(pair=_Namespace(lennard_jones=lennard_jones)),
+    potentials=_Namespace(pair=_Namespace(lennard_jones=lennard_jones, mie=mie, morse=morse, power_law=power_law)),
     forces=_Namespace(pair=pair),
     integrators=_Namespace(verlet=verlet, verlet_nvt_andersen=verlet_nvt_andersen),
 )

@@ -45,6 +45,12 @@ extern "C" {
 #define HMD_TRUNC_SMOOTH_R4 2      /* truncations/smooth_r4.hpp */
 #define HMD_TRUNC_FORCE_SHIFTED 3  /* truncations/force_shifted.hpp */
 
+/* pair potentials (mdsim/gpu/potentials/pair/*.cpp; every truncation applies to each) */
+#define HMD_POTENTIAL_LENNARD_JONES 0  /* lennard_jones.cpp (default) */
+#define HMD_POTENTIAL_MIE 1            /* mie.cpp: epsilon, sigma, index_repulsion m, index_attraction n */
+#define HMD_POTENTIAL_MORSE 2          /* morse.cpp: epsilon, sigma, r_min, distortion B */
+#define HMD_POTENTIAL_POWER_LAW 3      /* power_law.cpp: epsilon, sigma, index n */
+
 #define HMD_INTEGRATOR_VERLET 0    /* integrators/verlet.cpp */
 #define HMD_INTEGRATOR_ANDERSEN 1  /* integrators/verlet_nvt_andersen.cpp */
 
@@ -59,6 +65,10 @@ typedef struct hmd_dynamics hmd_dynamics;
  * particle(nparticle, nspecies)            lua/halmd/mdsim/particle.lua.in:229-290
  * box(edges)                               mdsim/box.cpp:40-60
  * lennard_jones(epsilon, sigma)            mdsim/gpu/potentials/pair/lennard_jones.cpp:45-71
+ * mie(epsilon, sigma, index_repulsion, index_attraction)
+ *                                          mdsim/gpu/potentials/pair/mie.cpp, lua/.../pair/mie.lua.in:66-72
+ * morse(epsilon, sigma, r_min, distortion) mdsim/gpu/potentials/pair/morse.cpp, lua/.../pair/morse.lua.in:75-81
+ * power_law(epsilon, sigma, index)         mdsim/gpu/potentials/pair/power_law.cpp, lua/.../pair/power_law.lua.in:56-61
  *   :truncate{kind, cutoff, h}             lua/halmd/mdsim/potentials/pair/adapters/truncate.lua.in:287-305
  * neighbour{skin, occupancy, sort}         lua/halmd/mdsim/neighbour.lua.in:151-306, from_binning.cpp:96-119
  * binning{occupancy}                       mdsim/gpu/binning.cpp:47-116
@@ -84,6 +94,12 @@ typedef struct hmd_system_desc {
     double collision_rate;       /* Andersen collision rate nu */
     uint64_t seed;               /* Andersen random stream */
     int32_t sort;                /* 1: Hilbert reorder at every list rebuild (default) */
+    int32_t potential;           /* HMD_POTENTIAL_* (default lennard_jones) */
+    uint32_t index_repulsion[HMD_MAX_SPECIES * HMD_MAX_SPECIES];   /* mie m: even, > n (default 12) */
+    uint32_t index_attraction[HMD_MAX_SPECIES * HMD_MAX_SPECIES];  /* mie n: even, >= 2 (default 6) */
+    uint32_t index[HMD_MAX_SPECIES * HMD_MAX_SPECIES];             /* power_law n >= 1 (default 12) */
+    double r_min[HMD_MAX_SPECIES * HMD_MAX_SPECIES];      /* morse: position of the minimum (required) */
+    double distortion[HMD_MAX_SPECIES * HMD_MAX_SPECIES]; /* morse: B > 0 (default 1) */
 } hmd_system_desc;
 
 /* per-system state readable after any call (hmd_info) */

@@ -38,6 +38,7 @@ def lib():
         D = ctypes.c_double
         L.orc_pot_sizeof.restype = ctypes.c_size_t
         L.orc_pot_init.argtypes = [P, I, P, P, P, I, D]
+        L.orc_pot_init_any.argtypes = [P, I, I, P, P, P, I, D, P, P, P, P]
         L.orc_pot_eval.argtypes = [P, D, I, I, P, P]
         L.orc_accumulate.argtypes = [I, P, P]
         L.orc_binning_sizing.argtypes = [I, P, D, D, D, P]
@@ -75,10 +76,18 @@ def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
 
 
-class Potential:
-    """Lennard-Jones with a truncation, FP64 (host potential restatement)."""
+POTENTIAL = {"lennard_jones": 0, "mie": 1, "morse": 2, "power_law": 3}
 
-    def __init__(self, epsilon, sigma, r_cut, truncation="shifted", h=0.005):
+
+class Potential:
+    """A pair potential with a truncation, FP64 (host potential restatement).
+
+    potential: lennard_jones (epsilon, sigma), mie (+ index_repulsion,
+    index_attraction), morse (+ r_min, distortion), power_law (+ index).
+    """
+
+    def __init__(self, epsilon, sigma, r_cut, truncation="shifted", h=0.005, potential="lennard_jones",
+                 index_repulsion=None, index_attraction=None, index=None, r_min=None, distortion=None):
         self.eps = np.ascontiguousarray(epsilon, dtype=np.float64)
         self.ns = int(round(np.sqrt(self.eps.size)))
         self.sigma = np.ascontiguousarray(sigma, dtype=np.float64).reshape(self.ns, self.ns)
@@ -87,10 +96,23 @@ class Potential:
             rc = np.full((self.ns, self.ns), float(rc))
         self.r_cut_sigma = np.ascontiguousarray(rc.reshape(self.ns, self.ns))
         self.truncation = truncation
+        self.potential = potential
         self.h = h
+
+        def mat(v, dtype, default):
+            a = np.asarray(default if v is None else v, dtype=dtype)
+            if a.size == 1:
+                a = np.full((self.ns, self.ns), a.reshape(()))
+            return np.ascontiguousarray(a.reshape(self.ns, self.ns), dtype=dtype)
+
+        idx_m = mat(index if potential == "power_law" else index_repulsion, np.uint32, 12)
+        idx_n = mat(index_attraction, np.uint32, 6)
+        self.r_min = mat(r_min, np.float64, 1.0)
+        self.distortion = mat(distortion, np.float64, 1.0)
         self._buf = np.zeros(lib().orc_pot_sizeof(), dtype=np.uint8)
-        rc_ = lib().orc_pot_init(_p(self._buf), self.ns, _p(self.eps), _p(self.sigma), _p(self.r_cut_sigma),
-                                 TRUNC[truncation], float(h))
+        rc_ = lib().orc_pot_init_any(_p(self._buf), POTENTIAL[potential], self.ns, _p(self.eps), _p(self.sigma),
+                                     _p(self.r_cut_sigma), TRUNC[truncation], float(h), _p(idx_m), _p(idx_n),
+                                     _p(self.r_min), _p(self.distortion))
         if rc_ != 0:
             raise ValueError("bad potential parameters")
 

@@ -69,9 +69,12 @@ static const u32 PLACEHOLDER = 0xFFFFFFFFu;
 enum { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3 };
 enum { ORC_MAX_SPECIES = 8 };
 
+enum { POT_LJ = 0, POT_MIE = 1, POT_MORSE = 2, POT_POWER_LAW = 3 };
+
 struct orc_pot {
     int ns;
     int trunc;
+    int pot;
     double h;
     double rri_smooth;
     double eps[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
@@ -80,6 +83,13 @@ struct orc_pot {
     double rrcut[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
     double encut[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
     double fcut[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
+    /* mie: m, n and eps C(m, n); power_law: index; morse: r_min / sigma, B */
+    unsigned idx_m[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
+    unsigned idx_n[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
+    double eps_C[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
+    double sigma[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
+    double rmin_sigma[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
+    double distortion[ORC_MAX_SPECIES * ORC_MAX_SPECIES];
 };
 
 ORC_API size_t orc_pot_sizeof(void) { return sizeof(orc_pot); }
@@ -95,24 +105,99 @@ static inline void lj_bare(const orc_pot* p, double rr, int ab, double* fval, do
     *en = 4 * eps_r6i * (r6i - 1);
 }
 
-/* rcut_sigma: cutoff in units of sigma (as the reference's `cutoff` matrix) */
-ORC_API int orc_pot_init(orc_pot* p, int ns, const double* eps, const double* sigma,
-                         const double* rcut_sigma, int trunc, double h)
+/* integer power (numeric/pow.hpp) */
+static inline double ipow_d(double x, unsigned n)
+{
+    double y = 1;
+    for (; n; n >>= 1, x *= x)
+        if (n & 1) y *= x;
+    return y;
+}
+
+/* mdsim/host/potentials/pair/mie.hpp:63-73 (prefactor mie.cpp:85-92) */
+static inline void mie_bare(const orc_pot* p, double rr, int ab, double* fval, double* en)
+{
+    const double sigma2 = p->sigma2[ab];
+    const unsigned m_2 = p->idx_m[ab] / 2, n_2 = p->idx_n[ab] / 2;
+    const double rri = sigma2 / rr;
+    const double rni = ipow_d(rri, n_2);
+    const double rmni = (m_2 - n_2 == n_2) ? rni : ipow_d(rri, m_2 - n_2);
+    const double eps_rni = p->eps_C[ab] * rni;
+    *fval = 2 * rri * eps_rni * (m_2 * rmni - n_2) / sigma2;
+    *en = eps_rni * (rmni - 1);
+}
+
+/* mdsim/host/potentials/pair/morse.hpp:64-77 */
+static inline void morse_bare(const orc_pot* p, double rr, int ab, double* fval, double* en)
+{
+    const double B = p->distortion[ab];
+    const double r_sigma_B = std::sqrt(rr) / p->sigma[ab] / B;
+    const double dr = p->rmin_sigma[ab] / B - r_sigma_B;
+    const double exp_dr = std::exp(dr);
+    const double A = 2 * B * B - 1;
+    const double exp_A_dr = (A == 1) ? exp_dr : std::exp(A * dr);
+    const double eps_exp_dr = p->eps[ab] * exp_dr / A;
+    *fval = (A + 1) * eps_exp_dr * (exp_A_dr - 1) * r_sigma_B / rr;
+    *en = eps_exp_dr * (exp_A_dr - A - 1);
+}
+
+/* mdsim/host/potentials/pair/power_law.hpp:129-148 */
+static inline void power_law_bare(const orc_pot* p, double rr, int ab, double* fval, double* en)
+{
+    const unsigned n = p->idx_m[ab];
+    const double rri = p->sigma2[ab] / rr;
+    double rni = ipow_d(rri, n / 2);
+    if (n % 2) rni *= std::sqrt(rri);
+    const double eps_rni = p->eps[ab] * rni;
+    *fval = n * eps_rni / rr;
+    *en = eps_rni;
+}
+
+static inline void pot_bare(const orc_pot* p, double rr, int ab, double* fval, double* en)
+{
+    switch (p->pot) {
+    case POT_MIE: mie_bare(p, rr, ab, fval, en); break;
+    case POT_MORSE: morse_bare(p, rr, ab, fval, en); break;
+    case POT_POWER_LAW: power_law_bare(p, rr, ab, fval, en); break;
+    default: lj_bare(p, rr, ab, fval, en); break;
+    }
+}
+
+/* any potential: idx_m = mie m or power_law index, idx_n = mie n; r_min and
+ * distortion for morse (r_min in absolute units); null where unused */
+ORC_API int orc_pot_init_any(orc_pot* p, int pot, int ns, const double* eps, const double* sigma,
+                             const double* rcut_sigma, int trunc, double h, const unsigned* idx_m,
+                             const unsigned* idx_n, const double* r_min, const double* distortion)
 {
     if (ns < 1 || ns > ORC_MAX_SPECIES) return -1;
-    if (trunc < 0 || trunc > 3) return -1;
+    if (trunc < 0 || trunc > 3 || pot < 0 || pot > 3) return -1;
     std::memset(p, 0, sizeof(*p));
     p->ns = ns;
     p->trunc = trunc;
+    p->pot = pot;
     p->h = h;
     p->rri_smooth = (trunc == TRUNC_SMOOTH_R4) ? std::pow(h, -2) : 0;
     for (int ab = 0; ab < ns * ns; ++ab) {
         p->eps[ab] = eps[ab];
+        p->sigma[ab] = sigma[ab];
         p->sigma2[ab] = sigma[ab] * sigma[ab];
         p->rcut[ab] = sigma[ab] * rcut_sigma[ab];
         p->rrcut[ab] = p->rcut[ab] * p->rcut[ab];
+        if (pot == POT_MIE) {
+            const unsigned m = idx_m[ab], n = idx_n[ab];
+            if ((m & 1) || (n & 1) || m <= n || n == 0) return -2;   /* mie.cpp:72-83 */
+            p->idx_m[ab] = m;
+            p->idx_n[ab] = n;
+            const double md = m, nd = n;
+            p->eps_C[ab] = eps[ab] * (md / (md - nd) * std::pow(md / nd, nd / (md - nd)));
+        } else if (pot == POT_POWER_LAW) {
+            p->idx_m[ab] = idx_m[ab];
+        } else if (pot == POT_MORSE) {
+            p->rmin_sigma[ab] = r_min[ab] / sigma[ab];
+            p->distortion[ab] = distortion[ab];
+        }
         double f, e;
-        lj_bare(p, p->rrcut[ab], ab, &f, &e);
+        pot_bare(p, p->rrcut[ab], ab, &f, &e);
         p->encut[ab] = (trunc == TRUNC_SHARP) ? 0 : e;
         /* force_shifted.hpp:63-64 stores F_c = fval(rc) * rc */
         p->fcut[ab] = (trunc == TRUNC_FORCE_SHIFTED) ? f * p->rcut[ab] : 0;
@@ -120,12 +205,19 @@ ORC_API int orc_pot_init(orc_pot* p, int ns, const double* eps, const double* si
     return 0;
 }
 
+/* rcut_sigma: cutoff in units of sigma (as the reference's `cutoff` matrix) */
+ORC_API int orc_pot_init(orc_pot* p, int ns, const double* eps, const double* sigma,
+                         const double* rcut_sigma, int trunc, double h)
+{
+    return orc_pot_init_any(p, POT_LJ, ns, eps, sigma, rcut_sigma, trunc, h, nullptr, nullptr, nullptr, nullptr);
+}
+
 /* truncations/{sharp,shifted,smooth_r4,force_shifted}.hpp operator() */
 ORC_API void orc_pot_eval(const orc_pot* p, double rr, int a, int b, double* fval, double* en)
 {
     int ab = a * p->ns + b;
     double f, e;
-    lj_bare(p, rr, ab, &f, &e);
+    pot_bare(p, rr, ab, &f, &e);
     switch (p->trunc) {
     case TRUNC_SHARP:
         break;

@@ -11,6 +11,8 @@ Outputs (committed; small):
   lj_tables.json        (r, fval, U) rows of test/unit/mdsim/potentials/pair/lennard_jones.cpp:77-211
                         for sharp / shifted / force_shifted / smooth_r4, species AA/AB/BB
   smooth_r4_tables.json near-cutoff rows of test/unit/mdsim/forces/trunc/smooth_r4.cpp:59-149
+  other_potential_tables.json  (r, fval, U) rows and parameters of the host tests
+                        test/unit/mdsim/potentials/pair/{mie,morse,power_law}.cpp (shifted)
   accumulator.json      expected statistics of test/unit/numeric/accumulator.cpp:28-39
   hilbert_keys.json     keys of the reference's hilbert_kernel::map on seeded points
   dsfun.json            dsadd / dssub / dsmul of the reference's dsfun.hpp on seeded operands
@@ -55,6 +57,38 @@ def lj_tables(ref):
         "tolerance_eps_double": 5,
         "tables": out,
     }
+
+
+def _matrix(src, name, cast=float):
+    """The 2x2 matrix `name_array <<= a, b, c, d;` of a reference unit test."""
+    m = re.search(r"%s_array <<=\s*(.*?);" % name, src, re.S)
+    vals = [cast(float(x)) for x in re.findall(r"[-+0-9.eE]+", m.group(1))]
+    assert len(vals) == 4, (name, vals)
+    return [vals[0:2], vals[2:4]]
+
+
+def other_potential_tables(ref):
+    """(r, fval, U) rows of the host tests of mie, morse and power_law (shifted truncation)."""
+    out = {}
+    extra = {"mie": [("index_m", int), ("index_n", int)], "morse": [("r_min", float), ("distortion", float)],
+             "power_law": [("index", int)]}
+    for pot, fields in extra.items():
+        path = "test/unit/mdsim/potentials/pair/%s.cpp" % pot
+        src = open(os.path.join(ref, path)).read()
+        host = src[: src.find("#ifdef HALMD_WITH_GPU", src.find("BOOST_AUTO_TEST_CASE"))]
+        entry = {"source": path, "truncation": "shifted",
+                 "r_cut_sigma": _matrix(host, "cutoff"), "epsilon": _matrix(host, "epsilon"),
+                 "sigma": _matrix(host, "sigma")}
+        for name, cast in fields:
+            entry[name] = _matrix(host, name, cast)
+        tables = {}
+        for pair in ("aa", "ab", "bb"):
+            mm = re.search(r"results_%s = \{\{(.*?)\}\};" % pair, host, re.S)
+            tables[pair] = parse_rows(mm.group(1))
+            assert len(tables[pair]) >= 5, (pot, pair)
+        entry["tables"] = tables
+        out[pot] = entry
+    return out
 
 
 def smooth_r4_tables(ref):
@@ -144,6 +178,7 @@ def main():
     fixtures = {
         "lj_tables.json": lj_tables(args.reference),
         "smooth_r4_tables.json": smooth_r4_tables(args.reference),
+        "other_potential_tables.json": other_potential_tables(args.reference),
         "accumulator.json": accumulator_expect(args.reference),
         "hilbert_keys.json": hilbert_keys(args.harness),
         "dsfun.json": dsfun_vectors(args.harness),

@@ -48,15 +48,23 @@ def test_null_handles_are_rejected(lib):
 
 
 def test_struct_layout_matches_header(lib):
-    # the ctypes mirrors must have the C sizes (catches drift between header and binding)
-    exe = os.path.join(_lib.REPO, "_build", "sizeof_check")
+    # the ctypes mirrors must have the C sizes and field offsets (catches drift
+    # between header and binding)
+    exe = os.path.join(_lib.REPO, "_build", "layout_check")
     os.makedirs(os.path.dirname(exe), exist_ok=True)
-    code =('#include "halmd_gb300.h"\n#include <stdio.h>\nint main(void){printf("%zu %zu\\n",'
-            'sizeof(hmd_system_desc), sizeof(hmd_system_info));return 0;}\n')
-    c_path = os.path.join(_lib.REPO, "_build", "sizeof_check.c")
+    lines = ['#include "halmd_gb300.h"', "#include <stdio.h>", "#include <stddef.h>", "int main(void){"]
+    for cname, cls in (("hmd_system_desc", _lib.SystemDesc), ("hmd_system_info", _lib.SystemInfo)):
+        lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
+        for field, _ in cls._fields_:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, field))
+    lines.append("return 0;}")
+    c_path = exe + ".c"
     with open(c_path, "w") as fh:
-        fh.write(code)
+        fh.write("\n".join(lines) + "\n")
     subprocess.run(["gcc", "-I", os.path.join(_lib.REPO, "include"), "-o", exe, c_path], check=True)
-    a, b = map(int, subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split())
-    assert a == ctypes.sizeof(_lib.SystemDesc)
-    assert b == ctypes.sizeof(_lib.SystemInfo)
+    got = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    want = []
+    for cls in (_lib.SystemDesc, _lib.SystemInfo):
+        want.append(ctypes.sizeof(cls))
+        want.extend(getattr(cls, f).offset for f, _ in cls._fields_)
+    assert got == want

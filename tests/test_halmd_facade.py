@@ -71,3 +71,31 @@ def test_argument_errors(halmd):
         halmd.mdsim.forces.pair(box=box, particle=p, potential=halmd.mdsim.potentials.pair.lennard_jones())
     with pytest.raises(RuntimeError):
         p._desc()                                                  # no force / integrator yet
+
+
+@pytest.mark.parametrize("name,kw,check", [
+    ("mie", dict(index_repulsion=[[12, 10], [10, 14]], index_attraction=6),
+     lambda d: [d.index_repulsion[k] for k in range(4)] == [12, 10, 10, 14] and d.index_attraction[3] == 6),
+    ("morse", dict(r_min=1.1, distortion=[[1, 1.41], [1.41, 1.5]]),
+     lambda d: d.r_min[0] == 1.1 and [d.distortion[k] for k in range(4)] == [1, 1.41, 1.41, 1.5]),
+    ("power_law", dict(index=[[12, 9], [9, 6]]), lambda d: [d.index[k] for k in range(4)] == [12, 9, 9, 6]),
+])
+def test_other_potentials_map_onto_the_description(halmd, name, kw, check):
+    box = halmd.mdsim.box(length=[10, 10, 10])
+    p = halmd.mdsim.particle(particles=500, species=2)
+    pot = getattr(halmd.mdsim.potentials.pair, name)(epsilon=[[1, 1.5], [1.5, 0.5]], **kw)
+    pot = pot.truncate({1: "force_shifted", "cutoff": 2.5})
+    halmd.mdsim.forces.pair(box=box, particle=p, potential=pot)
+    halmd.mdsim.integrators.verlet(box=box, particle=p, timestep=0.001)
+    d = p._desc()
+    assert d.potential == _lib.POTENTIAL[name] and d.truncation == _lib.TRUNCATION["force_shifted"]
+    assert check(d)
+
+
+def test_other_potentials_defaults_and_errors(halmd):
+    assert halmd.mdsim.potentials.pair.power_law().params["index"] == 12      # power_law.lua.in:140
+    assert halmd.mdsim.potentials.pair.morse(minimum=1.2).params["distortion"] == 1.0   # morse.lua.in:178-185
+    with pytest.raises(ValueError):
+        halmd.mdsim.potentials.pair.morse()                                  # r_min has no default
+    with pytest.raises(ValueError):
+        halmd.mdsim.potentials.pair.mie(index_repulsion=12)                  # both indices are required

@@ -27,6 +27,47 @@ def test_lj_tables(golden, trunc):
             assert abs(e - en) <= tol * abs(en) or (en == 0 and abs(e) < 1e-12), (trunc, pair, r, e, en)
 
 
+# tolerances of the reference's host tests, in units of double epsilon:
+# mie.cpp:126 (6), morse.cpp:142-184 (fval 2x: 4 / 5 / 8; U: 2 / 2.5 / 4),
+# power_law.cpp:132-172 (1 + n/2)
+def _other_tolerance(pot, pair, g, quantity):
+    if pot == "mie":
+        return 6
+    if pot == "morse":
+        k = {"aa": 2, "ab": 2.5, "bb": 4}[pair]
+        return 2 * k if quantity == "fval" else k
+    a, b = {"aa": (0, 0), "ab": (0, 1), "bb": (1, 1)}[pair]
+    return 1 + g["index"][a][b] // 2
+
+
+@pytest.mark.parametrize("pot", ["mie", "morse", "power_law"])
+def test_other_potential_tables(golden, pot):
+    g = golden("other_potential_tables.json")[pot]
+    kw = {}
+    if pot == "mie":
+        kw = dict(index_repulsion=g["index_m"], index_attraction=g["index_n"])
+    elif pot == "morse":
+        kw = dict(r_min=g["r_min"], distortion=g["distortion"])
+    else:
+        kw = dict(index=g["index"])
+    P = oracle.Potential(g["epsilon"], g["sigma"], g["r_cut_sigma"], g["truncation"], potential=pot, **kw)
+    for pair, (a, b) in {"aa": (0, 0), "ab": (0, 1), "bb": (1, 1)}.items():
+        for r, fval, en in g["tables"][pair]:
+            f, e = P(r * r, a, b)
+            tf = _other_tolerance(pot, pair, g, "fval") * EPS64
+            te = _other_tolerance(pot, pair, g, "en") * EPS64
+            # BOOST_CHECK_CLOSE_FRACTION; exact zeros of the tables compare absolutely
+            assert abs(f - fval) <= tf * abs(fval) or (fval == 0 and abs(f) < 1e-14), (pot, pair, r, f, fval)
+            assert abs(e - en) <= te * abs(en) or (en == 0 and abs(e) < 1e-14), (pot, pair, r, e, en)
+
+
+def test_mie_rejects_bad_indices():
+    # mdsim/host/potentials/pair/mie.cpp:72-83: odd indices, m <= n
+    for m, n in ((13, 6), (12, 7), (6, 6), (4, 6)):
+        with pytest.raises(ValueError):
+            oracle.Potential(1.0, 1.0, 2.5, potential="mie", index_repulsion=m, index_attraction=n)
+
+
 def test_smooth_r4_near_cutoff(golden):
     g = golden("smooth_r4_tables.json")
     pot = oracle.Potential(g["epsilon"], g["sigma"], g["r_cut_sigma"], "smooth_r4", h=g["h"])
