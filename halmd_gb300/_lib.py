@@ -17,7 +17,8 @@ HEADER = os.path.join(REPO, "include", "halmd_gb300.h")
 HMD_OK = 0
 PRECISION = {"float": 0, "single": 0, "dsfloat": 1, "double-single": 1}
 TRUNCATION = {"sharp": 0, "shifted": 1, "smooth_r4": 2, "force_shifted": 3}
-INTEGRATOR = {"verlet": 0, "verlet_nvt_andersen": 1, "andersen": 1}
+INTEGRATOR = {"verlet": 0, "verlet_nvt_andersen": 1, "andersen": 1, "verlet_nvt_hoover": 2, "hoover": 2,
+              "verlet_nvt_boltzmann": 3, "boltzmann": 3, "euler": 4}
 POTENTIAL = {"lennard_jones": 0, "mie": 1, "morse": 2, "power_law": 3}
 MAX_SPECIES = 4
 NTHERMO = 14
@@ -57,6 +58,7 @@ class SystemDesc(ctypes.Structure):
         ("index", ctypes.c_uint32 * 16),
         ("r_min", ctypes.c_double * 16),
         ("distortion", ctypes.c_double * 16),
+        ("resonance_frequency", ctypes.c_double),
     ]
 
 
@@ -131,6 +133,7 @@ def load():
         "hmd_minimize": (I, [P, U, U, D, D]),
         "hmd_max_displacement": (I, [P, U, P]),
         "hmd_thermo": (I, [P, U, P]),
+        "hmd_integrator_state": (I, [P, U, P]),
         "hmd_neighbour_lists": (I, [P, U, P, P, U]),
         "hmd_hilbert_keys": (I, [P, U, P]),
         "hmd_profile_enable": (I, [P, I]),
@@ -176,7 +179,8 @@ def check(rc, handle=None):
 def system_desc(nparticle, box, epsilon=1.0, sigma=1.0, r_cut=2.5, truncation="shifted", smoothing=0.005,
                 skin=0.5, cell_occupancy=0.5, neighbour_occupancy=0.4, timestep=0.001, integrator="verlet",
                 temperature=1.0, collision_rate=0.0, seed=0, sort=True, nspecies=None, potential="lennard_jones",
-                index_repulsion=12, index_attraction=6, index=12, r_min=None, distortion=1.0):
+                index_repulsion=12, index_attraction=6, index=12, r_min=None, distortion=1.0,
+                resonance_frequency=0.0):
     """Build an hmd_system_desc from keyword arguments (Lua module names).
 
     potential: lennard_jones (epsilon, sigma), mie (index_repulsion m,
@@ -215,6 +219,7 @@ def system_desc(nparticle, box, epsilon=1.0, sigma=1.0, r_cut=2.5, truncation="s
     d.collision_rate = collision_rate
     d.seed = int(seed)
     d.sort = 1 if sort else 0
+    d.resonance_frequency = float(resonance_frequency)
     d.potential = POTENTIAL[potential]
     if potential == "morse" and r_min is None:
         raise ValueError("morse needs r_min")
@@ -376,6 +381,13 @@ class Engine:
         self._check(self._L.hmd_thermo(self._h, s, _ptr(out)))
         return dict(mv2=out[0], momentum=out[1:4].copy(), mass=out[4], epot=out[5], virial=out[6],
                     stress=out[7:13].copy(), count=out[13])
+
+    def integrator_state(self, s=0):
+        """Chain positions xi, velocities v_xi and energy per particle (Nose-Hoover);
+        the centre-of-mass velocity of the last draw (Maxwell-Boltzmann)."""
+        out = np.zeros(8)
+        self._check(self._L.hmd_integrator_state(self._h, s, _ptr(out)))
+        return dict(xi=out[0:2].copy(), v_xi=out[2:4].copy(), internal_energy=out[4], vcm=out[5:8].copy())
 
     def neighbour_lists(self, maxn=None, s=0):
         n = self.n(s)

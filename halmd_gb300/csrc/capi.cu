@@ -75,6 +75,7 @@ void hmd_system_desc_init(hmd_system_desc* d)
         d->r_min[k] = 0.0;
         d->distortion[k] = 1.0;
     }
+    d->resonance_frequency = 0.0;   /* required for verlet_nvt_hoover (verlet_nvt_hoover.lua.in:176) */
 }
 
 int hmd_last_error(const hmd_engine* h, char* buf, size_t size)
@@ -254,6 +255,13 @@ int hmd_thermo(hmd_engine* h, uint32_t sys, double* out)
     ENGINE_OR_FAIL(h);
     if (!out) return HMD_ERR_INVALID;
     return guard(h, [&] { h->e->thermo(sys, out); });
+}
+
+int hmd_integrator_state(hmd_engine* h, uint32_t sys, double* out)
+{
+    ENGINE_OR_FAIL(h);
+    if (!out) return HMD_ERR_INVALID;
+    return guard(h, [&] { h->e->integrator_state(sys, out); });
 }
 
 int hmd_neighbour_lists(hmd_engine* h, uint32_t sys, uint32_t* counts, uint32_t* lists, uint32_t maxn)

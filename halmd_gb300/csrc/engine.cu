@@ -128,14 +128,28 @@ static void pot_double(const hmd_system_desc& d, uint32_t ab, double rr, double&
     }
 }
 
+// HMD_INTEGRATOR_* -> Integrator
+static uint32_t integrator_of(int32_t k)
+{
+    switch (k) {
+    case HMD_INTEGRATOR_ANDERSEN: return INTEG_ANDERSEN;
+    case HMD_INTEGRATOR_HOOVER: return INTEG_HOOVER;
+    case HMD_INTEGRATOR_BOLTZMANN: return INTEG_BOLTZMANN;
+    case HMD_INTEGRATOR_EULER: return INTEG_EULER;
+    default: return INTEG_VERLET;
+    }
+}
+
 uint32_t Engine::add_system(const hmd_system_desc& d)
 {
     if (committed_ && !capacity_) throw Error(HMD_ERR_STATE, "systems must be added before commit");
     if (d.nparticle == 0) throw Error(HMD_ERR_INVALID, "nparticle must be positive");
     if (d.nspecies < 1 || d.nspecies > HMD_MAX_SPECIES) throw Error(HMD_ERR_INVALID, "nspecies out of range [1, 4]");
     if (d.truncation < 0 || d.truncation > 3) throw Error(HMD_ERR_INVALID, "unknown truncation");
-    if (d.integrator != HMD_INTEGRATOR_VERLET && d.integrator != HMD_INTEGRATOR_ANDERSEN)
+    if (d.integrator < HMD_INTEGRATOR_VERLET || d.integrator > HMD_INTEGRATOR_EULER)
         throw Error(HMD_ERR_INVALID, "unknown integrator");
+    if (capacity_ && d.integrator != HMD_INTEGRATOR_VERLET && d.integrator != HMD_INTEGRATOR_ANDERSEN)
+        throw Error(HMD_ERR_INVALID, "engines with a reserved capacity take verlet and verlet_nvt_andersen systems");
     if (!(d.timestep > 0)) throw Error(HMD_ERR_INVALID, "timestep must be positive");
     if (!(d.skin >= 0)) throw Error(HMD_ERR_INVALID, "skin must be non-negative");
     if (!(d.cell_occupancy > 0) || !(d.neighbour_occupancy > 0)) throw Error(HMD_ERR_INVALID, "occupancy must be positive");
@@ -163,6 +177,10 @@ uint32_t Engine::add_system(const hmd_system_desc& d)
         if (!(d.box[q] > 0)) throw Error(HMD_ERR_INVALID, "box edges must be positive");
     if (d.integrator == HMD_INTEGRATOR_ANDERSEN && (!(d.temperature >= 0) || !(d.collision_rate >= 0)))
         throw Error(HMD_ERR_INVALID, "bad thermostat parameters");
+    if (d.integrator == HMD_INTEGRATOR_HOOVER && (!(d.temperature > 0) || !(d.resonance_frequency > 0)))
+        throw Error(HMD_ERR_INVALID, "verlet_nvt_hoover needs a temperature and a resonance frequency > 0");
+    if (d.integrator == HMD_INTEGRATOR_BOLTZMANN && (!(d.temperature >= 0) || !(d.collision_rate > 0)))
+        throw Error(HMD_ERR_INVALID, "verlet_nvt_boltzmann needs a temperature >= 0 and a rate > 0");
     if (committed_) return add_live_system(d);   // joins a running engine with a reserved capacity
     if (sys_.size() >= 65536) throw Error(HMD_ERR_INVALID, "too many systems");
     if (capacity_ && sys_.size() >= cap_systems_) throw Error(HMD_ERR_NOMEM, "system table full");
@@ -186,7 +204,7 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
     P.pot = (uint32_t)d.potential;
     P.active = 1;
     P.sort_enable = d.sort ? 1u : 0u;
-    P.integrator = (uint32_t)d.integrator;
+    P.integrator = integrator_of(d.integrator);
     double rc_max = 0, rcs_max = 0;
     h.pairs.resize(ns * ns);
     for (uint32_t ab = 0; ab < ns * ns; ++ab) {
@@ -242,6 +260,20 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
     }
     P.seed_lo = (uint32_t)d.seed;
     P.seed_hi = (uint32_t)(d.seed >> 32);
+    // verlet_nvt_boltzmann.lua.in: coupling interval max(1, round(1 / (rate dt)))
+    P.interval = (d.integrator == HMD_INTEGRATOR_BOLTZMANN)
+                     ? (uint32_t)std::max(1.0, std::floor(1.0 / (d.collision_rate * d.timestep) + 0.5)) : 1u;
+    if (d.integrator == HMD_INTEGRATOR_HOOVER) {
+        // verlet_nvt_hoover.cpp:58-84: masses of the heat-bath variables after
+        // Martyna et al., J. Chem. Phys. 97, 2635 (1992)
+        const double omega_sq = std::pow(2 * M_PI * d.resonance_frequency, 2);
+        const double dof = 3.0 * d.nparticle;
+        P.nhc_mass[0] = dof * d.temperature / omega_sq;
+        P.nhc_mass[1] = d.temperature / omega_sq;
+        P.nhc_target2 = dof * d.temperature;
+        P.nhc_T = d.temperature;
+        P.nhc_dt = d.timestep;
+    }
     {
         // a near pair (closer than NEAR_SIGMA sigma at the build) is within
         // NEAR_SIGMA sigma + skin at force time in every coordinate; from twice
@@ -342,6 +374,9 @@ void Engine::reserve(uint32_t slots, uint32_t systems, uint32_t neighbour_capaci
 {
     if (committed_) throw Error(HMD_ERR_STATE, "capacity must be reserved before commit");
     if (slots == 0 || systems == 0) throw Error(HMD_ERR_INVALID, "capacity must be positive");
+    for (const SysHost& h : sys_)
+        if (h.desc.integrator != HMD_INTEGRATOR_VERLET && h.desc.integrator != HMD_INTEGRATOR_ANDERSEN)
+            throw Error(HMD_ERR_INVALID, "engines with a reserved capacity take verlet and verlet_nvt_andersen systems");
     capacity_ = true;
     cap_slots_ = round_up(slots, SORT_TILE);
     cap_systems_ = systems;
@@ -400,6 +435,7 @@ void Engine::commit()
     any_sort_ = false;
     uint32_t shift = 0;
     force_kinds_ = 0;
+    integ_kinds_ = 0;
     if (!capacity_) {
         table_size_ = (uint32_t)sys_.size();
         null_sys_ = PLACEHOLDER;
@@ -418,6 +454,7 @@ void Engine::commit()
             shift = std::max(shift, 3 * h.P.depth);
             any_sort_ = any_sort_ || h.P.sort_enable;
             force_kinds_ |= 1u << force_kind(h.P);
+            integ_kinds_ |= 1u << h.P.integrator;
         }
         // each system sorts its own slot range with 3*depth-bit Hilbert keys,
         // in tiles that never straddle two systems
@@ -688,6 +725,7 @@ Dev Engine::dev() const
     d.lb_log2 = block() == 8u ? 3u : 2u;
     d.nbr_scan = nbr_scan_;   // 0: each system by its own size (k_neighbour)
     d.force_kinds = force_kinds_;
+    d.integ_kinds = integ_kinds_;
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
     d.S = S_; d.nsys = table_size_;
@@ -764,7 +802,6 @@ void Engine::set(uint32_t s, const std::string& name, const void* host, size_t c
         }
         return;
     }
-    const size_t S = S_;
     std::vector<uint32_t> slot = slots_of(s);
     if (name == "mass") {
         need(n);
@@ -1137,6 +1174,7 @@ cudaGraphExec_t Engine::capture(int nsteps, bool aux_last)
         std::vector<cudaGraphConditionalHandle> hs(nsteps);
         for (int k = 0; k < nsteps; ++k)
             HMD_CUDA(cudaGraphConditionalHandleCreate(&hs[k], g, 0, cudaGraphCondAssignDefault));
+        launch_integrate_prepare(d, stream_);
         launch_integrate(d, ds(), hs[0], true, stream_);
         for (int k = 0; k < nsteps; ++k) {
             const cudaGraphConditionalHandle h = hs[k];
@@ -1158,11 +1196,14 @@ cudaGraphExec_t Engine::capture(int nsteps, bool aux_last)
             cudaGraph_t body_out;
             HMD_CUDA(cudaStreamEndCapture(side_, &body_out));
             launch_force(d, aux_last && k == nsteps - 1, stream_);
-            if (k + 1 < nsteps && fuse_) {
+            if (k + 1 < nsteps && fused()) {
                 launch_finalize_integrate(d, ds(), hs[k + 1], stream_);
             } else {
                 launch_finalize(d, ds(), stream_);
-                if (k + 1 < nsteps) launch_integrate(d, ds(), hs[k + 1], true, stream_);
+                if (k + 1 < nsteps) {
+                    launch_integrate_prepare(d, stream_);
+                    launch_integrate(d, ds(), hs[k + 1], true, stream_);
+                }
             }
         }
     } catch (...) {
@@ -1284,6 +1325,26 @@ bool Engine::grow_after_overflow(uint32_t status)
     return changed;
 }
 
+// captured chunks fuse the finalize of step k with the integrate of step
+// k + 1 unless a thermostat runs between them (Nose-Hoover, Maxwell-Boltzmann)
+bool Engine::fused() const
+{
+    return fuse_ && !(integ_kinds_ & ((1u << INTEG_HOOVER) | (1u << INTEG_BOLTZMANN)));
+}
+
+// step kernels of a captured chunk of n steps (rebuild chains not included):
+// fused, integrate + n force launches + (n - 1) fused finalize + integrate +
+// finalize; otherwise n times the kernels of one step
+uint64_t Engine::chunk_kernels(int n) const
+{
+    const Dev d = dev();
+    if (fused()) {
+        const int nforce = d.force_kinds ? __builtin_popcount(d.force_kinds) : 1;
+        return (uint64_t)n * (nforce + 1) + 1;
+    }
+    return (uint64_t)n * step_kernel_count(d);
+}
+
 void Engine::run_steps(uint64_t nsteps, bool aux_last)
 {
     if (!g_chunk_) build_graphs();
@@ -1295,19 +1356,19 @@ void Engine::run_steps(uint64_t nsteps, bool aux_last)
         if (left >= (uint64_t)CHUNK_STEPS && !(aux_last && left == (uint64_t)CHUNK_STEPS)) {
             HMD_CUDA(cudaGraphLaunch(g_chunk_, stream_));
             left -= CHUNK_STEPS;
-            step_kernels_ += fuse_ ? 2 * CHUNK_STEPS + 1 : 3 * CHUNK_STEPS;
+            step_kernels_ += chunk_kernels(CHUNK_STEPS);
         } else if (left >= (uint64_t)SHORT_STEPS && !(aux_last && left == (uint64_t)SHORT_STEPS)) {
             HMD_CUDA(cudaGraphLaunch(g_short_, stream_));
             left -= SHORT_STEPS;
-            step_kernels_ += fuse_ ? 2 * SHORT_STEPS + 1 : 3 * SHORT_STEPS;
+            step_kernels_ += chunk_kernels(SHORT_STEPS);
         } else if (left == 1 && aux_last) {
             HMD_CUDA(cudaGraphLaunch(g_one_aux_, stream_));
             left -= 1;
-            step_kernels_ += 3;
+            step_kernels_ += chunk_kernels(1);
         } else {
             HMD_CUDA(cudaGraphLaunch(g_one_, stream_));
             left -= 1;
-            step_kernels_ += 3;
+            step_kernels_ += chunk_kernels(1);
         }
     }
 }
@@ -1389,6 +1450,7 @@ void Engine::integrate()
     check_committed();
     ensure_forces(false);
     tic();
+    launch_integrate_prepare(dev(), stream_);
     launch_integrate(dev(), ds(), 0, false, stream_);
     HMD_CUDA(cudaGetLastError());
     toc("integrate");
@@ -1447,6 +1509,27 @@ void Engine::finalize()
     HMD_CUDA(cudaGetLastError());
     toc("finalize");
     sync();
+}
+
+// verlet_nvt_hoover.cpp:134-140 (en_nhc per particle) and the chain state;
+// the last Maxwell-Boltzmann draw's centre-of-mass velocity
+void Engine::integrator_state(uint32_t s, double* out)
+{
+    check_sys(s);
+    sync();
+    const SysState t = read_state()[s];
+    const SysParam& P = sys_[s].P;
+    for (int k = 0; k < 8; ++k) out[k] = 0.0;
+    if (P.integrator == INTEG_HOOVER) {
+        const double dof = 3.0 * P.n;
+        double en = P.nhc_T * (dof * t.xi[0] + t.xi[1]);
+        for (int k = 0; k < 2; ++k) en += P.nhc_mass[k] * t.v_xi[k] * t.v_xi[k] / 2;
+        out[0] = t.xi[0]; out[1] = t.xi[1];
+        out[2] = t.v_xi[0]; out[3] = t.v_xi[1];
+        out[4] = en / P.n;
+    } else if (P.integrator == INTEG_BOLTZMANN) {
+        out[5] = t.vcm[0]; out[6] = t.vcm[1]; out[7] = t.vcm[2];
+    }
 }
 
 double Engine::max_displacement(uint32_t s)

@@ -109,6 +109,7 @@ public:
     int64_t get_option(const std::string& name) const;
     double max_displacement(uint32_t s);
     void thermo(uint32_t s, double* out);
+    void integrator_state(uint32_t s, double* out);
     void neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint32_t maxn);
     void hilbert_keys(uint32_t s, uint32_t* keys);
     void profile_enable(bool on);
@@ -140,6 +141,8 @@ private:
     void build_graphs();
     void destroy_graphs();
     cudaGraphExec_t capture(int nsteps, bool aux_last);
+    bool fused() const;
+    uint64_t chunk_kernels(int n) const;
     void snapshot();
     void restore();
     bool grow_after_overflow(uint32_t status);
@@ -169,6 +172,7 @@ private:
     uint32_t lb_ = 0;          // list block width option (0 auto, 4, 8)
     uint32_t nbr_scan_ = 0;   // list build: 0 auto, 1 per lane, 2 shared scan per warp
     uint32_t force_kinds_ = 0;  // Dev::force_kinds: kinds of the committed systems (0 in capacity mode)
+    uint32_t integ_kinds_ = 0;  // Dev::integ_kinds: integrators of the committed systems
     int sort_passes_ = 0;       // radix passes of the segmented sort (even)
     uint32_t ntiles_ = 0;
     DevBuf<uint2> tiles_;

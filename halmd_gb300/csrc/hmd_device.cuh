@@ -35,8 +35,13 @@ __host__ __device__ constexpr uint32_t list_block(uint32_t w) { return w < 4u ? 
 
 enum Trunc : uint32_t { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3 };
 enum Pot : uint32_t { POT_LJ = 0, POT_MIE = 1, POT_MORSE = 2, POT_POWER_LAW = 3 };
-// INTEG_DESCENT: steepest-descent energy minimisation (positions only)
-enum Integrator : uint32_t { INTEG_VERLET = 0, INTEG_ANDERSEN = 1, INTEG_DESCENT = 2 };
+// INTEG_DESCENT: steepest-descent energy minimisation (positions only);
+// INTEG_HOOVER: Nose-Hoover chain of two; INTEG_BOLTZMANN: Verlet with
+// Maxwell-Boltzmann velocities drawn every `interval` steps; INTEG_EULER:
+// r += v dt only
+enum Integrator : uint32_t {
+    INTEG_VERLET = 0, INTEG_ANDERSEN = 1, INTEG_DESCENT = 2, INTEG_HOOVER = 3, INTEG_BOLTZMANN = 4, INTEG_EULER = 5
+};
 enum Status : uint32_t {
     ST_CELL_OVERFLOW = 1u,
     ST_NBR_OVERFLOW = 2u,
@@ -95,6 +100,12 @@ struct SysParam {
     float descent_step;        // INTEG_DESCENT: move = descent_step * F ...
     float descent_max;         // ... capped at this length per particle and step
     uint32_t pot;              // pair potential (Pot)
+    uint32_t interval;         // INTEG_BOLTZMANN: steps between velocity draws
+    // INTEG_HOOVER (verlet_nvt_hoover.cpp:58-84): chain masses, dim N T, T, dt
+    double nhc_mass[2];
+    double nhc_target2;
+    double nhc_T;
+    double nhc_dt;
 };
 
 // mutable per-system device state
@@ -109,6 +120,13 @@ struct SysState {
     uint32_t live;             // 1: the system advances in the current step
     uint32_t rebuild_request;  // host-set: rebuild at the next opportunity
     uint32_t pad;
+    // thermostat state (INTEG_HOOVER: chain positions and velocities, the
+    // velocity scale of the current half step; INTEG_BOLTZMANN: the
+    // centre-of-mass velocity of the last draw)
+    double xi[2], v_xi[2];
+    double vcm[3];
+    float scale;
+    uint32_t pad2;
 };
 
 // device pointers of one engine (passed by value to every kernel)
@@ -129,6 +147,7 @@ struct Dev {
     uint32_t lb_log2;          // log2 of the list block width LB (4 or 8)
     uint32_t nbr_scan;         // list build: 0 by system size, 1 per lane, 2 shared per warp of 32 particles
     uint32_t force_kinds;      // bit k: a system of force kind k (kernels.h ForceKind); 0: unknown, one kernel for all
+    uint32_t integ_kinds;      // bit k: a system with integrator k (Integrator)
     uint32_t* cell;            // cell contents
     uint32_t* cell_count;      // [total_cells]
     const uint32_t* cell_sys;  // [total_cells] owning system

@@ -184,8 +184,10 @@ class particle:
             kw["smoothing"] = pot.h
         if nb.get("occupancy") is not None:
             kw["neighbour_occupancy"] = nb["occupancy"]
-        if integ.kind == "andersen":
+        if integ.kind in ("andersen", "boltzmann"):
             kw.update(temperature=integ.temperature, collision_rate=integ.rate, seed=integ.seed)
+        if integ.kind == "hoover":
+            kw.update(temperature=integ.temperature, resonance_frequency=integ.resonance_frequency)
         return system_desc(self.nparticle, self._box.length, nspecies=self.nspecies, **kw)
 
 
@@ -293,10 +295,13 @@ class _Integrator:
         self.particle = a["particle"]
         a["particle"]._box = a.get("box", a["particle"]._box)
         a["particle"]._integrator = self
-        if kind == "andersen":
+        if kind in ("andersen", "boltzmann"):
             self.temperature = float(a["temperature"])
             self.rate = float(a["rate"])
             self.seed = int(a.get("seed", 0))
+        if kind == "hoover":
+            self.temperature = float(a["temperature"])
+            self.resonance_frequency = float(a["resonance_frequency"])
 
 
 def verlet(args=None, **kw):
@@ -309,11 +314,38 @@ def verlet_nvt_andersen(args=None, **kw):
     return _Integrator("andersen", _args(args, kw))
 
 
+def verlet_nvt_hoover(args=None, **kw):
+    """halmd.mdsim.integrators.verlet_nvt_hoover{box, particle, timestep, temperature, resonance_frequency}
+    (verlet_nvt_hoover.lua.in:170-180; both thermostat arguments are required)."""
+    a = _args(args, kw)
+    for k in ("temperature", "resonance_frequency"):
+        if k not in a:
+            raise ValueError("missing keyword argument '%s'" % k)
+    return _Integrator("hoover", a)
+
+
+def verlet_nvt_boltzmann(args=None, **kw):
+    """halmd.mdsim.integrators.verlet_nvt_boltzmann{box, particle, timestep, temperature, rate}:
+    velocity Verlet with Maxwell-Boltzmann velocities every max(1, round(1 / (rate timestep))) steps."""
+    a = _args(args, kw)
+    for k in ("temperature", "rate"):
+        if k not in a:
+            raise ValueError("missing keyword argument '%s'" % k)
+    return _Integrator("boltzmann", a)
+
+
+def euler(args=None, **kw):
+    """halmd.mdsim.integrators.euler{box, particle, timestep}: r += v dt."""
+    return _Integrator("euler", _args(args, kw))
+
+
 mdsim = _Namespace(
     box=box, particle=particle, neighbour=neighbour,
     potentials=_Namespace(pair=_Namespace(lennard_jones=lennard_jones, mie=mie, morse=morse, power_law=power_law)),
     forces=_Namespace(pair=pair),
-    integrators=_Namespace(verlet=verlet, verlet_nvt_andersen=verlet_nvt_andersen),
+    integrators=_Namespace(verlet=verlet, verlet_nvt_andersen=verlet_nvt_andersen,
+                           verlet_nvt_hoover=verlet_nvt_hoover, verlet_nvt_boltzmann=verlet_nvt_boltzmann,
+                           euler=euler),
 )
 
 

@@ -53,6 +53,9 @@ extern "C" {
 
 #define HMD_INTEGRATOR_VERLET 0    /* integrators/verlet.cpp */
 #define HMD_INTEGRATOR_ANDERSEN 1  /* integrators/verlet_nvt_andersen.cpp */
+#define HMD_INTEGRATOR_HOOVER 2    /* integrators/verlet_nvt_hoover.cpp (Nose-Hoover chain of two) */
+#define HMD_INTEGRATOR_BOLTZMANN 3 /* lua/halmd/mdsim/integrators/verlet_nvt_boltzmann.lua.in */
+#define HMD_INTEGRATOR_EULER 4     /* integrators/euler.cpp */
 
 #define HMD_MAX_SPECIES 4
 #define HMD_NTHERMO 14
@@ -72,8 +75,10 @@ typedef struct hmd_dynamics hmd_dynamics;
  *   :truncate{kind, cutoff, h}             lua/halmd/mdsim/potentials/pair/adapters/truncate.lua.in:287-305
  * neighbour{skin, occupancy, sort}         lua/halmd/mdsim/neighbour.lua.in:151-306, from_binning.cpp:96-119
  * binning{occupancy}                       mdsim/gpu/binning.cpp:47-116
- * verlet(dt) / verlet_nvt_andersen(dt, T, rate)
- *                                          lua/halmd/mdsim/integrators/{verlet,verlet_nvt_andersen}.lua.in
+ * verlet(dt) / verlet_nvt_andersen(dt, T, rate) / verlet_nvt_hoover(dt, T, resonance_frequency)
+ *   / verlet_nvt_boltzmann(dt, T, rate) / euler(dt)
+ *                                          lua/halmd/mdsim/integrators/{verlet,verlet_nvt_andersen,
+ *                                          verlet_nvt_hoover,verlet_nvt_boltzmann,euler}.lua.in
  * Matrices are nspecies x nspecies, row-major; r_cut in units of sigma.
  */
 typedef struct hmd_system_desc {
@@ -100,6 +105,7 @@ typedef struct hmd_system_desc {
     uint32_t index[HMD_MAX_SPECIES * HMD_MAX_SPECIES];             /* power_law n >= 1 (default 12) */
     double r_min[HMD_MAX_SPECIES * HMD_MAX_SPECIES];      /* morse: position of the minimum (required) */
     double distortion[HMD_MAX_SPECIES * HMD_MAX_SPECIES]; /* morse: B > 0 (default 1) */
+    double resonance_frequency;  /* verlet_nvt_hoover: heat-bath resonance frequency (required, > 0) */
 } hmd_system_desc;
 
 /* per-system state readable after any call (hmd_info) */
@@ -245,6 +251,16 @@ HMD_API int hmd_max_displacement(hmd_engine* engine, uint32_t sys, double* displ
  *   Σ m v², Σ m v (3), Σ m, Σ E_pot, Σ tr(stress), stress (6), N
  */
 HMD_API int hmd_thermo(hmd_engine* engine, uint32_t sys, double* out);
+
+/*
+ * Thermostat state of a system (verlet_nvt_hoover.cpp:252-283 properties
+ * `position`, `velocity`, `internal_energy`): out[0..1] chain positions xi,
+ * out[2..3] chain velocities v_xi, out[4] the chain's energy per particle
+ * (en_nhc, verlet_nvt_hoover.cpp:134-140), out[5..7] the centre-of-mass
+ * velocity removed by the last Maxwell-Boltzmann draw (verlet_nvt_boltzmann).
+ * Zero for the other integrators.
+ */
+HMD_API int hmd_integrator_state(hmd_engine* engine, uint32_t sys, double* out);
 
 /*
  * Neighbour lists of the last build (neighbours/from_binning.cpp g_neighbour()):

@@ -66,6 +66,7 @@ def lib():
         L.orc_wavevectors.argtypes = [I, P, P, D, I, P, I, P, P]
         L.orc_fcc_lattice.argtypes = [I, D, P]
         L.orc_md_run.argtypes = [I, P, P, P, P, P, P, P, D, D, I, D, D, ctypes.c_uint64, P]
+        L.orc_md_run_any.argtypes = [I, P, P, P, P, P, P, P, D, D, I, I, D, D, D, ctypes.c_uint64, P, P]
         L.orc_minimize.argtypes = [I, P, P, P, P, P, D, I, D, D, P]
         L.orc_tcf.argtypes = [I, I, I, P, P, P]
         _lib = L
@@ -342,7 +343,13 @@ def minimize(r, species, L, pot, skin, nsteps, step=1e-3, max_move=0.05, image=N
     return r, image, dict(epot=stats[0], fmax=stats[1])
 
 
-def md_run(r, v, species, mass, L, pot, skin, dt, nsteps, temperature=0.0, coll_rate=0.0, seed=0, image=None):
+INTEGRATOR = {"verlet": 0, "andersen": 1, "hoover": 2, "boltzmann": 3, "euler": 4}
+
+
+def md_run(r, v, species, mass, L, pot, skin, dt, nsteps, temperature=0.0, coll_rate=0.0, seed=0, image=None,
+           integrator=None, resonance_frequency=0.0):
+    """FP64 host-backend MD run; integrator verlet (default), andersen (when
+    coll_rate > 0 and no integrator is named), hoover, boltzmann or euler."""
     r = np.array(r, dtype=np.float64, copy=True)
     v = np.array(v, dtype=np.float64, copy=True)
     n = r.shape[0]
@@ -350,7 +357,12 @@ def md_run(r, v, species, mass, L, pot, skin, dt, nsteps, temperature=0.0, coll_
     sp = np.ascontiguousarray(species, dtype=np.uint32)
     m = np.ascontiguousarray(mass, dtype=np.float64)
     L = np.ascontiguousarray(L, dtype=np.float64)
+    if integrator is None:
+        integrator = "andersen" if coll_rate > 0 else "verlet"
     stats = np.zeros(3)
-    lib().orc_md_run(n, _p(r), _p(v), _p(image), _p(sp), _p(m), _p(L), pot.ptr, float(skin), float(dt),
-                     int(nsteps), float(temperature), float(coll_rate), int(seed), _p(stats))
-    return r, v, image, dict(rebuilds=stats[0], epot=stats[1], ekin=stats[2])
+    chain = np.zeros(5)
+    lib().orc_md_run_any(n, _p(r), _p(v), _p(image), _p(sp), _p(m), _p(L), pot.ptr, float(skin), float(dt),
+                         int(nsteps), INTEGRATOR[integrator], float(temperature), float(coll_rate),
+                         float(resonance_frequency), int(seed), _p(stats), _p(chain))
+    return r, v, image, dict(rebuilds=stats[0], epot=stats[1], ekin=stats[2], xi=chain[0:2], v_xi=chain[2:4],
+                             en_nhc=chain[4])

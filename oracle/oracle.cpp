@@ -1142,9 +1142,62 @@ ORC_API void orc_fcc_lattice(int ncell, double L, double* r)
  * r, v, image are updated in place; stats[0] = number of rebuilds,
  * stats[1] = final potential energy, stats[2] = final kinetic energy.
  */
+/*
+ * Nose-Hoover chain of two, one half step (host/integrators/verlet_nvt_hoover.cpp
+ * propagate_chain, the same algorithm as the GPU module's
+ * gpu/integrators/verlet_nvt_hoover.cpp:141-185); en_kin_2 = sum m v^2.
+ * Returns the velocity scale.
+ */
+struct orc_chain {
+    double xi[2], v_xi[2], mass[2], target2, T;
+};
+
+static double chain_half_step(orc_chain& c, double en_kin_2, double dt)
+{
+    c.v_xi[1] += (c.mass[0] * c.v_xi[0] * c.v_xi[0] - c.T) / c.mass[1] * (dt / 4);
+    const double t = std::exp(-c.v_xi[1] * (dt / 8));
+    c.v_xi[0] *= t;
+    c.v_xi[0] += (en_kin_2 - c.target2) / c.mass[0] * (dt / 4);
+    c.v_xi[0] *= t;
+    for (int k = 0; k < 2; ++k) c.xi[k] += c.v_xi[k] * (dt / 2);
+    const double s = std::exp(-c.v_xi[0] * (dt / 2));
+    en_kin_2 *= s * s;
+    c.v_xi[0] *= t;
+    c.v_xi[0] += (en_kin_2 - c.target2) / c.mass[0] * (dt / 4);
+    c.v_xi[0] *= t;
+    c.v_xi[1] += (c.mass[0] * c.v_xi[0] * c.v_xi[0] - c.T) / c.mass[1] * (dt / 4);
+    return s;
+}
+
+enum { ORC_VERLET = 0, ORC_ANDERSEN = 1, ORC_HOOVER = 2, ORC_BOLTZMANN = 3, ORC_EULER = 4 };
+
+ORC_API int orc_md_run_any(int n, double* r, double* v, double* image, const u32* sp_in, const double* mass_in,
+                           const double* L, const orc_pot* p, double skin, double dt, int nsteps, int integrator,
+                           double temperature, double coll_rate, double resonance_frequency, uint64_t seed,
+                           double* stats, double* chain_out);
+
 ORC_API int orc_md_run(int n, double* r, double* v, double* image, const u32* sp_in, const double* mass_in,
                        const double* L, const orc_pot* p, double skin, double dt, int nsteps,
                        double temperature, double coll_rate, uint64_t seed, double* stats)
+{
+    return orc_md_run_any(n, r, v, image, sp_in, mass_in, L, p, skin, dt, nsteps,
+                          coll_rate > 0 ? ORC_ANDERSEN : ORC_VERLET, temperature, coll_rate, 0, seed, stats, nullptr);
+}
+
+/*
+ * FP64 MD run with the host integrators: velocity Verlet
+ * (host/integrators/verlet.cpp:59-101), Andersen (verlet_nvt_andersen.cpp:96-137,
+ * collisions from the engine's Philox stream), Nose-Hoover chain
+ * (verlet_nvt_hoover.cpp), Maxwell-Boltzmann draws every
+ * max(1, round(1 / (rate dt))) steps (verlet_nvt_boltzmann.lua.in with
+ * velocities/boltzmann: N(0, sqrt T) / sqrt(m), centre-of-mass velocity
+ * removed), Euler (host/integrators/euler.cpp: r += v dt).
+ * chain_out (Nose-Hoover): xi[2], v_xi[2], energy per particle.
+ */
+ORC_API int orc_md_run_any(int n, double* r, double* v, double* image, const u32* sp_in, const double* mass_in,
+                           const double* L, const orc_pot* p, double skin, double dt, int nsteps, int integrator,
+                           double temperature, double coll_rate, double resonance_frequency, uint64_t seed,
+                           double* stats, double* chain_out)
 {
     std::vector<u32> sp(sp_in, sp_in + n);
     std::vector<double> m(mass_in, mass_in + n);
@@ -1157,8 +1210,26 @@ ORC_API int orc_md_run(int n, double* r, double* v, double* image, const u32* sp
     int rebuilds = 0;
     double totals[2] = {0, 0};
     double sqrtT = std::sqrt(temperature);
-    u32 thresh = (u32)std::min(4294967295.0, std::floor(coll_rate * dt * 4294967296.0));
+    u32 thresh = (integrator == ORC_ANDERSEN)
+                     ? (u32)std::min(4294967295.0, std::floor(coll_rate * dt * 4294967296.0)) : 0u;
     u32 key[2] = {(u32)seed, (u32)(seed >> 32)};
+    const uint64_t interval = (integrator == ORC_BOLTZMANN)
+                                  ? (uint64_t)std::max(1.0, std::floor(1.0 / (coll_rate * dt) + 0.5)) : 1u;
+    orc_chain chain = {};
+    if (integrator == ORC_HOOVER) {
+        const double omega_sq = std::pow(2 * M_PI * resonance_frequency, 2);
+        const double dof = 3.0 * n;
+        chain.mass[0] = dof * temperature / omega_sq;
+        chain.mass[1] = temperature / omega_sq;
+        chain.target2 = dof * temperature;
+        chain.T = temperature;
+    }
+    auto en_kin_2 = [&]() {
+        double e = 0;
+        for (int i = 0; i < n; ++i)
+            e += m[i] * (v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]);
+        return e;
+    };
 
     auto rebuild = [&]() {
         /* Hilbert reorder (host/sorts/hilbert.cpp:91-111 orders by cell; the
@@ -1200,15 +1271,46 @@ ORC_API int orc_md_run(int n, double* r, double* v, double* image, const u32* sp
     rebuild();
     force_half(n, r, sp.data(), L, p, hl, 0, nullptr, nullptr, f.data(), nullptr, nullptr, totals);
     for (int s = 0; s < nsteps; ++s) {
+        const uint64_t step = (uint64_t)s + 1;   /* 1-based step of this integration */
+        if (integrator == ORC_HOOVER) {
+            const double sc = chain_half_step(chain, en_kin_2(), dt);
+            for (int k = 0; k < 3 * n; ++k) v[k] *= sc;
+        }
         for (int i = 0; i < n; ++i) {
             for (int d = 0; d < 3; ++d) {
-                v[3 * i + d] += f[3 * i + d] * (dt / 2) / m[i];
+                if (integrator != ORC_EULER) v[3 * i + d] += f[3 * i + d] * (dt / 2) / m[i];
                 r[3 * i + d] += v[3 * i + d] * dt;
                 image[3 * i + d] += reduce_periodic_d(r[3 * i + d], L[d]);
             }
         }
         if (max_disp_exceeded()) rebuild();
         force_half(n, r, sp.data(), L, p, hl, 0, nullptr, nullptr, f.data(), nullptr, nullptr, totals);
+        if (integrator == ORC_EULER) continue;
+        if (integrator == ORC_BOLTZMANN && step % interval == 0) {
+            double mv[3] = {0, 0, 0}, msum = 0;
+            for (int i = 0; i < n; ++i) {
+                u32 ctr[4] = {id[i], (u32)step, (u32)(step >> 32), 0x424F4C5Au}, w[4];
+                orc_philox4x32_10(ctr, key, w);
+                const double rad0 = std::sqrt(-2 * std::log(u01(w[0])));
+                const double rad1 = std::sqrt(-2 * std::log(u01(w[2])));
+                const double q = std::sqrt(m[i]);
+                v[3 * i + 0] = sqrtT * rad0 * std::cos(2 * M_PI * u01(w[1])) / q;
+                v[3 * i + 1] = sqrtT * rad0 * std::sin(2 * M_PI * u01(w[1])) / q;
+                v[3 * i + 2] = sqrtT * rad1 * std::cos(2 * M_PI * u01(w[3])) / q;
+                for (int d = 0; d < 3; ++d) mv[d] += m[i] * v[3 * i + d];
+                msum += m[i];
+            }
+            for (int i = 0; i < n; ++i)
+                for (int d = 0; d < 3; ++d) v[3 * i + d] -= mv[d] / msum;
+            continue;
+        }
+        if (integrator == ORC_HOOVER) {
+            for (int i = 0; i < n; ++i)
+                for (int d = 0; d < 3; ++d) v[3 * i + d] += f[3 * i + d] * (dt / 2) / m[i];
+            const double sc = chain_half_step(chain, en_kin_2(), dt);
+            for (int k = 0; k < 3 * n; ++k) v[k] *= sc;
+            continue;
+        }
         for (int i = 0; i < n; ++i) {
             bool collide = false;
             if (coll_rate > 0) {
@@ -1246,6 +1348,14 @@ ORC_API int orc_md_run(int n, double* r, double* v, double* image, const u32* sp
     for (int i = 0; i < n; ++i)
         ek += 0.5 * m[i] * (v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2]);
     if (stats) { stats[0] = rebuilds; stats[1] = totals[0]; stats[2] = ek; }
+    if (chain_out) {
+        /* verlet_nvt_hoover.cpp:134-140 */
+        double en = chain.T * (3.0 * n * chain.xi[0] + chain.xi[1]);
+        for (int k = 0; k < 2; ++k) en += chain.mass[k] * chain.v_xi[k] * chain.v_xi[k] / 2;
+        chain_out[0] = chain.xi[0]; chain_out[1] = chain.xi[1];
+        chain_out[2] = chain.v_xi[0]; chain_out[3] = chain.v_xi[1];
+        chain_out[4] = en / n;
+    }
     return 0;
 }
 
