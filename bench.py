@@ -42,6 +42,21 @@ def workload(name):
     if name == "lj4k":
         return dict(name="LJ-4k", n=4000, rho=0.8442, T=1.5, dt=0.005, trunc="shifted", skin=0.3, nspecies=1,
                     rate=0.0)
+    # the reference's own benchmark configurations (examples/benchmarks/*), whose
+    # published H100 double-single timings are the baseline of vs_baseline
+    # (doc/benchmarks.rst.in:29 and :79): equilibrated at T with Andersen
+    # collisions, then NVE
+    if name == "ref-lj64k":
+        # lennard_jones/{generate_configuration,run_benchmark}.lua: rho 0.4, T 1.2, r_c 3, skin 0.7, dt 0.002
+        return dict(name="reference LJ-64k (rho 0.4)", n=64000, rho=0.4, T=1.2, dt=0.002, trunc="shifted", rc=3.0,
+                    skin=0.7, nspecies=1, rate=0.0, equilibrate=dict(steps=4000, rate=2.0, dt=0.002),
+                    published=1.0 / 3.4e-9)
+    if name == "ref-ka256k":
+        # kob_andersen/{generate_configuration,run_benchmark}.lua: 256000, rho 1.2, T 0.7, shifted r_c 2.5 sigma,
+        # skin 0.3, list occupancy 0.7, dt 0.001
+        return dict(name="reference KA-256k (rho 1.2)", n=256000, rho=1.2, T=0.7, dt=0.001, trunc="shifted",
+                    rc=2.5, skin=0.3, occupancy=0.7, nspecies=2, rate=0.0,
+                    equilibrate=dict(steps=4000, rate=2.0, dt=0.002), published=1.0 / 1.79e-9)
     raise SystemExit("unknown workload " + name)
 
 
@@ -51,7 +66,8 @@ RELAX_MAX_MOVE = 0.05     # ... at most this far per step
 
 
 def initial_state(w, seed=2024):
-    """Seeded synthetic input: fcc lattice (LJ) or uniform random positions
+    """Seeded synthetic input: fcc lattice (LJ; simple cubic where n is not
+    4 k^3) or uniform random positions
     with random 80:20 species (KA; relaxed afterwards by steepest descent),
     Maxwell-Boltzmann velocities with zero momentum."""
     n = w["n"]
@@ -60,12 +76,19 @@ def initial_state(w, seed=2024):
     if w["nspecies"] == 2:
         L = (n / w["rho"]) ** (1 / 3)
         r = rng.uniform(-0.5 * L, 0.5 * L, size=(n, 3))
-    else:
+    elif 4 * ncell ** 3 == n:
         L = ncell * (4 / w["rho"]) ** (1 / 3)
         a = L / ncell
         basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
         c = np.stack(np.meshgrid(*(np.arange(ncell),) * 3, indexing="ij"), -1).reshape(-1, 1, 3)
         r = ((c + basis[None] + 0.25) * a - 0.5 * L).reshape(-1, 3)
+        r = r + rng.uniform(-0.02, 0.02, size=r.shape)
+    else:
+        # n is not 4 k^3: the first n sites of a simple cubic lattice
+        L = (n / w["rho"]) ** (1 / 3)
+        m = int(np.ceil(n ** (1 / 3) - 1e-9))
+        g = (np.arange(m) + 0.5) * (L / m) - 0.5 * L
+        r = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)[:n]
         r = r + rng.uniform(-0.02, 0.02, size=r.shape)
     v = rng.normal(0, np.sqrt(w["T"]), size=(n, 3))
     v -= v.mean(axis=0)
@@ -79,18 +102,39 @@ def initial_state(w, seed=2024):
 def make_engine(w, L, seed=7):
     import halmd_gb300 as hg
     eng = hg.Engine("dsfloat")
+    extra = {}
+    if w.get("occupancy"):
+        extra["neighbour_occupancy"] = w["occupancy"]
     if w["nspecies"] == 2:
-        d = hg.system_desc(w["n"], L, epsilon=KA["eps"], sigma=KA["sigma"], r_cut=2.5, truncation="smooth_r4",
-                           smoothing=0.005, skin=w["skin"], timestep=w["dt"],
+        d = hg.system_desc(w["n"], L, epsilon=KA["eps"], sigma=KA["sigma"], r_cut=w.get("rc", 2.5),
+                           truncation=w["trunc"], smoothing=0.005, skin=w["skin"], timestep=w["dt"],
                            integrator="andersen" if w["rate"] > 0 else "verlet", temperature=w["T"],
-                           collision_rate=w["rate"], seed=seed)
+                           collision_rate=w["rate"], seed=seed, **extra)
     else:
-        d = hg.system_desc(w["n"], L, r_cut=2.5, truncation=w["trunc"], skin=w["skin"], timestep=w["dt"],
-                           integrator="andersen" if w["rate"] > 0 else "verlet", temperature=w["T"],
-                           collision_rate=w["rate"], seed=seed)
+        d = hg.system_desc(w["n"], L, r_cut=w.get("rc", 2.5), truncation=w["trunc"], skin=w["skin"],
+                           timestep=w["dt"], integrator="andersen" if w["rate"] > 0 else "verlet",
+                           temperature=w["T"], collision_rate=w["rate"], seed=seed, **extra)
     eng.add_system(d)
     eng.commit()
     return eng
+
+
+def equilibrated_state(w, r, v, species, L, seed=7):
+    """The reference benchmarks start from configurations equilibrated at T
+    (examples/benchmarks/*/generate_configuration.lua): the synthetic start
+    (relaxed by steepest descent for KA) advanced with Andersen collisions."""
+    e = w["equilibrate"]
+    weq = dict(w, rate=e["rate"], dt=e["dt"])
+    eng = make_engine(weq, L, seed=seed)
+    eng.set("species", species)
+    eng.set("position", r)
+    if w["nspecies"] == 2:
+        eng.minimize(RELAX_STEPS, RELAX_STEP_SIZE, RELAX_MAX_MOVE)
+    eng.set("velocity", v)
+    eng.step(e["steps"])
+    r, v = eng.get("position"), eng.get("velocity")
+    eng.close()
+    return r, v
 
 
 class ClockSampler:
@@ -220,9 +264,9 @@ def cpu_baseline(w, r, v, species, L, budget_s=15.0):
     """FP64 single-thread host backend restatement on a bounded sample."""
     import oracle
     if w["nspecies"] == 2:
-        pot = oracle.Potential(KA["eps"], KA["sigma"], 2.5, "smooth_r4", h=0.005)
+        pot = oracle.Potential(KA["eps"], KA["sigma"], w.get("rc", 2.5), w["trunc"], h=0.005)
     else:
-        pot = oracle.Potential(1.0, 1.0, 2.5, w["trunc"])
+        pot = oracle.Potential(1.0, 1.0, w.get("rc", 2.5), w["trunc"])
     n = w["n"]
     mass = np.ones(n)
     t0 = time.perf_counter()
@@ -246,9 +290,9 @@ def run_reference(args, w):
     r, v, species, L = initial_state(w)
     import oracle
     if w["nspecies"] == 2:
-        pot = oracle.Potential(KA["eps"], KA["sigma"], 2.5, "smooth_r4", h=0.005)
+        pot = oracle.Potential(KA["eps"], KA["sigma"], w.get("rc", 2.5), w["trunc"], h=0.005)
     else:
-        pot = oracle.Potential(1.0, 1.0, 2.5, w["trunc"])
+        pot = oracle.Potential(1.0, 1.0, w.get("rc", 2.5), w["trunc"])
     n = w["n"]
     mass = np.ones(n)
     relax = 0
@@ -576,7 +620,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--workload", default="ka64k")
+    ap.add_argument("--workload", default="ka64k",
+                    help="ka64k, lj1m, lj4k, ens256, serve; ref-lj64k, ref-ka256k: the reference's own benchmarks")
     ap.add_argument("--md-steps", type=int, default=100, help="MD steps per bench step")
     ap.add_argument("--ref-steps", type=int, default=20, help="MD steps per bench step of the reference arm")
     ap.add_argument("--ref-relax", type=int, default=100,
@@ -623,6 +668,8 @@ def main():
         dist.init_process_group("nccl")
 
     r, v, species, L = initial_state(w, seed=2024 + rank)
+    if w.get("equilibrate"):
+        r, v = equilibrated_state(w, r, v, species, L, seed=7 + rank)
     eng = make_engine(w, L, seed=7 + rank)
     eng.set_option("fuse_steps", args.fuse_steps)
     if args.neighbour_scan:
@@ -630,7 +677,7 @@ def main():
     n = w["n"]
     eng.set("species", species)
     eng.set("position", r)
-    if w["nspecies"] == 2:
+    if w["nspecies"] == 2 and not w.get("equilibrate"):
         eng.minimize(RELAX_STEPS, RELAX_STEP_SIZE, RELAX_MAX_MOVE)
         r = eng.get("position")
     eng.set("velocity", v)
@@ -721,10 +768,13 @@ def main():
 
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / md_steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (dsfloat state)",
+            "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": value / w["published"] if w.get("published") and world == 1 else None,
+            "dtype": "f32 (dsfloat state)",
             "data": "synthetic",
             "config": {"workload": w["name"], "n": n, "density": w["rho"], "temperature": w["T"], "dt": w["dt"],
                        "md_steps_per_bench_step": M, "truncation": w["trunc"], "skin": w["skin"],
+                       "r_cut": w.get("rc", 2.5),
                        "precision": "dsfloat", "l2": "flushed (256 MB write) between timed bench steps",
                        "rebuilds_in_timed_region": rebuilds, "parallelism": "replicas" if world > 1 else "single",
                        "force_lanes": lanes, "list_block": eng.get_option("list_block"),
