@@ -149,3 +149,81 @@ def test_thermostat_arguments_are_checked():
     with pytest.raises(hg.HmdError):
         eng.add_system(hg.system_desc(100, 10.0, integrator="euler"))
     eng.close()
+
+
+def ideal_gas(n, rho, ratios, T, seed):
+    """Force-free particles (epsilon = 0) on distinct sites of a simple cubic
+    grid in a box of the given aspect ratios; Maxwell-Boltzmann velocities."""
+    box = np.asarray(ratios) * (n / rho / np.prod(ratios)) ** (1 / 3)
+    m = np.ceil(box * (n / np.prod(box)) ** (1 / 3) * 1.0001).astype(int)
+    axes = [(np.arange(k) + 0.5) * (b / k) - 0.5 * b for k, b in zip(m, box)]
+    sites = np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, 3)
+    r = sites[np.random.default_rng(seed).permutation(sites.shape[0])[:n]]
+    return r, maxwell_boltzmann(n, T, seed=seed + 1), box
+
+
+def test_ideal_gas_verlet():
+    # test/unit/mdsim/integrators/verlet.cpp:110-170: 1000 free particles,
+    # rho = 1, T = 1, dt = 0.001, 1000 NVE steps in a 1 : 2 : 1.01 box
+    n, rho, T = 1000, 1.0, 1.0
+    r, v, box = ideal_gas(n, rho, [1.0, 2.0, 1.01], T, seed=31)
+    eng = hg.Engine("dsfloat")
+    # epsilon = 0 and a tiny sigma: no force, and no pair ever close enough
+    # for the (zero-weighted) r^-12 term to overflow
+    eng.add_system(hg.system_desc(n, box, epsilon=0.0, sigma=0.01, r_cut=2.5, skin=0.5, timestep=0.001))
+    eng.commit()
+    eng.set("position", r)
+    eng.set("velocity", v)
+    th0 = eng.thermo()
+    eng.step(1000, aux_last=True)
+    th = eng.thermo()
+    vcm = th["momentum"] / th["mass"]
+    assert np.max(np.abs(vcm)) < 1e-12
+    assert abs(th["mv2"] - th0["mv2"]) <= 10 * np.finfo(np.float64).eps * th0["mv2"]   # no force: no change
+    temp = th["mv2"] / (3 * n)
+    volume = np.prod(box)
+    press = (th["mv2"] + th["virial"]) / (3 * volume)
+    tol = 5 / np.sqrt(n)
+    assert abs(temp - T) / T < tol
+    assert abs(press / temp / rho - 1.0) < tol
+    # ballistic motion: r(t) = r(0) + v t
+    np.testing.assert_allclose(eng.get("unwrapped_position"), r + v * 1000 * np.float32(0.001), atol=1e-5)
+    eng.close()
+
+
+def test_andersen_statistics():
+    # test/unit/mdsim/integrators/verlet_nvt_andersen.cpp:100-200 (GPU case):
+    # 5000 free particles, rho = 0.3, T = 1, collision rate 10, dt = 0.01,
+    # 500 time units sampled every round(3 / (rate dt)) = 30 steps
+    n, rho, T, rate, dt = 5000, 0.3, 1.0, 10.0, 0.01
+    r, v, box = ideal_gas(n, rho, [1.0, 2.0, 1.01], 2.0, seed=41)
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, box, epsilon=0.0, sigma=0.01, r_cut=2.5, skin=0.5, timestep=dt,
+                                  integrator="andersen",
+                                  temperature=T, collision_rate=rate, seed=42))
+    eng.commit()
+    eng.set("position", r)
+    eng.set("velocity", v)
+    period = int(round(3 / (rate * dt)))
+    steps = int(np.ceil(500 / dt))
+    eng.step(period * 10)                     # a few periods to thermalise from T = 2
+    temps, vcms = [], []
+    for _ in range(steps // period):
+        eng.step(period)
+        th = eng.thermo()
+        temps.append(th["mv2"] / (3 * n))
+        vcms.append(th["momentum"] / th["mass"])
+    temps, vcms = np.array(temps), np.array(vcms)
+    c = len(temps)
+    # instantaneous values at the end (4.5 sigma)
+    assert np.max(np.abs(vcms[-1])) < 4.5 * np.sqrt(T / (n - 1))
+    assert abs(temps[-1] - T) / T < 4.5 * np.sqrt(2.0 / (3 * n)) / T
+    # averages over the run
+    assert np.max(np.abs(vcms.mean(axis=0))) < 4.5 * np.sqrt(T / (n * c - 1))
+    assert abs(temps.mean() - T) / T < 4.5 * np.sqrt(2.0 / (3 * n * (c - 1))) / T
+    # kinetic specific heat from temperature fluctuations: 3/2
+    cv = 1.5 ** 2 * n * temps.var(ddof=1)
+    cv_tol = 4.5 * np.sqrt(1.5 * (3 + 6.0 / n) / c) / 1.5
+    print("andersen: <T> %.5f, c_V %.4f (tol %.3f), %d samples" % (temps.mean(), cv, cv_tol, c))
+    assert abs(cv - 1.5) / 1.5 < cv_tol
+    eng.close()
