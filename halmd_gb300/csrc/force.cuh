@@ -516,6 +516,35 @@ __device__ __forceinline__ void fold_lanes2(const ForceAcc2& B, ForceAcc& A)
     }
 }
 
+// The list is a stream read once per launch: it is loaded without
+// allocating in L1, which then keeps the neighbour positions the gathers
+// reuse (HMD_FORCE_LIST_NOALLOC 0: ordinary read-only loads)
+#ifndef HMD_FORCE_LIST_NOALLOC
+#define HMD_FORCE_LIST_NOALLOC 1
+#endif
+__device__ __forceinline__ uint4 ld_list(const uint4* p)
+{
+    if (!HMD_FORCE_LIST_NOALLOC) return __ldg(p);
+    uint4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint2 ld_list(const uint2* p)
+{
+    if (!HMD_FORCE_LIST_NOALLOC) return __ldg(p);
+    uint2 v;
+    asm("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_list(const uint32_t* p)
+{
+    if (!HMD_FORCE_LIST_NOALLOC) return __ldg(p);
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
 // E list entries per lane and block, read with one vector load
 template <int E> struct IdxVec;
 template <> struct IdxVec<1> { using T = uint32_t; };
@@ -551,7 +580,7 @@ __device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t 
     if (NS1) p1 = spp[0];
     const uint32_t nblk = (cnt + LB - 1) / LB;
     for (uint32_t b = 0; b < nblk; ++b, lst += step) {
-        const V jv = __ldg(lst);
+        const V jv = ld_list(lst);
         float4 rj[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -591,16 +620,16 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
     if (NS1) p1 = pack_params(spp[0], spp[0]);
     const uint32_t nblk = (cnt + LB - 1) / LB;
     V jv;
-    if (HMD_FORCE_PREFETCH && nblk > 0) jv = __ldg(lst);
+    if (HMD_FORCE_PREFETCH && nblk > 0) jv = ld_list(lst);
     for (uint32_t b = 0; b < nblk; ++b, lst += step) {
         // the list stream comes from HBM: the next block's indices are
         // loaded one iteration ahead of their gathers
         V jn;
         if (HMD_FORCE_PREFETCH) {
             jn = jv;
-            if (b + 1 < nblk) jn = __ldg(lst + step);
+            if (b + 1 < nblk) jn = ld_list(lst + step);
         } else {
-            jv = __ldg(lst);
+            jv = ld_list(lst);
         }
         float4 rj[E];
         bool in[E];
@@ -806,7 +835,7 @@ __device__ __forceinline__ void force_blocks_pot(const Dev& d, uint32_t i, uint3
     const PairParam* row = spp + a * ns;
     const uint32_t nblk = (cnt + LB - 1) / LB;
     for (uint32_t b = 0; b < nblk; ++b, lst += step) {
-        const V jv = __ldg(lst);
+        const V jv = ld_list(lst);
         float4 rj[E];
         bool in[E];
 #pragma unroll
