@@ -144,3 +144,46 @@ def test_mqd_vacf_blocking_scheme():
     assert vmean[0, 0, 0] > 0 and vmean[0, 0, 0] > vmean[0, block - 1, 0]
     dyn.close()
     eng.close()
+
+
+def test_fcc_static_structure_factor():
+    # test/unit/observables/ssf.cpp:100-300: the density modes of a perfect
+    # fcc lattice in a rectangular box; S(q) = N for wavevectors whose
+    # (h, k, l) are integers of one parity, 0 otherwise.  The intermediate
+    # scattering function at lag 0 is S(k) averaged over each shell.
+    ncell = np.array([4, 8, 5])
+    a = (4 / 0.8) ** (1 / 3)
+    box = a * ncell
+    n = int(4 * np.prod(ncell))
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    cells = np.stack(np.meshgrid(*(np.arange(k) for k in ncell), indexing="ij"), -1).reshape(-1, 1, 3)
+    r = ((cells + basis[None] + 0.25) * a - 0.5 * box).reshape(-1, 3)   # lattice.cpp offset of 1/4
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, box, r_cut=2.5, skin=0.3, timestep=0.001))
+    eng.commit()
+    eng.set("position", r)
+    q_lat = 2 * np.pi / a
+    wavenumber = sorted(set([q_lat / k for k in ncell] + [np.sqrt(m) * q_lat for m in (1, 2, 3, 4, 5, 6, 8, 9, 10, 12)]))
+    dyn = hg.Dynamics(eng, 0.001, 0.001, block_size=2)
+    k_isf = dyn.add_isf(wavenumber, tolerance=1e-3, max_count=6, first=0, last=n, norm=n)
+    dyn.sample()
+    dyn.finalise()
+    mean, err, cnt = dyn.result(k_isf)
+    s_gpu = mean[0, 0, :]
+
+    Lf = np.array(eng.info().box_f32, dtype=np.float32).astype(np.float64)
+    q, shells = oracle.wavevectors(wavenumber, Lf, 1e-3, 6)
+    keep = [s for s in range(len(shells)) if shells[s, 1] > shells[s, 0]]
+    np.testing.assert_allclose(dyn.wavenumbers(k_isf), np.array(wavenumber)[keep])
+    s_ref = []
+    for s in keep:
+        qs = q[shells[s, 0]:shells[s, 1]]
+        hkl_ncell = np.rint(np.abs(qs) * Lf / (2 * np.pi)).astype(int)
+        lattice = np.all(hkl_ncell % ncell == 0, axis=1)
+        n_odd = np.sum((hkl_ncell // ncell) % 2, axis=1)
+        s_ref.append(n * np.mean(lattice & ((n_odd == 0) | (n_odd == 3))))
+    s_ref = np.array(s_ref)
+    print("S(k):", np.round(s_gpu, 4), "reference", s_ref)
+    assert np.any(s_ref > 0) and np.any(s_ref == 0)
+    np.testing.assert_allclose(s_gpu, s_ref, rtol=1e-4, atol=1e-4 * n)
+    eng.close()
