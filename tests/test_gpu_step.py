@@ -264,17 +264,26 @@ def test_andersen_collisions():
     eng.close()
 
 
-def test_graph_step_equals_module_calls():
-    a, r, v, L = lj_engine()
-    b, *_ = lj_engine()
-    a.step(7)
-    for _ in range(7):
+@pytest.mark.parametrize("steps", [7, 237])
+@pytest.mark.parametrize("system", ["lj", "ka_andersen"])
+def test_graph_step_equals_module_calls(system, steps):
+    # 237 steps: two 100-step chunks, three 10-step chunks and single steps,
+    # list rebuilds on the way; the chunks fuse the finalize of step k with
+    # the integrate of step k + 1
+    def make():
+        if system == "lj":
+            return lj_engine()[0]
+        return ka_engine(integrator="andersen", temperature=0.7, collision_rate=20.0, seed=99)[0]
+    a, b = make(), make()
+    a.step(steps)
+    for _ in range(steps):
         b.integrate()
         b.force()
         b.finalize()
     for name in ("position", "velocity", "image"):
         assert np.array_equal(a.get(name), b.get(name)), name
-    assert a.info().step == b.info().step == 7
+    assert a.info().step == b.info().step == steps
+    assert a.info().rebuilds == b.info().rebuilds
     a.close()
     b.close()
 
