@@ -134,6 +134,8 @@ def load():
         "hmd_max_displacement": (I, [P, U, P]),
         "hmd_thermo": (I, [P, U, P]),
         "hmd_integrator_state": (I, [P, U, P]),
+        "hmd_positions_lattice": (I, [P, U, P]),
+        "hmd_velocities_boltzmann": (I, [P, U, D, ctypes.c_uint64]),
         "hmd_neighbour_lists": (I, [P, U, P, P, U]),
         "hmd_hilbert_keys": (I, [P, U, P]),
         "hmd_profile_enable": (I, [P, I]),
@@ -381,6 +383,15 @@ class Engine:
         self._check(self._L.hmd_thermo(self._h, s, _ptr(out)))
         return dict(mv2=out[0], momentum=out[1:4].copy(), mass=out[4], epot=out[5], virial=out[6],
                     stress=out[7:13].copy(), count=out[13])
+
+    def lattice(self, slab=None, s=0):
+        """positions.lattice: fcc sites filling the slab (fractions of the box edges) at the box centre."""
+        sl = None if slab is None else np.ascontiguousarray(np.broadcast_to(np.asarray(slab, dtype=np.float64), (3,)))
+        self._check(self._L.hmd_positions_lattice(self._h, s, _ptr(sl) if sl is not None else None))
+
+    def boltzmann(self, temperature, seed=0, s=0):
+        """velocities.boltzmann set(): Maxwell-Boltzmann velocities at temperature, zero momentum."""
+        self._check(self._L.hmd_velocities_boltzmann(self._h, s, float(temperature), int(seed)))
 
     def integrator_state(self, s=0):
         """Chain positions xi, velocities v_xi and energy per particle (Nose-Hoover);

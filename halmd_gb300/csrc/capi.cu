@@ -257,6 +257,18 @@ int hmd_thermo(hmd_engine* h, uint32_t sys, double* out)
     return guard(h, [&] { h->e->thermo(sys, out); });
 }
 
+int hmd_positions_lattice(hmd_engine* h, uint32_t sys, const double* slab)
+{
+    ENGINE_OR_FAIL(h);
+    return guard(h, [&] { h->e->lattice(sys, slab); });
+}
+
+int hmd_velocities_boltzmann(hmd_engine* h, uint32_t sys, double temperature, uint64_t seed)
+{
+    ENGINE_OR_FAIL(h);
+    return guard(h, [&] { h->e->boltzmann(sys, temperature, seed); });
+}
+
 int hmd_integrator_state(hmd_engine* h, uint32_t sys, double* out)
 {
     ENGINE_OR_FAIL(h);

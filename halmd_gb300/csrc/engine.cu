@@ -770,6 +770,73 @@ std::vector<uint32_t> Engine::slots_of(uint32_t s)
     return r;
 }
 
+// positions.lattice (mdsim/host/positions/lattice.cpp:63-175): fcc sites in
+// the slab (fraction of each box edge) at the centre of the box, with the
+// smallest lattice constant that gives enough sites, the vacancies spread
+// evenly; the image counters are zeroed.  Sites are generated on the device.
+void Engine::lattice(uint32_t s, const double* slab_in)
+{
+    check_sys(s);
+    const SysHost& h = sys_[s];
+    const uint32_t n = h.P.n;
+    double slab[3] = {1.0, 1.0, 1.0};
+    if (slab_in)
+        for (int q = 0; q < 3; ++q) slab[q] = slab_in[q];
+    for (int q = 0; q < 3; ++q)   // lattice.cpp:52-57
+        if (!(slab[q] > 0 && slab[q] <= 1)) throw Error(HMD_ERR_STATE, "slab extents must be a fraction between 0 and 1");
+    double length[3], offset[3];
+    for (int q = 0; q < 3; ++q) {
+        length[q] = h.desc.box[q] * slab[q];
+        offset[q] = -length[q] / 2;
+    }
+    // lattice.cpp:124-146: the smallest lattice distance a with
+    // 4 prod floor(L_i / a) >= n, growing the cell counts from the cube root
+    const double u = 4;
+    double a = std::pow(length[0] * length[1] * length[2] / std::ceil(n / u), 1.0 / 3);
+    uint32_t c[3];
+    for (int q = 0; q < 3; ++q) c[q] = (uint32_t)(length[q] / a);
+    while ((double)n > u * (double)c[0] * c[1] * c[2]) {
+        double t = 0;
+        for (int q = 0; q < 3; ++q) t = std::max(t, length[q] / (c[q] + 1));
+        a = t;
+        bool same = true;
+        for (int q = 0; q < 3; ++q) {
+            const uint32_t m = std::max(c[q], (uint32_t)(length[q] / a));
+            same = same && m == c[q];
+            c[q] = m;
+        }
+        if (same)
+            for (int q = 0; q < 3; ++q) c[q] += 1;
+    }
+    const uint64_t N = 4ull * c[0] * c[1] * c[2];
+    // lattice.cpp:150-165: a vacancy every `skip` sites
+    const uint32_t skip = (N > n) ? (uint32_t)std::ceil((double)N / (double)(N - n)) : 0u;
+    HMD_CUDA(cudaMemsetAsync(img_.p + h.P.off, 0, h.P.A * sizeof(float4), stream_));
+    stage(3 * (size_t)n);
+    launch_lattice(io_.p, n, c, a, offset, skip, stream_);
+    launch_set_vector(dev(), s, n, 0, ds(), io_.p, stream_);
+    HMD_CUDA(cudaGetLastError());
+    sync();
+    forces_valid_ = false;
+    request_rebuild(s);
+}
+
+// velocities.boltzmann set() (mdsim/gpu/velocities/boltzmann.cpp): each
+// component N(0, sqrt(T)) / sqrt(m), then the centre-of-mass velocity
+// removed; drawn on the device from a Philox stream keyed by (seed, tag)
+void Engine::boltzmann(uint32_t s, double temperature, uint64_t seed)
+{
+    check_sys(s);
+    if (!(temperature >= 0)) throw Error(HMD_ERR_INVALID, "temperature must be non-negative");
+    const uint32_t n = sys_[s].P.n;
+    const size_t blocks = (n + 255) / 256;
+    stage(3 * (size_t)n + 4 * blocks + 3);
+    launch_boltzmann(dev(), s, n, temperature, seed, io_.p, io_.p + 3 * (size_t)n, stream_);
+    launch_set_vector(dev(), s, n, 1, ds(), io_.p, stream_);
+    HMD_CUDA(cudaGetLastError());
+    sync();
+}
+
 // staging buffer of the device-side set / get conversions (grows on demand)
 void Engine::stage(size_t doubles)
 {

@@ -110,6 +110,8 @@ public:
     double max_displacement(uint32_t s);
     void thermo(uint32_t s, double* out);
     void integrator_state(uint32_t s, double* out);
+    void lattice(uint32_t s, const double* slab);
+    void boltzmann(uint32_t s, double temperature, uint64_t seed);
     void neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint32_t maxn);
     void hilbert_keys(uint32_t s, uint32_t* keys);
     void profile_enable(bool on);

@@ -58,6 +58,12 @@ void launch_density_modes(const Dev& d, const uint32_t* range, uint32_t nrange, 
 // 3 force, 4 image (arrays of 3 n doubles on the device)
 void launch_set_vector(const Dev& d, uint32_t s, uint32_t n, int what, bool ds, const double* in, cudaStream_t st);
 void launch_get_vector(const Dev& d, uint32_t s, uint32_t n, int what, double* out, cudaStream_t st);
+// set-up (kernels_io.cu): fcc lattice positions and Maxwell-Boltzmann
+// velocities of tags < n into out[3 n] on the device
+void launch_lattice(double* out, uint32_t n, const uint32_t cells[3], double a, const double offset[3], uint32_t skip,
+                    cudaStream_t st);
+void launch_boltzmann(const Dev& d, uint32_t s, uint32_t n, double T, uint64_t seed, double* out, double* scratch,
+                      cudaStream_t st);
 
 // MSD of one sample pair with fixed scratch and no allocation (msd_noalloc.cu)
 void msd_pair_noalloc(const double* origin, const double* position, uint32_t count, double* out, cudaStream_t st);

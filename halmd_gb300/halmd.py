@@ -79,6 +79,9 @@ class _Script:
                 if name in p._pending:
                     eng.set(name, p._pending[name], p._index)
             p._pending.clear()
+            for call in p._setup:
+                call(eng, p._index)
+            p._setup.clear()
         self.engine = eng
         for b in self.blocking:
             b._attach()
@@ -157,6 +160,7 @@ class particle:
         self.memory = "gpu"
         self.data = _Data(self)
         self._pending = {}
+        self._setup = []       # set-up calls (lattice, Boltzmann) waiting for the engine
         self._index = None
         self._box = self._potential = self._neighbour = self._integrator = None
         _script.particles.append(self)
@@ -339,8 +343,42 @@ def euler(args=None, **kw):
     return _Integrator("euler", _args(args, kw))
 
 
+class _SetUp:
+    def __init__(self, particle, call):
+        self.particle, self._call = particle, call
+
+    def set(self):
+        """Run on the device now, or when the engine is built."""
+        if _script.committed():
+            self._call(_script.engine, self.particle._index)
+        else:
+            self.particle._setup.append(self._call)
+
+
+def lattice(args=None, **kw):
+    """halmd.mdsim.positions.lattice{box, particle, slab = {1, 1, 1}}:set(): fcc sites filling the slab
+    (mdsim/host/positions/lattice.cpp; positions/lattice.lua.in)."""
+    a = _args(args, kw)
+    slab = a.get("slab")
+    p = a["particle"]
+    if "box" in a:
+        p._box = a["box"]
+    return _SetUp(p, lambda eng, s: eng.lattice(slab, s))
+
+
+def boltzmann(args=None, **kw):
+    """halmd.mdsim.velocities.boltzmann{particle, temperature}:set(): Maxwell-Boltzmann velocities
+    with zero total momentum (velocities/boltzmann.lua.in)."""
+    a = _args(args, kw)
+    if "temperature" not in a:
+        raise ValueError("missing keyword argument 'temperature'")
+    T, seed = float(a["temperature"]), int(a.get("seed", 0))
+    return _SetUp(a["particle"], lambda eng, s: eng.boltzmann(T, seed, s))
+
+
 mdsim = _Namespace(
     box=box, particle=particle, neighbour=neighbour,
+    positions=_Namespace(lattice=lattice), velocities=_Namespace(boltzmann=boltzmann),
     potentials=_Namespace(pair=_Namespace(lennard_jones=lennard_jones, mie=mie, morse=morse, power_law=power_law)),
     forces=_Namespace(pair=pair),
     integrators=_Namespace(verlet=verlet, verlet_nvt_andersen=verlet_nvt_andersen,

@@ -253,6 +253,23 @@ HMD_API int hmd_max_displacement(hmd_engine* engine, uint32_t sys, double* displ
 HMD_API int hmd_thermo(hmd_engine* engine, uint32_t sys, double* out);
 
 /*
+ * positions.lattice (mdsim/host/positions/lattice.cpp:63-175,
+ * gpu/positions/lattice_kernel.cu): place the particles of a committed
+ * system on an fcc lattice filling the slab (slab[3]: fraction of each box
+ * edge at the centre of the box; NULL = the whole box) with the smallest
+ * lattice constant that gives enough sites, vacancies spread evenly, image
+ * counters zeroed.  HMD_ERR_STATE for slab extents outside (0, 1].
+ */
+HMD_API int hmd_positions_lattice(hmd_engine* engine, uint32_t sys, const double* slab);
+/*
+ * velocities.boltzmann set() (mdsim/gpu/velocities/boltzmann.cpp,
+ * boltzmann_kernel.cu:47-140): each velocity component N(0, sqrt(T)) divided
+ * by sqrt(m), then the centre-of-mass velocity removed.  The random stream is
+ * Philox4x32-10 keyed by (seed, tag) (the reference draws from rand48).
+ */
+HMD_API int hmd_velocities_boltzmann(hmd_engine* engine, uint32_t sys, double temperature, uint64_t seed);
+
+/*
  * Thermostat state of a system (verlet_nvt_hoover.cpp:252-283 properties
  * `position`, `velocity`, `internal_energy`): out[0..1] chain positions xi,
  * out[2..3] chain velocities v_xi, out[4] the chain's energy per particle

@@ -66,6 +66,9 @@ def lib():
         L.orc_wavevectors.argtypes = [I, P, P, D, I, P, I, P, P]
         L.orc_fcc_lattice.argtypes = [I, D, P]
         L.orc_md_run.argtypes = [I, P, P, P, P, P, P, P, D, D, I, D, D, ctypes.c_uint64, P]
+        L.orc_lattice.argtypes = [I, P, P, P]
+        L.orc_lattice.restype = ctypes.c_long
+        L.orc_boltzmann.argtypes = [I, P, D, ctypes.c_uint64, P]
         L.orc_md_run_any.argtypes = [I, P, P, P, P, P, P, P, D, D, I, I, D, D, D, ctypes.c_uint64, P, P]
         L.orc_minimize.argtypes = [I, P, P, P, P, P, D, I, D, D, P]
         L.orc_tcf.argtypes = [I, I, I, P, P, P]
@@ -322,6 +325,22 @@ def wavevectors(radii, box_length, tolerance, max_count, filt=(1, 1, 1), max_out
     total = lib().orc_wavevectors(radii.size, _p(radii), _p(unit), float(tolerance), int(max_count), _p(filt),
                                   max_out, _p(q), _p(shell))
     return q[:total], shell
+
+
+def lattice(n, box, slab=(1.0, 1.0, 1.0)):
+    """positions.lattice: (positions [n, 3], number of sites)."""
+    out = np.zeros((n, 3))
+    box = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
+    slab = np.ascontiguousarray(np.broadcast_to(np.asarray(slab, dtype=np.float64), (3,)))
+    sites = lib().orc_lattice(int(n), _p(box), _p(slab), _p(out))
+    return out, int(sites)
+
+
+def boltzmann(mass, temperature, seed):
+    mass = np.ascontiguousarray(mass, dtype=np.float64)
+    out = np.zeros((mass.size, 3))
+    lib().orc_boltzmann(int(mass.size), _p(mass), float(temperature), int(seed), _p(out))
+    return out
 
 
 def fcc_lattice(ncell, L):

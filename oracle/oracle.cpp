@@ -1128,6 +1128,75 @@ ORC_API void orc_fcc_lattice(int ncell, double L, double* r)
     }
 }
 
+/*
+ * positions.lattice set() (mdsim/host/positions/lattice.cpp:63-175 with
+ * mdsim/positions/lattice_primitive.hpp close_packed_lattice): fcc sites in
+ * the slab (fractions of the box edges) at the centre of the box, the smallest
+ * lattice distance with enough sites, a vacancy every `skip` sites.
+ * out[3 n]; returns the number of sites.
+ */
+ORC_API long orc_lattice(int n, const double* box, const double* slab, double* out)
+{
+    double length[3], offset[3];
+    for (int q = 0; q < 3; ++q) {
+        length[q] = box[q] * slab[q];
+        offset[q] = -length[q] / 2;
+    }
+    const double u = 4;
+    double V = length[0] * length[1] * length[2] / std::ceil(n / u);
+    double a = std::pow(V, 1.0 / 3);
+    unsigned c[3];
+    for (int q = 0; q < 3; ++q) c[q] = (unsigned)(length[q] / a);
+    while (n > u * c[0] * c[1] * c[2]) {
+        double t[3];
+        for (int q = 0; q < 3; ++q) t[q] = length[q] / (c[q] + 1);
+        a = *std::max_element(t, t + 3);
+        unsigned m[3] = {c[0], c[1], c[2]};
+        for (int q = 0; q < 3; ++q) c[q] = std::max(m[q], (unsigned)(length[q] / a));
+        if (m[0] == c[0] && m[1] == c[1] && m[2] == c[2])
+            for (int q = 0; q < 3; ++q) c[q] += 1;
+    }
+    const unsigned long N = 4ul * c[0] * c[1] * c[2];
+    const unsigned long skip = (N > (unsigned long)n) ? (unsigned long)std::ceil((double)N / (N - n)) : 0;
+    unsigned long i = 0;
+    for (int t = 0; t < n; ++t, ++i) {
+        if (skip && i % skip == skip - 1) ++i;
+        const unsigned long cell = i >> 2, b = i & 3;
+        const double r[3] = {(double)(cell % c[0]) + (double)((((b ^ (b >> 1)) & 1) * 2 + 1)) / 4,
+                             (double)((cell / c[0]) % c[1]) + (double)(((b & 1) * 2 + 1)) / 4,
+                             (double)(cell / ((unsigned long)c[0] * c[1])) + (double)(((b & 2) + 1)) / 4};
+        for (int q = 0; q < 3; ++q) out[3 * t + q] = r[q] * a + offset[q];
+    }
+    return (long)N;
+}
+
+/*
+ * velocities.boltzmann set() as the engine draws it: each component
+ * N(0, sqrt(T)) / sqrt(m) by Box-Muller in FP64 on the Philox4x32-10 words of
+ * (tag, 0, 0, 'BOLT') under the seed, then the centre-of-mass velocity
+ * removed (gpu/velocities/boltzmann_kernel.cu:47-140 draws from rand48).
+ */
+ORC_API void orc_boltzmann(int n, const double* mass, double T, uint64_t seed, double* out)
+{
+    const u32 key[2] = {(u32)seed, (u32)(seed >> 32)};
+    double mv[3] = {0, 0, 0}, msum = 0;
+    for (int t = 0; t < n; ++t) {
+        u32 ctr[4] = {(u32)t, 0u, 0u, 0x424F4C54u}, w[4];
+        orc_philox4x32_10(ctr, key, w);
+        const double inv = 1.0 / 4294967296.0;
+        const double u0 = (w[0] + 0.5) * inv, u1 = (w[1] + 0.5) * inv, u2 = (w[2] + 0.5) * inv, u3 = (w[3] + 0.5) * inv;
+        const double r0 = std::sqrt(-2.0 * std::log(u0)), r1 = std::sqrt(-2.0 * std::log(u2));
+        const double f = std::sqrt(T / mass[t]);
+        out[3 * t + 0] = f * r0 * std::cos(2 * M_PI * u1);
+        out[3 * t + 1] = f * r0 * std::sin(2 * M_PI * u1);
+        out[3 * t + 2] = f * r1 * std::cos(2 * M_PI * u3);
+        for (int q = 0; q < 3; ++q) mv[q] += mass[t] * out[3 * t + q];
+        msum += mass[t];
+    }
+    for (int t = 0; t < n; ++t)
+        for (int q = 0; q < 3; ++q) out[3 * t + q] -= mv[q] / msum;
+}
+
 /* ------------------------------------------------------------------------ */
 /* the host backend's MD loop in FP64 (the timed CPU baseline)                */
 /* ------------------------------------------------------------------------ */

@@ -5,6 +5,7 @@ import pytest
 
 import halmd_gb300 as hg
 from halmd_gb300 import halmd
+import oracle
 from _systems import lj_system
 
 pytestmark = pytest.mark.gpu
@@ -69,4 +70,49 @@ def test_facade_script_equals_engine_calls():
     assert abs(thermo.potential_energy() - t["epot"] / n) < 1e-15
     dyn.close()
     eng.close()
+    halmd.reset()
+
+
+def test_lattice_and_boltzmann_set_up():
+    # positions.lattice and velocities.boltzmann on the device against the oracle
+    import halmd_gb300 as hg
+    n, box = 3000, np.array([12.0, 20.0, 12.5])
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, box, r_cut=2.5, skin=0.3, timestep=0.001))
+    eng.commit()
+    eng.set("position", np.zeros((n, 3)) + 0.1)
+    eng.lattice(slab=[1.0, 0.8, 1.0])
+    ref, sites = oracle.lattice(n, box, [1.0, 0.8, 1.0])
+    np.testing.assert_allclose(eng.get("position"), ref, rtol=0, atol=1e-12)
+    assert np.all(eng.get("image") == 0)
+    mass = np.linspace(0.5, 2.0, n).astype(np.float32).astype(np.float64)   # the engine keeps floats
+    eng.set("mass", mass)
+    eng.boltzmann(1.3, seed=11)
+    v = eng.get("velocity")
+    np.testing.assert_allclose(v, oracle.boltzmann(mass, 1.3, 11), rtol=0, atol=1e-12)
+    assert np.max(np.abs((mass[:, None] * v).sum(axis=0))) < 1e-9
+    temp = np.sum(mass[:, None] * v * v) / (3 * n)
+    assert abs(temp - 1.3) / 1.3 < 4.5 * np.sqrt(2.0 / (3 * n))
+    eng.step(20)
+    assert np.all(np.isfinite(eng.get("position")))
+    eng.close()
+
+
+def test_facade_lattice_boltzmann_script():
+    from halmd_gb300 import halmd
+    halmd.reset()
+    box = halmd.mdsim.box(length=[16.796, 16.796, 16.796])
+    p = halmd.mdsim.particle(particles=4000)
+    halmd.mdsim.positions.lattice(box=box, particle=p).set()
+    halmd.mdsim.velocities.boltzmann(particle=p, temperature=1.5).set()
+    pot = halmd.mdsim.potentials.pair.lennard_jones().truncate(cutoff=2.5)
+    halmd.mdsim.forces.pair(box=box, particle=p, potential=pot, neighbour={"skin": 0.3})
+    halmd.mdsim.integrators.verlet(box=box, particle=p, timestep=0.005)
+    r = p.get("position")
+    ref, _ = oracle.lattice(4000, [16.796] * 3)
+    np.testing.assert_allclose(r, ref, atol=1e-12)
+    thermo = halmd.observables.thermodynamics(box=box, group=p)
+    assert abs(thermo.temperature() - 1.5) < 4.5 * 1.5 * np.sqrt(2.0 / 12000)
+    halmd.observables.sampler.run(10)
+    assert abs(thermo.center_of_mass_velocity()).max() < 1e-9
     halmd.reset()

@@ -120,3 +120,18 @@ def test_philox_known_answers():
     ]
     for ctr, key, want in cases:
         assert oracle.philox4x32_10(ctr, key).tolist() == list(want)
+
+
+def test_lattice_restatement():
+    # mdsim/host/positions/lattice.cpp:63-175: n = 4 k^3 in a cube fills k^3
+    # cells of edge L / k exactly; other counts leave vacancies spread evenly
+    k, L = 6, 10.0
+    r, sites = oracle.lattice(4 * k ** 3, [L, L, L])
+    assert sites == 4 * k ** 3
+    a = L / k
+    assert np.allclose(r.min(axis=0), -L / 2 + a / 4) and np.allclose(r.max(axis=0), L / 2 - a / 4)
+    d = np.linalg.norm(r[None, :40] - r[:40, None], axis=-1) + np.eye(40) * 1e9
+    assert np.isclose(d.min(), a / np.sqrt(2))
+    r, sites = oracle.lattice(1000, [7.9, 15.8, 7.99], slab=[1.0, 0.5, 1.0])
+    assert sites >= 1000 and np.unique(r, axis=0).shape[0] == 1000
+    assert np.all(np.abs(r[:, 1]) <= 15.8 * 0.25)
