@@ -576,8 +576,28 @@ class blocking_scheme:
             self._dyn.close()
 
 
+class phase_space:
+    """halmd.observables.phase_space{box, group}: acquire() a tag-ordered sample of the
+    group's particles (observables/phase_space.lua.in, gpu/phase_space.cpp), set(sample)."""
+
+    FIELDS = ("position", "velocity", "image", "species", "mass")
+
+    def __init__(self, args=None, **kw):
+        a = _args(args, kw)
+        self.box = a["box"]
+        self.group = a.get("group", a.get("particle"))
+
+    def acquire(self):
+        return {name: self.group.get(name) for name in self.FIELDS}
+
+    def set(self, sample):
+        for name in ("species", "mass", "position", "image", "velocity"):
+            if name in sample:
+                self.group.set(name, sample[name])
+
+
 observables = _Namespace(
-    thermodynamics=thermodynamics, sampler=sampler,
+    thermodynamics=thermodynamics, sampler=sampler, phase_space=phase_space,
     dynamics=_Namespace(blocking_scheme=blocking_scheme, mean_square_displacement=mean_square_displacement,
                         mean_quartic_displacement=mean_quartic_displacement,
                         velocity_autocorrelation=velocity_autocorrelation,

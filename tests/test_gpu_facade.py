@@ -116,3 +116,25 @@ def test_facade_lattice_boltzmann_script():
     halmd.observables.sampler.run(10)
     assert abs(thermo.center_of_mass_velocity()).max() < 1e-9
     halmd.reset()
+
+
+def test_phase_space_acquire_and_set():
+    from halmd_gb300 import halmd
+    halmd.reset()
+    box = halmd.mdsim.box(length=[12.0, 12.0, 12.0])
+    p = halmd.mdsim.particle(particles=500, species=2)
+    halmd.mdsim.positions.lattice(box=box, particle=p).set()
+    halmd.mdsim.velocities.boltzmann(particle=p, temperature=1.0, seed=3).set()
+    pot = halmd.mdsim.potentials.pair.lennard_jones(epsilon=[[1, 1.5], [1.5, 0.5]]).truncate(cutoff=2.5)
+    halmd.mdsim.forces.pair(box=box, particle=p, potential=pot)
+    halmd.mdsim.integrators.verlet(box=box, particle=p, timestep=0.002)
+    ps = halmd.observables.phase_space(box=box, group=p)
+    s0 = ps.acquire()
+    halmd.observables.sampler.run(50)
+    s1 = ps.acquire()
+    assert not np.array_equal(s0["position"], s1["position"])
+    ps.set(s0)                                   # back to the first sample
+    s2 = ps.acquire()
+    for name in ("position", "velocity", "species", "mass"):
+        np.testing.assert_array_equal(s2[name], s0[name])
+    halmd.reset()
