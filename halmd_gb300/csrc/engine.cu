@@ -562,6 +562,8 @@ void Engine::commit()
         sync();
     }
     committed_ = true;
+    grid_slots_ = grid_cells_ = 0;
+    update_grid_extent();
     for (uint32_t s = 0; s < table_size_; ++s)
         if (!capacity_ || sys_[s].used) install(s);
     sync();
@@ -654,6 +656,7 @@ uint32_t Engine::add_live_system(const hmd_system_desc& d)
         throw Error(HMD_ERR_NOMEM, "no room in the reserved capacity");
     }
     install(s);
+    update_grid_extent();
     return s;
 }
 
@@ -681,6 +684,40 @@ void Engine::remove_system(uint32_t s)
     sync();
     unplace(s);
     sys_[s] = SysHost();
+    update_grid_extent();
+}
+
+// Launch-grid extents (Dev::S_grid, cells_grid, tiles_grid).  A fixed layout
+// covers everything.  With a reserved capacity the grids cover the slots and
+// cells below the high-water mark of the systems present (first-fit
+// placement keeps them low), rounded up to a power of two, instead of the
+// whole reservation: they grow as soon as a system needs it and shrink once
+// the mark falls below a quarter, and the captured step graphs, which carry
+// the grid sizes, are recaptured on a change.
+void Engine::update_grid_extent()
+{
+    uint32_t slots = S_, cells = total_cells_;
+    if (capacity_) {
+        uint32_t hs = SORT_TILE, hc = 64;
+        for (const SysHost& h : sys_) {
+            if (!h.used) continue;
+            hs = std::max(hs, h.P.off + h.P.A);
+            hc = std::max(hc, h.P.cell_off + h.P.ncells);
+        }
+        auto bucket = [](uint32_t need, uint32_t cur, uint32_t full) {
+            uint32_t b = 1;
+            while (b < need) b <<= 1;
+            b = std::min(b, full);
+            return (need > cur || (uint64_t)need * 4 <= cur) ? b : cur;
+        };
+        slots = bucket(hs, grid_slots_, S_);
+        cells = bucket(hc, grid_cells_, total_cells_);
+    }
+    if (slots != grid_slots_ || cells != grid_cells_) {
+        grid_slots_ = slots;
+        grid_cells_ = cells;
+        destroy_graphs();
+    }
 }
 
 void Engine::capacity_info(uint64_t* out) const
@@ -729,6 +766,9 @@ Dev Engine::dev() const
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
     d.S = S_; d.nsys = table_size_;
+    d.S_grid = grid_slots_ ? grid_slots_ : S_;
+    d.cells_grid = grid_cells_ ? grid_cells_ : total_cells_;
+    d.tiles_grid = capacity_ ? d.S_grid / SORT_TILE : ntiles_;
     d.status = status_.p; d.done = done_.p; d.any_rebuild = any_rebuild_.p;
     d.key[0] = key0_.p; d.key[1] = key1_.p; d.val[0] = val0_.p; d.val[1] = val1_.p; d.hist = hist_.p;
     d.tiles = tiles_.p; d.ntiles = ntiles_;

@@ -990,7 +990,7 @@ __global__ void __launch_bounds__(128, HMD_FORCE_MINB) k_force(Dev d)
 template <int W, int E, int KIND>
 static void launch_force_shape(const Dev& d, bool aux, cudaStream_t st)
 {
-    const unsigned grid = (unsigned)((size_t)d.S * W / 128);
+    const unsigned grid = (unsigned)((size_t)d.S_grid * W / 128);
     if (aux) k_force<W, E, KIND, true><<<grid, 128, 0, st>>>(d);
     else k_force<W, E, KIND, false><<<grid, 128, 0, st>>>(d);
 }

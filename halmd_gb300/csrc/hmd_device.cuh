@@ -157,6 +157,10 @@ struct Dev {
     const PairParam* pair;
     const uint32_t* chunk_sys; // [S / CHUNK]
     uint32_t S, nsys;
+    // extents the launch grids cover (fixed layout: everything; capacity
+    // mode: the slots, sort tiles and cells below the high-water mark of the
+    // systems present, rounded up to a power of two)
+    uint32_t S_grid, cells_grid, tiles_grid;
     uint32_t* status;          // ST_* bits
     uint32_t* done;            // last-block ticket counter
     uint32_t* any_rebuild;      // [0] this step rebuilds, [1] count of steps that ran the rebuild chain

@@ -620,13 +620,13 @@ int radix_passes(uint32_t key_bits) { return (int)((key_bits + 7) / 8); }
 // val[passes % 2]
 void launch_sort(const Dev& d, int passes, cudaStream_t st)
 {
-    k_seg_keys<<<d.S / 256, 256, 0, st>>>(d);
+    k_seg_keys<<<d.S_grid / 256, 256, 0, st>>>(d);
     for (int p = 0; p < passes; ++p) {
         const uint32_t shift = 8u * p;
         const int cur = p & 1;
-        k_seg_hist<<<d.ntiles, RADIX_THREADS, 0, st>>>(d, d.key[cur], shift);
+        k_seg_hist<<<d.tiles_grid, RADIX_THREADS, 0, st>>>(d, d.key[cur], shift);
         k_seg_scan<<<d.nsys, 1024, 0, st>>>(d);
-        k_seg_scatter<<<d.ntiles, RADIX_THREADS, 0, st>>>(d, d.key[cur], d.val[cur], d.key[1 - cur], d.val[1 - cur],
+        k_seg_scatter<<<d.tiles_grid, RADIX_THREADS, 0, st>>>(d, d.key[cur], d.val[cur], d.key[1 - cur], d.val[1 - cur],
                                                           shift);
     }
 }
@@ -635,26 +635,26 @@ int sort_kernel_count(int passes) { return 1 + 3 * passes; }
 
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st)
 {
-    const unsigned grid = d.S / 256;
+    const unsigned grid = d.S_grid / 256;
     if (ds) { k_rearrange<true><<<grid, 256, 0, st>>>(d, perm); k_copyback<true><<<grid, 256, 0, st>>>(d); }
     else { k_rearrange<false><<<grid, 256, 0, st>>>(d, perm); k_copyback<false><<<grid, 256, 0, st>>>(d); }
 }
 
 void launch_binning(const Dev& d, cudaStream_t st)
 {
-    k_cell_clear<<<(d.total_cells + 255) / 256, 256, 0, st>>>(d);
-    k_bin<<<d.S / 256, 256, 0, st>>>(d);
-    k_cell_sort<<<(d.total_cells + 3) / 4, 128, 0, st>>>(d);
+    k_cell_clear<<<(d.cells_grid + 255) / 256, 256, 0, st>>>(d);
+    k_bin<<<d.S_grid / 256, 256, 0, st>>>(d);
+    k_cell_sort<<<(d.cells_grid + 3) / 4, 128, 0, st>>>(d);
 }
 
 void launch_neighbour(const Dev& d, cudaStream_t st)
 {
-    k_neighbour<<<d.S / 128, 128, 0, st>>>(d);
+    k_neighbour<<<d.S_grid / 128, 128, 0, st>>>(d);
 }
 
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
 {
-    k_hilbert_keys<<<(d.S + 255) / 256, 256, 0, st>>>(d, keys);
+    k_hilbert_keys<<<(d.S_grid + 255) / 256, 256, 0, st>>>(d, keys);
 }
 
 } // namespace hmd

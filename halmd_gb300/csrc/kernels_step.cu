@@ -290,14 +290,14 @@ __global__ void __launch_bounds__(256) k_thermo_reduce(Dev d)
 
 void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool use_handle, cudaStream_t st)
 {
-    const unsigned grid = d.S / 256;
+    const unsigned grid = d.S_grid / 256;
     if (ds) k_integrate<true, false><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
     else k_integrate<false, false><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
 }
 
 void launch_finalize_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, cudaStream_t st)
 {
-    const unsigned grid = d.S / 256;
+    const unsigned grid = d.S_grid / 256;
     if (ds) k_integrate<true, true><<<grid, 256, 0, st>>>(d, h, 1);
     else k_integrate<false, true><<<grid, 256, 0, st>>>(d, h, 1);
 }
@@ -328,7 +328,7 @@ void launch_force(const Dev& d, bool aux, cudaStream_t st)
 // thermostat, and the velocities are rescaled or shifted
 void launch_finalize(const Dev& d, bool ds, cudaStream_t st)
 {
-    const unsigned grid = d.S / 256;
+    const unsigned grid = d.S_grid / 256;
     const bool thermo = (d.integ_kinds & ((1u << INTEG_HOOVER) | (1u << INTEG_BOLTZMANN))) != 0u;
     if (!thermo) {
         if (ds) k_finalize<true, false><<<grid, 256, 0, st>>>(d);
@@ -347,7 +347,7 @@ void launch_finalize(const Dev& d, bool ds, cudaStream_t st)
 void launch_integrate_prepare(const Dev& d, cudaStream_t st)
 {
     if (!(d.integ_kinds & (1u << INTEG_HOOVER))) return;
-    k_moments<<<d.S / 256, 256, 0, st>>>(d);
+    k_moments<<<d.S_grid / 256, 256, 0, st>>>(d);
     k_thermostat<<<d.nsys, 256, 0, st>>>(d, 0);
 }
 
@@ -361,7 +361,7 @@ int step_kernel_count(const Dev& d)
 
 void launch_thermo(const Dev& d, cudaStream_t st)
 {
-    k_thermo_partial<<<d.S / 256, 256, 0, st>>>(d);
+    k_thermo_partial<<<d.S_grid / 256, 256, 0, st>>>(d);
     k_thermo_reduce<<<d.nsys, 256, 0, st>>>(d);
 }
 
