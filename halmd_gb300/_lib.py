@@ -332,13 +332,20 @@ class Engine:
         a = np.ascontiguousarray(array, dtype=dtype)
         self._check(self._L.hmd_set(self._h, s, name.encode(), _ptr(a), a.size))
 
-    def get(self, name, s=0):
+    def get(self, name, s=0, out=None):
+        """Tag-ordered array `name` of system s; into `out` (C-contiguous, right shape and
+        dtype, e.g. page-locked host memory) when given."""
         n = self.n(s)
         shapes = {"position": (n, 3), "unwrapped_position": (n, 3), "velocity": (n, 3), "image": (n, 3),
                   "force": (n, 3), "mass": (n,), "species": (n,), "potential_energy": (n,),
-                  "stress_pot": (n, 6), "reverse_id": (n,), "id": (self.info(s).slots,)}
+                  "stress_pot": (n, 6), "reverse_id": (n,), "id": (self.info(s).slots,) if out is None else out.shape}
         dtype = np.uint32 if name in ("species", "reverse_id", "id") else np.float64
-        a = np.zeros(shapes[name], dtype=dtype)
+        if out is not None:
+            if out.shape != shapes[name] or out.dtype != dtype or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous %s array of shape %s" % (np.dtype(dtype), shapes[name]))
+            a = out
+        else:
+            a = np.zeros(shapes[name], dtype=dtype)
         self._check(self._L.hmd_get(self._h, s, name.encode(), _ptr(a), a.size))
         return a
 

@@ -524,7 +524,9 @@ void Engine::commit()
     cell_sys_.alloc(std::max<uint32_t>(total_cells_, 1));
     chunk_sys_.alloc(S / CHUNK);
     key0_.alloc(S); key1_.alloc(S); val0_.alloc(S); val1_.alloc(S);
-    status_.alloc(1); done_.alloc(1); any_rebuild_.alloc(2);   // [0] this step rebuilds, [1] rebuild chains run
+    // done_: [0] last-block ticket counter, [1] flag of launch_check_finite;
+    // any_rebuild_: [0] this step rebuilds, [1] rebuild chains run
+    status_.alloc(1); done_.alloc(2); any_rebuild_.alloc(2);
     dsys_.alloc(table_size_); dst_.alloc(table_size_);
     dpair_.alloc((size_t)table_size_ * MAX_SPECIES * MAX_SPECIES);
     partial_.alloc((S / 256) * NTHERMO + 1); thermo_.alloc((size_t)table_size_ * NTHERMO);
@@ -895,11 +897,15 @@ void Engine::set(uint32_t s, const std::string& name, const void* host, size_t c
         // one copy into the staging buffer, then the conversion on the device
         need(3 * (size_t)n);
         const double* x = static_cast<const double*>(host);
-        if (name == "position")
-            for (size_t k = 0; k < 3 * (size_t)n; ++k)
-                if (!std::isfinite(x[k])) throw Error(HMD_ERR_INVALID, "positions must be finite");
         stage(3 * (size_t)n);
         HMD_CUDA(cudaMemcpyAsync(io_.p, x, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        if (name == "position") {
+            // checked on the device copy, before anything is stored
+            launch_check_finite(io_.p, 3 * (size_t)n, done_.p + 1, stream_);
+            uint32_t bad = 0;
+            download(done_, 1, 1, &bad);
+            if (bad) throw Error(HMD_ERR_INVALID, "positions must be finite");
+        }
         launch_set_vector(dev(), s, n, name == "position" ? 0 : 1, ds(), io_.p, stream_);
         HMD_CUDA(cudaGetLastError());
         sync();

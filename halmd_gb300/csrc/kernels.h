@@ -58,6 +58,8 @@ void launch_density_modes(const Dev& d, const uint32_t* range, uint32_t nrange, 
 // 3 force, 4 image (arrays of 3 n doubles on the device)
 void launch_set_vector(const Dev& d, uint32_t s, uint32_t n, int what, bool ds, const double* in, cudaStream_t st);
 void launch_get_vector(const Dev& d, uint32_t s, uint32_t n, int what, double* out, cudaStream_t st);
+// *flag = 1 if any of in[0, n) is not finite (a staged set array)
+void launch_check_finite(const double* in, size_t n, uint32_t* flag, cudaStream_t st);
 // set-up (kernels_io.cu): fcc lattice positions and Maxwell-Boltzmann
 // velocities of tags < n into out[3 n] on the device
 void launch_lattice(double* out, uint32_t n, const uint32_t cells[3], double a, const double offset[3], uint32_t skip,

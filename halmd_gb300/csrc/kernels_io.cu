@@ -6,6 +6,7 @@
 // a host loop and a write per array.  Double arithmetic uses the _rn
 // intrinsics: no contraction, the same rounding as the host formulas.
 #include "hmd_device.cuh"
+#include <algorithm>
 #include "kernels.h"
 
 namespace hmd {
@@ -197,6 +198,22 @@ void launch_boltzmann(const Dev& d, uint32_t s, uint32_t n, double T, uint64_t s
     k_boltzmann<<<grid, 256, 0, st>>>(d, s, T, (uint32_t)seed, (uint32_t)(seed >> 32), out, scratch);
     k_boltzmann_vcm<<<1, 256, 0, st>>>(scratch, grid, vcm);
     k_shift<<<grid, 256, 0, st>>>(out, n, vcm);
+}
+
+// flag[0] = 1 if any of the n values is not finite
+__global__ void __launch_bounds__(256) k_check_finite(const double* in, size_t n, uint32_t* flag)
+{
+    bool bad = false;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        bad |= !isfinite(in[k]);
+    if (__any_sync(0xFFFFFFFFu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
+void launch_check_finite(const double* in, size_t n, uint32_t* flag, cudaStream_t st)
+{
+    cudaMemsetAsync(flag, 0, sizeof(uint32_t), st);
+    const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 1024);
+    if (grid > 0) k_check_finite<<<grid, 256, 0, st>>>(in, n, flag);
 }
 
 void launch_set_vector(const Dev& d, uint32_t s, uint32_t n, int what, bool ds, const double* in, cudaStream_t st)

@@ -138,3 +138,25 @@ def test_phase_space_acquire_and_set():
     for name in ("position", "velocity", "species", "mass"):
         np.testing.assert_array_equal(s2[name], s0[name])
     halmd.reset()
+
+
+def test_non_finite_positions_are_rejected_unchanged():
+    # the check runs on the device copy before anything is stored
+    import halmd_gb300 as hg
+    r, v, L = lj_system(ncell=4)
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(r.shape[0], L, r_cut=2.5, skin=0.3, timestep=0.001))
+    eng.commit()
+    eng.set("position", r)
+    before = eng.get("position")
+    bad = r.copy()
+    bad[17, 1] = np.nan
+    with pytest.raises(hg.HmdError):
+        eng.set("position", bad)
+    bad[17, 1] = np.inf
+    with pytest.raises(hg.HmdError):
+        eng.set("position", bad)
+    np.testing.assert_array_equal(eng.get("position"), before)
+    out = np.empty_like(before)
+    assert eng.get("position", out=out) is out and np.array_equal(out, before)
+    eng.close()
