@@ -283,45 +283,77 @@ def cpu_baseline(w, r, v, species, L, budget_s=15.0):
                       (w["name"], steps)}
 
 
+def _ref_potential(w):
+    import oracle
+    if w["nspecies"] == 2:
+        return oracle.Potential(KA["eps"], KA["sigma"], w.get("rc", 2.5), w["trunc"], h=0.005)
+    return oracle.Potential(1.0, 1.0, w.get("rc", 2.5), w["trunc"])
+
+
+def ref_steps_per_sample(args, w):
+    """MD steps of the reference arm per bench step: args.ref_steps, fewer
+    for large systems so that one bench step stays near a second or two."""
+    return max(1, min(int(args.ref_steps), int(2e6 // w["n"])))
+
+
+def _ref_worker(wname, k, warmup, steps, per, relax, barrier, queue):
+    """One replica of the reference arm (a spawned process): its own seeded
+    copy of the workload, FP64 host-backend restatement, one thread."""
+    import oracle
+    w = workload(wname)
+    r, v, species, L = initial_state(w, seed=2024 + k)
+    pot = _ref_potential(w)
+    mass = np.ones(w["n"])
+    if w["nspecies"] == 2 and relax:
+        r, _, _ = oracle.minimize(r, species, [L] * 3, pot, w["skin"], relax, RELAX_STEP_SIZE, RELAX_MAX_MOVE)
+    for _ in range(warmup):
+        oracle.md_run(r, v, species, mass, [L] * 3, pot, w["skin"], w["dt"], 1, temperature=w["T"],
+                      coll_rate=w["rate"], seed=1)
+    barrier.wait()
+    t0 = time.perf_counter()
+    for j in range(steps):
+        oracle.md_run(r, v, species, mass, [L] * 3, pot, w["skin"], w["dt"], per, temperature=w["T"],
+                      coll_rate=w["rate"], seed=1 + j)
+    queue.put(time.perf_counter() - t0)
+
+
 def run_reference(args, w):
+    """The reference arm: the reference's host backend (its FP64 restatement,
+    single-threaded as the reference is) as one independent replica per
+    host core, started together; value = all replicas' particle-steps over
+    the slowest replica's time."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    r, v, species, L = initial_state(w)
-    import oracle
-    if w["nspecies"] == 2:
-        pot = oracle.Potential(KA["eps"], KA["sigma"], w.get("rc", 2.5), w["trunc"], h=0.005)
-    else:
-        pot = oracle.Potential(1.0, 1.0, w.get("rc", 2.5), w["trunc"])
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    per = ref_steps_per_sample(args, w)
+    # the random KA start relaxed by FP64 steepest descent (fewer steps than the
+    # GPU arm's RELAX_STEPS: the CPU port needs ~0.14 s per step at 64k)
+    relax = max(0, int(args.ref_relax)) if w["nspecies"] == 2 else 0
+    barrier = ctx.Barrier(cores)
+    queue = ctx.Queue()
+    procs = [ctx.Process(target=_ref_worker, args=(args.workload, k, args.warmup, args.steps, per, relax, barrier, queue))
+             for k in range(cores)]
+    for p in procs:
+        p.start()
+    times = [queue.get() for _ in procs]
+    for p in procs:
+        p.join()
+    dt = max(times)
     n = w["n"]
-    mass = np.ones(n)
-    relax = 0
-    if w["nspecies"] == 2:
-        # the random start relaxed by the FP64 steepest descent (fewer steps than the
-        # GPU arm's RELAX_STEPS: the CPU port needs ~0.14 s per step at this size)
-        relax = max(0, int(args.ref_relax))
-        r, _, _ = oracle.minimize(r, species, [L] * 3, pot, w["skin"], relax, RELAX_STEP_SIZE, RELAX_MAX_MOVE)
-    # sample size per bench step: a few MD steps so the whole run stays within minutes
-    per = max(1, int(args.ref_steps))
-    for _ in range(args.warmup):
-        oracle.md_run(r, v, species, mass, [L] * 3, pot, w["skin"], w["dt"], 1, temperature=w["T"],
-                      coll_rate=w["rate"], seed=1)
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        oracle.md_run(r, v, species, mass, [L] * 3, pot, w["skin"], w["dt"], per, temperature=w["T"],
-                      coll_rate=w["rate"], seed=1 + k)
-    dt = time.perf_counter() - t0
-    value = n * per * args.steps / dt
+    value = cores * n * per * args.steps / dt
+    sample = ("%s: %d independent replicas (one per host core), each %d x %d MD steps, FP64 host-backend "
+              "restatement, one thread per replica (the reference host backend is single-threaded)%s"
+              % (w["name"], cores, args.steps, per, ", starts relaxed by %d descent steps" % relax if relax else ""))
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / (per * args.steps), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": w["name"], "n": n, "md_steps_per_bench_step": per},
-            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": 1, "kind": "port",
-                             "sample": "%s, %d x %d MD steps, FP64 host-backend restatement, 1 thread "
-                                       "(the reference host backend is single-threaded)%s"
-                                       % (w["name"], args.steps, per,
-                                          ", start relaxed by %d descent steps" % relax if relax else "")},
+            "config": {"workload": w["name"], "n": n, "md_steps_per_bench_step": per, "replicas": cores},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
             "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -623,7 +655,8 @@ def main():
     ap.add_argument("--workload", default="ka64k",
                     help="ka64k, lj1m, lj4k, ens256, serve; ref-lj64k, ref-ka256k: the reference's own benchmarks")
     ap.add_argument("--md-steps", type=int, default=100, help="MD steps per bench step")
-    ap.add_argument("--ref-steps", type=int, default=20, help="MD steps per bench step of the reference arm")
+    ap.add_argument("--ref-steps", type=int, default=20,
+                    help="MD steps per bench step of the reference arm (at most 2e6 / N)")
     ap.add_argument("--ref-relax", type=int, default=100,
                     help="steepest-descent steps of the reference arm's KA start (CPU)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
