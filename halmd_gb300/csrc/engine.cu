@@ -527,6 +527,8 @@ void Engine::commit()
     // done_: [0] last-block ticket counter, [1] flag of launch_check_finite;
     // any_rebuild_: [0] this step rebuilds, [1] rebuild chains run
     status_.alloc(1); done_.alloc(2); any_rebuild_.alloc(2);
+    // rebuild list: count, systems, and RB_UNITS prefix sums of n + 1 entries
+    rb_.alloc(1 + table_size_ + (size_t)RB_UNITS * (table_size_ + 1));
     dsys_.alloc(table_size_); dst_.alloc(table_size_);
     dpair_.alloc((size_t)table_size_ * MAX_SPECIES * MAX_SPECIES);
     partial_.alloc((S / 256) * NTHERMO + 1); thermo_.alloc((size_t)table_size_ * NTHERMO);
@@ -773,7 +775,7 @@ Dev Engine::dev() const
     d.tiles_grid = capacity_ ? d.S_grid / SORT_TILE : ntiles_;
     d.status = status_.p; d.done = done_.p; d.any_rebuild = any_rebuild_.p;
     d.key[0] = key0_.p; d.key[1] = key1_.p; d.val[0] = val0_.p; d.val[1] = val1_.p; d.hist = hist_.p;
-    d.tiles = tiles_.p; d.ntiles = ntiles_;
+    d.tiles = tiles_.p; d.ntiles = ntiles_; d.rb = rb_.p;
     d.tpos = tpos_.p; d.tvel = tvel_.p; d.timg = timg_.p; d.tid = tid_.p;
     d.partial = partial_.p; d.thermo = thermo_.p;
     return d;
@@ -1242,6 +1244,7 @@ void Engine::minimize(uint32_t s, uint32_t steps, double step_size, double max_m
 void Engine::rebuild_chain(cudaStream_t st)
 {
     const Dev d = dev();
+    launch_rebuild_list(d, st);
     if (any_sort_) {
         launch_sort(d, sort_passes_, st);
         launch_rearrange(d, ds(), d.val[sort_passes_ & 1], st);   // pass p writes val[1 - p % 2]
@@ -1554,8 +1557,9 @@ void Engine::profile_get(const std::string& phase, double* total_ms, uint64_t* c
 
 uint32_t Engine::rebuild_kernel_count() const
 {
-    // sort keys + (hist, scan, scatter) per pass + rearrange + copy back; cell clear, bin, sort; list build
-    return (any_sort_ ? (uint32_t)sort_kernel_count(sort_passes_) + 2u : 0u) + 3u + 1u;
+    // rebuild list; sort keys + (hist, scan, scatter) per pass + rearrange + copy back; cell clear, bin,
+    // sort; list build
+    return 1u + (any_sort_ ? (uint32_t)sort_kernel_count(sort_passes_) + 2u : 0u) + 3u + 1u;
 }
 
 void Engine::integrate()

@@ -26,6 +26,9 @@ namespace hmd {
 constexpr uint32_t PLACEHOLDER = 0xFFFFFFFFu;
 constexpr int MAX_SPECIES = 4;
 constexpr int SLOT_ALIGN = 256;   // slots per system are a multiple of this
+// units of the rebuild list: slots / 256, sorting slots / 256, sort tiles,
+// cells / 256, cells / 4
+constexpr uint32_t RB_UNITS = 5;
 constexpr int CHUNK = 64;         // granularity of the slot -> system map
 
 // default entries per block of the neighbour-list layout for a force kernel
@@ -161,6 +164,9 @@ struct Dev {
     // mode: the slots, sort tiles and cells below the high-water mark of the
     // systems present, rounded up to a power of two)
     uint32_t S_grid, cells_grid, tiles_grid;
+    // work list of the rebuild chain (k_rebuild_list): [0] count, then the
+    // rebuilding systems and the prefix sums of their virtual blocks
+    uint32_t* rb;
     uint32_t* status;          // ST_* bits
     uint32_t* done;            // last-block ticket counter
     uint32_t* any_rebuild;      // [0] this step rebuilds, [1] count of steps that ran the rebuild chain

@@ -33,6 +33,7 @@ int step_kernel_count(const Dev& d);
 // rebuild (kernels_rebuild.cu)
 int radix_passes(uint32_t key_bits);
 constexpr uint32_t SORT_TILE = 2048;   // keys per tile of the segmented radix sort
+void launch_rebuild_list(const Dev& d, cudaStream_t st);
 void launch_sort(const Dev& d, int passes, cudaStream_t st);
 int sort_kernel_count(int passes);
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st);

@@ -75,6 +75,114 @@ __global__ void k_hilbert_keys(Dev d, uint32_t* keys)
 }
 
 // ---------------------------------------------------------------------------
+// Work list of the rebuild chain.  The chain runs whenever any system
+// rebuilds; in an engine of many systems only a few do, so instead of a grid
+// over every slot (and cell) whose blocks mostly exit, k_rebuild_list
+// compacts the rebuilding systems and the prefix sums of their virtual blocks
+// in each unit the chain's kernels use, and those kernels loop over the
+// virtual blocks with a grid of at most RB_GRID blocks.  A virtual block
+// covers the same slots (or cells) as one block of a launch over everything,
+// so results do not change.
+// ---------------------------------------------------------------------------
+
+constexpr unsigned RB_GRID = 152 * 8;
+
+struct RbList {
+    uint32_t n;
+    const uint32_t* sys;
+    const uint32_t* p[RB_UNITS];   // prefix sums, n + 1 entries each
+};
+
+__device__ __forceinline__ RbList rb_list(const Dev& d)
+{
+    RbList L;
+    L.n = d.rb[0];
+    L.sys = d.rb + 1;
+    for (uint32_t u = 0; u < RB_UNITS; ++u) L.p[u] = d.rb + 1 + d.nsys + u * (d.nsys + 1);
+    return L;
+}
+
+// the list entry k with p[k] <= v < p[k + 1] (entries of zero width are skipped)
+__device__ __forceinline__ uint32_t rb_find(const uint32_t* p, uint32_t n, uint32_t v)
+{
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (p[mid] <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// one block: compact the active systems that rebuild, in system order
+__global__ void __launch_bounds__(1024) k_rebuild_list(Dev d)
+{
+    __shared__ uint32_t s_warp[32][RB_UNITS + 1];
+    __shared__ uint32_t s_carry[RB_UNITS + 1];
+    uint32_t* sys = d.rb + 1;
+    uint32_t* pre[RB_UNITS];
+    for (uint32_t u = 0; u < RB_UNITS; ++u) pre[u] = d.rb + 1 + d.nsys + u * (d.nsys + 1);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x <= RB_UNITS) s_carry[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < d.nsys; base += blockDim.x) {
+        const uint32_t s = base + threadIdx.x;
+        uint32_t c[RB_UNITS + 1] = {0, 0, 0, 0, 0, 0};   // [0]: rebuilds, then the units
+        if (s < d.nsys) {
+            const SysParam& P = d.sys[s];
+            if (P.active && d.st[s].rebuild) {
+                c[0] = 1;
+                c[1] = P.A / 256;
+                if (P.sort_enable) { c[2] = P.A / 256; c[3] = P.sort_ntiles; }
+                c[4] = (P.ncells + 255) / 256;
+                c[5] = (P.ncells + 3) / 4;
+            }
+        }
+        uint32_t incl[RB_UNITS + 1];
+#pragma unroll
+        for (uint32_t u = 0; u <= RB_UNITS; ++u) {
+            uint32_t x = c[u];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                if (lane >= (uint32_t)o) x += y;
+            }
+            incl[u] = x;
+            if (lane == 31) s_warp[warp][u] = x;
+        }
+        __syncthreads();
+        if (warp == 0) {
+#pragma unroll
+            for (uint32_t u = 0; u <= RB_UNITS; ++u) {
+                const uint32_t v = lane < nw ? s_warp[lane][u] : 0u;
+                uint32_t x = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                    if (lane >= (uint32_t)o) x += y;
+                }
+                if (lane < nw) s_warp[lane][u] = x - v;   // exclusive over warps
+            }
+        }
+        __syncthreads();
+        if (c[0]) {
+            const uint32_t k = s_carry[0] + s_warp[warp][0] + incl[0] - 1u;
+            sys[k] = s;
+#pragma unroll
+            for (uint32_t u = 0; u < RB_UNITS; ++u) pre[u][k] = s_carry[u + 1] + s_warp[warp][u + 1] + incl[u + 1] - c[u + 1];
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1)
+            for (uint32_t u = 0; u <= RB_UNITS; ++u) s_carry[u] += s_warp[warp][u] + incl[u];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t n = s_carry[0];
+        for (uint32_t u = 0; u < RB_UNITS; ++u) pre[u][n] = s_carry[u + 1];
+        d.rb[0] = n;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Segmented stable LSD radix sort, 8-bit digits (algorithm/gpu/radix_sort_kernel.cu:76-230
 // restated per system): the slot range of every system is cut into tiles of
 // 2048 keys that never straddle two systems (tile table d.tiles); each pass
@@ -98,42 +206,58 @@ __device__ __forceinline__ bool sort_live(const Dev& d, uint32_t s)
 // keys (Hilbert code, ghosts last) and identity values of the sorting systems
 __global__ void __launch_bounds__(256) k_seg_keys(Dev d)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t s = d.chunk_sys[i / CHUNK];
-    if (!sort_live(d, s)) return;
-    d.key[0][i] = slot_key(d, d.sys[s], i);
-    d.val[0][i] = i;
+    const RbList L = rb_list(d);
+    const uint32_t total = L.p[1][L.n];
+    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+        const uint32_t k = rb_find(L.p[1], L.n, v);
+        const SysParam& P = d.sys[L.sys[k]];
+        const uint32_t i = P.off + (v - L.p[1][k]) * 256u + threadIdx.x;
+        d.key[0][i] = slot_key(d, P, i);
+        d.val[0][i] = i;
+    }
 }
 
 __global__ void __launch_bounds__(RADIX_THREADS) k_seg_hist(Dev d, const uint32_t* keys, uint32_t shift)
 {
-    const uint32_t t = blockIdx.x;
-    if (t >= d.ntiles) return;
-    const uint2 tl = d.tiles[t];
-    if (!sort_live(d, tl.x)) return;   // block-uniform
-    const SysParam& P = d.sys[tl.x];
-    const uint32_t end = min(tl.y + (uint32_t)RADIX_TILE, P.off + P.A);
-    const uint32_t local = (tl.y - P.off) / RADIX_TILE;
+    const RbList L = rb_list(d);
+    const uint32_t total = L.p[2][L.n];
     __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
-    __syncthreads();
+    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+        const uint32_t k = rb_find(L.p[2], L.n, v);
+        const SysParam& P = d.sys[L.sys[k]];
+        const uint32_t local = v - L.p[2][k];
+        const uint32_t first = P.off + local * RADIX_TILE;
+        const uint32_t end = min(first + (uint32_t)RADIX_TILE, P.off + P.A);
+        h[threadIdx.x] = 0;
+        __syncthreads();
 #pragma unroll
-    for (int r = 0; r < RADIX_ROUNDS; ++r) {
-        const uint32_t idx = tl.y + r * RADIX_THREADS + threadIdx.x;
-        if (idx < end) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+        for (int r = 0; r < RADIX_ROUNDS; ++r) {
+            const uint32_t idx = first + r * RADIX_THREADS + threadIdx.x;
+            if (idx < end) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        d.hist[P.sort_hist_off + threadIdx.x * P.sort_ntiles + local] = h[threadIdx.x];
+        __syncthreads();
     }
-    __syncthreads();
-    d.hist[P.sort_hist_off + threadIdx.x * P.sort_ntiles + local] = h[threadIdx.x];
 }
 
 // exclusive scan of one system's histogram (digit-major over its tiles) by one
 // block of 1024 threads: each warp owns a contiguous chunk, reads it
 // lane-strided (coalesced) once to total it and once more to scan it with
 // warp shuffles and a running carry; offsets come out as absolute slots
+__device__ void seg_scan_system(const Dev& d, uint32_t s);
+
 __global__ void __launch_bounds__(1024) k_seg_scan(Dev d)
 {
-    const uint32_t s = blockIdx.x;
-    if (s >= d.nsys || !sort_live(d, s)) return;
+    const RbList L = rb_list(d);
+    for (uint32_t k = blockIdx.x; k < L.n; k += gridDim.x) {
+        const uint32_t s = L.sys[k];
+        if (sort_live(d, s)) seg_scan_system(d, s);   // block-uniform
+    }
+}
+
+__device__ void seg_scan_system(const Dev& d, uint32_t s)
+{
     const SysParam& P = d.sys[s];
     uint32_t* hist = d.hist + P.sort_hist_off;
     const uint32_t total = 256u * P.sort_ntiles;
@@ -171,18 +295,30 @@ __global__ void __launch_bounds__(1024) k_seg_scan(Dev d)
         if (k < e) hist[k] = carry + incl - v;
         carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
+    __syncthreads();   // s_warp is reused by the next system of the block
 }
+
+__device__ __forceinline__ void seg_scatter_tile(const Dev& d, const SysParam& P, uint32_t local, const uint32_t* kin,
+                                                 const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t shift);
 
 __global__ void __launch_bounds__(RADIX_THREADS) k_seg_scatter(Dev d, const uint32_t* kin, const uint32_t* vin,
                                                                uint32_t* kout, uint32_t* vout, uint32_t shift)
 {
-    const uint32_t t = blockIdx.x;
-    if (t >= d.ntiles) return;
-    const uint2 tl = d.tiles[t];
-    if (!sort_live(d, tl.x)) return;   // block-uniform
-    const SysParam& P = d.sys[tl.x];
-    const uint32_t end = min(tl.y + (uint32_t)RADIX_TILE, P.off + P.A);
-    const uint32_t local = (tl.y - P.off) / RADIX_TILE;
+    const RbList L = rb_list(d);
+    const uint32_t total = L.p[2][L.n];
+    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+        const uint32_t k = rb_find(L.p[2], L.n, v);
+        seg_scatter_tile(d, d.sys[L.sys[k]], v - L.p[2][k], kin, vin, kout, vout, shift);
+        __syncthreads();
+    }
+}
+
+// one tile of 2048 keys of a system: stable scatter by the current digit
+__device__ __forceinline__ void seg_scatter_tile(const Dev& d, const SysParam& P, uint32_t local, const uint32_t* kin,
+                                                 const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t shift)
+{
+    const uint32_t first = P.off + local * RADIX_TILE;
+    const uint32_t end = min(first + (uint32_t)RADIX_TILE, P.off + P.A);
     __shared__ uint32_t s_w[RADIX_THREADS / 32][256];
     __shared__ uint32_t s_base[256];
     __shared__ uint32_t s_goff[256];
@@ -194,7 +330,7 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_seg_scatter(Dev d, const uint
     __syncthreads();
     const uint32_t lt = (1u << lane) - 1u;
     for (int r = 0; r < RADIX_ROUNDS; ++r) {
-        const uint32_t idx = tl.y + r * RADIX_THREADS + th;
+        const uint32_t idx = first + r * RADIX_THREADS + th;
         const bool valid = idx < end;
         uint32_t key = 0, val = 0, dg = 256u;
         if (valid) { key = kin[idx]; val = vin[idx]; dg = (key >> shift) & 255u; }
@@ -232,12 +368,23 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_seg_scatter(Dev d, const uint
 // ---------------------------------------------------------------------------
 
 template <bool DS>
+__device__ __forceinline__ void rearrange_slot(const Dev& d, const SysParam& P, uint32_t i, const uint32_t* perm);
+
+template <bool DS>
 __global__ void __launch_bounds__(256) k_rearrange(Dev d, const uint32_t* perm)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t s = d.chunk_sys[i / CHUNK];
-    const SysParam& P = d.sys[s];
-    if (!(P.active && P.sort_enable && d.st[s].rebuild)) return;
+    const RbList L = rb_list(d);
+    const uint32_t total = L.p[1][L.n];
+    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+        const uint32_t k = rb_find(L.p[1], L.n, v);
+        const SysParam& P = d.sys[L.sys[k]];
+        rearrange_slot<DS>(d, P, P.off + (v - L.p[1][k]) * 256u + threadIdx.x, perm);
+    }
+}
+
+template <bool DS>
+__device__ __forceinline__ void rearrange_slot(const Dev& d, const SysParam& P, uint32_t i, const uint32_t* perm)
+{
     const uint32_t src = perm[i];
     d.tpos[i] = d.pos[src];
     d.tvel[i] = d.vel[src];
@@ -254,18 +401,20 @@ __global__ void __launch_bounds__(256) k_rearrange(Dev d, const uint32_t* perm)
 template <bool DS>
 __global__ void __launch_bounds__(256) k_copyback(Dev d)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t s = d.chunk_sys[i / CHUNK];
-    const SysParam& P = d.sys[s];
-    if (!(P.active && P.sort_enable && d.st[s].rebuild)) return;
-    d.pos[i] = d.tpos[i];
-    d.vel[i] = d.tvel[i];
-    if (DS) {
-        d.pos[d.S + i] = d.tpos[d.S + i];
-        d.vel[d.S + i] = d.tvel[d.S + i];
+    const RbList L = rb_list(d);
+    const uint32_t total = L.p[1][L.n];
+    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+        const uint32_t k = rb_find(L.p[1], L.n, v);
+        const uint32_t i = d.sys[L.sys[k]].off + (v - L.p[1][k]) * 256u + threadIdx.x;
+        d.pos[i] = d.tpos[i];
+        d.vel[i] = d.tvel[i];
+        if (DS) {
+            d.pos[d.S + i] = d.tpos[d.S + i];
+            d.vel[d.S + i] = d.tvel[d.S + i];
+        }
+        d.img[i] = d.timg[i];
+        d.id[i] = d.tid[i];
     }
-    d.img[i] = d.timg[i];
-    d.id[i] = d.tid[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -284,39 +433,58 @@ __device__ __forceinline__ void cell_coords(const SysParam& P, float4 r, int& cx
     cz = (int)(((uint32_t)z) % (uint32_t)P.ncell[2]);
 }
 
-__global__ void k_cell_clear(Dev d)
+__global__ void __launch_bounds__(256) k_cell_clear(Dev d)
 {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= d.total_cells) return;
-    const uint32_t s = d.cell_sys[c];
-    if (d.st[s].rebuild) d.cell_count[c] = 0;
+    const RbList L = rb_list(d);
+    const uint32_t total = L.p[3][L.n];
+    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+        const uint32_t k = rb_find(L.p[3], L.n, v);
+        const SysParam& P = d.sys[L.sys[k]];
+        const uint32_t local = (v - L.p[3][k]) * 256u + threadIdx.x;
+        if (local < P.ncells) d.cell_count[P.cell_off + local] = 0;
+    }
 }
 
 __global__ void __launch_bounds__(256) k_bin(Dev d)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t s = d.chunk_sys[i / CHUNK];
-    const SysParam& P = d.sys[s];
-    if (!(P.active && d.st[s].rebuild)) return;
-    const float4 r = d.pos[i];
-    if (species_bits(r.w) == PLACEHOLDER) return;
-    int cx, cy, cz;
-    cell_coords(P, r, cx, cy, cz);
-    const uint32_t c = ((uint32_t)cz * P.ncell[1] + cy) * P.ncell[0] + cx;
-    const uint32_t k = atomicAdd(&d.cell_count[P.cell_off + c], 1u);
-    if (k < P.cell_size) d.cell[P.cell_word_off + c * P.cell_size + k] = i;
+    const RbList L = rb_list(d);
+    const uint32_t total = L.p[0][L.n];
+    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+        const uint32_t k = rb_find(L.p[0], L.n, v);
+        const SysParam& P = d.sys[L.sys[k]];
+        const uint32_t i = P.off + (v - L.p[0][k]) * 256u + threadIdx.x;
+        const float4 r = d.pos[i];
+        if (species_bits(r.w) == PLACEHOLDER) continue;
+        int cx, cy, cz;
+        cell_coords(P, r, cx, cy, cz);
+        const uint32_t c = ((uint32_t)cz * P.ncell[1] + cy) * P.ncell[0] + cx;
+        const uint32_t q = atomicAdd(&d.cell_count[P.cell_off + c], 1u);
+        if (q < P.cell_size) d.cell[P.cell_word_off + c * P.cell_size + q] = i;
+    }
 }
+
+__device__ __forceinline__ void cell_sort_one(const Dev& d, uint32_t s, uint32_t c, uint32_t* buf, uint32_t lane);
 
 // one warp per cell: sort the occupied slots ascending, pad with placeholders
 __global__ void __launch_bounds__(128) k_cell_sort(Dev d)
 {
     __shared__ uint32_t s_buf[4][256];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t c = blockIdx.x * 4 + warp;
-    if (c >= d.total_cells) return;
-    const uint32_t s = d.cell_sys[c];
+    const RbList L = rb_list(d);
+    const uint32_t total = L.p[4][L.n];
+    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+        const uint32_t k = rb_find(L.p[4], L.n, v);
+        const uint32_t s = L.sys[k];
+        const SysParam& P = d.sys[s];
+        const uint32_t local = (v - L.p[4][k]) * 4u + warp;
+        if (local < P.ncells) cell_sort_one(d, s, P.cell_off + local, s_buf[warp], lane);
+        __syncwarp();
+    }
+}
+
+__device__ __forceinline__ void cell_sort_one(const Dev& d, uint32_t s, uint32_t c, uint32_t* buf, uint32_t lane)
+{
     const SysParam& P = d.sys[s];
-    if (!(P.active && d.st[s].rebuild)) return;
     const uint32_t cs = P.cell_size;
     const uint32_t cnt = d.cell_count[c];
     if (lane == 0) {
@@ -325,7 +493,6 @@ __global__ void __launch_bounds__(128) k_cell_sort(Dev d)
     }
     const uint32_t n = min(cnt, cs);
     uint32_t* cell = d.cell + P.cell_word_off + (c - P.cell_off) * cs;
-    uint32_t* buf = s_buf[warp];
     for (uint32_t k = lane; k < n; k += 32) buf[k] = cell[k];
     __syncwarp();
     uint32_t mine[8];
@@ -513,22 +680,43 @@ __device__ __forceinline__ void cluster_scan(const Dev& d, const SysParam& P, fl
     }
 }
 
+__device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_t i, const float* s_rrcs,
+                                               const float* s_rrnear, float4* s_pos, uint32_t* s_j, uint32_t lane);
+
+// two virtual blocks of 128 slots per 256-slot unit of a rebuilding system
 __global__ void __launch_bounds__(128) k_neighbour(Dev d)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t s = d.chunk_sys[i / CHUNK];
-    const SysParam& P = d.sys[s];
     __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
     __shared__ float s_rrnear[MAX_SPECIES * MAX_SPECIES];
     __shared__ float4 s_pos[4][32];
     __shared__ uint32_t s_j[4][32];
-    if (threadIdx.x < P.ns * P.ns) {
-        s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
-        s_rrnear[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_near;
+    const RbList L = rb_list(d);
+    const uint32_t total = 2u * L.p[0][L.n];
+    uint32_t loaded = PLACEHOLDER;
+    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+        const uint32_t k = rb_find(L.p[0], L.n, v >> 1);
+        const uint32_t s = L.sys[k];
+        const SysParam& P = d.sys[s];
+        if (s != loaded) {   // block-uniform
+            __syncthreads();
+            if (threadIdx.x < P.ns * P.ns) {
+                s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
+                s_rrnear[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_near;
+            }
+            __syncthreads();
+            loaded = s;
+        }
+        const uint32_t i = P.off + (v - 2u * L.p[0][k]) * 128u + threadIdx.x;
+        neighbour_slot(d, s, i, s_rrcs, s_rrnear, s_pos[warp], s_j[warp], lane);
     }
-    __syncthreads();
-    if (!(P.active && d.st[s].rebuild)) return;   // block-uniform
+}
+
+// the Verlet list of slot i (one lane; the warp's 32 slots scan together)
+__device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_t i, const float* s_rrcs,
+                                               const float* s_rrnear, float4* s_pos, uint32_t* s_j, uint32_t lane)
+{
+    const SysParam& P = d.sys[s];
     const float4 ri = d.pos[i];
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;
@@ -584,11 +772,9 @@ __global__ void __launch_bounds__(128) k_neighbour(Dev d)
         const bool shared = d.nbr_scan == 2u || (d.nbr_scan == 0u && P.n >= NBR_SHARED_MIN_N);
         if (shared && ncells <= NBR_CLUSTER_MAX_CELLS) {
             if (wrap)
-                cluster_scan<true>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos[warp],
-                                   s_j[warp], lane);
+                cluster_scan<true>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos, s_j, lane);
             else
-                cluster_scan<false>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos[warp],
-                                    s_j[warp], lane);
+                cluster_scan<false>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos, s_j, lane);
         } else if (real) {
             lane_scan(d, P, ri, i, rrcs, rrnear, o);
         }
@@ -618,16 +804,27 @@ int radix_passes(uint32_t key_bits) { return (int)((key_bits + 7) / 8); }
 
 // Sort the slot ranges of the systems that rebuild; the permutation ends in
 // val[passes % 2]
+// Launch grids of the rebuild chain: the kernels loop over the virtual blocks
+// of the rebuild list, so a grid never needs more blocks than the work the
+// engine could hold (the old one-block-per-unit upper bound) nor more than a
+// few waves of resident blocks.
+static unsigned rb_grid(uint32_t upper) { return std::max(1u, std::min(upper, RB_GRID)); }
+
+void launch_rebuild_list(const Dev& d, cudaStream_t st)
+{
+    k_rebuild_list<<<1, 1024, 0, st>>>(d);
+}
+
 void launch_sort(const Dev& d, int passes, cudaStream_t st)
 {
-    k_seg_keys<<<d.S_grid / 256, 256, 0, st>>>(d);
+    k_seg_keys<<<rb_grid(d.S_grid / 256), 256, 0, st>>>(d);
     for (int p = 0; p < passes; ++p) {
         const uint32_t shift = 8u * p;
         const int cur = p & 1;
-        k_seg_hist<<<d.tiles_grid, RADIX_THREADS, 0, st>>>(d, d.key[cur], shift);
-        k_seg_scan<<<d.nsys, 1024, 0, st>>>(d);
-        k_seg_scatter<<<d.tiles_grid, RADIX_THREADS, 0, st>>>(d, d.key[cur], d.val[cur], d.key[1 - cur], d.val[1 - cur],
-                                                          shift);
+        k_seg_hist<<<rb_grid(d.tiles_grid), RADIX_THREADS, 0, st>>>(d, d.key[cur], shift);
+        k_seg_scan<<<rb_grid(d.nsys), 1024, 0, st>>>(d);
+        k_seg_scatter<<<rb_grid(d.tiles_grid), RADIX_THREADS, 0, st>>>(d, d.key[cur], d.val[cur], d.key[1 - cur],
+                                                                       d.val[1 - cur], shift);
     }
 }
 
@@ -635,21 +832,21 @@ int sort_kernel_count(int passes) { return 1 + 3 * passes; }
 
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st)
 {
-    const unsigned grid = d.S_grid / 256;
+    const unsigned grid = rb_grid(d.S_grid / 256);
     if (ds) { k_rearrange<true><<<grid, 256, 0, st>>>(d, perm); k_copyback<true><<<grid, 256, 0, st>>>(d); }
     else { k_rearrange<false><<<grid, 256, 0, st>>>(d, perm); k_copyback<false><<<grid, 256, 0, st>>>(d); }
 }
 
 void launch_binning(const Dev& d, cudaStream_t st)
 {
-    k_cell_clear<<<(d.cells_grid + 255) / 256, 256, 0, st>>>(d);
-    k_bin<<<d.S_grid / 256, 256, 0, st>>>(d);
-    k_cell_sort<<<(d.cells_grid + 3) / 4, 128, 0, st>>>(d);
+    k_cell_clear<<<rb_grid((d.cells_grid + 255) / 256 + d.nsys), 256, 0, st>>>(d);
+    k_bin<<<rb_grid(d.S_grid / 256), 256, 0, st>>>(d);
+    k_cell_sort<<<rb_grid((d.cells_grid + 3) / 4 + d.nsys), 128, 0, st>>>(d);
 }
 
 void launch_neighbour(const Dev& d, cudaStream_t st)
 {
-    k_neighbour<<<d.S_grid / 128, 128, 0, st>>>(d);
+    k_neighbour<<<rb_grid(d.S_grid / 128), 128, 0, st>>>(d);
 }
 
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
