@@ -16,7 +16,7 @@ HEADER = os.path.join(REPO, "include", "halmd_gb300.h")
 
 HMD_OK = 0
 PRECISION = {"float": 0, "single": 0, "dsfloat": 1, "double-single": 1}
-TRUNCATION = {"sharp": 0, "shifted": 1, "smooth_r4": 2, "force_shifted": 3}
+TRUNCATION = {"sharp": 0, "shifted": 1, "smooth_r4": 2, "force_shifted": 3, "none": 4}
 INTEGRATOR = {"verlet": 0, "verlet_nvt_andersen": 1, "andersen": 1, "verlet_nvt_hoover": 2, "hoover": 2,
               "verlet_nvt_boltzmann": 3, "boltzmann": 3, "euler": 4}
 POTENTIAL = {"lennard_jones": 0, "mie": 1, "morse": 2, "power_law": 3}
@@ -187,7 +187,9 @@ def system_desc(nparticle, box, epsilon=1.0, sigma=1.0, r_cut=2.5, truncation="s
 
     potential: lennard_jones (epsilon, sigma), mie (index_repulsion m,
     index_attraction n: even, m > n), morse (r_min, required; distortion B),
-    power_law (index n); every truncation applies to each.
+    power_law (index n); every truncation applies to each.  truncation "none"
+    is the untruncated potential over all pairs (pair_full): r_cut and skin
+    are then ignored.
     """
     L = load()
     d = SystemDesc()

@@ -145,7 +145,10 @@ uint32_t Engine::add_system(const hmd_system_desc& d)
     if (committed_ && !capacity_) throw Error(HMD_ERR_STATE, "systems must be added before commit");
     if (d.nparticle == 0) throw Error(HMD_ERR_INVALID, "nparticle must be positive");
     if (d.nspecies < 1 || d.nspecies > HMD_MAX_SPECIES) throw Error(HMD_ERR_INVALID, "nspecies out of range [1, 4]");
-    if (d.truncation < 0 || d.truncation > 3) throw Error(HMD_ERR_INVALID, "unknown truncation");
+    if (d.truncation < HMD_TRUNC_SHARP || d.truncation > HMD_TRUNC_NONE) throw Error(HMD_ERR_INVALID, "unknown truncation");
+    const bool full = d.truncation == HMD_TRUNC_NONE;
+    if (capacity_ && full)
+        throw Error(HMD_ERR_INVALID, "engines with a reserved capacity take truncated potentials");
     if (d.integrator < HMD_INTEGRATOR_VERLET || d.integrator > HMD_INTEGRATOR_EULER)
         throw Error(HMD_ERR_INVALID, "unknown integrator");
     if (capacity_ && d.integrator != HMD_INTEGRATOR_VERLET && d.integrator != HMD_INTEGRATOR_ANDERSEN)
@@ -158,7 +161,7 @@ uint32_t Engine::add_system(const hmd_system_desc& d)
     if (d.potential < HMD_POTENTIAL_LENNARD_JONES || d.potential > HMD_POTENTIAL_POWER_LAW)
         throw Error(HMD_ERR_INVALID, "unknown potential");
     for (uint32_t ab = 0; ab < ns * ns; ++ab) {
-        if (!(d.sigma[ab] > 0) || !(d.r_cut[ab] > 0) || !(d.epsilon[ab] >= 0))
+        if (!(d.sigma[ab] > 0) || !(full || d.r_cut[ab] > 0) || !(d.epsilon[ab] >= 0))
             throw Error(HMD_ERR_INVALID, "bad potential parameters");
         if (d.potential == HMD_POTENTIAL_MIE) {
             const uint32_t m = d.index_repulsion[ab], n = d.index_attraction[ab];
@@ -203,24 +206,26 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
     P.trunc = (uint32_t)d.truncation;
     P.pot = (uint32_t)d.potential;
     P.active = 1;
-    P.sort_enable = d.sort ? 1u : 0u;
+    const bool full = d.truncation == HMD_TRUNC_NONE;
+    P.sort_enable = (d.sort && !full) ? 1u : 0u;
     P.integrator = integrator_of(d.integrator);
     double rc_max = 0, rcs_max = 0;
     h.pairs.resize(ns * ns);
     for (uint32_t ab = 0; ab < ns * ns; ++ab) {
         const double sigma = d.sigma[ab], eps = d.epsilon[ab];
         const double sigma2 = sigma * sigma;
-        const double rc = sigma * d.r_cut[ab];
+        // untruncated (pair_full): every pair is in range and nothing is shifted
+        const double rc = full ? INFINITY : sigma * d.r_cut[ab];
         const double rcs = rc + d.skin;
-        double fc, ec;
-        pot_double(d, ab, rc * rc, fc, ec);
+        double fc = 0, ec = 0;
+        if (!full) pot_double(d, ab, rc * rc, fc, ec);
         PairParam& p = h.pairs[ab];
         p.eps4 = (float)(4 * eps);
         p.c48 = (float)(48 * eps / sigma2);
         p.sigma2 = (float)sigma2;
         p.rr_cut = (float)(rc * rc);
         p.r_cut = (float)rc;
-        p.rr_cut_skin = (float)(rcs * rcs);
+        p.rr_cut_skin = full ? 0.0f : (float)(rcs * rcs);
         p.en_cut = (d.truncation == HMD_TRUNC_SHARP) ? 0.0f : (float)ec;
         p.f_cut = (d.truncation == HMD_TRUNC_FORCE_SHIFTED) ? (float)(fc * rc) : 0.0f;
         p.rr_near = (float)(NEAR_SIGMA * NEAR_SIGMA * sigma2);
@@ -245,13 +250,14 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
             p.q3 = (float)(d.index[ab] % 2);
         }
         p.pad = 0.0f;
+        if (full) continue;
         rc_max = std::max(rc_max, rc);
         rcs_max = std::max(rcs_max, rcs);
     }
     P.rri_smooth = (d.truncation == HMD_TRUNC_SMOOTH_R4) ? (float)std::pow(d.smoothing, -2) : 0.0f;
     P.dt = (float)d.timestep;
     P.dt_half = (float)(d.timestep / 2);
-    P.rr_half_skin = (float)(0.25 * d.skin * d.skin);
+    P.rr_half_skin = full ? INFINITY : (float)(0.25 * d.skin * d.skin);   // pair_full never rebuilds
     P.sqrt_T = (float)std::sqrt(d.temperature);
     {
         const double q = d.collision_rate * d.timestep;
@@ -287,7 +293,7 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
         // particle moved < skin/2 since the build); particles farther than
         // that from every face have no partner across the box
         const double in = 0.5 * d.box[q] - (rcs_max + d.skin) - 1e-4 * d.box[q];
-        P.inner[q] = in > 0 ? (float)in : 0.0f;
+        P.inner[q] = (in > 0 && !full) ? (float)in : 0.0f;
     }
     float Lmax = 0;
     for (int q = 0; q < 3; ++q) {
@@ -300,6 +306,17 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
     }
     // Hilbert depth (gpu/sorts/hilbert.cpp:51-54)
     P.depth = std::min(10u, (uint32_t)std::ceil(std::log((double)Lmax) / M_LN2));
+    if (full) {
+        // no binning and no list; one placeholder cell keeps the tables uniform
+        for (int q = 0; q < 3; ++q) {
+            P.ncell[q] = 1;
+            P.cell_len[q] = P.L[q];
+        }
+        P.ncells = 1;
+        P.cell_size = 32;
+        h.nbr_size = 8;
+        return;
+    }
     // binning sizing (gpu/binning.cpp:81-101)
     const double warp = 32;
     const double nwarps = d.nparticle / (d.cell_occupancy * warp);
@@ -418,6 +435,7 @@ void Engine::unplace(uint32_t s)
 // counterpart is force_kind_of in force.cuh)
 static int force_kind(const SysParam& P)
 {
+    if (P.trunc == TRUNC_NONE) return FK_FULL;
     if (P.pot != POT_LJ) return FK_POT;
     if (P.trunc == TRUNC_SHARP || P.trunc == TRUNC_SHIFTED) return P.ns == 1 ? FK_LJ1 : FK_SHIFTED;
     return P.trunc == TRUNC_SMOOTH_R4 ? FK_SMOOTH : FK_FSHIFT;
@@ -1682,6 +1700,8 @@ void Engine::thermo(uint32_t s, double* out)
 void Engine::neighbour_lists(uint32_t s, uint32_t* counts, uint32_t* lists, uint32_t maxn)
 {
     check_sys(s);
+    if (sys_[s].P.trunc == TRUNC_NONE)
+        throw Error(HMD_ERR_STATE, "an untruncated potential (pair_full) has no neighbour list");
     ensure_forces(false);
     const SysParam& P = sys_[s].P;
     std::vector<uint32_t> slot = slots_of(s);

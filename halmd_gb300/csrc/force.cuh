@@ -903,6 +903,7 @@ __device__ __forceinline__ float lane_sum(float v)
 // kind of pair interaction of a system (FK_*), the template selector of k_force
 __device__ __forceinline__ int force_kind_of(const SysParam& P)
 {
+    if (P.trunc == TRUNC_NONE) return FK_FULL;
     if (P.pot != POT_LJ) return FK_POT;
     if (P.trunc == TRUNC_SHARP || P.trunc == TRUNC_SHIFTED) return P.ns == 1 ? FK_LJ1 : FK_SHIFTED;
     return P.trunc == TRUNC_SMOOTH_R4 ? FK_SMOOTH : FK_FSHIFT;
@@ -932,6 +933,7 @@ __global__ void __launch_bounds__(128, HMD_FORCE_MINB) k_force(Dev d)
     __syncthreads();
     if (!P.active || !d.st[s].live || *d.status != 0u) return;   // block-uniform
     if (KIND != FK_GENERIC && force_kind_of(P) != KIND) return;      // another kind's launch
+    if (KIND == FK_GENERIC && force_kind_of(P) == FK_FULL) return;   // no list: k_force_full
     const float4 ri = d.pos[i];
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;

@@ -36,7 +36,8 @@ constexpr int CHUNK = 64;         // granularity of the slot -> system map
 // the engine also accepts 8 for w = 2 and w = 4)
 __host__ __device__ constexpr uint32_t list_block(uint32_t w) { return w < 4u ? 4u : w; }
 
-enum Trunc : uint32_t { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3 };
+// TRUNC_NONE: untruncated potential over all pairs (forces/pair_full.hpp)
+enum Trunc : uint32_t { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3, TRUNC_NONE = 4 };
 enum Pot : uint32_t { POT_LJ = 0, POT_MIE = 1, POT_MORSE = 2, POT_POWER_LAW = 3 };
 // INTEG_DESCENT: steepest-descent energy minimisation (positions only);
 // INTEG_HOOVER: Nose-Hoover chain of two; INTEG_BOLTZMANN: Verlet with

@@ -12,9 +12,11 @@ struct Dev;
 // FK_LJ1 one species with a sharp or shifted truncation, FK_SHIFTED several
 // species with a sharp or shifted truncation, FK_SMOOTH smooth_r4, FK_FSHIFT
 // force_shifted, FK_POT the other pair potentials (mie, morse, power_law) with
-// any truncation; FK_GENERIC handles every kind in one kernel
-enum ForceKind : int { FK_GENERIC = 0, FK_LJ1 = 1, FK_SHIFTED = 2, FK_SMOOTH = 3, FK_FSHIFT = 4, FK_POT = 5 };
+// any truncation; FK_GENERIC handles every list kind in one kernel; FK_FULL
+// untruncated potentials over all pairs (no list, launch_force_full)
+enum ForceKind : int { FK_GENERIC = 0, FK_LJ1 = 1, FK_SHIFTED = 2, FK_SMOOTH = 3, FK_FSHIFT = 4, FK_POT = 5, FK_FULL = 6 };
 template <int KIND> void launch_force_kind(const Dev& d, bool aux, cudaStream_t st);
+void launch_force_full(const Dev& d, bool aux, cudaStream_t st);
 
 // step (kernels_step.cu)
 void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool use_handle, cudaStream_t st);

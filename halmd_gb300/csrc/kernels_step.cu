@@ -210,7 +210,8 @@ __global__ void k_mark(Dev d, int rebuild_all)
         SysState& t = d.st[q];
         const bool lv = d.sys[q].active != 0u;
         t.live = lv;
-        t.rebuild = (lv && (rebuild_all || t.rebuild_request)) ? 1u : 0u;
+        // an untruncated system (pair_full) has no list and never rebuilds
+        t.rebuild = (lv && d.sys[q].trunc != TRUNC_NONE && (rebuild_all || t.rebuild_request)) ? 1u : 0u;
         if (t.rebuild) { t.rebuild_request = 0u; t.rebuilds += 1ull; }
     }
 }
@@ -321,6 +322,7 @@ void launch_force(const Dev& d, bool aux, cudaStream_t st)
     if (d.force_kinds & (1u << FK_SMOOTH)) launch_force_kind<FK_SMOOTH>(d, aux, st);
     if (d.force_kinds & (1u << FK_FSHIFT)) launch_force_kind<FK_FSHIFT>(d, aux, st);
     if (d.force_kinds & (1u << FK_POT)) launch_force_kind<FK_POT>(d, aux, st);
+    if (d.force_kinds & (1u << FK_FULL)) launch_force_full(d, aux, st);
 }
 
 // engines with a Nose-Hoover or Maxwell-Boltzmann system: the finalize

@@ -282,7 +282,7 @@ __device__ __forceinline__ void step_decision(const Dev& d, SysState& st, float 
         const SysParam& Q = d.sys[q];
         const bool lv = ok && Q.active && t.steps_left != 0u;
         const float disp = __uint_as_float(atomicExch(&t.disp2_bits, 0u));
-        const uint32_t rb = lv && (disp > Q.rr_half_skin || t.rebuild_request != 0u);
+        const uint32_t rb = lv && Q.trunc != TRUNC_NONE && (disp > Q.rr_half_skin || t.rebuild_request != 0u);
         t.rebuild = rb;
         t.live = lv;
         if (lv) {

@@ -181,7 +181,9 @@ class particle:
         if self._box is None or self._potential is None or self._integrator is None:
             raise RuntimeError("particle '%s' needs a box, a pair force and an integrator" % self.label)
         pot, nb, integ = self._potential, self._neighbour or {}, self._integrator
-        kw = dict(epsilon=pot.epsilon, sigma=pot.sigma, r_cut=pot.cutoff, truncation=pot.kind,
+        # an untruncated potential: the pair_full force (forces/pair.lua.in:78-83)
+        kw = dict(epsilon=pot.epsilon, sigma=pot.sigma, r_cut=0.0 if pot.kind is None else pot.cutoff,
+                  truncation=pot.kind or "none",
                   skin=nb.get("skin", 0.5), timestep=integ.timestep, integrator=integ.kind,
                   sort=not nb.get("disable_sorting", False), potential=pot.potential, **pot.params)
         if pot.kind == "smooth_r4":
@@ -277,11 +279,11 @@ def neighbour(args=None, **kw):
 
 
 def pair(args=None, **kw):
-    """halmd.mdsim.forces.pair{box, particle, potential, neighbour}."""
+    """halmd.mdsim.forces.pair{box, particle, potential, neighbour}: the truncated
+    force (pair_trunc) for a potential with a cutoff, else the untruncated
+    force over all pairs (pair_full; forces/pair.lua.in:78-83)."""
     a = _args(args, kw)
     pot = a["potential"]
-    if pot.kind is None:
-        raise ValueError("untruncated pair potentials (pair_full) are not on this path: call :truncate")
     parts = a["particle"] if isinstance(a["particle"], (list, tuple)) else [a["particle"]]
     if len(parts) != 1:
         raise ValueError("forces between two particle instances are not supported")

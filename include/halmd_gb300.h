@@ -44,6 +44,10 @@ extern "C" {
 #define HMD_TRUNC_SHIFTED 1        /* truncations/shifted.hpp (truncate.lua.in:289 default) */
 #define HMD_TRUNC_SMOOTH_R4 2      /* truncations/smooth_r4.hpp */
 #define HMD_TRUNC_FORCE_SHIFTED 3  /* truncations/force_shifted.hpp */
+/* no truncation: the untruncated potential over all pairs, no neighbour list
+ * (forces/pair_full.hpp; lua/halmd/mdsim/forces/pair.lua.in:78-83 picks it
+ * when the potential has no r_cut); r_cut and skin are ignored */
+#define HMD_TRUNC_NONE 4
 
 /* pair potentials (mdsim/gpu/potentials/pair/*.cpp; every truncation applies to each) */
 #define HMD_POTENTIAL_LENNARD_JONES 0  /* lennard_jones.cpp (default) */

@@ -13,7 +13,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "liboracle.so")
 
-TRUNC = {"sharp": 0, "shifted": 1, "smooth_r4": 2, "force_shifted": 3}
+TRUNC = {"sharp": 0, "shifted": 1, "smooth_r4": 2, "force_shifted": 3, "none": 4}
 PLACEHOLDER = 0xFFFFFFFF
 
 

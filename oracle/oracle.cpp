@@ -66,7 +66,10 @@ static const u32 PLACEHOLDER = 0xFFFFFFFFu;
 /* Lennard-Jones potential with truncations (FP64)                           */
 /* ------------------------------------------------------------------------ */
 
-enum { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3 };
+/* TRUNC_NONE: the untruncated potential (host/forces/pair_full.hpp): an
+ * infinite cutoff, so the half list below holds every pair i < j exactly
+ * once, as pair_full.hpp:237-239 loops j from i + 1 */
+enum { TRUNC_SHARP = 0, TRUNC_SHIFTED = 1, TRUNC_SMOOTH_R4 = 2, TRUNC_FORCE_SHIFTED = 3, TRUNC_NONE = 4 };
 enum { ORC_MAX_SPECIES = 8 };
 
 enum { POT_LJ = 0, POT_MIE = 1, POT_MORSE = 2, POT_POWER_LAW = 3 };
@@ -170,7 +173,7 @@ ORC_API int orc_pot_init_any(orc_pot* p, int pot, int ns, const double* eps, con
                              const unsigned* idx_n, const double* r_min, const double* distortion)
 {
     if (ns < 1 || ns > ORC_MAX_SPECIES) return -1;
-    if (trunc < 0 || trunc > 3 || pot < 0 || pot > 3) return -1;
+    if (trunc < 0 || trunc > TRUNC_NONE || pot < 0 || pot > 3) return -1;
     std::memset(p, 0, sizeof(*p));
     p->ns = ns;
     p->trunc = trunc;
@@ -181,7 +184,7 @@ ORC_API int orc_pot_init_any(orc_pot* p, int pot, int ns, const double* eps, con
         p->eps[ab] = eps[ab];
         p->sigma[ab] = sigma[ab];
         p->sigma2[ab] = sigma[ab] * sigma[ab];
-        p->rcut[ab] = sigma[ab] * rcut_sigma[ab];
+        p->rcut[ab] = (trunc == TRUNC_NONE) ? INFINITY : sigma[ab] * rcut_sigma[ab];
         p->rrcut[ab] = p->rcut[ab] * p->rcut[ab];
         if (pot == POT_MIE) {
             const unsigned m = idx_m[ab], n = idx_n[ab];
@@ -196,8 +199,8 @@ ORC_API int orc_pot_init_any(orc_pot* p, int pot, int ns, const double* eps, con
             p->rmin_sigma[ab] = r_min[ab] / sigma[ab];
             p->distortion[ab] = distortion[ab];
         }
-        double f, e;
-        pot_bare(p, p->rrcut[ab], ab, &f, &e);
+        double f = 0, e = 0;
+        if (trunc != TRUNC_NONE) pot_bare(p, p->rrcut[ab], ab, &f, &e);
         p->encut[ab] = (trunc == TRUNC_SHARP) ? 0 : e;
         /* force_shifted.hpp:63-64 stores F_c = fval(rc) * rc */
         p->fcut[ab] = (trunc == TRUNC_FORCE_SHIFTED) ? f * p->rcut[ab] : 0;
@@ -220,6 +223,7 @@ ORC_API void orc_pot_eval(const orc_pot* p, double rr, int a, int b, double* fva
     pot_bare(p, rr, ab, &f, &e);
     switch (p->trunc) {
     case TRUNC_SHARP:
+    case TRUNC_NONE:
         break;
     case TRUNC_SHIFTED:
         e = e - p->encut[ab];

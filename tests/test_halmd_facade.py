@@ -67,10 +67,18 @@ def test_argument_errors(halmd):
         halmd.mdsim.potentials.pair.lennard_jones().truncate("smooth_r4", cutoff=2.5)  # no h
     box = halmd.mdsim.box(length=[5, 5, 5])
     p = halmd.mdsim.particle(particles=10)
-    with pytest.raises(ValueError):
-        halmd.mdsim.forces.pair(box=box, particle=p, potential=halmd.mdsim.potentials.pair.lennard_jones())
     with pytest.raises(RuntimeError):
         p._desc()                                                  # no force / integrator yet
+
+
+def test_untruncated_potential_maps_onto_pair_full(halmd):
+    # forces/pair.lua.in:78-83: a potential without r_cut takes the pair_full force
+    box = halmd.mdsim.box(length=[5, 5, 5])
+    p = halmd.mdsim.particle(particles=10)
+    halmd.mdsim.forces.pair(box=box, particle=p, potential=halmd.mdsim.potentials.pair.lennard_jones())
+    halmd.mdsim.integrators.verlet(box=box, particle=p, timestep=0.001)
+    d = p._desc()
+    assert d.truncation == 4
 
 
 @pytest.mark.parametrize("name,kw,check", [
