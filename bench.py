@@ -416,6 +416,8 @@ def run_ensemble(args):
     for s in specs:
         batch.add_system(hg.system_desc(s["n"], s["L"], **s["desc"]))
     batch.commit()
+    if args.neighbour_scan:
+        batch.set_option("neighbour_scan", args.neighbour_scan)
     for k, s in enumerate(specs):
         load(batch, k, s)
     batch.step(M)

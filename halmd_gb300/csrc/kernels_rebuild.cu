@@ -538,6 +538,12 @@ __device__ __forceinline__ void cell_sort_one(const Dev& d, uint32_t s, uint32_t
 // appended in cell order and, within a cell, in slot order (deterministic).
 // ---------------------------------------------------------------------------
 
+// resident blocks of 128 threads per SM that the list build's register
+// allocation aims for
+#ifndef HMD_NBR_MINB
+#define HMD_NBR_MINB 8
+#endif
+
 constexpr uint32_t NBR_CLUSTER_MAX_CELLS = 150;   // larger cell ranges: per-lane scan
 // The shared scan does a warp's 32 particles in one serial pass over the cells
 // around them; it pays off once a rebuild has enough warps per SM to hide that
@@ -548,13 +554,43 @@ struct NbrOut {
     uint32_t* out;        // this slot's row in the blocked list
     size_t bstride;       // words between list blocks
     uint32_t lw, lmask;   // log2 of the block width, width - 1
-    uint32_t cap;
+    uint32_t cap;         // a multiple of the block width
     uint32_t nn = 0, nf = 0;
     __device__ __forceinline__ void add(uint32_t j, bool near)
     {
         const uint32_t e = near ? nn : cap - 1u - nf;
         if (nn + nf < cap) out[(e >> lw) * bstride + (e & lmask)] = j;
         if (near) ++nn; else ++nf;
+    }
+};
+
+// The per-lane scan's writer: the same layout, with pn and pf following the
+// next near and far entry incrementally, so an append costs no 64-bit
+// multiply (the shared scan keeps NbrOut: its register budget is tighter).
+// Entry e sits at (e / LB) * bstride + e % LB; nothing is stored once the two
+// parts meet (the counts still grow: overflow is detected).
+struct NbrOutInc {
+    NbrOut& o;
+    uint32_t* pn;
+    uint32_t* pf;
+    __device__ __forceinline__ explicit NbrOutInc(NbrOut& base) : o(base)
+    {
+        pn = o.out + (o.nn >> o.lw) * o.bstride + (o.nn & o.lmask);
+        const uint32_t e = o.cap - 1u - o.nf;
+        pf = o.out + (e >> o.lw) * o.bstride + (e & o.lmask);
+    }
+    __device__ __forceinline__ void add(uint32_t j, bool near)
+    {
+        if (o.nn + o.nf < o.cap) *(near ? pn : pf) = j;
+        const ptrdiff_t jump = (ptrdiff_t)(o.bstride - o.lmask);   // from the end of a block to the next
+        if (near) {
+            ++o.nn;
+            pn += (o.nn & o.lmask) ? (ptrdiff_t)1 : jump;
+        } else {
+            const uint32_t e = o.cap - 1u - o.nf;
+            ++o.nf;
+            pf -= (e & o.lmask) ? (ptrdiff_t)1 : jump;
+        }
     }
 };
 
@@ -582,13 +618,69 @@ __device__ __forceinline__ void nbr_test(const NbrBox& B, float4 ri, uint32_t i,
     if (b < B.ns && rr <= rrcs[b]) o.add(j, rr < rrnear[b]);
 }
 
-// the 27 cells around the particle, for one lane
-__device__ __forceinline__ void lane_scan(const Dev& d, const SysParam& P, float4 ri, uint32_t i, const float* rrcs,
-                                          const float* rrnear, NbrOut& o)
+// Pair cut-offs of the lane's particle for the per-lane scan: held in
+// registers for one or two species, read from shared memory per pair above
+template <int NS>
+struct LaneCut {
+    float c0, c1, n0, n1;
+    const float* rc;
+    const float* rn;
+    uint32_t ns;
+    __device__ __forceinline__ LaneCut(const float* rrcs, const float* rrnear, uint32_t ns_)
+        : c0(rrcs[0]), c1(NS == 2 ? rrcs[1] : 0.0f), n0(rrnear[0]), n1(NS == 2 ? rrnear[1] : 0.0f), rc(rrcs),
+          rn(rrnear), ns(ns_) {}
+    // false for a slot of no species of the system
+    __device__ __forceinline__ bool get(uint32_t b, float& c, float& n) const
+    {
+        if (NS == 1) { c = c0; n = n0; return b == 0u; }
+        if (NS == 2) { c = b ? c1 : c0; n = b ? n1 : n0; return b < 2u; }
+        const bool ok = b < ns;
+        c = rc[ok ? b : 0u];
+        n = rn[ok ? b : 0u];
+        return ok;
+    }
+};
+
+// nbr_test of the per-lane scan: the same criterion, in the same order
+template <bool WRAP, int NS>
+__device__ __forceinline__ void lane_test(const NbrBox& B, float4 ri, uint32_t i, float4 rj, uint32_t j,
+                                          const LaneCut<NS>& cut, NbrOutInc& o)
 {
+    const float sx = __fsub_rn(ri.x, rj.x), sy = __fsub_rn(ri.y, rj.y), sz = __fsub_rn(ri.z, rj.z);
+    const float dx = WRAP ? min_image(sx, B.L[0], B.Linv[0]) : sx;
+    const float dy = WRAP ? min_image(sy, B.L[1], B.Linv[1]) : sy;
+    const float dz = WRAP ? min_image(sz, B.L[2], B.Linv[2]) : sz;
+    const float rr = rr_exact(dx, dy, dz);
+    float c, n;
+    const bool ok = cut.get(species_bits(rj.w), c, n);
+    if (ok && rr <= c && j != i) o.add(j, rr < n);
+}
+
+// Positions are canonical, |x| <= L/2, and the binning maps x and x + L to
+// one cell (cells are anchored at x = 0, so the periodic seam of the box
+// may run through a cell).  A particle farther than 2.5 cell lengths from
+// every face therefore sees, in its 27 cells, only particles of the same
+// periodic image within two cell lengths (plus rounding) in each coordinate;
+// that distance is below L/2 (the condition implies at least 6 cells), where
+// min_image returns the separation unchanged (rint of a ratio below 1/2 is
+// zero), so the minimum-image arithmetic is skipped without changing any
+// result.  The cell indices still wrap.
+__device__ __forceinline__ bool far_from_faces(const SysParam& P, float4 r)
+{
+    return fabsf(r.x) + 2.5f * P.cell_len[0] < 0.5f * P.L[0] && fabsf(r.y) + 2.5f * P.cell_len[1] < 0.5f * P.L[1] &&
+           fabsf(r.z) + 2.5f * P.cell_len[2] < 0.5f * P.L[2];
+}
+
+// the 27 cells around the particle, for one lane (each distinct cell once
+// when a dimension has fewer than 3 cells); WRAP = false only when every
+// lane of the warp is far from the faces (far_from_faces)
+template <bool WRAP, int NS>
+__device__ __forceinline__ void lane_scan(const SysParam& P, const float4* pos, const uint32_t* cells,
+                                          const uint32_t* counts, float4 ri, uint32_t i, int cx, int cy, int cz,
+                                          const LaneCut<NS>& cut, NbrOut& base)
+{
+    NbrOutInc o(base);
     const NbrBox B(P);
-    int cx, cy, cz;
-    cell_coords(P, ri, cx, cy, cz);
     const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
     const int lox = nx >= 3 ? -1 : 0, hix = nx >= 2 ? 1 : 0;
     const int loy = ny >= 3 ? -1 : 0, hiy = ny >= 2 ? 1 : 0;
@@ -602,22 +694,60 @@ __device__ __forceinline__ void lane_scan(const Dev& d, const SysParam& P, float
                 const int x = (cx + ox + nx) % nx;
                 const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
                 // occupied slots of the cell (ascending), four at a time so the
-                // position gathers are independent of one another
-                const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
-                const uint4* cell4 = reinterpret_cast<const uint4*>(d.cell + P.cell_word_off + c * cs);
-                for (uint32_t k = 0; k < nc; k += 4) {
+                // position gathers are independent of one another; a cell holds
+                // a multiple of 32 words, so the last group's load stays inside
+                const uint32_t nc = min(counts[c], cs);
+                const uint4* cell4 = reinterpret_cast<const uint4*>(cells + c * cs);
+                uint32_t k = 0;
+                for (; k + 4 <= nc; k += 4) {
                     const uint4 jj = __ldg(cell4 + (k >> 2));
-                    const uint32_t jv[4] = {jj.x, jj.y, jj.z, jj.w};
-                    float4 rv[4];
+                    const float4 r0 = __ldg(pos + jj.x), r1 = __ldg(pos + jj.y);
+                    const float4 r2 = __ldg(pos + jj.z), r3 = __ldg(pos + jj.w);
+                    lane_test<WRAP, NS>(B, ri, i, r0, jj.x, cut, o);
+                    lane_test<WRAP, NS>(B, ri, i, r1, jj.y, cut, o);
+                    lane_test<WRAP, NS>(B, ri, i, r2, jj.z, cut, o);
+                    lane_test<WRAP, NS>(B, ri, i, r3, jj.w, cut, o);
+                }
+                if (k < nc) {
+                    const uint4 jj = __ldg(cell4 + (k >> 2));
+                    const uint32_t jv[3] = {jj.x, jj.y, jj.z};
+                    float4 rv[3];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) rv[u] = (k + u < nc) ? __ldg(d.pos + jv[u]) : make_float4(0, 0, 0, 0);
+                    for (int u = 0; u < 3; ++u) rv[u] = (k + u < nc) ? __ldg(pos + jv[u]) : make_float4(0, 0, 0, 0);
 #pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                        if (k + u < nc) nbr_test<true>(B, ri, i, rv[u], jv[u], rrcs, rrnear, o);
+                    for (int u = 0; u < 3; ++u)
+                        if (k + u < nc) lane_test<WRAP, NS>(B, ri, i, rv[u], jv[u], cut, o);
                 }
             }
         }
     }
+}
+
+// The per-lane scan of one particle, out of line: it then gets its own
+// register allocation instead of sharing the shared scan's (inlined
+// together, the two spilled).  Pointers are passed by value, not the kernel
+// parameter block; the list counts come back as (near, far).
+template <bool WRAP>
+__device__ __noinline__ uint2 lane_scan_call(const SysParam* Pp, const float4* pos, const uint32_t* cell,
+                                             const uint32_t* cell_count, float4 ri, uint32_t i, const float* rrcs,
+                                             const float* rrnear, uint32_t* out, size_t bstride, uint32_t lw,
+                                             uint32_t cap)
+{
+    const SysParam& P = *Pp;
+    NbrOut o;
+    o.out = out;
+    o.bstride = bstride;
+    o.lw = lw;
+    o.lmask = (1u << lw) - 1u;
+    o.cap = cap;
+    int cx, cy, cz;
+    cell_coords(P, ri, cx, cy, cz);
+    const uint32_t* cells = cell + P.cell_word_off;
+    const uint32_t* counts = cell_count + P.cell_off;
+    if (P.ns == 1) lane_scan<WRAP, 1>(P, pos, cells, counts, ri, i, cx, cy, cz, LaneCut<1>(rrcs, rrnear, 1u), o);
+    else if (P.ns == 2) lane_scan<WRAP, 2>(P, pos, cells, counts, ri, i, cx, cy, cz, LaneCut<2>(rrcs, rrnear, 2u), o);
+    else lane_scan<WRAP, 0>(P, pos, cells, counts, ri, i, cx, cy, cz, LaneCut<0>(rrcs, rrnear, P.ns), o);
+    return make_uint2(o.nn, o.nf);
 }
 
 // the cells around the warp's bounding box [lo, hi] (cell ranges c0 + [0, nc)
@@ -683,32 +813,36 @@ __device__ __forceinline__ void cluster_scan(const Dev& d, const SysParam& P, fl
 __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_t i, const float* s_rrcs,
                                                const float* s_rrnear, float4* s_pos, uint32_t* s_j, uint32_t lane);
 
-// two virtual blocks of 128 slots per 256-slot unit of a rebuilding system
-__global__ void __launch_bounds__(128) k_neighbour(Dev d)
+// two virtual blocks of 128 slots per 256-slot unit of a rebuilding system.
+// Only v stays live across the scan: the list bounds are read again each
+// round (the list stores may alias them, so they are not kept in
+// registers) and the pair table is staged again per virtual block.
+// LOOP = false: the grid has a block per virtual block (one-system engines);
+// without the loop the shared scan spills less (LJ-1M rebuild chain 1.43 ms
+// against 1.49 ms with the loop).
+template <bool LOOP>
+__global__ void __launch_bounds__(128, HMD_NBR_MINB) k_neighbour(Dev d)
 {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
     __shared__ float s_rrnear[MAX_SPECIES * MAX_SPECIES];
     __shared__ float4 s_pos[4][32];
     __shared__ uint32_t s_j[4][32];
-    const RbList L = rb_list(d);
-    const uint32_t total = 2u * L.p[0][L.n];
-    uint32_t loaded = PLACEHOLDER;
-    for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    for (uint32_t v = blockIdx.x;; v += gridDim.x) {
+        const RbList L = rb_list(d);
+        if (v >= 2u * L.p[0][L.n]) break;
         const uint32_t k = rb_find(L.p[0], L.n, v >> 1);
         const uint32_t s = L.sys[k];
         const SysParam& P = d.sys[s];
-        if (s != loaded) {   // block-uniform
-            __syncthreads();
-            if (threadIdx.x < P.ns * P.ns) {
-                s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
-                s_rrnear[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_near;
-            }
-            __syncthreads();
-            loaded = s;
-        }
         const uint32_t i = P.off + (v - 2u * L.p[0][k]) * 128u + threadIdx.x;
+        __syncthreads();
+        if (threadIdx.x < P.ns * P.ns) {
+            s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
+            s_rrnear[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_near;
+        }
+        __syncthreads();
         neighbour_slot(d, s, i, s_rrcs, s_rrnear, s_pos[warp], s_j[warp], lane);
+        if (!LOOP) break;
     }
 }
 
@@ -775,8 +909,16 @@ __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_
                 cluster_scan<true>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos, s_j, lane);
             else
                 cluster_scan<false>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos, s_j, lane);
-        } else if (real) {
-            lane_scan(d, P, ri, i, rrcs, rrnear, o);
+        } else {
+            const bool lwrap = __any_sync(0xFFFFFFFFu, real && !far_from_faces(P, ri));
+            if (real) {
+                const uint2 c = lwrap ? lane_scan_call<true>(d.sys + s, d.pos, d.cell, d.cell_count, ri, i, rrcs,
+                                                             rrnear, o.out, o.bstride, o.lw, o.cap)
+                                      : lane_scan_call<false>(d.sys + s, d.pos, d.cell, d.cell_count, ri, i, rrcs,
+                                                              rrnear, o.out, o.bstride, o.lw, o.cap);
+                o.nn = c.x;
+                o.nf = c.y;
+            }
         }
     }
     uint32_t count = 0;
@@ -806,9 +948,15 @@ int radix_passes(uint32_t key_bits) { return (int)((key_bits + 7) / 8); }
 // val[passes % 2]
 // Launch grids of the rebuild chain: the kernels loop over the virtual blocks
 // of the rebuild list, so a grid never needs more blocks than the work the
-// engine could hold (the old one-block-per-unit upper bound) nor more than a
-// few waves of resident blocks.
-static unsigned rb_grid(uint32_t upper) { return std::max(1u, std::min(upper, RB_GRID)); }
+// engine could hold (one block per unit of every system).  An engine of
+// several systems caps the grid at RB_GRID, so the systems that do not
+// rebuild cost no blocks; an engine of one system (nothing to compact)
+// launches one block per unit, which the block scheduler balances better
+// than a fixed share per block.
+static unsigned rb_grid(const Dev& d, uint32_t upper)
+{
+    return std::max(1u, d.nsys == 1 ? upper : std::min(upper, RB_GRID));
+}
 
 void launch_rebuild_list(const Dev& d, cudaStream_t st)
 {
@@ -817,13 +965,13 @@ void launch_rebuild_list(const Dev& d, cudaStream_t st)
 
 void launch_sort(const Dev& d, int passes, cudaStream_t st)
 {
-    k_seg_keys<<<rb_grid(d.S_grid / 256), 256, 0, st>>>(d);
+    k_seg_keys<<<rb_grid(d, d.S_grid / 256), 256, 0, st>>>(d);
     for (int p = 0; p < passes; ++p) {
         const uint32_t shift = 8u * p;
         const int cur = p & 1;
-        k_seg_hist<<<rb_grid(d.tiles_grid), RADIX_THREADS, 0, st>>>(d, d.key[cur], shift);
-        k_seg_scan<<<rb_grid(d.nsys), 1024, 0, st>>>(d);
-        k_seg_scatter<<<rb_grid(d.tiles_grid), RADIX_THREADS, 0, st>>>(d, d.key[cur], d.val[cur], d.key[1 - cur],
+        k_seg_hist<<<rb_grid(d, d.tiles_grid), RADIX_THREADS, 0, st>>>(d, d.key[cur], shift);
+        k_seg_scan<<<rb_grid(d, d.nsys), 1024, 0, st>>>(d);
+        k_seg_scatter<<<rb_grid(d, d.tiles_grid), RADIX_THREADS, 0, st>>>(d, d.key[cur], d.val[cur], d.key[1 - cur],
                                                                        d.val[1 - cur], shift);
     }
 }
@@ -832,21 +980,23 @@ int sort_kernel_count(int passes) { return 1 + 3 * passes; }
 
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st)
 {
-    const unsigned grid = rb_grid(d.S_grid / 256);
+    const unsigned grid = rb_grid(d, d.S_grid / 256);
     if (ds) { k_rearrange<true><<<grid, 256, 0, st>>>(d, perm); k_copyback<true><<<grid, 256, 0, st>>>(d); }
     else { k_rearrange<false><<<grid, 256, 0, st>>>(d, perm); k_copyback<false><<<grid, 256, 0, st>>>(d); }
 }
 
 void launch_binning(const Dev& d, cudaStream_t st)
 {
-    k_cell_clear<<<rb_grid((d.cells_grid + 255) / 256 + d.nsys), 256, 0, st>>>(d);
-    k_bin<<<rb_grid(d.S_grid / 256), 256, 0, st>>>(d);
-    k_cell_sort<<<rb_grid((d.cells_grid + 3) / 4 + d.nsys), 128, 0, st>>>(d);
+    k_cell_clear<<<rb_grid(d, (d.cells_grid + 255) / 256 + d.nsys), 256, 0, st>>>(d);
+    k_bin<<<rb_grid(d, d.S_grid / 256), 256, 0, st>>>(d);
+    k_cell_sort<<<rb_grid(d, (d.cells_grid + 3) / 4 + d.nsys), 128, 0, st>>>(d);
 }
 
 void launch_neighbour(const Dev& d, cudaStream_t st)
 {
-    k_neighbour<<<rb_grid(d.S_grid / 128), 128, 0, st>>>(d);
+    // one-system engines launch a block per virtual block (rb_grid)
+    if (d.nsys == 1) k_neighbour<false><<<rb_grid(d, d.S_grid / 128), 128, 0, st>>>(d);
+    else k_neighbour<true><<<rb_grid(d, d.S_grid / 128), 128, 0, st>>>(d);
 }
 
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
