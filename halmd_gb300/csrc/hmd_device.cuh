@@ -29,6 +29,12 @@ constexpr int SLOT_ALIGN = 256;   // slots per system are a multiple of this
 // units of the rebuild list: slots / 256, sorting slots / 256, sort tiles,
 // cells / 256, cells / 4
 constexpr uint32_t RB_UNITS = 5;
+// The shared list scan does a warp's 32 particles in one serial pass over the
+// cells around them; it pays off once a rebuild has enough warps per SM to
+// hide that pass's latency (measured: 1M particles 1.8x faster, 64k
+// particles 1.4x slower), so by default systems of at least this many
+// particles use it
+constexpr uint32_t NBR_SHARED_MIN_N = 1u << 18;
 constexpr int CHUNK = 64;         // granularity of the slot -> system map
 
 // default entries per block of the neighbour-list layout for a force kernel

@@ -538,18 +538,17 @@ __device__ __forceinline__ void cell_sort_one(const Dev& d, uint32_t s, uint32_t
 // appended in cell order and, within a cell, in slot order (deterministic).
 // ---------------------------------------------------------------------------
 
-// resident blocks of 128 threads per SM that the list build's register
-// allocation aims for
-#ifndef HMD_NBR_MINB
-#define HMD_NBR_MINB 8
-#endif
+// Resident blocks of 128 threads per SM that the list build's register
+// allocation aims for.  The shared scan runs without spills at 7 (72
+// registers); at 8 (64 registers) spill traffic in its inner loop raised its
+// instruction count by 14 % (LJ-1M rebuild chain 1.39 ms against 1.43 ms).
+// The per-lane scan of small systems is latency-bound and prefers the
+// occupancy of 8 (KA-64k 0.301 against 0.310 ms, ENS-256 0.458 against
+// 0.471 ms).  A one-system engine on the shared scan takes the first.
+constexpr int NBR_MINB_SHARED = 7;
+constexpr int NBR_MINB_LANE = 8;
 
 constexpr uint32_t NBR_CLUSTER_MAX_CELLS = 150;   // larger cell ranges: per-lane scan
-// The shared scan does a warp's 32 particles in one serial pass over the cells
-// around them; it pays off once a rebuild has enough warps per SM to hide that
-// pass's latency (measured: 1M particles 1.8x faster, 64k particles 1.4x slower)
-constexpr uint32_t NBR_SHARED_MIN_N = 1u << 18;
-
 struct NbrOut {
     uint32_t* out;        // this slot's row in the blocked list
     size_t bstride;       // words between list blocks
@@ -725,7 +724,7 @@ __device__ __forceinline__ void lane_scan(const SysParam& P, const float4* pos, 
 
 // The per-lane scan of one particle, out of line: it then gets its own
 // register allocation instead of sharing the shared scan's (inlined
-// together, the two spilled).  Pointers are passed by value, not the kernel
+// together, the two spilled, and the rebuild chains measured 1-2 % slower).  Pointers are passed by value, not the kernel
 // parameter block; the list counts come back as (near, far).
 template <bool WRAP>
 __device__ __noinline__ uint2 lane_scan_call(const SysParam* Pp, const float4* pos, const uint32_t* cell,
@@ -820,8 +819,8 @@ __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_
 // LOOP = false: the grid has a block per virtual block (one-system engines);
 // without the loop the shared scan spills less (LJ-1M rebuild chain 1.43 ms
 // against 1.49 ms with the loop).
-template <bool LOOP>
-__global__ void __launch_bounds__(128, HMD_NBR_MINB) k_neighbour(Dev d)
+template <bool LOOP, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_neighbour(Dev d)
 {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
@@ -992,11 +991,14 @@ void launch_binning(const Dev& d, cudaStream_t st)
     k_cell_sort<<<rb_grid(d, (d.cells_grid + 3) / 4 + d.nsys), 128, 0, st>>>(d);
 }
 
-void launch_neighbour(const Dev& d, cudaStream_t st)
+void launch_neighbour(const Dev& d, bool shared_scan, cudaStream_t st)
 {
-    // one-system engines launch a block per virtual block (rb_grid)
-    if (d.nsys == 1) k_neighbour<false><<<rb_grid(d, d.S_grid / 128), 128, 0, st>>>(d);
-    else k_neighbour<true><<<rb_grid(d, d.S_grid / 128), 128, 0, st>>>(d);
+    // one-system engines launch a block per virtual block; otherwise one
+    // wave of resident blocks loops over the virtual blocks
+    const unsigned all = std::max(1u, d.S_grid / 128);
+    if (d.nsys == 1 && shared_scan) k_neighbour<false, NBR_MINB_SHARED><<<all, 128, 0, st>>>(d);
+    else if (d.nsys == 1) k_neighbour<false, NBR_MINB_LANE><<<all, 128, 0, st>>>(d);
+    else k_neighbour<true, NBR_MINB_LANE><<<std::min(all, 152u * NBR_MINB_LANE), 128, 0, st>>>(d);
 }
 
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
