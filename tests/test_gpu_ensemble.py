@@ -88,3 +88,32 @@ def test_small_box_lists_match_all_pairs():
                                               dtype=np.float32), inf.neighbour_capacity)
         assert np.array_equal(counts, rc) and np.array_equal(lists, rl)
         eng.close()
+
+
+@pytest.mark.parametrize("scan", [1, 2])
+def test_batched_lists_match_oracle_with_either_scan(scan):
+    # a many-system engine builds its lists in one looped launch over the
+    # rebuilding systems' virtual blocks, with either scan
+    import oracle
+    S = specs()
+    batch = hg.Engine("dsfloat")
+    for sp in S:
+        batch.add_system(hg.system_desc(len(sp["r"]), sp["L"], **sp["desc"]))
+    batch.commit()
+    batch.set_option("neighbour_scan", scan)
+    for k, sp in enumerate(S):
+        load(batch, k, sp)
+    batch.step(30)
+    for k in range(len(S)):
+        batch.request_rebuild(k)
+    batch.force()
+    for k in range(len(S)):
+        inf = batch.info(k)
+        ns = inf.nspecies
+        pos4 = batch.get_raw("r0", k)[batch.get("reverse_id", k)]
+        counts, lists = batch.neighbour_lists(inf.neighbour_capacity, k)
+        rc, rl, mx = oracle.neighbour_full_f32(pos4, np.array(inf.box_f32),
+                                               np.array(inf.rr_cut_skin[:ns * ns], dtype=np.float32),
+                                               inf.neighbour_capacity)
+        assert np.array_equal(counts, rc) and np.array_equal(lists, rl), k
+    batch.close()
