@@ -1268,8 +1268,7 @@ void Engine::rebuild_chain(cudaStream_t st)
         launch_rearrange(d, ds(), d.val[sort_passes_ & 1], st);   // pass p writes val[1 - p % 2]
     }
     launch_binning(d, st);
-    const bool shared_scan = sys_.size() == 1 && (nbr_scan_ == 2u || (nbr_scan_ == 0u && sys_[0].P.n >= NBR_SHARED_MIN_N));
-    launch_neighbour(d, shared_scan, st);
+    launch_neighbour(d, st);
 }
 
 void Engine::ensure_forces(bool aux)

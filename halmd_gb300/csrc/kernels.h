@@ -40,9 +40,7 @@ void launch_sort(const Dev& d, int passes, cudaStream_t st);
 int sort_kernel_count(int passes);
 void launch_rearrange(const Dev& d, bool ds, const uint32_t* perm, cudaStream_t st);
 void launch_binning(const Dev& d, cudaStream_t st);
-// shared_scan: the engine's one system uses the shared list scan (picks the
-// list build's register budget)
-void launch_neighbour(const Dev& d, bool shared_scan, cudaStream_t st);
+void launch_neighbour(const Dev& d, cudaStream_t st);
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st);
 
 // observables (kernels_obs.cu)

@@ -538,15 +538,12 @@ __device__ __forceinline__ void cell_sort_one(const Dev& d, uint32_t s, uint32_t
 // appended in cell order and, within a cell, in slot order (deterministic).
 // ---------------------------------------------------------------------------
 
-// Resident blocks of 128 threads per SM that the list build's register
-// allocation aims for.  The shared scan runs without spills at 7 (72
-// registers); at 8 (64 registers) spill traffic in its inner loop raised its
-// instruction count by 14 % (LJ-1M rebuild chain 1.39 ms against 1.43 ms).
-// The per-lane scan of small systems is latency-bound and prefers the
-// occupancy of 8 (KA-64k 0.301 against 0.310 ms, ENS-256 0.458 against
-// 0.471 ms).  A one-system engine on the shared scan takes the first.
-constexpr int NBR_MINB_SHARED = 7;
-constexpr int NBR_MINB_LANE = 8;
+// Resident blocks of 128 threads per SM of the list build (64 registers).
+// Both scans run without spills at this budget as long as the one-system
+// variant recomputes its slot from the block index (held in a register, it
+// pushed spill traffic into the shared scan's inner loop: 14 % more
+// instructions, and 72 registers without spills measured 1 % slower than 64).
+constexpr int NBR_MINB = 8;
 
 constexpr uint32_t NBR_CLUSTER_MAX_CELLS = 150;   // larger cell ranges: per-lane scan
 struct NbrOut {
@@ -816,11 +813,9 @@ __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_
 // Only v stays live across the scan: the list bounds are read again each
 // round (the list stores may alias them, so they are not kept in
 // registers) and the pair table is staged again per virtual block.
-// LOOP = false: the grid has a block per virtual block (one-system engines);
-// without the loop the shared scan spills less (LJ-1M rebuild chain 1.43 ms
-// against 1.49 ms with the loop).
-template <bool LOOP, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_neighbour(Dev d)
+// LOOP = false: the grid has a block per virtual block (one-system engines).
+template <bool LOOP>
+__global__ void __launch_bounds__(128, NBR_MINB) k_neighbour(Dev d)
 {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
@@ -830,10 +825,12 @@ __global__ void __launch_bounds__(128, MINB) k_neighbour(Dev d)
     for (uint32_t v = blockIdx.x;; v += gridDim.x) {
         const RbList L = rb_list(d);
         if (v >= 2u * L.p[0][L.n]) break;
-        const uint32_t k = rb_find(L.p[0], L.n, v >> 1);
-        const uint32_t s = L.sys[k];
+        // one system (LOOP = false): system 0 at slot 0, so the slot is
+        // recomputed from the block index instead of held in a register
+        const uint32_t k = LOOP ? rb_find(L.p[0], L.n, v >> 1) : 0u;
+        const uint32_t s = LOOP ? L.sys[k] : 0u;
         const SysParam& P = d.sys[s];
-        const uint32_t i = P.off + (v - 2u * L.p[0][k]) * 128u + threadIdx.x;
+        const uint32_t i = LOOP ? P.off + (v - 2u * L.p[0][k]) * 128u + threadIdx.x : blockIdx.x * 128u + threadIdx.x;
         __syncthreads();
         if (threadIdx.x < P.ns * P.ns) {
             s_rrcs[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_cut_skin;
@@ -991,14 +988,13 @@ void launch_binning(const Dev& d, cudaStream_t st)
     k_cell_sort<<<rb_grid(d, (d.cells_grid + 3) / 4 + d.nsys), 128, 0, st>>>(d);
 }
 
-void launch_neighbour(const Dev& d, bool shared_scan, cudaStream_t st)
+void launch_neighbour(const Dev& d, cudaStream_t st)
 {
     // one-system engines launch a block per virtual block; otherwise one
     // wave of resident blocks loops over the virtual blocks
     const unsigned all = std::max(1u, d.S_grid / 128);
-    if (d.nsys == 1 && shared_scan) k_neighbour<false, NBR_MINB_SHARED><<<all, 128, 0, st>>>(d);
-    else if (d.nsys == 1) k_neighbour<false, NBR_MINB_LANE><<<all, 128, 0, st>>>(d);
-    else k_neighbour<true, NBR_MINB_LANE><<<std::min(all, 152u * NBR_MINB_LANE), 128, 0, st>>>(d);
+    if (d.nsys == 1) k_neighbour<false><<<all, 128, 0, st>>>(d);
+    else k_neighbour<true><<<std::min(all, 152u * NBR_MINB), 128, 0, st>>>(d);
 }
 
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
