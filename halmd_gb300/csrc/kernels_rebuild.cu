@@ -80,9 +80,10 @@ __global__ void k_hilbert_keys(Dev d, uint32_t* keys)
 // over every slot (and cell) whose blocks mostly exit, k_rebuild_list
 // compacts the rebuilding systems and the prefix sums of their virtual blocks
 // in each unit the chain's kernels use, and those kernels loop over the
-// virtual blocks with a grid of at most RB_GRID blocks.  A virtual block
-// covers the same slots (or cells) as one block of a launch over everything,
-// so results do not change.
+// virtual blocks with a grid of at most RB_GRID blocks (an engine of one
+// system, with nothing to compact, launches a block per virtual block).  A
+// virtual block covers the same slots (or cells) as one block of a launch
+// over everything, so results do not change.
 // ---------------------------------------------------------------------------
 
 constexpr unsigned RB_GRID = 152 * 8;
