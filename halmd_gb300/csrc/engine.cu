@@ -28,6 +28,9 @@ Engine::Engine(int precision, int device) : precision_(precision), device_(devic
     HMD_CUDA(cudaGetDeviceCount(&ndev));
     if (device < 0 || device >= ndev) throw Error(HMD_ERR_INVALID, "no such CUDA device");
     HMD_CUDA(cudaSetDevice(device));
+    int sms = 0;
+    HMD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    sm_count_ = (uint32_t)std::max(sms, 1);
     HMD_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     HMD_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
 }
@@ -791,6 +794,7 @@ Dev Engine::dev() const
     d.S_grid = grid_slots_ ? grid_slots_ : S_;
     d.cells_grid = grid_cells_ ? grid_cells_ : total_cells_;
     d.tiles_grid = capacity_ ? d.S_grid / SORT_TILE : ntiles_;
+    d.sm_count = sm_count_;
     d.status = status_.p; d.done = done_.p; d.any_rebuild = any_rebuild_.p;
     d.key[0] = key0_.p; d.key[1] = key1_.p; d.val[0] = val0_.p; d.val[1] = val1_.p; d.hist = hist_.p;
     d.tiles = tiles_.p; d.ntiles = ntiles_; d.rb = rb_.p;

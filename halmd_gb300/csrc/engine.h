@@ -173,6 +173,7 @@ private:
     uint32_t lanes_ = 0;        // force-kernel lanes per particle (0: choose at commit)
     uint32_t lb_ = 0;          // list block width option (0 auto, 4, 8)
     uint32_t nbr_scan_ = 0;   // list build: 0 auto, 1 per lane, 2 shared scan per warp
+    uint32_t sm_count_ = 0;   // SMs of the device
     uint32_t grid_slots_ = 0, grid_cells_ = 0;   // launch-grid extents (update_grid_extent)
     void update_grid_extent();
     uint32_t force_kinds_ = 0;  // Dev::force_kinds: kinds of the committed systems (0 in capacity mode)

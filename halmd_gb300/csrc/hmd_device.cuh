@@ -171,6 +171,7 @@ struct Dev {
     // mode: the slots, sort tiles and cells below the high-water mark of the
     // systems present, rounded up to a power of two)
     uint32_t S_grid, cells_grid, tiles_grid;
+    uint32_t sm_count;         // SMs of the device (grids of one resident wave)
     // work list of the rebuild chain (k_rebuild_list): [0] count, then the
     // rebuilding systems and the prefix sums of their virtual blocks
     uint32_t* rb;

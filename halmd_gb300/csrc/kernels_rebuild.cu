@@ -80,13 +80,13 @@ __global__ void k_hilbert_keys(Dev d, uint32_t* keys)
 // over every slot (and cell) whose blocks mostly exit, k_rebuild_list
 // compacts the rebuilding systems and the prefix sums of their virtual blocks
 // in each unit the chain's kernels use, and those kernels loop over the
-// virtual blocks with a grid of at most RB_GRID blocks (an engine of one
+// virtual blocks with a grid of at most RB_WAVE blocks per SM (an engine of one
 // system, with nothing to compact, launches a block per virtual block).  A
 // virtual block covers the same slots (or cells) as one block of a launch
 // over everything, so results do not change.
 // ---------------------------------------------------------------------------
 
-constexpr unsigned RB_GRID = 152 * 8;
+constexpr unsigned RB_WAVE = 8;   // blocks per SM of a capped rebuild-chain grid
 
 struct RbList {
     uint32_t n;
@@ -946,13 +946,13 @@ int radix_passes(uint32_t key_bits) { return (int)((key_bits + 7) / 8); }
 // Launch grids of the rebuild chain: the kernels loop over the virtual blocks
 // of the rebuild list, so a grid never needs more blocks than the work the
 // engine could hold (one block per unit of every system).  An engine of
-// several systems caps the grid at RB_GRID, so the systems that do not
-// rebuild cost no blocks; an engine of one system (nothing to compact)
-// launches one block per unit, which the block scheduler balances better
-// than a fixed share per block.
+// several systems caps the grid at RB_WAVE blocks per SM, so the systems
+// that do not rebuild cost no blocks; an engine of one system (nothing to
+// compact) launches one block per unit, which the block scheduler balances
+// better than a fixed share per block.
 static unsigned rb_grid(const Dev& d, uint32_t upper)
 {
-    return std::max(1u, d.nsys == 1 ? upper : std::min(upper, RB_GRID));
+    return std::max(1u, d.nsys == 1 ? upper : std::min(upper, RB_WAVE * d.sm_count));
 }
 
 void launch_rebuild_list(const Dev& d, cudaStream_t st)
@@ -995,7 +995,7 @@ void launch_neighbour(const Dev& d, cudaStream_t st)
     // wave of resident blocks loops over the virtual blocks
     const unsigned all = std::max(1u, d.S_grid / 128);
     if (d.nsys == 1) k_neighbour<false><<<all, 128, 0, st>>>(d);
-    else k_neighbour<true><<<std::min(all, 152u * NBR_MINB), 128, 0, st>>>(d);
+    else k_neighbour<true><<<std::min(all, d.sm_count * NBR_MINB), 128, 0, st>>>(d);
 }
 
 void launch_hilbert_keys(const Dev& d, uint32_t* keys, cudaStream_t st)
