@@ -289,18 +289,29 @@ __global__ void __launch_bounds__(256) k_thermo_reduce(Dev d)
 // host launchers
 // ---------------------------------------------------------------------------
 
+// threads per block of the integrate kernels (at most 256: step_decision's
+// per-warp maxima; at least 64 so blocks stay inside one system).  128
+// measured the same as 256 (KA-64k 1.023e9 against 1.022e9, LJ-1M 3.59e9
+// against 3.57e9 particle-steps/s, one run each)
+#ifndef HMD_STEP_THREADS
+#define HMD_STEP_THREADS 256
+#endif
+static_assert(HMD_STEP_THREADS >= 64 && HMD_STEP_THREADS <= 256 && HMD_STEP_THREADS % 64 == 0, "step block size");
+
 void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool use_handle, cudaStream_t st)
 {
-    const unsigned grid = d.S_grid / 256;
-    if (ds) k_integrate<true, false><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
-    else k_integrate<false, false><<<grid, 256, 0, st>>>(d, h, use_handle ? 1 : 0);
+    constexpr unsigned T = HMD_STEP_THREADS;
+    const unsigned grid = d.S_grid / T;
+    if (ds) k_integrate<true, false><<<grid, T, 0, st>>>(d, h, use_handle ? 1 : 0);
+    else k_integrate<false, false><<<grid, T, 0, st>>>(d, h, use_handle ? 1 : 0);
 }
 
 void launch_finalize_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, cudaStream_t st)
 {
-    const unsigned grid = d.S_grid / 256;
-    if (ds) k_integrate<true, true><<<grid, 256, 0, st>>>(d, h, 1);
-    else k_integrate<false, true><<<grid, 256, 0, st>>>(d, h, 1);
+    constexpr unsigned T = HMD_STEP_THREADS;
+    const unsigned grid = d.S_grid / T;
+    if (ds) k_integrate<true, true><<<grid, T, 0, st>>>(d, h, 1);
+    else k_integrate<false, true><<<grid, T, 0, st>>>(d, h, 1);
 }
 
 void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st)
