@@ -61,16 +61,17 @@ class Server:
     """Admit, advance and retire jobs in one engine with reserved capacity.
 
     budget_fraction: share of the GPU's memory the engine may reserve;
-    max_slots caps the reservation (the engine's launch grids span it)."""
+    max_slots caps the reservation (the engine's launch grids span it);
+    engine_factory(precision) makes the engine (the C-ABI Engine)."""
 
     def __init__(self, budget_fraction=0.8, max_slots=1 << 24, max_jobs=1024, neighbour_capacity=288,
-                 precision="dsfloat", chunk=100, force_lanes=None, total_bytes=None):
+                 precision="dsfloat", chunk=100, force_lanes=None, total_bytes=None, engine_factory=Engine):
         total = total_bytes if total_bytes is not None else device_memory_bytes()
         # device bytes per slot: phase space (+ copies), list slots and snapshots
         per_slot = 360 + 4 * neighbour_capacity
         budget_slots = int(budget_fraction * total // per_slot) if total else max_slots
         slots = max(2048, min(max_slots, budget_slots))
-        self.engine = Engine(precision)
+        self.engine = engine_factory(precision)
         self.engine.reserve(slots, max_jobs, neighbour_capacity)
         if force_lanes:
             self.engine.set_option("force_lanes", force_lanes)
