@@ -77,3 +77,55 @@ def test_isolated_pairs_match_host_functor(trunc):
         assert abs(2 * en[2 * k] - u) <= TOL * scale, (trunc, a, b, r, 2 * en[2 * k], u)
         assert abs(2 * en[2 * k + 1] - u) <= TOL * scale, (trunc, a, b, r)
     eng.close()
+
+
+def test_smooth_r4_near_cutoff_pairs_match_host_functor():
+    # test/unit/mdsim/forces/trunc/smooth_r4.cpp: r_c = 2.5, 2, 2^(1/6) sigma,
+    # h = 1/256, rows close to r_c; the GPU bar there (:88-91) is
+    # tol = 8 eps (1 + r_c / (r_c - r)) + 10 eps, forces within
+    # 2 tol max(|F|, 1), energies within 2 tol relative
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "smooth_r4_tables.json")))
+    eps, sigma, rcs, h = g["epsilon"], g["sigma"], np.asarray(g["r_cut_sigma"], dtype=float), g["h"]
+    skin = 0.3
+    rc = rcs * np.asarray(sigma, dtype=float)
+    pairs = []
+    for name, (a, b) in {"aa": (0, 0), "ab": (0, 1), "bb": (1, 1)}.items():
+        for row in g["tables"][name]:
+            if row[0] < rc[a, b]:
+                pairs.append((a, b, row[0]))
+    assert len(pairs) >= 10
+    spacing = 2 * (rc.max() + skin) + 5.0
+    L = np.array([2 * spacing * (len(pairs) + 1), 2 * rc.max() + 10.0, 2 * rc.max() + 10.0])
+    n = 2 * len(pairs)
+    pos = np.zeros((n, 3))
+    sp = np.zeros(n, dtype=np.uint32)
+    for k, (a, b, r) in enumerate(pairs):
+        x0 = (k + 1) * spacing         # x0 >= r: the float difference is exact
+        pos[2 * k] = (x0, 0.0, 0.0)
+        pos[2 * k + 1] = (x0 + r, 0.0, 0.0)
+        sp[2 * k], sp[2 * k + 1] = a, b
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, L, epsilon=eps, sigma=sigma, r_cut=rcs, truncation="smooth_r4",
+                                  smoothing=h, skin=skin, timestep=0.001))
+    eng.commit()
+    eng.set("species", sp)
+    eng.set("position", pos)
+    eng.set("velocity", np.zeros((n, 3)))
+    eng.force(aux=True)
+    f = eng.get("force")
+    en = eng.get("potential_energy")
+    x = eng.get_raw("position_hi")[eng.get("reverse_id")][:, 0].astype(np.float64)
+    pot = oracle.Potential(eps, sigma, rcs, "smooth_r4", h=h)
+    worst = 0.0
+    for k, (a, b, r) in enumerate(pairs):
+        d = x[2 * k] - x[2 * k + 1]
+        fval, u = pot(d * d, a, b)
+        tol = 8 * EPS_F * (1 + rc[a, b] / (rc[a, b] - abs(d))) + 10 * EPS_F
+        for q in (2 * k, 2 * k + 1):
+            fref = fval * d if q == 2 * k else -fval * d
+            err = abs(f[q, 0] - fref) / (2 * tol * max(abs(fref), 1.0))
+            worst = max(worst, err)
+            assert err <= 1.0, (a, b, r, f[q, 0], fref)
+            assert abs(2 * en[q] - u) <= 2 * tol * abs(u), (a, b, r, 2 * en[q], u)
+    print("largest force error / bound: %.3g" % worst)
+    eng.close()
