@@ -1625,15 +1625,18 @@ void Engine::force(bool aux)
     toc(aux ? "force_aux" : "force");
     uint32_t status = 0;
     download(status_, 0, 1, &status);
-    if (status != 0) {
+    // A cell overflow also hides list lengths (the lists were built from
+    // truncated cells), so capacities can grow in stages: rebuild until the
+    // build fits.  Each round grows a capacity strictly (cells up to 256
+    // slots, lists until an allocation fails) or gives up, so this ends.
+    while (status != 0) {
         if (!grow_after_overflow(status)) throw Error(HMD_ERR_OVERFLOW, "capacity overflow in list rebuild");
         HMD_CUDA(cudaMemsetAsync(status_.p, 0, 4, stream_));
-        launch_mark(d, true, stream_);
         const Dev d2 = dev();
+        launch_mark(d2, true, stream_);
         rebuild_chain(stream_);
         launch_force(d2, aux, stream_);
         download(status_, 0, 1, &status);
-        if (status != 0) throw Error(HMD_ERR_OVERFLOW, "capacity overflow in list rebuild");
     }
     forces_valid_ = true;
     aux_valid_ = aux;

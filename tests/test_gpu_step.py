@@ -194,6 +194,34 @@ def test_binning_bit_exact():
     eng.close()
 
 
+def test_binning_non_uniform_density():
+    # test/unit/mdsim/binning.cpp:120-200 bins non-uniform densities: here
+    # the density grows as u^3 along x (4x the mean at the dense end), which
+    # overflows cells sized for a uniform fluid; after the capacity recovery
+    # every particle is binned exactly once, in the oracle's cell and order
+    eng, r, v, L = lj_engine(ncell=8)
+    n = r.shape[0]
+    rng = np.random.default_rng(21)
+    u = rng.uniform(size=n) ** 0.25
+    pos = np.column_stack([(u - 0.5) * L, rng.uniform(-0.5 * L, 0.5 * L, size=(n, 2))])
+    cs0 = eng.info().cell_size
+    eng.set("position", pos)
+    eng.force()
+    inf = eng.info()
+    assert inf.cell_size > cs0            # the dense end overflowed the first sizing
+    ncell = np.array(inf.ncell[:], dtype=np.int32)
+    Lf = np.array(inf.box_f32, dtype=np.float32)
+    cell_len = Lf / ncell.astype(np.float32)
+    pos4 = eng.get_raw("position_hi")
+    cells, _, maxocc = oracle.binning_f32(pos4, ncell, cell_len, inf.cell_size)
+    got = eng.get_raw("cells")
+    assert maxocc == inf.max_cell_occupancy
+    assert np.array_equal(got, cells)
+    real = got[got != 0xFFFFFFFF]
+    assert real.size == n and np.unique(real).size == n
+    eng.close()
+
+
 def test_hilbert_keys_and_sort_permutation():
     eng, r, v, L = lj_engine(ncell=8)
     n = r.shape[0]
