@@ -117,3 +117,29 @@ def test_batched_lists_match_oracle_with_either_scan(scan):
                                                inf.neighbour_capacity)
         assert np.array_equal(counts, rc) and np.array_equal(lists, rl), k
     batch.close()
+
+
+def test_tiny_systems_one_and_two_particles():
+    # the smallest inputs: one particle has an empty list and no force, so it
+    # moves in a straight line; two particles interact as a pair (equal and
+    # opposite forces); both advance beside each other in one engine
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(1, 10.0, r_cut=2.5, truncation="shifted", skin=0.3, timestep=0.001))
+    eng.add_system(hg.system_desc(2, 10.0, r_cut=2.5, truncation="shifted", skin=0.3, timestep=0.001))
+    eng.commit()
+    eng.set("position", np.array([[0.5, -0.25, 1.0]]), 0)
+    eng.set("velocity", np.array([[0.3, -0.2, 0.1]]), 0)
+    eng.set("position", np.array([[0.0, 0.0, 0.0], [1.2, 0.0, 0.0]]), 1)
+    eng.set("velocity", np.zeros((2, 3)), 1)
+    eng.force()
+    assert np.all(eng.get("force", 0) == 0)
+    counts, _ = eng.neighbour_lists(s=0)
+    assert counts[0] == 0
+    f = eng.get("force", 1)
+    assert f[0, 0] != 0 and f[0, 0] == -f[1, 0]
+    eng.step(100)
+    np.testing.assert_allclose(eng.get("unwrapped_position", 0), [[0.53, -0.27, 1.01]], atol=1e-6)
+    np.testing.assert_allclose(eng.get("velocity", 0), [[0.3, -0.2, 0.1]], atol=1e-12)
+    v = eng.get("velocity", 1)
+    assert abs(v[0, 0] + v[1, 0]) < 1e-6      # momentum conserved
+    eng.close()
