@@ -68,3 +68,21 @@ def test_struct_layout_matches_header(lib):
         want.append(ctypes.sizeof(cls))
         want.extend(getattr(cls, f).offset for f, _ in cls._fields_)
     assert got == want
+
+
+def test_enum_constants_agree_with_the_header():
+    # the binding's and the oracle's name -> value maps against the header's
+    # #defines (the oracle's own integrator enum is internal and not checked)
+    import re
+    import oracle
+    text = open(os.path.join(os.path.dirname(_lib.LIB_PATH), "..", "include", "halmd_gb300.h")).read()
+
+    def defines(prefix):
+        return {m.group(1).lower(): int(m.group(2))
+                for m in re.finditer(r"#define HMD_%s_(\w+)\s+(\d+)" % prefix, text)}
+
+    trunc, pot, integ = defines("TRUNC"), defines("POTENTIAL"), defines("INTEGRATOR")
+    assert trunc == _lib.TRUNCATION == oracle.TRUNC
+    assert pot == _lib.POTENTIAL == oracle.POTENTIAL
+    short = {k: v for k, v in _lib.INTEGRATOR.items() if not k.startswith("verlet_")}
+    assert integ == short
