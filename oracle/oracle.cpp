@@ -166,6 +166,9 @@ static inline void pot_bare(const orc_pot* p, double rr, int ab, double* fval, d
     }
 }
 
+/* host/potentials/pair/{lennard_jones.hpp:56-66, mie.cpp:72-92, morse.hpp:64-77,
+ * power_law.hpp:129-148}; truncation constants as truncations/{shifted,
+ * force_shifted,smooth_r4}.hpp */
 /* any potential: idx_m = mie m or power_law index, idx_n = mie n; r_min and
  * distortion for morse (r_min in absolute units); null where unused */
 ORC_API int orc_pot_init_any(orc_pot* p, int pot, int ns, const double* eps, const double* sigma,
@@ -278,6 +281,7 @@ static inline void acc_merge(orc_acc& a, orc_acc const& b)
     }
 }
 
+/* numeric/accumulator.hpp:83-119 */
 /* out[0..4] = count, mean, variance, sigma, error_of_mean, sum */
 ORC_API void orc_accumulate(int n, const double* x, double* out)
 {
@@ -307,6 +311,7 @@ static inline double reduce_periodic_d(double& r, double L)
 /* FP32 conventions shared with the CUDA kernels (bit-exact)                  */
 /* ------------------------------------------------------------------------ */
 
+/* mdsim/gpu/box_kernel.cuh:37-59 */
 /* minimum image in float: k = rint(dr * (1/L)); dr -= k * L */
 static inline float min_image_f(float dr, float L, float Linv)
 {
@@ -314,6 +319,7 @@ static inline float min_image_f(float dr, float L, float Linv)
     return dr - k * L;
 }
 
+/* the list criterion of from_binning_kernel.cu:144-163 */
 /* squared distance in float, fixed evaluation order, no contraction */
 static inline float rr_f(float dx, float dy, float dz)
 {
@@ -323,6 +329,7 @@ static inline float rr_f(float dx, float dy, float dz)
     return (xx + yy) + zz;
 }
 
+/* species stored as the bits of position.w (mdsim/gpu/particle.hpp:56-88) */
 static inline u32 species_of(const float* pos4, int i)
 {
     u32 s;
@@ -352,6 +359,7 @@ ORC_API int orc_binning_sizing(int n, const double* L, double r_cut_max, double 
     return (int)(warp * std::ceil(nwarps / ncells));
 }
 
+/* mdsim/gpu/binning_kernel.cu:36-75 */
 /* cell index of a float position: (uint)(r / cell_length + ncell) % ncell */
 static inline u32 cell_index_f(const float* r, const float* cell_len, const int* ncell)
 {
@@ -363,6 +371,7 @@ static inline u32 cell_index_f(const float* r, const float* cell_len, const int*
     return (idx[2] * ncell[1] + idx[1]) * ncell[0] + idx[0];
 }
 
+/* mdsim/gpu/binning_kernel.cu:60-139 (compute_cell, gen_index, find_cell_offset, assign_cells) */
 /*
  * Fill `cells` [ncells * cell_size] with the particle indices of every cell
  * in ascending order, padded with 0xFFFFFFFF (same contents as the
@@ -629,6 +638,7 @@ static void force_half(int n, const double* r, const u32* sp, const double* L, c
     if (totals) { totals[0] = epot; totals[1] = vir; }
 }
 
+/* host/forces/pair_trunc.hpp:219-344 over host/neighbours/from_binning.cpp:118-229 */
 /*
  * Pair forces of a snapshot in FP64 (cell list + half list, complete for
  * pairs inside r_cut).  totals[0] = total potential energy, totals[1] =
@@ -744,6 +754,7 @@ ORC_API void orc_integrate_f32(int n, int ds, float* r4, float* v4, float* img4,
     }
 }
 
+/* second half-kick in float / dsfloat (gpu/integrators/verlet_kernel.cu:78-98) */
 ORC_API void orc_finalize_f32(int n, int ds, const float* r4, float* v4, const float* f4, float dt_half)
 {
     float* vlo = v4 + 4 * (size_t)n;
@@ -790,6 +801,8 @@ static inline void mulhilo(u32 a, u32 b, u32& hi, u32& lo)
     lo = (u32)p;
 }
 
+/* the engine's keyed stream; it replaces the reference's rand48
+ * (random/gpu/rand48_kernel.cuh:61-78), whose state is per thread */
 ORC_API void orc_philox4x32_10(const u32* ctr_in, const u32* key_in, u32* out)
 {
     u32 c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
@@ -881,6 +894,7 @@ static inline void hswap(u32& v, u32& a, u32& b, u32 mask)
     std::swap(a, b);
 }
 
+/* mdsim/sorts/hilbert_kernel.hpp:70-230 */
 /* r: coordinates already divided by the box length */
 static u32 hilbert_map3(float x0, float x1, float x2, unsigned depth)
 {
@@ -942,6 +956,7 @@ ORC_API void orc_stable_argsort_u32(int n, const u32* keys, u32* perm)
 /* observables                                                               */
 /* ------------------------------------------------------------------------ */
 
+/* observables/gpu/thermodynamics.cpp:68-190, thermodynamics_kernel.cu:35-106 */
 /*
  * Σ m v², Σ m v (3), Σ e_pot, Σ virial trace in double; out[0] = 0.5 Σ m v²,
  * out[1..3] = Σ m v, out[4] = Σ m.
@@ -1040,6 +1055,7 @@ ORC_API void orc_isf(int nshell, const int* shell, const double* rho1, const dou
     }
 }
 
+/* part of pick_lattice_points_from_shell (algorithm/host/pick_lattice_points.hpp:74-160) */
 static bool is_coprime3(const unsigned* h)
 {
     auto gcd = [](unsigned a, unsigned b) { while (b) { unsigned t = a % b; a = b; b = t; } return a; };
@@ -1242,6 +1258,8 @@ static double chain_half_step(orc_chain& c, double en_kin_2, double dt)
     return s;
 }
 
+/* host/integrators/{verlet.cpp:59-101, verlet_nvt_andersen.cpp:96-137,
+ * verlet_nvt_hoover.cpp, euler.cpp} with the skin/2 rule of from_binning.cpp:130 */
 enum { ORC_VERLET = 0, ORC_ANDERSEN = 1, ORC_HOOVER = 2, ORC_BOLTZMANN = 3, ORC_EULER = 4 };
 
 ORC_API int orc_md_run_any(int n, double* r, double* v, double* image, const u32* sp_in, const double* mass_in,
