@@ -44,6 +44,9 @@ __device__ __forceinline__ void block_moments(const Dev& d, double* acc)
     }
 }
 
+// Second half-kick (gpu/integrators/verlet_kernel.cu:78-98) or Andersen
+// collisions (verlet_nvt_andersen_kernel.cu:97-171, with the per-particle
+// host convention of host/integrators/verlet_nvt_andersen.cpp:111-137).
 // MOM: also the per-block moments of the new velocities (engines with a
 // Nose-Hoover or Maxwell-Boltzmann thermostat)
 template <bool DS, bool MOM>
@@ -182,6 +185,9 @@ __global__ void __launch_bounds__(256) k_thermostat_apply(Dev d)
     if (DS) d.vel[d.S + i] = vl;
 }
 
+// First half-kick, drift and wrap (gpu/integrators/verlet_kernel.cu:38-72)
+// with the displacement maximum (max_displacement_kernel.cu:37-68) and the
+// skin/2 rebuild decision (neighbours/from_binning.cpp:130).
 // FIN: the finalize of the previous step (its force is in d.force) runs
 // first, on the same registers: one pass over the phase space per step
 // inside a captured chunk.  The per-system flags it reads (live,
@@ -202,8 +208,9 @@ __global__ void __launch_bounds__(256) k_integrate(Dev d, cudaGraphConditionalHa
 }
 
 // Mark systems live for a force evaluation outside a step (set-up, or a
-// force requested through the module interface); `rebuild_all` also flags
-// every active system for a list rebuild.
+// force requested through the module interface, as particle.cpp:221-253
+// evaluates forces on demand); `rebuild_all` also flags every active
+// system for a list rebuild.
 __global__ void k_mark(Dev d, int rebuild_all)
 {
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < d.nsys; q += gridDim.x * blockDim.x) {
