@@ -5,11 +5,21 @@ HMD_ERR_NOMEM), retirement when a job's step count is reached, the
 reservation arithmetic, and the errors the server passes on.  The device
 side of the same server is tested in test_gpu_serve.py.
 """
+import os
+
 import numpy as np
 import pytest
 
-from halmd_gb300 import serve
+from halmd_gb300 import _lib, serve
 from halmd_gb300._lib import HmdError
+
+
+@pytest.fixture(autouse=True, scope="module")
+def built():
+    # system descriptions come from the C library (no GPU needed)
+    if not os.path.exists(_lib.LIB_PATH):
+        from halmd_gb300 import build
+        build.build()
 
 
 class FakeEngine:
