@@ -556,10 +556,13 @@ void Engine::commit()
 
     // everything starts as ghosts owned by the null system (capacity mode)
     {
-        std::vector<float4> hpos(S, make_float4(0, 0, 0, f32_from_bits(PLACEHOLDER)));
-        HMD_CUDA(cudaMemcpyAsync(pos_.p, hpos.data(), S * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+        std::vector<float4> hpos(2 * S, make_float4(0, 0, 0, 0));
+        for (size_t k = 0; k < S; ++k) hpos[2 * k].w = f32_from_bits(PLACEHOLDER);   // hi words: ghosts
+        HMD_CUDA(cudaMemcpyAsync(pos_.p, hpos.data(), 2 * S * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+        sync();
+        for (size_t k = 0; k < S; ++k) hpos[k] = make_float4(0, 0, 0, f32_from_bits(PLACEHOLDER));
         HMD_CUDA(cudaMemcpyAsync(r0_.p, hpos.data(), S * sizeof(float4), cudaMemcpyHostToDevice, stream_));
-        HMD_CUDA(cudaMemsetAsync(pos_.p + S, 0, S * sizeof(float4), stream_));
+        sync();   // the staging vector goes out of scope
         HMD_CUDA(cudaMemsetAsync(vel_.p, 0, vel_.bytes(), stream_));
         HMD_CUDA(cudaMemsetAsync(img_.p, 0, img_.bytes(), stream_));
         HMD_CUDA(cudaMemsetAsync(force_.p, 0, force_.bytes(), stream_));
@@ -612,9 +615,9 @@ void Engine::install(uint32_t s)
         ids[t] = real ? t : PLACEHOLDER;
         rids[t] = P.off + t;
     }
-    HMD_CUDA(cudaMemcpyAsync(pos_.p + P.off, hp.data(), P.A * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    upload_pos(false, P.off, P.A, hp.data());
     HMD_CUDA(cudaMemcpyAsync(r0_.p + P.off, hp.data(), P.A * sizeof(float4), cudaMemcpyHostToDevice, stream_));
-    HMD_CUDA(cudaMemsetAsync(pos_.p + S + P.off, 0, P.A * sizeof(float4), stream_));
+    HMD_CUDA(cudaMemset2DAsync(pos_.p + 2 * (size_t)P.off + 1, 2 * sizeof(float4), 0, sizeof(float4), P.A, stream_));
     HMD_CUDA(cudaMemcpyAsync(vel_.p + P.off, hv.data(), P.A * sizeof(float4), cudaMemcpyHostToDevice, stream_));
     HMD_CUDA(cudaMemsetAsync(vel_.p + S + P.off, 0, P.A * sizeof(float4), stream_));
     HMD_CUDA(cudaMemsetAsync(img_.p + P.off, 0, P.A * sizeof(float4), stream_));
@@ -691,7 +694,7 @@ void Engine::remove_system(uint32_t s)
     if (!capacity_) throw Error(HMD_ERR_STATE, "systems leave only engines with a reserved capacity");
     SysParam P = sys_[s].P;
     std::vector<float4> ghost(P.A, make_float4(0, 0, 0, f32_from_bits(PLACEHOLDER)));
-    HMD_CUDA(cudaMemcpyAsync(pos_.p + P.off, ghost.data(), P.A * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    upload_pos(false, P.off, P.A, ghost.data());
     HMD_CUDA(cudaMemsetAsync(id_.p + P.off, 0xFF, P.A * 4, stream_));
     std::vector<uint32_t> own(std::max<uint32_t>(P.A / CHUNK, P.ncells), null_sys_);
     HMD_CUDA(cudaMemcpyAsync(chunk_sys_.p + P.off / CHUNK, own.data(), (P.A / CHUNK) * 4, cudaMemcpyHostToDevice, stream_));
@@ -791,6 +794,7 @@ Dev Engine::dev() const
     d.cell = cell_.p; d.cell_count = cell_count_.p; d.cell_sys = cell_sys_.p; d.total_cells = total_cells_;
     d.sys = dsys_.p; d.st = dst_.p; d.pair = dpair_.p; d.chunk_sys = chunk_sys_.p;
     d.S = S_; d.nsys = table_size_;
+    d.ds = ds() ? 1u : 0u;
     d.S_grid = grid_slots_ ? grid_slots_ : S_;
     d.cells_grid = grid_cells_ ? grid_cells_ : total_cells_;
     d.tiles_grid = capacity_ ? d.S_grid / SORT_TILE : ntiles_;
@@ -816,6 +820,22 @@ void Engine::upload(DevBuf<T>& b, size_t first, size_t count, const T* host)
 {
     if (count == 0) return;
     HMD_CUDA(cudaMemcpyAsync(b.p + first, host, count * sizeof(T), cudaMemcpyHostToDevice, stream_));
+    sync();
+}
+
+void Engine::download_pos(bool lo, size_t first, size_t count, float4* host)
+{
+    if (count == 0) return;
+    HMD_CUDA(cudaMemcpy2DAsync(host, sizeof(float4), pos_.p + 2 * first + (lo ? 1 : 0), 2 * sizeof(float4),
+                               sizeof(float4), count, cudaMemcpyDeviceToHost, stream_));
+    sync();
+}
+
+void Engine::upload_pos(bool lo, size_t first, size_t count, const float4* host)
+{
+    if (count == 0) return;
+    HMD_CUDA(cudaMemcpy2DAsync(pos_.p + 2 * first + (lo ? 1 : 0), 2 * sizeof(float4), host, sizeof(float4),
+                               sizeof(float4), count, cudaMemcpyHostToDevice, stream_));
     sync();
 }
 
@@ -954,12 +974,12 @@ void Engine::set(uint32_t s, const std::string& name, const void* host, size_t c
         need(n);
         const uint32_t* x = static_cast<const uint32_t*>(host);
         std::vector<float4> hi(P.A);
-        download(pos_, P.off, P.A, hi.data());
+        download_pos(false, P.off, P.A, hi.data());
         for (uint32_t t = 0; t < n; ++t) {
             if (x[t] >= P.ns) throw Error(HMD_ERR_INVALID, "species out of range");
             hi[slot[t] - P.off].w = f32_from_bits(x[t]);
         }
-        upload(pos_, P.off, P.A, hi.data());
+        upload_pos(false, P.off, P.A, hi.data());
         forces_valid_ = false;
         request_rebuild(s);
     } else if (name == "image") {
@@ -1010,8 +1030,8 @@ void Engine::get(uint32_t s, const std::string& name, void* host, size_t count)
     } else if (name == "position" || name == "unwrapped_position") {
         need(3 * (size_t)n);
         std::vector<float4> hi(P.A), lo(P.A), im(P.A);
-        download(pos_, P.off, P.A, hi.data());
-        download(pos_, S + P.off, P.A, lo.data());
+        download_pos(false, P.off, P.A, hi.data());
+        download_pos(true, P.off, P.A, lo.data());
         download(img_, P.off, P.A, im.data());
         double* o = static_cast<double*>(host);
         const bool unwrap = name == "unwrapped_position";
@@ -1039,7 +1059,7 @@ void Engine::get(uint32_t s, const std::string& name, void* host, size_t count)
         need(n);
         std::vector<float4> b(P.A);
         if (name == "mass") download(vel_, P.off, P.A, b.data());
-        else download(pos_, P.off, P.A, b.data());
+        else download_pos(false, P.off, P.A, b.data());
         for (uint32_t t = 0; t < n; ++t) {
             const float w = b[slot[t] - P.off].w;
             if (name == "mass") static_cast<double*>(host)[t] = w;
@@ -1091,8 +1111,8 @@ void Engine::get_raw(uint32_t s, const std::string& name, void* host, size_t byt
     }
     need((size_t)P.A * 16);
     float4* o = static_cast<float4*>(host);
-    if (name == "position_hi") download(pos_, P.off, P.A, o);
-    else if (name == "position_lo") download(pos_, S + P.off, P.A, o);
+    if (name == "position_hi") download_pos(false, P.off, P.A, o);
+    else if (name == "position_lo") download_pos(true, P.off, P.A, o);
     else if (name == "velocity_hi") download(vel_, P.off, P.A, o);
     else if (name == "velocity_lo") download(vel_, S + P.off, P.A, o);
     else if (name == "image") download(img_, P.off, P.A, o);
@@ -1678,21 +1698,14 @@ double Engine::max_displacement(uint32_t s)
 {
     check_sys(s);
     const SysParam& P = sys_[s].P;
-    std::vector<float4> r(P.A), q(P.A);
-    download(pos_, P.off, P.A, r.data());
-    download(r0_, P.off, P.A, q.data());
-    float m = 0;
-    for (uint32_t k = 0; k < P.A; ++k) {
-        if (bits_of(r[k].w) == PLACEHOLDER) continue;
-        float dd[3] = {r[k].x - q[k].x, r[k].y - q[k].y, r[k].z - q[k].z};
-        float rr = 0;
-        for (int c = 0; c < 3; ++c) {
-            const float kk = std::rint(dd[c] * P.Linv[c]);
-            dd[c] = dd[c] - kk * P.L[c];
-            rr += dd[c] * dd[c];
-        }
-        m = std::max(m, rr);
-    }
+    // on the device (k_max_displacement); the done_ word 1 is free outside
+    // launch_check_finite, which the host reads before it returns
+    launch_max_displacement(dev(), s, P.A, done_.p + 1, stream_);
+    HMD_CUDA(cudaGetLastError());
+    uint32_t bits = 0;
+    download(done_, 1, 1, &bits);
+    float m;
+    std::memcpy(&m, &bits, sizeof(m));
     return std::sqrt((double)m);
 }
 

@@ -153,6 +153,10 @@ private:
     void write_state(const std::vector<SysState>& st);
     template <typename T> void download(const DevBuf<T>& b, size_t first, size_t count, T* host);
     template <typename T> void upload(DevBuf<T>& b, size_t first, size_t count, const T* host);
+    // the hi (lo = false) or lo words of slots [first, first + count) of the
+    // interleaved position array (hmd_device.cuh), as a packed float4 array
+    void download_pos(bool lo, size_t first, size_t count, float4* host);
+    void upload_pos(bool lo, size_t first, size_t count, const float4* host);
     std::vector<uint32_t> slots_of(uint32_t s);   // slot (absolute) of each tag
 
     int precision_;

@@ -95,7 +95,11 @@ __device__ __forceinline__ void pair_eval(const PairParam& p, float rr, float rr
     al = __fmaf_rn(p.c48_lo, rri, al);
     const float bl = __fmaf_rn(a, ri6l, __fmaf_rn(al, ri6, __fmaf_rn(a, ri6, -b)));
     flo = __fmaf_rn(b, ul, __fmaf_rn(bl, u, __fmaf_rn(b, u, -fval)));
-    en = p.eps4 * ri6 * (ri6 - 1.0f) - p.en_cut;
+    // the energy from rri^3 with its residual: rrl carries the lo words of
+    // dsfloat positions, which can shift a close pair's r^-12 by far more
+    // than the float rounding
+    const float ri6c = __fadd_rn(ri6, ri6l);
+    en = p.eps4 * ri6c * (ri6c - 1.0f) - p.en_cut;
     if (TR == TRUNC_SMOOTH_R4) {
         const float rinv = rsqrtf(rr);
         const float r = rr * rinv;
@@ -175,8 +179,12 @@ __device__ __forceinline__ bool pair_of(const PairParam* row, const PairParam& p
 // distance per coordinate) has the same sign and lies within a factor of two:
 // ri - rj is exact (Sterbenz) and its TwoSum error is zero, so the
 // error terms are dropped without changing any bit of the result
-template <int TR, bool AUX, bool WRAP, bool EXACT>
-__device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A)
+// LO: dsfloat positions; li / lj are the lo words of the two particles, and
+// the separation carries their difference in its residual, so the force is
+// that of the double-single state, not of its float hi part
+template <int TR, bool AUX, bool WRAP, bool EXACT, bool LO = false>
+__device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A,
+                                          float4 li = float4(), float4 lj = float4())
 {
     const float sx = __fsub_rn(ri.x, rj.x);
     const float sy = __fsub_rn(ri.y, rj.y);
@@ -196,9 +204,14 @@ __device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P,
         dyl = two_sum_err(ri.y, -rj.y, sy);
         dzl = two_sum_err(ri.z, -rj.z, sz);
     }
+    if (LO) {
+        dxl = __fadd_rn(dxl, __fsub_rn(li.x, lj.x));
+        dyl = __fadd_rn(dyl, __fsub_rn(li.y, lj.y));
+        dzl = __fadd_rn(dzl, __fsub_rn(li.z, lj.z));
+    }
     float rrl = __fadd_rn(__fadd_rn(__fmaf_rn(dx, dx, -px), __fmaf_rn(dy, dy, -py)), __fmaf_rn(dz, dz, -pz));
     rrl = __fadd_rn(rrl, __fadd_rn(fast_err_pos(px, py, pxy), fast_err_pos(pxy, pz, rr)));
-    if (!EXACT) rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
+    if (!EXACT || LO) rrl = __fmaf_rn(2.0f, __fmaf_rn(dx, dxl, __fmaf_rn(dy, dyl, __fmul_rn(dz, dzl))), rrl);
     float fval, flo, e;
     pair_eval<TR>(p, rr, rrl, P.rri_smooth, fval, flo, e);
     const float tx = __fmul_rn(fval, dx), ty = __fmul_rn(fval, dy), tz = __fmul_rn(fval, dz);
@@ -208,7 +221,7 @@ __device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P,
     float cx = __fadd_rn(A.cx, __fmaf_rn(fval, dx, -tx));
     float cy = __fadd_rn(A.cy, __fmaf_rn(fval, dy, -ty));
     float cz = __fadd_rn(A.cz, __fmaf_rn(fval, dz, -tz));
-    if (!EXACT) {
+    if (!EXACT || LO) {
         cx = __fmaf_rn(fval, dxl, cx);
         cy = __fmaf_rn(fval, dyl, cy);
         cz = __fmaf_rn(fval, dzl, cz);
@@ -228,8 +241,9 @@ __device__ __forceinline__ void near_pair(const PairParam& p, const SysParam& P,
 }
 
 // one far pair: plain FP32 (forces of order eps / sigma or less)
-template <int TR, bool AUX, bool WRAP>
-__device__ __forceinline__ void far_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A)
+template <int TR, bool AUX, bool WRAP, bool LO = false>
+__device__ __forceinline__ void far_pair(const PairParam& p, const SysParam& P, float4 ri, float4 rj, ForceAcc& A,
+                                         float4 li = float4(), float4 lj = float4())
 {
     const float sx = __fsub_rn(ri.x, rj.x);
     const float sy = __fsub_rn(ri.y, rj.y);
@@ -239,15 +253,27 @@ __device__ __forceinline__ void far_pair(const PairParam& p, const SysParam& P, 
     float dz = WRAP ? min_image(sz, P.L[2], P.Linv[2]) : sz;
     float rr = rr_exact(dx, dy, dz);
     if (!(rr < p.rr_cut)) return;
-    if (WRAP) {
+    if (WRAP || LO) {
         // across the box ri - rj is of order L and its rounding error (up to
         // ulp(L)/2) would dominate the separation error: add the TwoSum error
-        // back (the cut-off decision above keeps the rounded rr of the list
-        // criterion)
-        dx = __fadd_rn(dx, two_sum_err(ri.x, -rj.x, sx));
-        dy = __fadd_rn(dy, two_sum_err(ri.y, -rj.y, sy));
-        dz = __fadd_rn(dz, two_sum_err(ri.z, -rj.z, sz));
-        rr = rr_exact(dx, dy, dz);
+        // back; dsfloat positions add the difference of the lo words.  The
+        // cut-off decision above keeps the rounded rr of the list criterion;
+        // rr takes the residual e to first order (|e| << |d|)
+        float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+        if (WRAP) {
+            ex = two_sum_err(ri.x, -rj.x, sx);
+            ey = two_sum_err(ri.y, -rj.y, sy);
+            ez = two_sum_err(ri.z, -rj.z, sz);
+        }
+        if (LO) {
+            ex = __fadd_rn(ex, __fsub_rn(li.x, lj.x));
+            ey = __fadd_rn(ey, __fsub_rn(li.y, lj.y));
+            ez = __fadd_rn(ez, __fsub_rn(li.z, lj.z));
+        }
+        rr = __fmaf_rn(2.0f, __fmaf_rn(dx, ex, __fmaf_rn(dy, ey, __fmul_rn(dz, ez))), rr);
+        dx = __fadd_rn(dx, ex);
+        dy = __fadd_rn(dy, ey);
+        dz = __fadd_rn(dz, ez);
     }
     float fval, e;
     pair_eval_fast<TR>(p, rr, P.rri_smooth, fval, e);
@@ -392,7 +418,8 @@ __device__ __forceinline__ void pair_eval2(const PP2& p, float2 rr, float2 rrl, 
     al = fma2(p.c48_lo, rri, al);
     const float2 bl = fma2(a, ri6l, fma2(al, ri6, fma2(a, ri6, neg2(b))));
     flo = fma2(b, ul, fma2(bl, u, fma2(b, u, neg2(fval))));
-    truncate2<TR, true>(p, rr, ri6, rri_smooth, fval, flo, en);
+    // energy from rri^3 with its residual (pair_eval)
+    truncate2<TR, true>(p, rr, add2(ri6, ri6l), rri_smooth, fval, flo, en);
 }
 
 template <bool AUX>
@@ -412,9 +439,10 @@ __device__ __forceinline__ void aux_acc2(ForceAcc2& A, float2 fval, float2 en, f
 
 // two near pairs (near_pair, lane by lane); va / vb: the entry is a real
 // neighbour of a species of the system
-template <int TR, bool AUX, bool WRAP, bool EXACT>
+// (LO: li, la, lb are the lo words of the particle and of the two partners)
+template <int TR, bool AUX, bool WRAP, bool EXACT, bool LO>
 __device__ __forceinline__ void near_pair2(const PP2& p, const SysParam& P, float4 ri, float4 ra, float4 rb,
-                                           bool va, bool vb, ForceAcc2& A)
+                                           bool va, bool vb, ForceAcc2& A, float4 li, float4 la, float4 lb)
 {
     const float2 sx = f2(__fsub_rn(ri.x, ra.x), __fsub_rn(ri.x, rb.x));
     const float2 sy = f2(__fsub_rn(ri.y, ra.y), __fsub_rn(ri.y, rb.y));
@@ -433,9 +461,19 @@ __device__ __forceinline__ void near_pair2(const PP2& p, const SysParam& P, floa
         dyl = diff_err2(ri.y, ra.y, rb.y, sy);
         dzl = diff_err2(ri.z, ra.z, rb.z, sz);
     }
+    if (LO) {
+        const float2 ex = f2(__fsub_rn(li.x, la.x), __fsub_rn(li.x, lb.x));
+        const float2 ey = f2(__fsub_rn(li.y, la.y), __fsub_rn(li.y, lb.y));
+        const float2 ez = f2(__fsub_rn(li.z, la.z), __fsub_rn(li.z, lb.z));
+        if (EXACT) {
+            dxl = ex; dyl = ey; dzl = ez;
+        } else {
+            dxl = add2(dxl, ex); dyl = add2(dyl, ey); dzl = add2(dzl, ez);
+        }
+    }
     float2 rrl = add2(add2(fma2(dx, dx, neg2(px)), fma2(dy, dy, neg2(py))), fma2(dz, dz, neg2(pz)));
     rrl = add2(rrl, add2(fast_err_pos2(px, py, pxy), fast_err_pos2(pxy, pz, rr)));
-    if (!EXACT) rrl = fma2(bc2(2.0f), fma2(dx, dxl, fma2(dy, dyl, mul2(dz, dzl))), rrl);
+    if (!EXACT || LO) rrl = fma2(bc2(2.0f), fma2(dx, dxl, fma2(dy, dyl, mul2(dz, dzl))), rrl);
     float2 fval, flo, e;
     pair_eval2<TR>(p, rr, rrl, P.rri_smooth, fval, flo, e);
     fval = sel2(ka, kb, fval);
@@ -447,7 +485,7 @@ __device__ __forceinline__ void near_pair2(const PP2& p, const SysParam& P, floa
     float2 cx = add2(A.cx, fma2(fval, dx, neg2(tx)));
     float2 cy = add2(A.cy, fma2(fval, dy, neg2(ty)));
     float2 cz = add2(A.cz, fma2(fval, dz, neg2(tz)));
-    if (!EXACT) {
+    if (!EXACT || LO) {
         cx = fma2(fval, dxl, cx);
         cy = fma2(fval, dyl, cy);
         cz = fma2(fval, dzl, cz);
@@ -459,9 +497,9 @@ __device__ __forceinline__ void near_pair2(const PP2& p, const SysParam& P, floa
 }
 
 // two far pairs (far_pair, lane by lane)
-template <int TR, bool AUX, bool WRAP>
+template <int TR, bool AUX, bool WRAP, bool LO>
 __device__ __forceinline__ void far_pair2(const PP2& p, const SysParam& P, float4 ri, float4 ra, float4 rb,
-                                          bool va, bool vb, ForceAcc2& A)
+                                          bool va, bool vb, ForceAcc2& A, float4 li, float4 la, float4 lb)
 {
     const float2 sx = f2(__fsub_rn(ri.x, ra.x), __fsub_rn(ri.x, rb.x));
     const float2 sy = f2(__fsub_rn(ri.y, ra.y), __fsub_rn(ri.y, rb.y));
@@ -472,12 +510,25 @@ __device__ __forceinline__ void far_pair2(const PP2& p, const SysParam& P, float
     float2 rr = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
     const bool ka = va && rr.x < p.rr_cut.x;
     const bool kb = vb && rr.y < p.rr_cut.y;
-    if (WRAP) {
-        // across the box: add the separation's rounding error back (far_pair)
-        dx = add2(dx, diff_err2(ri.x, ra.x, rb.x, sx));
-        dy = add2(dy, diff_err2(ri.y, ra.y, rb.y, sy));
-        dz = add2(dz, diff_err2(ri.z, ra.z, rb.z, sz));
-        rr = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
+    if (WRAP || LO) {
+        // the separation's residual e: across the box the rounding error of
+        // ri - rj, for dsfloat positions the difference of the lo words
+        // (far_pair); rr takes it to first order
+        float2 ex = bc2(0.0f), ey = bc2(0.0f), ez = bc2(0.0f);
+        if (LO) {
+            ex = f2(__fsub_rn(li.x, la.x), __fsub_rn(li.x, lb.x));
+            ey = f2(__fsub_rn(li.y, la.y), __fsub_rn(li.y, lb.y));
+            ez = f2(__fsub_rn(li.z, la.z), __fsub_rn(li.z, lb.z));
+        }
+        if (WRAP) {
+            ex = add2(ex, diff_err2(ri.x, ra.x, rb.x, sx));
+            ey = add2(ey, diff_err2(ri.y, ra.y, rb.y, sy));
+            ez = add2(ez, diff_err2(ri.z, ra.z, rb.z, sz));
+        }
+        rr = fma2(bc2(2.0f), fma2(dx, ex, fma2(dy, ey, mul2(dz, ez))), rr);
+        dx = add2(dx, ex);
+        dy = add2(dy, ey);
+        dz = add2(dz, ez);
     }
     float ya, yb;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ya) : "f"(rr.x));
@@ -562,9 +613,18 @@ __device__ __forceinline__ uint32_t idx_at(uint4 v, int e) { return e == 0 ? v.x
 // contiguous memory and each lane has E independent position gathers in
 // flight.  Entries past the count are never dereferenced (the lane gathers
 // its own position instead).
-template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool EXACT = false>
+// gather of a neighbour's position: hi and lo words with one 32-byte load
+// (LO), or the hi word alone
+template <bool LO>
+__device__ __forceinline__ void gather_pos(const Dev& d, uint32_t j, float4& hi, float4& lo)
+{
+    if (LO) ldg_pos2(d.pos, j, hi, lo);
+    else hi = ldg_hi(d.pos, j);
+}
+
+template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool LO, bool EXACT = false>
 __device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
-                                             const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
+                                             const PairParam* spp, float4 ri, float4 li, uint32_t a, ForceAcc& A)
 {
     constexpr bool NS1 = TRX >= ONE_SPECIES;
     constexpr int TR = TRX & (ONE_SPECIES - 1);
@@ -581,12 +641,12 @@ __device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t 
     const uint32_t nblk = (cnt + LB - 1) / LB;
     for (uint32_t b = 0; b < nblk; ++b, lst += step) {
         const V jv = ld_list(lst);
-        float4 rj[E];
+        float4 rj[E], lj[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const uint32_t o = q * E + e;
             const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
-            rj[e] = __ldg(d.pos + (k < cnt ? idx_at(jv, e) : i));
+            gather_pos<LO>(d, k < cnt ? idx_at(jv, e) : i, rj[e], lj[e]);
         }
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -594,16 +654,16 @@ __device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t 
             const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
             const PairParam* pp;
             if (k >= cnt || !pair_of<NS1>(row, p1, ns, rj[e].w, pp)) continue;
-            if (FAR) far_pair<TR, AUX, WRAP>(*pp, P, ri, rj[e], A);
-            else near_pair<TR, AUX, WRAP, EXACT>(*pp, P, ri, rj[e], A);
+            if (FAR) far_pair<TR, AUX, WRAP, LO>(*pp, P, ri, rj[e], A, li, lj[e]);
+            else near_pair<TR, AUX, WRAP, EXACT, LO>(*pp, P, ri, rj[e], A, li, lj[e]);
         }
     }
 }
 
 // force_blocks with the E entries of a load taken two at a time (E even)
-template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool EXACT = false>
+template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool LO, bool EXACT = false>
 __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
-                                              const PairParam* spp, float4 ri, uint32_t a, ForceAcc2& A)
+                                              const PairParam* spp, float4 ri, float4 li, uint32_t a, ForceAcc2& A)
 {
     static_assert(E % 2 == 0, "entries are taken in pairs");
     constexpr bool NS1 = TRX >= ONE_SPECIES;
@@ -631,14 +691,14 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
         } else {
             jv = ld_list(lst);
         }
-        float4 rj[E];
+        float4 rj[E], lj[E];
         bool in[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const uint32_t o = q * E + e;
             const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
             in[e] = k < cnt;
-            rj[e] = __ldg(d.pos + (in[e] ? idx_at(jv, e) : i));
+            gather_pos<LO>(d, in[e] ? idx_at(jv, e) : i, rj[e], lj[e]);
         }
 #pragma unroll
         for (int e = 0; e < E; e += 2) {
@@ -654,36 +714,36 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
                 vb = vb && bb < ns;
                 pp = pack_params(row[ba < ns ? ba : 0u], row[bb < ns ? bb : 0u]);
             }
-            if (FAR) far_pair2<TR, AUX, WRAP>(pp, P, ri, rj[e], rj[e + 1], va, vb, A);
-            else near_pair2<TR, AUX, WRAP, EXACT>(pp, P, ri, rj[e], rj[e + 1], va, vb, A);
+            if (FAR) far_pair2<TR, AUX, WRAP, LO>(pp, P, ri, rj[e], rj[e + 1], va, vb, A, li, lj[e], lj[e + 1]);
+            else near_pair2<TR, AUX, WRAP, EXACT, LO>(pp, P, ri, rj[e], rj[e + 1], va, vb, A, li, lj[e], lj[e + 1]);
         }
         if (HMD_FORCE_PREFETCH) jv = jn;
     }
 }
 
-template <int W, int E, int TR, bool AUX>
+template <int W, int E, int TR, bool AUX, bool LO>
 __device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf,
                                                bool wrap, bool exact, const SysParam& P, const PairParam* spp,
-                                               float4 ri, uint32_t a, ForceAcc& A)
+                                               float4 ri, float4 li, uint32_t a, ForceAcc& A)
 {
     if constexpr (E % 2 == 0) {
         ForceAcc2 B;
         if (wrap) {
-            force_blocks2<W, E, TR, AUX, true, false>(d, i, q, nn, P, spp, ri, a, B);
-            force_blocks2<W, E, TR, AUX, true, true>(d, i, q, nf, P, spp, ri, a, B);
+            force_blocks2<W, E, TR, AUX, true, false, LO>(d, i, q, nn, P, spp, ri, li, a, B);
+            force_blocks2<W, E, TR, AUX, true, true, LO>(d, i, q, nf, P, spp, ri, li, a, B);
         } else {
-            if (exact) force_blocks2<W, E, TR, AUX, false, false, true>(d, i, q, nn, P, spp, ri, a, B);
-            else force_blocks2<W, E, TR, AUX, false, false>(d, i, q, nn, P, spp, ri, a, B);
-            force_blocks2<W, E, TR, AUX, false, true>(d, i, q, nf, P, spp, ri, a, B);
+            if (exact) force_blocks2<W, E, TR, AUX, false, false, LO, true>(d, i, q, nn, P, spp, ri, li, a, B);
+            else force_blocks2<W, E, TR, AUX, false, false, LO>(d, i, q, nn, P, spp, ri, li, a, B);
+            force_blocks2<W, E, TR, AUX, false, true, LO>(d, i, q, nf, P, spp, ri, li, a, B);
         }
         fold_lanes2<AUX>(B, A);
     } else if (wrap) {
-        force_blocks<W, E, TR, AUX, true, false>(d, i, q, nn, P, spp, ri, a, A);
-        force_blocks<W, E, TR, AUX, true, true>(d, i, q, nf, P, spp, ri, a, A);
+        force_blocks<W, E, TR, AUX, true, false, LO>(d, i, q, nn, P, spp, ri, li, a, A);
+        force_blocks<W, E, TR, AUX, true, true, LO>(d, i, q, nf, P, spp, ri, li, a, A);
     } else {
-        if (exact) force_blocks<W, E, TR, AUX, false, false, true>(d, i, q, nn, P, spp, ri, a, A);
-        else force_blocks<W, E, TR, AUX, false, false>(d, i, q, nn, P, spp, ri, a, A);
-        force_blocks<W, E, TR, AUX, false, true>(d, i, q, nf, P, spp, ri, a, A);
+        if (exact) force_blocks<W, E, TR, AUX, false, false, LO, true>(d, i, q, nn, P, spp, ri, li, a, A);
+        else force_blocks<W, E, TR, AUX, false, false, LO>(d, i, q, nn, P, spp, ri, li, a, A);
+        force_blocks<W, E, TR, AUX, false, true, LO>(d, i, q, nf, P, spp, ri, li, a, A);
     }
     // fold the plain far-pair sums into the compensated accumulators
     two_sum_acc(A.fx, A.cx, A.gx);
@@ -767,9 +827,10 @@ __device__ __forceinline__ void truncate_any(const PairParam& p, uint32_t trunc,
     }
 }
 
-template <int POT, bool AUX, bool WRAP, bool NEAR>
+template <int POT, bool AUX, bool WRAP, bool NEAR, bool LO>
 __device__ __forceinline__ void pot_pair2(const PairParam& pa, const PairParam& pb, const SysParam& P, float4 ri,
-                                          float4 ra, float4 rb, bool va, bool vb, ForceAcc2& A)
+                                          float4 ra, float4 rb, bool va, bool vb, ForceAcc2& A, float4 li,
+                                          float4 la, float4 lb)
 {
     const float2 sx = f2(__fsub_rn(ri.x, ra.x), __fsub_rn(ri.x, rb.x));
     const float2 sy = f2(__fsub_rn(ri.y, ra.y), __fsub_rn(ri.y, rb.y));
@@ -782,12 +843,21 @@ __device__ __forceinline__ void pot_pair2(const PairParam& pa, const PairParam& 
     const bool kb = vb && rr.y < pb.rr_cut;
     const bool smooth = P.trunc == TRUNC_SMOOTH_R4;   // block-uniform
     float2 rrl = bc2(0.0f);
-    if (WRAP || NEAR || smooth) {
-        // the separation's rounding error back in (the cut-off decision above
+    if (WRAP || NEAR || LO || smooth) {
+        // the separation's rounding error and, for dsfloat positions, the
+        // difference of the lo words back in (the cut-off decision above
         // keeps the rounded squared distance of the list criterion)
-        dx = add2(dx, diff_err2(ri.x, ra.x, rb.x, sx));
-        dy = add2(dy, diff_err2(ri.y, ra.y, rb.y, sy));
-        dz = add2(dz, diff_err2(ri.z, ra.z, rb.z, sz));
+        float2 ex = diff_err2(ri.x, ra.x, rb.x, sx);
+        float2 ey = diff_err2(ri.y, ra.y, rb.y, sy);
+        float2 ez = diff_err2(ri.z, ra.z, rb.z, sz);
+        if (LO) {
+            ex = add2(ex, f2(__fsub_rn(li.x, la.x), __fsub_rn(li.x, lb.x)));
+            ey = add2(ey, f2(__fsub_rn(li.y, la.y), __fsub_rn(li.y, lb.y)));
+            ez = add2(ez, f2(__fsub_rn(li.z, la.z), __fsub_rn(li.z, lb.z)));
+        }
+        dx = add2(dx, ex);
+        dy = add2(dy, ey);
+        dz = add2(dz, ez);
         const float2 px = mul2(dx, dx), py = mul2(dy, dy), pz = mul2(dz, dz);
         const float2 pxy = add2(px, py);
         rr = add2(pxy, pz);
@@ -820,10 +890,10 @@ __device__ __forceinline__ void pot_pair2(const PairParam& pa, const PairParam& 
 
 // force_blocks2 for the other potentials; an odd E pairs the last entry of
 // a load with a masked copy of the particle itself
-template <int W, int E, int POT, bool AUX, bool WRAP, bool FAR>
+template <int W, int E, int POT, bool AUX, bool WRAP, bool FAR, bool LO>
 __device__ __forceinline__ void force_blocks_pot(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt,
-                                                 const SysParam& P, const PairParam* spp, float4 ri, uint32_t a,
-                                                 ForceAcc2& A)
+                                                 const SysParam& P, const PairParam* spp, float4 ri, float4 li,
+                                                 uint32_t a, ForceAcc2& A)
 {
     constexpr uint32_t LB = W * E;
     using V = typename IdxVec<E>::T;
@@ -836,41 +906,42 @@ __device__ __forceinline__ void force_blocks_pot(const Dev& d, uint32_t i, uint3
     const uint32_t nblk = (cnt + LB - 1) / LB;
     for (uint32_t b = 0; b < nblk; ++b, lst += step) {
         const V jv = ld_list(lst);
-        float4 rj[E];
+        float4 rj[E], lj[E];
         bool in[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const uint32_t o = q * E + e;
             const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
             in[e] = k < cnt;
-            rj[e] = __ldg(d.pos + (in[e] ? idx_at(jv, e) : i));
+            gather_pos<LO>(d, in[e] ? idx_at(jv, e) : i, rj[e], lj[e]);
         }
 #pragma unroll
         for (int e = 0; e < E; e += 2) {
             const bool two = e + 1 < E;
             const float4 ra = rj[e], rb = two ? rj[e + 1 < E ? e + 1 : e] : ri;
+            const float4 la = lj[e], lb = two ? lj[e + 1 < E ? e + 1 : e] : li;
             const uint32_t ba = species_bits(ra.w), bb = species_bits(rb.w);
             const bool va = in[e] && ba < ns;
             const bool vb = two && in[e + 1 < E ? e + 1 : e] && bb < ns;
             const PairParam& pa = row[ba < ns ? ba : 0u];
             const PairParam& pb = row[vb ? bb : 0u];
-            pot_pair2<POT, AUX, WRAP, !FAR>(pa, pb, P, ri, ra, rb, va, vb, A);
+            pot_pair2<POT, AUX, WRAP, !FAR, LO>(pa, pb, P, ri, ra, rb, va, vb, A, li, la, lb);
         }
     }
 }
 
-template <int W, int E, int POT, bool AUX>
+template <int W, int E, int POT, bool AUX, bool LO>
 __device__ __forceinline__ void force_dispatch_pot(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf,
                                                    bool wrap, const SysParam& P, const PairParam* spp, float4 ri,
-                                                   uint32_t a, ForceAcc& A)
+                                                   float4 li, uint32_t a, ForceAcc& A)
 {
     ForceAcc2 B;
     if (wrap) {
-        force_blocks_pot<W, E, POT, AUX, true, false>(d, i, q, nn, P, spp, ri, a, B);
-        force_blocks_pot<W, E, POT, AUX, true, true>(d, i, q, nf, P, spp, ri, a, B);
+        force_blocks_pot<W, E, POT, AUX, true, false, LO>(d, i, q, nn, P, spp, ri, li, a, B);
+        force_blocks_pot<W, E, POT, AUX, true, true, LO>(d, i, q, nf, P, spp, ri, li, a, B);
     } else {
-        force_blocks_pot<W, E, POT, AUX, false, false>(d, i, q, nn, P, spp, ri, a, B);
-        force_blocks_pot<W, E, POT, AUX, false, true>(d, i, q, nf, P, spp, ri, a, B);
+        force_blocks_pot<W, E, POT, AUX, false, false, LO>(d, i, q, nn, P, spp, ri, li, a, B);
+        force_blocks_pot<W, E, POT, AUX, false, true, LO>(d, i, q, nf, P, spp, ri, li, a, B);
     }
     fold_lanes2<AUX>(B, A);
     two_sum_acc(A.fx, A.cx, A.gx);
@@ -909,18 +980,20 @@ __device__ __forceinline__ int force_kind_of(const SysParam& P)
     return P.trunc == TRUNC_SMOOTH_R4 ? FK_SMOOTH : FK_FSHIFT;
 }
 
-template <int W, int E, bool AUX>
+template <int W, int E, bool AUX, bool LO>
 __device__ __forceinline__ void force_pot(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf, bool wrap,
-                                          const SysParam& P, const PairParam* spp, float4 ri, uint32_t a, ForceAcc& A)
+                                          const SysParam& P, const PairParam* spp, float4 ri, float4 li, uint32_t a,
+                                          ForceAcc& A)
 {
     switch (P.pot) {
-    case POT_MIE: force_dispatch_pot<W, E, POT_MIE, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
-    case POT_MORSE: force_dispatch_pot<W, E, POT_MORSE, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
-    default: force_dispatch_pot<W, E, POT_POWER_LAW, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
+    case POT_MIE: force_dispatch_pot<W, E, POT_MIE, AUX, LO>(d, i, q, nn, nf, wrap, P, spp, ri, li, a, A); break;
+    case POT_MORSE: force_dispatch_pot<W, E, POT_MORSE, AUX, LO>(d, i, q, nn, nf, wrap, P, spp, ri, li, a, A); break;
+    default: force_dispatch_pot<W, E, POT_POWER_LAW, AUX, LO>(d, i, q, nn, nf, wrap, P, spp, ri, li, a, A); break;
     }
 }
 
-template <int W, int E, int KIND, bool AUX>
+// LO: the engine holds dsfloat positions (the separations carry the lo words)
+template <int W, int E, int KIND, bool AUX, bool LO>
 __global__ void __launch_bounds__(128, HMD_FORCE_MINB) k_force(Dev d)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -934,7 +1007,8 @@ __global__ void __launch_bounds__(128, HMD_FORCE_MINB) k_force(Dev d)
     if (!P.active || !d.st[s].live || *d.status != 0u) return;   // block-uniform
     if (KIND != FK_GENERIC && force_kind_of(P) != KIND) return;      // another kind's launch
     if (KIND == FK_GENERIC && force_kind_of(P) == FK_FULL) return;   // no list: k_force_full
-    const float4 ri = d.pos[i];
+    float4 ri, li = make_float4(0, 0, 0, 0);
+    gather_pos<LO>(d, i, ri, li);
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;
     const uint32_t packed = real ? d.nbr_count[i] : 0u;
@@ -947,22 +1021,22 @@ __global__ void __launch_bounds__(128, HMD_FORCE_MINB) k_force(Dev d)
     ForceAcc A;
     if (real) {
         if constexpr (KIND == FK_LJ1) {
-            force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+            force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A);
         } else if constexpr (KIND == FK_SHIFTED) {
-            force_dispatch<W, E, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+            force_dispatch<W, E, TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A);
         } else if constexpr (KIND == FK_SMOOTH) {
-            force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+            force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A);
         } else if constexpr (KIND == FK_FSHIFT) {
-            force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A);
+            force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A);
         } else if constexpr (KIND == FK_POT) {
-            force_pot<W, E, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A);
+            force_pot<W, E, AUX, LO>(d, i, q, nn, nf, wrap, P, spp, ri, li, a, A);
         } else {
             switch (force_kind_of(P)) {
-            case FK_LJ1: force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
-            case FK_SHIFTED: force_dispatch<W, E, TRUNC_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
-            case FK_SMOOTH: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
-            case FK_POT: force_pot<W, E, AUX>(d, i, q, nn, nf, wrap, P, spp, ri, a, A); break;
-            default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX>(d, i, q, nn, nf, wrap, exact, P, spp, ri, a, A); break;
+            case FK_LJ1: force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A); break;
+            case FK_SHIFTED: force_dispatch<W, E, TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A); break;
+            case FK_SMOOTH: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A); break;
+            case FK_POT: force_pot<W, E, AUX, LO>(d, i, q, nn, nf, wrap, P, spp, ri, li, a, A); break;
+            default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A); break;
             }
         }
     }
@@ -993,8 +1067,13 @@ template <int W, int E, int KIND>
 static void launch_force_shape(const Dev& d, bool aux, cudaStream_t st)
 {
     const unsigned grid = (unsigned)((size_t)d.S_grid * W / 128);
-    if (aux) k_force<W, E, KIND, true><<<grid, 128, 0, st>>>(d);
-    else k_force<W, E, KIND, false><<<grid, 128, 0, st>>>(d);
+    if (d.ds) {
+        if (aux) k_force<W, E, KIND, true, true><<<grid, 128, 0, st>>>(d);
+        else k_force<W, E, KIND, false, true><<<grid, 128, 0, st>>>(d);
+    } else {
+        if (aux) k_force<W, E, KIND, true, false><<<grid, 128, 0, st>>>(d);
+        else k_force<W, E, KIND, false, false><<<grid, 128, 0, st>>>(d);
+    }
 }
 
 // (lanes, list block) shapes the engine accepts: E = block / lanes entries per load

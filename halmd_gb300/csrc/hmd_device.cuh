@@ -4,9 +4,12 @@
 //   slots      every system s owns slots [off_s, off_s + A_s), A_s = n_s rounded
 //              up to SLOT_ALIGN; slots past n_s are ghosts (species 0xFFFFFFFF),
 //              following mdsim/gpu/particle.cpp:67-88 (ghost padding).
-//   position   float4 [2*S]: hi words (x, y, z, species bits), then lo words
-//              (dsfloat split, mdsim/gpu/particle.hpp:56-88).  FP32 engines
-//              keep only the hi half.
+//   position   float4 [2*S], the two words of a slot side by side: slot i
+//              holds its hi word (x, y, z, species bits) at 2i and its lo
+//              word (the dsfloat split, mdsim/gpu/particle.hpp:56-88) at
+//              2i + 1, so the force kernel gathers a neighbour's full
+//              position with one 32-byte load.  FP32 engines keep the lo
+//              words at zero.
 //   velocity   float4 [2*S]: (vx, vy, vz, mass) hi, then lo.
 //   image      float4 [S]; force float4 [S]; en_pot float [S];
 //              stress float [6*S] column-major (mdsim/force_kernel.hpp:64-80).
@@ -141,7 +144,7 @@ struct SysState {
 
 // device pointers of one engine (passed by value to every kernel)
 struct Dev {
-    float4* pos;               // [2S] hi | lo
+    float4* pos;               // [2S] slot i: hi at 2i, lo at 2i + 1
     float4* vel;               // [2S] hi | lo
     float4* img;               // [S]
     float4* force;             // [S]
@@ -167,6 +170,7 @@ struct Dev {
     const PairParam* pair;
     const uint32_t* chunk_sys; // [S / CHUNK]
     uint32_t S, nsys;
+    uint32_t ds;               // 1: dsfloat positions and velocities (lo words in use)
     // extents the launch grids cover (fixed layout: everything; capacity
     // mode: the slots, sort tiles and cells below the high-water mark of the
     // systems present, rounded up to a power of two)
@@ -197,6 +201,23 @@ struct Dev {
 constexpr int NTHERMO = 14;    // see k_thermo_partial
 
 __device__ __forceinline__ uint32_t species_bits(float w) { return __float_as_uint(w); }
+
+// hi / lo position word of slot i in an interleaved position array
+__device__ __forceinline__ float4& pos_hi(float4* p, uint32_t i) { return p[2 * (size_t)i]; }
+__device__ __forceinline__ float4& pos_lo(float4* p, uint32_t i) { return p[2 * (size_t)i + 1]; }
+__device__ __forceinline__ const float4& pos_hi(const float4* p, uint32_t i) { return p[2 * (size_t)i]; }
+__device__ __forceinline__ const float4& pos_lo(const float4* p, uint32_t i) { return p[2 * (size_t)i + 1]; }
+__device__ __forceinline__ float4 ldg_hi(const float4* p, uint32_t i) { return __ldg(p + 2 * (size_t)i); }
+
+// both words of slot i with one 256-bit read-only load (32-byte aligned:
+// the array comes from cudaMalloc and a slot spans 32 bytes)
+__device__ __forceinline__ void ldg_pos2(const float4* p, uint32_t i, float4& hi, float4& lo)
+{
+    const float4* a = p + 2 * (size_t)i;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(hi.x), "=f"(hi.y), "=f"(hi.z), "=f"(hi.w), "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w)
+        : "l"(a));
+}
 
 // minimum image: k = rint(dr / L) via dr * (1/L); dr - k L (box_kernel.cuh:37-47)
 // dr - rint(dr / L) L for dr = ri - rj of two in-box positions: |dr| <= L,

@@ -17,17 +17,20 @@ namespace hmd {
 constexpr uint32_t FULL_LANES = 4;
 constexpr uint32_t FULL_TILE = 128;
 
+// s_r holds the tile's hi and lo words side by side (slot u at 2u, 2u + 1)
 template <int POT, bool AUX>
-__device__ __forceinline__ void full_tile_pot(const SysParam& P, const PairParam* row, float4 ri, uint32_t i,
-                                              uint32_t base, const float4* s_r, uint32_t q, ForceAcc2& B)
+__device__ __forceinline__ void full_tile_pot(const SysParam& P, const PairParam* row, float4 ri, float4 li,
+                                              uint32_t i, uint32_t base, const float4* s_r, uint32_t q, ForceAcc2& B)
 {
     // entries u and u + FULL_LANES of the lane's share evaluated together
     for (uint32_t u = q; u < FULL_TILE; u += 2 * FULL_LANES) {
-        const float4 ra = s_r[u], rb = s_r[u + FULL_LANES];
+        const float4 ra = s_r[2 * u], rb = s_r[2 * (u + FULL_LANES)];
+        const float4 la = s_r[2 * u + 1], lb = s_r[2 * (u + FULL_LANES) + 1];
         const uint32_t ba = species_bits(ra.w), bb = species_bits(rb.w);
         const bool va = ba < P.ns && base + u != i;
         const bool vb = bb < P.ns && base + u + FULL_LANES != i;
-        pot_pair2<POT, AUX, true, true>(row[va ? ba : 0u], row[vb ? bb : 0u], P, ri, ra, rb, va, vb, B);
+        pot_pair2<POT, AUX, true, true, true>(row[va ? ba : 0u], row[vb ? bb : 0u], P, ri, ra, rb, va, vb, B, li,
+                                              la, lb);
     }
 }
 
@@ -40,12 +43,12 @@ __global__ void __launch_bounds__(128) k_force_full(Dev d)
     const uint32_t s = d.chunk_sys[(blockIdx.x * (blockDim.x / W)) / CHUNK];
     const SysParam& P = d.sys[s];
     __shared__ PairParam spp[MAX_SPECIES * MAX_SPECIES];
-    __shared__ float4 s_r[FULL_TILE];
+    __shared__ float4 s_r[2 * FULL_TILE];
     if (threadIdx.x < P.ns * P.ns) spp[threadIdx.x] = d.pair[P.pair_off + threadIdx.x];
     __syncthreads();
     if (!P.active || !d.st[s].live || *d.status != 0u) return;   // block-uniform
     if (force_kind_of(P) != FK_FULL) return;                       // a list kind's block
-    const float4 ri = d.pos[i];
+    const float4 ri = pos_hi(d.pos, i), li = pos_lo(d.pos, i);   // lo words 0 in FP32 engines
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;
     const PairParam* row = spp + (real ? a : 0u) * P.ns;
@@ -53,20 +56,22 @@ __global__ void __launch_bounds__(128) k_force_full(Dev d)
     ForceAcc2 B;
     for (uint32_t base = P.off; base < P.off + P.A; base += FULL_TILE) {
         __syncthreads();
-        s_r[threadIdx.x] = d.pos[base + threadIdx.x];
+        s_r[2 * threadIdx.x] = pos_hi(d.pos, base + threadIdx.x);
+        s_r[2 * threadIdx.x + 1] = pos_lo(d.pos, base + threadIdx.x);
         __syncthreads();
         if (!real) continue;
         switch (P.pot) {
         case POT_LJ:
             for (uint32_t u = q; u < FULL_TILE; u += W) {
-                const float4 rj = s_r[u];
+                const float4 rj = s_r[2 * u];
                 const uint32_t b = species_bits(rj.w);
-                if (b < P.ns && base + u != i) near_pair<TRUNC_SHARP, AUX, true, false>(row[b], P, ri, rj, A);
+                if (b < P.ns && base + u != i)
+                    near_pair<TRUNC_SHARP, AUX, true, false, true>(row[b], P, ri, rj, A, li, s_r[2 * u + 1]);
             }
             break;
-        case POT_MIE: full_tile_pot<POT_MIE, AUX>(P, row, ri, i, base, s_r, q, B); break;
-        case POT_MORSE: full_tile_pot<POT_MORSE, AUX>(P, row, ri, i, base, s_r, q, B); break;
-        default: full_tile_pot<POT_POWER_LAW, AUX>(P, row, ri, i, base, s_r, q, B); break;
+        case POT_MIE: full_tile_pot<POT_MIE, AUX>(P, row, ri, li, i, base, s_r, q, B); break;
+        case POT_MORSE: full_tile_pot<POT_MORSE, AUX>(P, row, ri, li, i, base, s_r, q, B); break;
+        default: full_tile_pot<POT_POWER_LAW, AUX>(P, row, ri, li, i, base, s_r, q, B); break;
         }
     }
     if (P.pot != POT_LJ) {

@@ -19,7 +19,7 @@ __global__ void __launch_bounds__(256) k_set_position(Dev d, uint32_t s, const d
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= P.n) return;
     const uint32_t k = d.rid[P.off + t];
-    float4 h = d.pos[k], g = d.img[k];
+    float4 h = pos_hi(d.pos, k), g = d.img[k];
     float4 l = make_float4(0, 0, 0, 0);
     float* hp = &h.x;
     float* lp = &l.x;
@@ -34,8 +34,8 @@ __global__ void __launch_bounds__(256) k_set_position(Dev d, uint32_t s, const d
         lp[q] = DS ? __double2float_rn(__dsub_rn(xr, (double)hp[q])) : 0.0f;
         gp[q] = __double2float_rn(__dadd_rn((double)gp[q], w));
     }
-    d.pos[k] = h;                       // w (species) unchanged
-    if (DS) d.pos[d.S + k] = l;
+    pos_hi(d.pos, k) = h;               // w (species) unchanged
+    if (DS) pos_lo(d.pos, k) = l;
     d.img[k] = g;
 }
 
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256) k_get_vector(Dev d, uint32_t s, int what,
     if (t >= P.n) return;
     const uint32_t k = d.rid[P.off + t];
     float4 a, b = make_float4(0, 0, 0, 0), g = make_float4(0, 0, 0, 0);
-    if (what <= 1) { a = d.pos[k]; b = d.pos[d.S + k]; if (what == 1) g = d.img[k]; }
+    if (what <= 1) { a = pos_hi(d.pos, k); b = pos_lo(d.pos, k); if (what == 1) g = d.img[k]; }
     else if (what == 2) { a = d.vel[k]; b = d.vel[d.S + k]; }
     else if (what == 3) a = d.force[k];
     else a = d.img[k];

@@ -17,9 +17,9 @@ __global__ void __launch_bounds__(256) k_sample_position(Dev d, uint32_t first, 
     const uint32_t i = first + blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t s = d.chunk_sys[i / CHUNK];
     const SysParam& P = d.sys[s];
-    const float4 r = d.pos[i];
+    const float4 r = pos_hi(d.pos, i);
     if (!P.active || species_bits(r.w) == PLACEHOLDER) return;
-    const float4 rl = d.pos[d.S + i];
+    const float4 rl = pos_lo(d.pos, i);
     const float4 im = d.img[i];
     const uint32_t tag = d.id[i];
     double* o = out + (size_t)tag * 3;
@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(256) k_sample_velocity(Dev d, uint32_t first, 
     const uint32_t i = first + blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t s = d.chunk_sys[i / CHUNK];
     const SysParam& P = d.sys[s];
-    if (!P.active || species_bits(d.pos[i].w) == PLACEHOLDER) return;
+    if (!P.active || species_bits(pos_hi(d.pos, i).w) == PLACEHOLDER) return;
     const float4 v = d.vel[i];
     const float4 vl = d.vel[d.S + i];
     double* o = out + (size_t)d.id[i] * 3;
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256) k_density_partial(Dev d, const uint32_t* 
     const uint32_t beg = blk_begin[b];
     const uint32_t end = min(beg + DM_CHUNK, range[2 * rg + 1]);
     const uint32_t cnt = end - beg;
-    for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) s_r[k] = d.pos[d.rid[beg + k]];
+    for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) s_r[k] = pos_hi(d.pos, d.rid[beg + k]);
     __syncthreads();
     for (uint32_t w = 0; w < nq; ++w) {
         const float4 qq = q[w];

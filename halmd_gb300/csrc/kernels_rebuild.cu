@@ -56,7 +56,7 @@ __device__ uint32_t hilbert_key(float x0, float x1, float x2, uint32_t depth)
 // range so the (stable) sort keeps them behind every real particle
 __device__ __forceinline__ uint32_t slot_key(const Dev& d, const SysParam& P, uint32_t i)
 {
-    const float4 r = d.pos[i];
+    const float4 r = pos_hi(d.pos, i);
     const uint32_t bits = 3u * P.depth;
     if (species_bits(r.w) == PLACEHOLDER) return (1u << bits) - 1u;
     return hilbert_key(__fdiv_rn(r.x, P.L[0]), __fdiv_rn(r.y, P.L[1]), __fdiv_rn(r.z, P.L[2]), P.depth);
@@ -68,7 +68,7 @@ __global__ void k_hilbert_keys(Dev d, uint32_t* keys)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.S) return;
     const SysParam& P = d.sys[d.chunk_sys[i / CHUNK]];
-    const float4 r = d.pos[i];
+    const float4 r = pos_hi(d.pos, i);
     keys[i] = (species_bits(r.w) == PLACEHOLDER)
         ? PLACEHOLDER
         : hilbert_key(__fdiv_rn(r.x, P.L[0]), __fdiv_rn(r.y, P.L[1]), __fdiv_rn(r.z, P.L[2]), P.depth);
@@ -387,10 +387,10 @@ template <bool DS>
 __device__ __forceinline__ void rearrange_slot(const Dev& d, const SysParam& P, uint32_t i, const uint32_t* perm)
 {
     const uint32_t src = perm[i];
-    d.tpos[i] = d.pos[src];
+    pos_hi(d.tpos, i) = pos_hi(d.pos, src);
     d.tvel[i] = d.vel[src];
     if (DS) {
-        d.tpos[d.S + i] = d.pos[d.S + src];
+        pos_lo(d.tpos, i) = pos_lo(d.pos, src);
         d.tvel[d.S + i] = d.vel[d.S + src];
     }
     d.timg[i] = d.img[src];
@@ -407,10 +407,10 @@ __global__ void __launch_bounds__(256) k_copyback(Dev d)
     for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
         const uint32_t k = rb_find(L.p[1], L.n, v);
         const uint32_t i = d.sys[L.sys[k]].off + (v - L.p[1][k]) * 256u + threadIdx.x;
-        d.pos[i] = d.tpos[i];
+        pos_hi(d.pos, i) = pos_hi(d.tpos, i);
         d.vel[i] = d.tvel[i];
         if (DS) {
-            d.pos[d.S + i] = d.tpos[d.S + i];
+            pos_lo(d.pos, i) = pos_lo(d.tpos, i);
             d.vel[d.S + i] = d.tvel[d.S + i];
         }
         d.img[i] = d.timg[i];
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(256) k_bin(Dev d)
         const uint32_t k = rb_find(L.p[0], L.n, v);
         const SysParam& P = d.sys[L.sys[k]];
         const uint32_t i = P.off + (v - L.p[0][k]) * 256u + threadIdx.x;
-        const float4 r = d.pos[i];
+        const float4 r = pos_hi(d.pos, i);
         if (species_bits(r.w) == PLACEHOLDER) continue;
         int cx, cy, cz;
         cell_coords(P, r, cx, cy, cz);
@@ -698,8 +698,8 @@ __device__ __forceinline__ void lane_scan(const SysParam& P, const float4* pos, 
                 uint32_t k = 0;
                 for (; k + 4 <= nc; k += 4) {
                     const uint4 jj = __ldg(cell4 + (k >> 2));
-                    const float4 r0 = __ldg(pos + jj.x), r1 = __ldg(pos + jj.y);
-                    const float4 r2 = __ldg(pos + jj.z), r3 = __ldg(pos + jj.w);
+                    const float4 r0 = ldg_hi(pos, jj.x), r1 = ldg_hi(pos, jj.y);
+                    const float4 r2 = ldg_hi(pos, jj.z), r3 = ldg_hi(pos, jj.w);
                     lane_test<WRAP, NS>(B, ri, i, r0, jj.x, cut, o);
                     lane_test<WRAP, NS>(B, ri, i, r1, jj.y, cut, o);
                     lane_test<WRAP, NS>(B, ri, i, r2, jj.z, cut, o);
@@ -710,7 +710,7 @@ __device__ __forceinline__ void lane_scan(const SysParam& P, const float4* pos, 
                     const uint32_t jv[3] = {jj.x, jj.y, jj.z};
                     float4 rv[3];
 #pragma unroll
-                    for (int u = 0; u < 3; ++u) rv[u] = (k + u < nc) ? __ldg(pos + jv[u]) : make_float4(0, 0, 0, 0);
+                    for (int u = 0; u < 3; ++u) rv[u] = (k + u < nc) ? ldg_hi(pos, jv[u]) : make_float4(0, 0, 0, 0);
 #pragma unroll
                     for (int u = 0; u < 3; ++u)
                         if (k + u < nc) lane_test<WRAP, NS>(B, ri, i, rv[u], jv[u], cut, o);
@@ -773,7 +773,7 @@ __device__ __forceinline__ void cluster_scan(const Dev& d, const SysParam& P, fl
                 for (uint32_t k = 0; k < nc; k += 32) {
                     const bool have = k + lane < nc;
                     const uint32_t j = have ? __ldg(cell + k + lane) : 0u;
-                    const float4 rj = have ? __ldg(d.pos + j) : make_float4(0, 0, 0, 0);
+                    const float4 rj = have ? ldg_hi(d.pos, j) : make_float4(0, 0, 0, 0);
                     bool keep = false;
                     if (have) {
                         // distance from the candidate to the bounding box
@@ -848,7 +848,7 @@ __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_
                                                const float* s_rrnear, float4* s_pos, uint32_t* s_j, uint32_t lane)
 {
     const SysParam& P = d.sys[s];
-    const float4 ri = d.pos[i];
+    const float4 ri = pos_hi(d.pos, i);
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;
     NbrOut o;

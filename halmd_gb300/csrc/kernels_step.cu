@@ -7,6 +7,7 @@
 // straddles two systems (blocks of <= 256 threads, systems padded to 256
 // slots), so per-system parameters are block-uniform.
 #include "hmd_device.cuh"
+#include <algorithm>
 #include "kernels.h"
 #include "step_device.cuh"
 
@@ -58,7 +59,7 @@ __global__ void __launch_bounds__(256) k_finalize(Dev d)
     const SysState& st = d.st[s];
     double acc[NMOM] = {0.0, 0.0, 0.0, 0.0, 0.0};
     const bool run = P.active && st.live && *d.status == 0u && P.integrator != INTEG_DESCENT;   // block-uniform
-    if (run && species_bits(d.pos[i].w) != PLACEHOLDER) {
+    if (run && species_bits(pos_hi(d.pos, i).w) != PLACEHOLDER) {
         float4 v = d.vel[i];
         float4 vl = make_float4(0, 0, 0, 0);
         if (DS) vl = d.vel[d.S + i];
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(256) k_moments(Dev d)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double acc[NMOM] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    const float4 r = d.pos[i];
+    const float4 r = pos_hi(d.pos, i);
     if (species_bits(r.w) != PLACEHOLDER) moment_terms(d.vel[i], d.vel[d.S + i], acc);
     block_moments(d, acc);
 }
@@ -154,7 +155,7 @@ __global__ void __launch_bounds__(256) k_thermostat_apply(Dev d)
     const SysState& st = d.st[s];
     const bool hoover = P.integrator == INTEG_HOOVER;
     if (!P.active || !st.live || *d.status != 0u || !(hoover || boltzmann_due(P, st))) return;
-    if (species_bits(d.pos[i].w) == PLACEHOLDER) return;
+    if (species_bits(pos_hi(d.pos, i).w) == PLACEHOLDER) return;
     float4 v = d.vel[i];
     float4 vl = make_float4(0, 0, 0, 0);
     if (DS) vl = d.vel[d.S + i];
@@ -237,7 +238,7 @@ __global__ void __launch_bounds__(256) k_thermo_partial(Dev d)
     double acc[NTHERMO];
 #pragma unroll
     for (int k = 0; k < NTHERMO; ++k) acc[k] = 0.0;
-    const float4 r = d.pos[i];
+    const float4 r = pos_hi(d.pos, i);
     if (species_bits(r.w) != PLACEHOLDER && d.sys[d.chunk_sys[i / CHUNK]].active) {
         const float4 vh = d.vel[i];
         const float4 vl = d.vel[d.S + i];
@@ -383,6 +384,36 @@ void launch_thermo(const Dev& d, cudaStream_t st)
 {
     k_thermo_partial<<<d.S_grid / 256, 256, 0, st>>>(d);
     k_thermo_reduce<<<d.nsys, 256, 0, st>>>(d);
+}
+
+// max_displacement::compute (mdsim/gpu/max_displacement.cpp:77-106, kernel
+// max_displacement_kernel.cu:37-68): the largest squared minimum-image
+// displacement since the last list build over the real particles of system
+// s, with the arithmetic of the integrate kernel's fused test (step_slot),
+// as float bits (non-negative floats order as their bit patterns)
+__global__ void __launch_bounds__(256) k_max_displacement(Dev d, uint32_t s, uint32_t* out)
+{
+    const SysParam& P = d.sys[s];
+    float rr = 0.0f;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < P.A; k += gridDim.x * blockDim.x) {
+        const uint32_t i = P.off + k;
+        const float4 r = pos_hi(d.pos, i);
+        if (species_bits(r.w) == PLACEHOLDER) continue;
+        const float4 q = d.r0[i];
+        const float dx = min_image(__fsub_rn(r.x, q.x), P.L[0], P.Linv[0]);
+        const float dy = min_image(__fsub_rn(r.y, q.y), P.L[1], P.Linv[1]);
+        const float dz = min_image(__fsub_rn(r.z, q.z), P.L[2], P.Linv[2]);
+        rr = fmaxf(rr, rr_exact(dx, dy, dz));
+    }
+    rr = warp_max(rr);
+    if ((threadIdx.x & 31) == 0 && rr > 0.0f) atomicMax(out, __float_as_uint(rr));
+}
+
+void launch_max_displacement(const Dev& d, uint32_t s, uint32_t slots, uint32_t* out, cudaStream_t st)
+{
+    cudaMemsetAsync(out, 0, sizeof(uint32_t), st);
+    const unsigned grid = std::max(1u, std::min((slots + 255u) / 256u, 8u * std::max(d.sm_count, 1u)));
+    k_max_displacement<<<grid, 256, 0, st>>>(d, s, out);
 }
 
 } // namespace hmd

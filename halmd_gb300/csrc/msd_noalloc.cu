@@ -17,6 +17,8 @@
 // per thread, pairwise Chan merge across the block, blocks of 8192
 // particles merged in index order), so both give the same (count, mean,
 // variance) for the same two samples.
+#include <cuda.h>
+
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -95,36 +97,88 @@ __global__ void k_msd_noalloc_merge(const double* partial, uint32_t nblk, double
     out[2] = n > 0 ? v / n : 0.0;
 }
 
-std::mutex g_setup_mutex;
-double* g_scratch_ptr[NOALLOC_MAX_DEVICES] = {};
+// Driver calls reached through the runtime's entry-point table, so the
+// library does not link the driver library itself (it must still load on
+// machines without a GPU driver, where nothing is launched).
+struct Driver {
+    CUresult (*ctx_get_current)(CUcontext*) = nullptr;
+    CUresult (*ctx_get_id)(CUcontext, unsigned long long*) = nullptr;
+    CUresult (*mem_get_address_range)(CUdeviceptr*, size_t*, CUdeviceptr) = nullptr;
+};
 
-// Device address of g_msd_scratch on the current device, looked up once per
-// device.  The first lookup on a device may load this library's device code
-// there; host code never uses the symbol itself as an address.
-double* scratch_for_current_device()
+template <typename F>
+void driver_entry(const char* name, F& fn)
 {
-    int dev = -1;
-    HMD_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
-        throw Error(HMD_ERR_INVALID, "hmd_msd_pair_noalloc: device index " + std::to_string(dev) +
-                                         " beyond the " + std::to_string(NOALLOC_MAX_DEVICES) + " it supports");
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_msd_scratch);
-        if (e != cudaSuccess || !p) {
-            (void)cudaGetLastError();
-            throw Error(HMD_ERR_CUDA, std::string("hmd_msd_pair_noalloc: cudaGetSymbolAddress of the scratch array "
-                                                  "failed: ") + cudaGetErrorString(e));
-        }
-        g_scratch_ptr[dev] = static_cast<double*>(p);
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+        (void)cudaGetLastError();
+        throw Error(HMD_ERR_CUDA, std::string("hmd_msd_pair_noalloc: driver entry point ") + name + " unavailable");
     }
-    return g_scratch_ptr[dev];
+    fn = reinterpret_cast<F>(p);
 }
 
-// the kernels read 3*count doubles behind r1 and r2 and write 3 behind out:
-// each must be device (or managed) memory of the current device, 8-byte aligned
-void check_pointer(const void* p, int dev, const char* what)
+std::mutex g_setup_mutex;
+Driver g_driver;
+bool g_driver_ready = false;
+
+// Scratch addresses by CUDA context.  A __device__ array's address belongs
+// to the context that loaded the module, not to the device: after
+// cudaDeviceReset the primary context, and with it the module and the
+// address, are new, and a context the caller made current through the
+// driver API has its own copy.  So the address is looked up once per
+// context (by its unique id) and again when the current context is one not
+// seen before.
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    double* ptr;
+};
+ScratchEntry g_scratch[NOALLOC_MAX_DEVICES];
+int g_nscratch = 0;
+
+const Driver& driver()
+{
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_driver_ready) {
+        driver_entry("cuCtxGetCurrent", g_driver.ctx_get_current);
+        driver_entry("cuCtxGetId", g_driver.ctx_get_id);
+        driver_entry("cuMemGetAddressRange", g_driver.mem_get_address_range);
+        g_driver_ready = true;
+    }
+    return g_driver;
+}
+
+// Device address of g_msd_scratch in the current context.  The first lookup
+// in a context may load this library's device code there; host code never
+// uses the symbol itself as an address.
+double* scratch_for_current_context()
+{
+    const Driver& drv = driver();
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (drv.ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx || drv.ctx_get_id(ctx, &id) != CUDA_SUCCESS)
+        throw Error(HMD_ERR_CUDA, "hmd_msd_pair_noalloc: no current CUDA context");
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    for (int k = 0; k < g_nscratch; ++k)
+        if (g_scratch[k].ctx_id == id) return g_scratch[k].ptr;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_msd_scratch);
+    if (e != cudaSuccess || !p) {
+        (void)cudaGetLastError();
+        throw Error(HMD_ERR_CUDA, std::string("hmd_msd_pair_noalloc: cudaGetSymbolAddress of the scratch array "
+                                              "failed: ") + cudaGetErrorString(e));
+    }
+    // a full table reuses a slot (contexts of past resets are gone)
+    const int k = g_nscratch < NOALLOC_MAX_DEVICES ? g_nscratch++ : (int)(id % NOALLOC_MAX_DEVICES);
+    g_scratch[k] = ScratchEntry{id, static_cast<double*>(p)};
+    return g_scratch[k].ptr;
+}
+
+// the kernels read `bytes` bytes behind r1 and r2 and write 24 behind out:
+// each must be device (or managed) memory of the current device, 8-byte
+// aligned, inside one allocation that holds all of those bytes
+void check_pointer(const void* p, int dev, const char* what, size_t bytes)
 {
     if (!p) throw Error(HMD_ERR_INVALID, std::string("hmd_msd_pair_noalloc: ") + what + " is null");
     if (reinterpret_cast<uintptr_t>(p) % alignof(double))
@@ -135,12 +189,20 @@ void check_pointer(const void* p, int dev, const char* what)
         (void)cudaGetLastError();
         throw Error(HMD_ERR_INVALID, std::string("hmd_msd_pair_noalloc: ") + what + ": " + cudaGetErrorString(e));
     }
-    if (a.type == cudaMemoryTypeManaged) return;
-    if (a.type != cudaMemoryTypeDevice)
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
         throw Error(HMD_ERR_INVALID, std::string("hmd_msd_pair_noalloc: ") + what + " is not device memory");
-    if (a.device != dev)
+    if (a.type == cudaMemoryTypeDevice && a.device != dev)
         throw Error(HMD_ERR_INVALID, std::string("hmd_msd_pair_noalloc: ") + what + " is on device " +
                                          std::to_string(a.device) + ", the current device is " + std::to_string(dev));
+    CUdeviceptr base = 0;
+    size_t size = 0;
+    const CUdeviceptr at = reinterpret_cast<CUdeviceptr>(p);
+    if (driver().mem_get_address_range(&base, &size, at) != CUDA_SUCCESS)
+        throw Error(HMD_ERR_INVALID, std::string("hmd_msd_pair_noalloc: ") + what + " is not inside an allocation");
+    if (at - base > size || size - (at - base) < bytes)
+        throw Error(HMD_ERR_INVALID, std::string("hmd_msd_pair_noalloc: ") + what + " holds " +
+                                         std::to_string(size - (at - base)) + " bytes, the call needs " +
+                                         std::to_string(bytes));
 }
 
 } // namespace
@@ -154,11 +216,11 @@ void msd_pair_noalloc(const double* origin, const double* position, uint32_t cou
     int dev = -1;
     HMD_CUDA(cudaGetDevice(&dev));
     if (count > 0) {
-        check_pointer(origin, dev, "origin");
-        check_pointer(position, dev, "position");
+        check_pointer(origin, dev, "origin", 3 * sizeof(double) * (size_t)count);
+        check_pointer(position, dev, "position", 3 * sizeof(double) * (size_t)count);
     }
-    check_pointer(out, dev, "out");
-    double* partial = scratch_for_current_device();
+    check_pointer(out, dev, "out", 3 * sizeof(double));
+    double* partial = scratch_for_current_context();
     const uint32_t nblk = (count + NOALLOC_CHUNK - 1) / NOALLOC_CHUNK;
     if (nblk > 0) k_msd_noalloc_partial<<<nblk, 256, 0, st>>>(origin, position, count, partial);
     k_msd_noalloc_merge<<<1, 32, 0, st>>>(partial, nblk, out);

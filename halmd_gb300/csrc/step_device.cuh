@@ -184,9 +184,9 @@ __device__ __forceinline__ float step_slot(const Dev& d, const SysParam& P, cons
                                            const float4* src, float4* dst, bool fin, bool live, float4 f)
 {
     float rr = 0.0f;
-    float4 r = src[i];
+    float4 r = pos_hi(src, i);
     float4 rl = make_float4(0, 0, 0, 0);
-    if (DS && (COPY || live)) rl = src[d.S + i];
+    if (DS && (COPY || live)) rl = pos_lo(src, i);
     const bool real = species_bits(r.w) != PLACEHOLDER;
     if (FIN && fin && !live && real) {
         // the system finished with the previous step: its last half-kick only
@@ -228,8 +228,8 @@ __device__ __forceinline__ float step_slot(const Dev& d, const SysParam& P, cons
             if (DS) d.vel[d.S + i] = vl;
         }
         if (!COPY) {
-            dst[i] = r;
-            if (DS) dst[d.S + i] = rl;
+            pos_hi(dst, i) = r;
+            if (DS) pos_lo(dst, i) = rl;
         }
         if (k.x != 0.0f || k.y != 0.0f || k.z != 0.0f) {
             // image counters are read and written only on a wrap
@@ -246,8 +246,8 @@ __device__ __forceinline__ float step_slot(const Dev& d, const SysParam& P, cons
         rr = rr_exact(dx, dy, dz);
     }
     if (COPY) {
-        dst[i] = r;
-        if (DS) dst[d.S + i] = rl;
+        pos_hi(dst, i) = r;
+        if (DS) pos_lo(dst, i) = rl;
     }
     return rr;
 }

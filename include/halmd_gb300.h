@@ -330,14 +330,13 @@ HMD_API int hmd_dynamics_shells(hmd_dynamics* dyn, int32_t tcf, uint32_t* nshell
 /* ---- allocation-free MSD of one sample pair ----------------------------- */
 
 /*
- * No counterpart in the reference: its MSD exists only inside the blocking
- * scheme (observables/gpu/dynamics/mean_square_displacement.cpp:55-68),
- * which owns its buffers.  This entry point is for callers that must not
- * allocate device memory when they sample: cudaMalloc/cudaFree synchronise
- * the whole device (stalling a simulation whose steps are in flight), and a
- * server that reserved nearly all of HBM for its engine may have no room
- * left.  It allocates nothing; its scratch is a fixed array of the library
- * in device memory (96 KiB per device).
+ * No counterpart in the reference.  This entry point is for callers that
+ * must not allocate device memory when they sample: cudaMalloc/cudaFree
+ * synchronise the whole device (stalling a simulation whose steps are in
+ * flight), and a server that reserved nearly all of HBM for its engine may
+ * have no room left.  It allocates nothing; its scratch is a fixed array of
+ * the library in device memory (96 KiB on every device that loads the
+ * library, held until the process exits).
  *
  * origin, position: device arrays of count x 3 doubles (unwrapped positions
  * in the same particle order).  out: device array of 3 doubles, written with
@@ -346,10 +345,13 @@ HMD_API int hmd_dynamics_shells(hmd_dynamics* dyn, int32_t tcf, uint32_t* nshell
  * stream); the call enqueues two kernels and returns without synchronising.
  *
  * - count above HMD_MSD_NOALLOC_MAX_PARTICLES (2^25) is rejected with
- *   HMD_ERR_INVALID, as are null, misaligned or non-device pointers.
- * - The first call on each device looks up the scratch array's address
- *   (which can load this library's device code there): make that first
- *   call, on every device used, before any stream capture begins.
+ *   HMD_ERR_INVALID, as are null, misaligned or non-device pointers and
+ *   buffers whose allocation ends before the bytes the call reads or writes.
+ * - The first call in each CUDA context (on a device: its primary context,
+ *   and again after cudaDeviceReset, which makes a new one) looks up the
+ *   scratch array's address, which can load this library's device code
+ *   there: make that first call, on every device used, before any stream
+ *   capture begins.
  * - Nothing needs to be zeroed first.
  * - All calls on one device share the one scratch array: calls that can
  *   overlap (different streams, or host threads without ordering) race and

@@ -649,7 +649,13 @@ ORC_API long orc_forces(int n, const double* r, const u32* sp, const double* L, 
                         double* f, double* en, double* stress, double* totals)
 {
     half_list hl;
-    build_half_list(n, r, sp, L, p, 0.0, hl);
+    /* with the float decision, candidates slightly beyond r_c in FP64 can be
+     * inside it in float: the candidate list reaches 1e-3 r_c further */
+    double reach = 0.0;
+    if (decide_f32)
+        for (int ab = 0; ab < p->ns * p->ns; ++ab)
+            if (std::isfinite(p->rcut[ab])) reach = std::max(reach, 1e-3 * p->rcut[ab]);
+    build_half_list(n, r, sp, L, p, reach, hl);
     force_half(n, r, sp, L, p, hl, decide_f32, pos4, Lf, f, en, stress, totals);
     long np = 0;
     for (auto& v : hl.nb) np += (long)v.size();

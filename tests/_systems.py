@@ -45,3 +45,19 @@ def rel_force_error(f, f64):
     frms = np.sqrt(np.mean(norm ** 2))
     e = np.linalg.norm(f - f64, axis=1) / np.maximum(norm, frms)
     return float(e.max()), float(np.median(e))
+
+
+def state_forces(eng, species, pot, s=0, state=True, aux=True):
+    """FP64 forces of an engine's phase-space state.
+
+    The positions are hi + lo of every slot (the double-single state; with
+    state=False the float hi words alone, the convention of the reference's
+    GPU kernels), the box is the engine's float box (the integrator wraps
+    with it, as box_kernel.cuh does), and the pair set is the one the
+    kernels use: r^2 < r_c^2 decided in float on the hi words, the list
+    criterion.  Returns the oracle's dict.
+    """
+    Lf = np.array(eng.info(s).box_f32, dtype=np.float32)
+    pos4 = eng.get_raw("position_hi", s)[eng.get("reverse_id", s)]
+    r = eng.get("position", s) if state else pos4[:, :3].astype(np.float64)
+    return oracle.forces(r, species, Lf.astype(np.float64), pot, pos4=pos4, Lf=Lf, aux=aux)

@@ -171,9 +171,12 @@ def dsfun_vectors(harness):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("HALMD_REFERENCE"),
+                    help="the reference checkout (default: the HALMD_REFERENCE environment variable)")
     ap.add_argument("--harness", default=os.path.join(REPO, "oracle", "_ref", "ref_harness"))
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("name the reference checkout with --reference or HALMD_REFERENCE")
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REFERENCE=" + args.reference])
     fixtures = {
         "lj_tables.json": lj_tables(args.reference),

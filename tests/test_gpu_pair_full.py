@@ -12,7 +12,7 @@ import pytest
 import halmd_gb300 as hg
 from halmd_gb300 import halmd
 import oracle
-from _systems import KA_EPS, KA_SIGMA, ka_system, lj_system, rel_force_error
+from _systems import KA_EPS, KA_SIGMA, ka_system, lj_system, rel_force_error, state_forces
 
 pytestmark = pytest.mark.gpu
 
@@ -47,10 +47,8 @@ def full_engine(potential="lennard_jones", ncell=5, dt=0.001):
 
 
 def oracle_reference(eng, sp, potential):
-    Lf = np.array(eng.info().box_f32, dtype=np.float32)
-    pos4 = eng.get_raw("position_hi")[eng.get("reverse_id")]
     pot = oracle.Potential(KA_EPS, KA_SIGMA, 1.0, "none", potential=potential, **PARAMS[potential])
-    return oracle.forces(pos4[:, :3].astype(np.float64), sp, Lf.astype(np.float64), pot, pos4=pos4, Lf=Lf)
+    return state_forces(eng, sp, pot)
 
 
 @pytest.mark.parametrize("potential", ["lennard_jones", "mie", "morse", "power_law"])

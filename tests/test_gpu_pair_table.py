@@ -8,7 +8,9 @@ row of the LJ tables (AA, AB, BB at r_c = 5 sigma) becomes an isolated
 particle pair on the x axis, far from every other pair, so each particle's
 list holds its partner alone; the force and energy the engine computes are
 compared with the FP64 host functor of the oracle (pinned to the same
-tables on the CPU, test_oracle_golden.py) at the pair's float separation.
+tables on the CPU, test_oracle_golden.py) at the pair's separation.  The
+positions are floats, so the lo words of the double-single state are zero,
+as the reference's test places its particles.
 """
 import json
 import os
@@ -38,9 +40,9 @@ def test_isolated_pairs_match_host_functor(trunc):
             if r < rc[a, b]:
                 pairs.append((a, b, r))
     spacing = 2 * (rc.max() + skin) + 5.0
-    # pairs at positive x with x0 >= r: the float difference of the two
-    # coordinates is exact (Sterbenz), so the kernel sees the separation d
-    # computed below
+    # pairs at positive x with x0 >= r, positions rounded to float: the lo
+    # words are zero and the float difference of the two hi words is exact
+    # (Sterbenz), so the kernel sees the separation d computed below
     L = np.array([2 * spacing * (len(pairs) + 1), 2 * rc.max() + 10.0, 2 * rc.max() + 10.0])
     n = 2 * len(pairs)
     pos = np.zeros((n, 3))
@@ -55,7 +57,7 @@ def test_isolated_pairs_match_host_functor(trunc):
                                   smoothing=g["h"], skin=skin, timestep=0.001))
     eng.commit()
     eng.set("species", sp)
-    eng.set("position", pos)
+    eng.set("position", pos.astype(np.float32).astype(np.float64))
     eng.set("velocity", np.zeros((n, 3)))
     eng.force(aux=True)
     f = eng.get("force")
@@ -109,7 +111,7 @@ def test_smooth_r4_near_cutoff_pairs_match_host_functor():
                                   smoothing=h, skin=skin, timestep=0.001))
     eng.commit()
     eng.set("species", sp)
-    eng.set("position", pos)
+    eng.set("position", pos.astype(np.float32).astype(np.float64))
     eng.set("velocity", np.zeros((n, 3)))
     eng.force(aux=True)
     f = eng.get("force")

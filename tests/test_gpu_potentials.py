@@ -10,7 +10,7 @@ import pytest
 
 import halmd_gb300 as hg
 import oracle
-from _systems import KA_EPS, KA_SIGMA, ka_system, rel_force_error
+from _systems import KA_EPS, KA_SIGMA, ka_system, rel_force_error, state_forces
 
 pytestmark = pytest.mark.gpu
 
@@ -47,11 +47,8 @@ def pot_engine(potential, truncation, lanes=0, block=0, precision="dsfloat"):
 
 
 def oracle_reference(eng, sp, potential, truncation):
-    inf = eng.info()
-    Lf = np.array(inf.box_f32, dtype=np.float32)
-    pos4 = eng.get_raw("position_hi")[eng.get("reverse_id")]
     pot = oracle.Potential(KA_EPS, KA_SIGMA, 2.5, truncation, h=0.005, potential=potential, **PARAMS[potential])
-    return oracle.forces(pos4[:, :3].astype(np.float64), sp, Lf.astype(np.float64), pot, pos4=pos4, Lf=Lf)
+    return state_forces(eng, sp, pot)
 
 
 @pytest.mark.parametrize("truncation", ["sharp", "shifted", "smooth_r4", "force_shifted"])

@@ -3,14 +3,14 @@
 Bars: bit-exact for integer/index work (cells, neighbour sets, Hilbert keys,
 sort permutation) and for the float/dsfloat integrator, which rounds every
 operation like the oracle; forces within the stated tolerance of an FP64
-evaluation on the same float positions.
+evaluation of the same double-single state.
 """
 import numpy as np
 import pytest
 
 import halmd_gb300 as hg
 import oracle
-from _systems import KA_EPS, KA_SIGMA, ka_system, lj_system, rel_force_error
+from _systems import KA_EPS, KA_SIGMA, ka_system, lj_system, rel_force_error, state_forces
 
 pytestmark = pytest.mark.gpu
 
@@ -49,11 +49,9 @@ def tag_order(eng, raw):
 
 
 def oracle_forces(eng, species, pot):
-    inf = eng.info()
-    Lf = np.array(inf.box_f32, dtype=np.float32)
+    # FP64 forces of the engine's state (hi + lo positions)
     pos4 = tag_order(eng, eng.get_raw("position_hi"))
-    r = pos4[:, :3].astype(np.float64)
-    return oracle.forces(r, species, Lf.astype(np.float64), pot, pos4=pos4, Lf=Lf), pos4
+    return state_forces(eng, species, pot), pos4
 
 
 @pytest.mark.parametrize("precision", ["dsfloat", "float"])

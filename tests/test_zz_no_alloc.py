@@ -55,9 +55,15 @@ def test_msd_noalloc_matches_dynamics_path():
     dev = torch.device("cuda:0")
     a = torch.from_numpy(first).to(dev).contiguous()
     b = torch.from_numpy(second).to(dev).contiguous()
+    outs = [torch.full((3,), float("nan"), dtype=torch.float64, device=dev) for _ in range(2)]
+    torch.cuda.synchronize()
     for call in range(2):                          # two calls in a row reuse the scratch
-        out = torch.full((3,), float("nan"), dtype=torch.float64, device=dev)
+        out = outs[call]
+        free0 = torch.cuda.mem_get_info(dev)[0]
         assert _noalloc(Lib, a, b, out) == 0, _lib.last_error()
+        torch.cuda.synchronize()
+        # the call takes no device memory (nothing else runs here)
+        assert torch.cuda.mem_get_info(dev)[0] == free0, call
         c, m, var = out.cpu().numpy()
         assert c == n, call
         np.testing.assert_allclose(m, ref_mean, rtol=RTOL, err_msg="call %d" % call)
@@ -81,6 +87,15 @@ def test_msd_noalloc_rejects_bad_arguments():
                                   ctypes.c_void_p(out.data_ptr()), None)
     assert rc == -1 and "not device memory" in _lib.last_error()
     assert Lib.hmd_msd_pair_noalloc(None, None, 16, ctypes.c_void_p(out.data_ptr()), None) == -1
+    # a buffer that ends before count x 3 doubles is refused before any
+    # launch: 8 particles' worth of bytes before the end of the allocation
+    # (the caching allocator's segment) that holds `a`, asked for 16
+    seg = [g for g in torch.cuda.memory_snapshot()
+           if g["address"] <= a.data_ptr() < g["address"] + g["total_size"]][0]
+    near_end = seg["address"] + seg["total_size"] - 8 * 3 * 8
+    rc = Lib.hmd_msd_pair_noalloc(ctypes.c_void_p(near_end), ctypes.c_void_p(a.data_ptr()), 16,
+                                  ctypes.c_void_p(out.data_ptr()), None)
+    assert rc == -1 and "bytes, the call needs" in _lib.last_error()
     # zero particles: (0, 0, 0)
     out.fill_(float("nan"))
     assert _noalloc(Lib, a, a, out, count=0) == 0, _lib.last_error()
