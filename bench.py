@@ -283,6 +283,30 @@ def cpu_baseline(w, r, v, species, L, budget_s=15.0):
                       (w["name"], steps)}
 
 
+def force_accuracy(eng, w):
+    """Force error of the engine's current state against the FP64 oracle, on
+    the CPU beside the baseline: max_i |F_i - F64_i| / max(|F64_i|, F_rms),
+    with F64 at the double-single state (hi + lo words) and, for comparison,
+    at the float hi words alone (what a kernel reading the hi words computes)."""
+    import oracle
+    n = w["n"]
+    pot = _ref_potential(w)
+    eng.force(aux=True)
+    f = eng.get("force")
+    Lf = np.array(eng.info().box_f32, dtype=np.float32)
+    pos4 = eng.get_raw("position_hi")[eng.get("reverse_id")]
+    species = eng.get("species")
+    out = {}
+    for key, r in (("vs_fp64_of_dsfloat_state", eng.get("position")),
+                   ("vs_fp64_at_float_hi_words", pos4[:, :3].astype(np.float64))):
+        ref = oracle.forces(r, species, Lf.astype(np.float64), pot, pos4=pos4, Lf=Lf, aux=False)["force"]
+        norm = np.linalg.norm(ref, axis=1)
+        e = np.linalg.norm(f - ref, axis=1) / np.maximum(norm, np.sqrt(np.mean(norm ** 2)))
+        out[key] = {"max": float(e.max()), "median": float(np.median(e))}
+    out["metric"] = "max_i |F_i - F64_i| / max(|F64_i|, F_rms), n = %d" % n
+    return out
+
+
 def _ref_potential(w):
     import oracle
     if w["nspecies"] == 2:
@@ -291,9 +315,10 @@ def _ref_potential(w):
 
 
 def ref_steps_per_sample(args, w):
-    """MD steps of the reference arm per bench step: args.ref_steps, fewer
-    for large systems so that one bench step stays near a second or two."""
-    return max(1, min(int(args.ref_steps), int(2e6 // w["n"])))
+    """MD steps of the reference arm per bench step: those of the GPU arm
+    (--md-steps) up to 1e7 particle-steps per bench step (about 7 s of one
+    core), fewer for larger systems."""
+    return max(1, min(int(args.md_steps), int(1e7 // w["n"])))
 
 
 def _ref_worker(wname, k, warmup, steps, per, relax, barrier, queue):
@@ -329,9 +354,9 @@ def run_reference(args, w):
     ctx = mp.get_context("spawn")
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
     per = ref_steps_per_sample(args, w)
-    # the random KA start relaxed by FP64 steepest descent (fewer steps than the
-    # GPU arm's RELAX_STEPS: the CPU port needs ~0.14 s per step at 64k)
-    relax = max(0, int(args.ref_relax)) if w["nspecies"] == 2 else 0
+    # the random KA start relaxed by FP64 steepest descent, as long as the
+    # GPU arm relaxes its own (each replica in parallel: ~0.14 s a step at 64k)
+    relax = RELAX_STEPS if w["nspecies"] == 2 else 0
     barrier = ctx.Barrier(cores)
     queue = ctx.Queue()
     procs = [ctx.Process(target=_ref_worker, args=(args.workload, k, args.warmup, args.steps, per, relax, barrier, queue))
@@ -351,11 +376,18 @@ def run_reference(args, w):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / (per * args.steps), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": w["name"], "n": n, "md_steps_per_bench_step": per, "replicas": cores},
+            "config": dict(workload_config(w, per), parallelism="replicas: one per host core (%d)" % cores),
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def workload_config(w, md_steps):
+    """The workload part of a line's config, the same for both arms."""
+    return {"workload": w["name"], "n": w["n"], "density": w["rho"], "temperature": w["T"], "dt": w["dt"],
+            "md_steps_per_bench_step": md_steps, "truncation": w["trunc"], "skin": w["skin"],
+            "r_cut": w.get("rc", 2.5)}
 
 
 def ensemble_specs(count=256, seed=256):
@@ -447,7 +479,7 @@ def run_ensemble(args):
     chains0, kernels0 = batch.get_option("rebuild_chains"), batch.get_option("step_kernels")
     clocks = ClockSampler(0)
     total_ms = 0.0
-    for _ in range(args.steps):
+    for _ in range(steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -657,11 +689,8 @@ def main():
     ap.add_argument("--workload", default="ka64k",
                     help="ka64k, lj1m, lj4k, ens256, serve; ref-lj64k, ref-ka256k: the reference's own benchmarks")
     ap.add_argument("--md-steps", type=int, default=100, help="MD steps per bench step")
-    ap.add_argument("--ref-steps", type=int, default=20,
-                    help="MD steps per bench step of the reference arm (at most 2e6 / N)")
-    ap.add_argument("--ref-relax", type=int, default=100,
-                    help="steepest-descent steps of the reference arm's KA start (CPU)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-lj1m", action="store_true", help="default workload: skip the LJ-1M sub-record")
     ap.add_argument("--phases", type=int, default=0,
                     help="run N MD steps through the module calls (integrate / force / finalize, one launch "
                          "each, no graph) with the per-phase CUDA-event timers, print the breakdown and exit; "
@@ -701,7 +730,25 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+    line = measure(args, w, world, rank, local, dist, args.steps, args.warmup, not args.no_cpu_baseline)
+    if world == 1 and args.workload == "ka64k" and not args.no_lj1m:
+        # the metric's second configuration: LJ-1M, fewer bench steps (each is
+        # 100 MD steps of a million particles)
+        sub = measure(args, workload("lj1m"), world, rank, local, dist, min(args.steps, 10), 3,
+                      not args.no_cpu_baseline)
+        line["lj1m"] = {k: sub[k] for k in ("value", "unit", "ms_per_step", "steps", "warmup", "config", "e2e",
+                                            "gpu_launches", "roofline", "clocks", "cpu_baseline", "accuracy")
+                        if k in sub}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
 
+
+def measure(args, w, world, rank, local, dist, steps, warmup, with_cpu):
+    """The GPU arm on one workload: K timed bench steps after W warm-up
+    steps; returns the JSON line (rank 0 holds the max over ranks)."""
+    import torch
     r, v, species, L = initial_state(w, seed=2024 + rank)
     if w.get("equilibrate"):
         r, v = equilibrated_state(w, r, v, species, L, seed=7 + rank)
@@ -733,14 +780,14 @@ def main():
             dist.barrier()
 
     M = args.md_steps
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         eng.step(M)
     inf0 = eng.info()
     k0, c0 = eng.get_option("step_kernels"), eng.get_option("rebuild_chains")
     barrier()
     clocks = ClockSampler(local)
     total_ms = 0.0
-    for _ in range(args.steps):
+    for _ in range(steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -757,7 +804,7 @@ def main():
     if dist is not None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     total_ms = float(t.item())
-    md_steps = M * args.steps
+    md_steps = M * steps
     value = world * n * md_steps / (total_ms * 1e-3)
     rebuilds = int(inf1.rebuilds - inf0.rebuilds)
     launches = (eng.get_option("step_kernels") - k0) + (eng.get_option("rebuild_chains") - c0) * inf1.rebuild_kernels
@@ -771,7 +818,7 @@ def main():
     vel = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     eng.get("position", out=pos)
     eng.get("velocity", out=vel)
-    for _ in range(max(1, args.steps // 2)):
+    for _ in range(max(1, steps // 2)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         eng.set("position", pos)
@@ -780,7 +827,7 @@ def main():
         eng.get("position", out=pos)
         eng.get("velocity", out=vel)
         e2e_ms += 1e3 * (time.perf_counter() - t0)
-    e2e_steps = M * max(1, args.steps // 2)
+    e2e_steps = M * max(1, steps // 2)
     # bytes the API moves per bench step: set(position) and set(velocity) copy 3 n doubles each up,
     # get(position) and get(velocity) 3 n doubles each down (converted on the device); the rebuild request
     # after set(position) reads and writes the per-system state table
@@ -801,23 +848,22 @@ def main():
     peak, peak_kind = peaks()
     traffic_bytes, traffic_from = dram_traffic(w["name"])
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    cpu = acc = None
+    if rank == 0 and world == 1 and with_cpu:
         cpu = cpu_baseline(w, r, v, species, L)
+        acc = force_accuracy(eng, w)
 
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / md_steps,
+            "steps": steps, "warmup": warmup, "ms_per_step": total_ms / md_steps,
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": value / w["published"] if w.get("published") and world == 1 else None,
             "dtype": "f32 (dsfloat state)",
             "data": "synthetic",
-            "config": {"workload": w["name"], "n": n, "density": w["rho"], "temperature": w["T"], "dt": w["dt"],
-                       "md_steps_per_bench_step": M, "truncation": w["trunc"], "skin": w["skin"],
-                       "r_cut": w.get("rc", 2.5),
-                       "precision": "dsfloat", "l2": "flushed (256 MB write) between timed bench steps",
-                       "rebuilds_in_timed_region": rebuilds, "parallelism": "replicas" if world > 1 else "single",
-                       "force_lanes": lanes, "list_block": eng.get_option("list_block"),
-                       "autotune_force_ms": {str(k): v for k, v in lane_ms.items()}},
+            "config": dict(workload_config(w, M), l2="flushed (256 MB write) between timed bench steps",
+                           parallelism="replicas" if world > 1 else "single"),
+            "run": {"precision": "dsfloat", "rebuilds_in_timed_region": rebuilds,
+                    "force_lanes": lanes, "list_block": eng.get_option("list_block"),
+                    "autotune_force_ms": {str(k): v for k, v in lane_ms.items()}},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "note": "per bench step: hmd_set(position, velocity) + hmd_step(%d) + "
@@ -832,11 +878,10 @@ def main():
             "clocks": clk}
     if cpu is not None:
         line["cpu_baseline"] = cpu
-    if rank == 0:
-        print(json.dumps(line))
+    if acc is not None:
+        line["accuracy"] = acc
     eng.close()
-    if dist is not None:
-        dist.destroy_process_group()
+    return line
 
 
 if __name__ == "__main__":

@@ -307,6 +307,17 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
         if (!(d.box[q] > 2 * rc_max))
             throw Error(HMD_ERR_INVALID, "box edge must exceed twice the largest cutoff (minimum image)");
     }
+    {
+        // unit of the lo-word codes of the force kernel's gather records:
+        // ulp of the binade of L_max / 2 (the largest |coordinate|) / 1024
+        int e = 0;
+        std::frexp(0.5 * (double)Lmax, &e);              // 0.5 Lmax in [2^(e-1), 2^e)
+        const int es = e - 1 - 23 - 10;                   // s = 2^es
+        P.lo_scale = (float)std::ldexp(1.0, es);
+        P.lo_inv_scale = (float)std::ldexp(1.0, -es);
+        P.lo_exp_bits = (uint32_t)(es + 23 + 127) << 23;  // the float 2^23 s
+        P.lo_bias = (float)std::ldexp(8388608.0 + 512.0, es);
+    }
     // Hilbert depth (gpu/sorts/hilbert.cpp:51-54)
     P.depth = std::min(10u, (uint32_t)std::ceil(std::log((double)Lmax) / M_LN2));
     if (full) {
@@ -536,6 +547,7 @@ void Engine::commit()
 
     const size_t S = S_;
     pos_.alloc(2 * S); vel_.alloc(2 * S); img_.alloc(S); force_.alloc(S); r0_.alloc(S);
+    if (ds()) fpos_.alloc(S);
     tpos_.alloc(2 * S); tvel_.alloc(2 * S); timg_.alloc(S); tid_.alloc(S);
     en_pot_.alloc(S); stress_.alloc(6 * S);
     id_.alloc(S); rid_.alloc(S);
@@ -784,6 +796,7 @@ Dev Engine::dev() const
     Dev d;
     std::memset(&d, 0, sizeof(d));
     d.pos = pos_.p; d.vel = vel_.p; d.img = img_.p; d.force = force_.p; d.r0 = r0_.p;
+    d.fpos = fpos_.p;
     d.en_pot = en_pot_.p; d.stress = stress_.p; d.id = id_.p; d.rid = rid_.p;
     d.nbr = nbr_.p; d.nbr_count = nbr_count_.p; d.nbr_cap = nbr_cap_;
     d.lanes = lanes_;
@@ -1301,6 +1314,7 @@ void Engine::ensure_forces(bool aux)
     const Dev d = dev();
     launch_mark(d, false, stream_);
     rebuild_chain(stream_);
+    launch_pack_fpos(d, stream_);
     launch_force(d, aux, stream_);
     HMD_CUDA(cudaGetLastError());
     uint32_t status = 0;
@@ -1640,6 +1654,7 @@ void Engine::force(bool aux)
         toc("rebuild");
     }
     tic();
+    launch_pack_fpos(d, stream_);
     launch_force(d, aux, stream_);
     HMD_CUDA(cudaGetLastError());
     toc(aux ? "force_aux" : "force");
@@ -1655,6 +1670,7 @@ void Engine::force(bool aux)
         const Dev d2 = dev();
         launch_mark(d2, true, stream_);
         rebuild_chain(stream_);
+        launch_pack_fpos(d2, stream_);
         launch_force(d2, aux, stream_);
         download(status_, 0, 1, &status);
     }

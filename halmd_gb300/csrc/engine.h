@@ -191,6 +191,7 @@ private:
     cudaStream_t side_ = nullptr;
 
     DevBuf<float4> pos_, vel_, img_, force_, r0_, tpos_, tvel_, timg_;
+    DevBuf<float4> fpos_;   // dsfloat engines: the force kernel's gather records
     DevBuf<float> en_pot_, stress_;
     DevBuf<uint32_t> id_, rid_, nbr_, nbr_count_, cell_, cell_count_, cell_sys_, chunk_sys_, tid_;
     DevBuf<uint32_t> key0_, key1_, val0_, val1_, hist_, status_, done_, any_rebuild_, rb_;

@@ -20,6 +20,13 @@ namespace hmd {
 #ifndef HMD_FORCE_MINB
 #define HMD_FORCE_MINB 7
 #endif
+// Resident blocks for the kernels of dsfloat engines, whose gathers carry
+// the lo words (32 bytes a neighbour): at LJ-1M 225 us with 5 blocks (96
+// registers, no spills) against 238 us with 6 and 245 us with 7 (spills);
+// at KA-64k 38.4 us against 42.4 and 43.1 us.
+#ifndef HMD_FORCE_MINB_DS
+#define HMD_FORCE_MINB_DS 6
+#endif
 // 1: load a lane's next list block one iteration ahead (force_blocks2)
 #ifndef HMD_FORCE_PREFETCH
 #define HMD_FORCE_PREFETCH 1
@@ -159,12 +166,12 @@ constexpr int ONE_SPECIES = 16;
 // Pair-parameter lookup for a neighbour of species b; false when b is not a
 // species of the system (lists hold real particles only: this keeps the
 // table lookup in bounds)
-template <bool NS1>
+template <bool NS1, bool LO = false>
 __device__ __forceinline__ bool pair_of(const PairParam* row, const PairParam& p1, uint32_t ns, float w,
                                         const PairParam*& pp)
 {
     if (NS1) { pp = &p1; return true; }
-    const uint32_t b = species_bits(w);
+    const uint32_t b = LO ? fpos_species(w) : species_bits(w);
     if (b >= ns) return false;
     pp = row + b;
     return true;
@@ -439,10 +446,11 @@ __device__ __forceinline__ void aux_acc2(ForceAcc2& A, float2 fval, float2 en, f
 
 // two near pairs (near_pair, lane by lane); va / vb: the entry is a real
 // neighbour of a species of the system
-// (LO: li, la, lb are the lo words of the particle and of the two partners)
+// (LO: lx, ly, lz are the lo words' contribution li - lj to the two
+// separations, record_dl2)
 template <int TR, bool AUX, bool WRAP, bool EXACT, bool LO>
 __device__ __forceinline__ void near_pair2(const PP2& p, const SysParam& P, float4 ri, float4 ra, float4 rb,
-                                           bool va, bool vb, ForceAcc2& A, float4 li, float4 la, float4 lb)
+                                           bool va, bool vb, ForceAcc2& A, float2 lx, float2 ly, float2 lz)
 {
     const float2 sx = f2(__fsub_rn(ri.x, ra.x), __fsub_rn(ri.x, rb.x));
     const float2 sy = f2(__fsub_rn(ri.y, ra.y), __fsub_rn(ri.y, rb.y));
@@ -462,13 +470,10 @@ __device__ __forceinline__ void near_pair2(const PP2& p, const SysParam& P, floa
         dzl = diff_err2(ri.z, ra.z, rb.z, sz);
     }
     if (LO) {
-        const float2 ex = f2(__fsub_rn(li.x, la.x), __fsub_rn(li.x, lb.x));
-        const float2 ey = f2(__fsub_rn(li.y, la.y), __fsub_rn(li.y, lb.y));
-        const float2 ez = f2(__fsub_rn(li.z, la.z), __fsub_rn(li.z, lb.z));
         if (EXACT) {
-            dxl = ex; dyl = ey; dzl = ez;
+            dxl = lx; dyl = ly; dzl = lz;
         } else {
-            dxl = add2(dxl, ex); dyl = add2(dyl, ey); dzl = add2(dzl, ez);
+            dxl = add2(dxl, lx); dyl = add2(dyl, ly); dzl = add2(dzl, lz);
         }
     }
     float2 rrl = add2(add2(fma2(dx, dx, neg2(px)), fma2(dy, dy, neg2(py))), fma2(dz, dz, neg2(pz)));
@@ -499,7 +504,7 @@ __device__ __forceinline__ void near_pair2(const PP2& p, const SysParam& P, floa
 // two far pairs (far_pair, lane by lane)
 template <int TR, bool AUX, bool WRAP, bool LO>
 __device__ __forceinline__ void far_pair2(const PP2& p, const SysParam& P, float4 ri, float4 ra, float4 rb,
-                                          bool va, bool vb, ForceAcc2& A, float4 li, float4 la, float4 lb)
+                                          bool va, bool vb, ForceAcc2& A, float2 lx, float2 ly, float2 lz)
 {
     const float2 sx = f2(__fsub_rn(ri.x, ra.x), __fsub_rn(ri.x, rb.x));
     const float2 sy = f2(__fsub_rn(ri.y, ra.y), __fsub_rn(ri.y, rb.y));
@@ -516,9 +521,9 @@ __device__ __forceinline__ void far_pair2(const PP2& p, const SysParam& P, float
         // (far_pair); rr takes it to first order
         float2 ex = bc2(0.0f), ey = bc2(0.0f), ez = bc2(0.0f);
         if (LO) {
-            ex = f2(__fsub_rn(li.x, la.x), __fsub_rn(li.x, lb.x));
-            ey = f2(__fsub_rn(li.y, la.y), __fsub_rn(li.y, lb.y));
-            ez = f2(__fsub_rn(li.z, la.z), __fsub_rn(li.z, lb.z));
+            ex = lx;
+            ey = ly;
+            ez = lz;
         }
         if (WRAP) {
             ex = add2(ex, diff_err2(ri.x, ra.x, rb.x, sx));
@@ -613,13 +618,39 @@ __device__ __forceinline__ uint32_t idx_at(uint4 v, int e) { return e == 0 ? v.x
 // contiguous memory and each lane has E independent position gathers in
 // flight.  Entries past the count are never dereferenced (the lane gathers
 // its own position instead).
-// gather of a neighbour's position: hi and lo words with one 32-byte load
-// (LO), or the hi word alone
+// gather of a neighbour's position: its 16-byte record (hmd_device.cuh
+// fpos_encode) in dsfloat engines (LO), else the hi word
 template <bool LO>
-__device__ __forceinline__ void gather_pos(const Dev& d, uint32_t j, float4& hi, float4& lo)
+__device__ __forceinline__ float4 gather_pos(const Dev& d, uint32_t j)
 {
-    if (LO) ldg_pos2(d.pos, j, hi, lo);
-    else hi = ldg_hi(d.pos, j);
+    return LO ? __ldg(d.fpos + j) : ldg_hi(d.pos, j);
+}
+
+// the lo words of a gathered record (exact multiples of the code unit s)
+__device__ __forceinline__ float4 record_lo(float w, const SysParam& P)
+{
+    return make_float4(__fsub_rn(fpos_fx(w, P.lo_exp_bits), P.lo_bias),
+                       __fsub_rn(fpos_fy(w, P.lo_exp_bits), P.lo_bias),
+                       __fsub_rn(fpos_fz(w, P.lo_exp_bits), P.lo_bias), 0.0f);
+}
+
+// li - lo of two gathered records, per component, two entries per
+// instruction: the separation residuals the lo words contribute
+__device__ __forceinline__ void record_dl2(float4 li, float wa, float wb, const SysParam& P, float2& ex, float2& ey,
+                                           float2& ez)
+{
+    const uint32_t eb = P.lo_exp_bits;
+    const float2 bias = bc2(P.lo_bias);
+    ex = sub2(bc2(li.x), sub2(f2(fpos_fx(wa, eb), fpos_fx(wb, eb)), bias));
+    ey = sub2(bc2(li.y), sub2(f2(fpos_fy(wa, eb), fpos_fy(wb, eb)), bias));
+    ez = sub2(bc2(li.z), sub2(f2(fpos_fz(wa, eb), fpos_fz(wb, eb)), bias));
+}
+
+// species of a gathered neighbour
+template <bool LO>
+__device__ __forceinline__ uint32_t nbr_species(float w)
+{
+    return LO ? fpos_species(w) : species_bits(w);
 }
 
 template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool LO, bool EXACT = false>
@@ -646,14 +677,15 @@ __device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t 
         for (int e = 0; e < E; ++e) {
             const uint32_t o = q * E + e;
             const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
-            gather_pos<LO>(d, k < cnt ? idx_at(jv, e) : i, rj[e], lj[e]);
+            rj[e] = gather_pos<LO>(d, k < cnt ? idx_at(jv, e) : i);
         }
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const uint32_t o = q * E + e;
             const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
+            lj[e] = LO ? record_lo(rj[e].w, P) : make_float4(0, 0, 0, 0);
             const PairParam* pp;
-            if (k >= cnt || !pair_of<NS1>(row, p1, ns, rj[e].w, pp)) continue;
+            if (k >= cnt || !pair_of<NS1, LO>(row, p1, ns, rj[e].w, pp)) continue;
             if (FAR) far_pair<TR, AUX, WRAP, LO>(*pp, P, ri, rj[e], A, li, lj[e]);
             else near_pair<TR, AUX, WRAP, EXACT, LO>(*pp, P, ri, rj[e], A, li, lj[e]);
         }
@@ -691,17 +723,19 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
         } else {
             jv = ld_list(lst);
         }
-        float4 rj[E], lj[E];
+        float4 rj[E];
         bool in[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const uint32_t o = q * E + e;
             const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
             in[e] = k < cnt;
-            gather_pos<LO>(d, in[e] ? idx_at(jv, e) : i, rj[e], lj[e]);
+            rj[e] = gather_pos<LO>(d, in[e] ? idx_at(jv, e) : i);
         }
 #pragma unroll
         for (int e = 0; e < E; e += 2) {
+            float2 lx = bc2(0.0f), ly = bc2(0.0f), lz = bc2(0.0f);
+            if (LO) record_dl2(li, rj[e].w, rj[e + 1].w, P, lx, ly, lz);
             PP2 pp;
             bool va = in[e], vb = in[e + 1];
             if (NS1) {
@@ -709,13 +743,13 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
             } else {
                 // a neighbour of no species of the system (lists hold real
                 // particles only) reads row entry 0 and is masked
-                const uint32_t ba = species_bits(rj[e].w), bb = species_bits(rj[e + 1].w);
+                const uint32_t ba = nbr_species<LO>(rj[e].w), bb = nbr_species<LO>(rj[e + 1].w);
                 va = va && ba < ns;
                 vb = vb && bb < ns;
                 pp = pack_params(row[ba < ns ? ba : 0u], row[bb < ns ? bb : 0u]);
             }
-            if (FAR) far_pair2<TR, AUX, WRAP, LO>(pp, P, ri, rj[e], rj[e + 1], va, vb, A, li, lj[e], lj[e + 1]);
-            else near_pair2<TR, AUX, WRAP, EXACT, LO>(pp, P, ri, rj[e], rj[e + 1], va, vb, A, li, lj[e], lj[e + 1]);
+            if (FAR) far_pair2<TR, AUX, WRAP, LO>(pp, P, ri, rj[e], rj[e + 1], va, vb, A, lx, ly, lz);
+            else near_pair2<TR, AUX, WRAP, EXACT, LO>(pp, P, ri, rj[e], rj[e + 1], va, vb, A, lx, ly, lz);
         }
         if (HMD_FORCE_PREFETCH) jv = jn;
     }
@@ -913,14 +947,17 @@ __device__ __forceinline__ void force_blocks_pot(const Dev& d, uint32_t i, uint3
             const uint32_t o = q * E + e;
             const uint32_t k = b * LB + (FAR ? LB - 1 - o : o);
             in[e] = k < cnt;
-            gather_pos<LO>(d, in[e] ? idx_at(jv, e) : i, rj[e], lj[e]);
+            rj[e] = gather_pos<LO>(d, in[e] ? idx_at(jv, e) : i);
         }
+#pragma unroll
+        for (int e = 0; e < E; ++e)
+            lj[e] = LO ? record_lo(rj[e].w, P) : make_float4(0, 0, 0, 0);
 #pragma unroll
         for (int e = 0; e < E; e += 2) {
             const bool two = e + 1 < E;
             const float4 ra = rj[e], rb = two ? rj[e + 1 < E ? e + 1 : e] : ri;
             const float4 la = lj[e], lb = two ? lj[e + 1 < E ? e + 1 : e] : li;
-            const uint32_t ba = species_bits(ra.w), bb = species_bits(rb.w);
+            const uint32_t ba = nbr_species<LO>(ra.w), bb = two ? nbr_species<LO>(rb.w) : species_bits(rb.w);
             const bool va = in[e] && ba < ns;
             const bool vb = two && in[e + 1 < E ? e + 1 : e] && bb < ns;
             const PairParam& pa = row[ba < ns ? ba : 0u];
@@ -994,7 +1031,7 @@ __device__ __forceinline__ void force_pot(const Dev& d, uint32_t i, uint32_t q, 
 
 // LO: the engine holds dsfloat positions (the separations carry the lo words)
 template <int W, int E, int KIND, bool AUX, bool LO>
-__global__ void __launch_bounds__(128, HMD_FORCE_MINB) k_force(Dev d)
+__global__ void __launch_bounds__(128, LO ? HMD_FORCE_MINB_DS : HMD_FORCE_MINB) k_force(Dev d)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = t / W, q = t % W;
@@ -1008,7 +1045,8 @@ __global__ void __launch_bounds__(128, HMD_FORCE_MINB) k_force(Dev d)
     if (KIND != FK_GENERIC && force_kind_of(P) != KIND) return;      // another kind's launch
     if (KIND == FK_GENERIC && force_kind_of(P) == FK_FULL) return;   // no list: k_force_full
     float4 ri, li = make_float4(0, 0, 0, 0);
-    gather_pos<LO>(d, i, ri, li);
+    if (LO) ldg_pos2(d.pos, i, ri, li);
+    else ri = ldg_hi(d.pos, i);
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;
     const uint32_t packed = real ? d.nbr_count[i] : 0u;

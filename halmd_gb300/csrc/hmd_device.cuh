@@ -112,6 +112,10 @@ struct SysParam {
     float exact_min;           // |coordinate| from which near-pair differences are exact (k_force)
     float descent_step;        // INTEG_DESCENT: move = descent_step * F ...
     float descent_max;         // ... capped at this length per particle and step
+    float lo_scale;            // unit s of the lo-word codes of Dev::fpos (a power of two)
+    float lo_inv_scale;        // 1 / s
+    uint32_t lo_exp_bits;      // bits of the float 2^23 s (a code field ORed in gives (2^23 + field) s)
+    float lo_bias;             // (2^23 + 512) s
     uint32_t pot;              // pair potential (Pot)
     uint32_t interval;         // INTEG_BOLTZMANN: steps between velocity draws
     // INTEG_HOOVER (verlet_nvt_hoover.cpp:58-84): chain masses, dim N T, T, dt
@@ -149,6 +153,7 @@ struct Dev {
     float4* img;               // [S]
     float4* force;             // [S]
     float4* r0;                // [S] hi positions at the last list build
+    float4* fpos;              // [S] dsfloat engines: the force kernel's gather records (fpos_encode)
     float* en_pot;             // [S]
     float* stress;             // [6S]
     uint32_t* id;              // [S] tag of the particle within its system
@@ -209,6 +214,45 @@ __device__ __forceinline__ const float4& pos_hi(const float4* p, uint32_t i) { r
 __device__ __forceinline__ const float4& pos_lo(const float4* p, uint32_t i) { return p[2 * (size_t)i + 1]; }
 __device__ __forceinline__ float4 ldg_hi(const float4* p, uint32_t i) { return __ldg(p + 2 * (size_t)i); }
 
+// The force kernel's gather record of a dsfloat slot, 16 bytes: the hi
+// word's x, y, z and in w the species (bits 0-1) and the lo words as
+// multiples c of the system's lo_scale s = ulp(L/2) / 1024, stored as the
+// 10-bit fields c + 512 (bits 2-11, 12-21, 22-31).  |lo| <= ulp(L/2)/2 =
+// 512 s, so c = lo / s rounded (clamped to +-511) is within s/2 of it (s a
+// power of two: the scaling is exact).  The full double-single word pair is
+// 32 bytes; the gathers of the force kernel are bound by the L1 data path,
+// and half the bytes halve that traffic.  A field ORed into the mantissa of
+// 2^23 s gives the float (2^23 + c + 512) s, so c s costs one subtraction
+// (record_lo), no integer conversion.
+__device__ __forceinline__ uint32_t lo_code(float lo, float inv_s)
+{
+    const int c = __float2int_rn(__fmul_rn(lo, inv_s));
+    return (uint32_t)(min(max(c, -511), 511) + 512);
+}
+
+__device__ __forceinline__ float4 fpos_encode(float4 hi, float4 lo, float inv_s)
+{
+    const uint32_t w = (species_bits(hi.w) & 3u) | (lo_code(lo.x, inv_s) << 2) | (lo_code(lo.y, inv_s) << 12) |
+                       (lo_code(lo.z, inv_s) << 22);
+    return make_float4(hi.x, hi.y, hi.z, __uint_as_float(w));
+}
+
+// species of a record's w word, and its three code fields as the floats
+// (2^23 + c + 512) s (exp_bits: SysParam::lo_exp_bits)
+__device__ __forceinline__ uint32_t fpos_species(float w) { return __float_as_uint(w) & 3u; }
+__device__ __forceinline__ float fpos_fx(float w, uint32_t exp_bits)
+{
+    return __uint_as_float(((__float_as_uint(w) >> 2) & 0x3FFu) | exp_bits);
+}
+__device__ __forceinline__ float fpos_fy(float w, uint32_t exp_bits)
+{
+    return __uint_as_float(((__float_as_uint(w) >> 12) & 0x3FFu) | exp_bits);
+}
+__device__ __forceinline__ float fpos_fz(float w, uint32_t exp_bits)
+{
+    return __uint_as_float((__float_as_uint(w) >> 22) | exp_bits);
+}
+
 // both words of slot i with one 256-bit read-only load (32-byte aligned:
 // the array comes from cudaMalloc and a slot spans 32 bytes)
 __device__ __forceinline__ void ldg_pos2(const float4* p, uint32_t i, float4& hi, float4& lo)
@@ -239,9 +283,28 @@ __device__ __forceinline__ float rr_exact(float dx, float dy, float dz)
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+// add and multiply with an explicit rounding modifier in PTX, so that no
+// compiler pass contracts a product and a sum into one FMA: the list
+// criterion and the cut-off test then round exactly as the oracle's float
+// restatement (a squared distance contracted to fma(z, z, x^2 + y^2) can
+// land on the other side of r_c^2)
+__device__ __forceinline__ float2 add2(float2 a, float2 b)
+{
+    unsigned long long c;
+    asm("add.rn.f32x2 %0, %1, %2;"
+        : "=l"(c) : "l"(*reinterpret_cast<const unsigned long long*>(&a)),
+          "l"(*reinterpret_cast<const unsigned long long*>(&b)));
+    return *reinterpret_cast<const float2*>(&c);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return add2(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b)
+{
+    unsigned long long c;
+    asm("mul.rn.f32x2 %0, %1, %2;"
+        : "=l"(c) : "l"(*reinterpret_cast<const unsigned long long*>(&a)),
+          "l"(*reinterpret_cast<const unsigned long long*>(&b)));
+    return *reinterpret_cast<const float2*>(&c);
+}
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 

@@ -27,6 +27,8 @@ void launch_finalize(const Dev& d, bool ds, cudaStream_t st);
 // finalize of step k fused with the integrate of step k + 1 (captured chunks)
 void launch_finalize_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, cudaStream_t st);
 void launch_thermo(const Dev& d, cudaStream_t st);
+// the force kernel's gather records of every real slot (dsfloat engines)
+void launch_pack_fpos(const Dev& d, cudaStream_t st);
 // largest |min_image(r - r0)|^2 of system s as float bits into *out
 void launch_max_displacement(const Dev& d, uint32_t s, uint32_t slots, uint32_t* out, cudaStream_t st);
 // engines with a Nose-Hoover system: the chain's half step before integrate

@@ -859,7 +859,10 @@ __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_
     o.cap = d.nbr_cap;
     const float* rrcs = s_rrcs + (real ? a : 0u) * P.ns;
     const float* rrnear = s_rrnear + (real ? a : 0u) * P.ns;
-    if (real) d.r0[i] = ri;
+    if (real) {
+        d.r0[i] = ri;
+        if (d.ds) d.fpos[i] = fpos_encode(ri, pos_lo(d.pos, i), P.lo_inv_scale);
+    }
     // bounding box of the warp's real particles
     float lo[3] = {real ? ri.x : INFINITY, real ? ri.y : INFINITY, real ? ri.z : INFINITY};
     float hi[3] = {real ? ri.x : -INFINITY, real ? ri.y : -INFINITY, real ? ri.z : -INFINITY};

@@ -416,4 +416,22 @@ void launch_max_displacement(const Dev& d, uint32_t s, uint32_t slots, uint32_t*
     k_max_displacement<<<grid, 256, 0, st>>>(d, s, out);
 }
 
+// the force kernel's gather records (fpos_encode) of every real slot of a
+// dsfloat engine; the integrate kernel and the list build write them as they
+// go, this pass serves force evaluations outside a step
+__global__ void __launch_bounds__(256) k_pack_fpos(Dev d)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const float4 r = pos_hi(d.pos, i);
+    if (species_bits(r.w) == PLACEHOLDER) return;
+    const SysParam& P = d.sys[d.chunk_sys[i / CHUNK]];
+    d.fpos[i] = fpos_encode(r, pos_lo(d.pos, i), P.lo_inv_scale);
+}
+
+void launch_pack_fpos(const Dev& d, cudaStream_t st)
+{
+    if (!d.ds || d.S_grid == 0) return;
+    k_pack_fpos<<<d.S_grid / 256, 256, 0, st>>>(d);
+}
+
 } // namespace hmd

@@ -229,7 +229,10 @@ __device__ __forceinline__ float step_slot(const Dev& d, const SysParam& P, cons
         }
         if (!COPY) {
             pos_hi(dst, i) = r;
-            if (DS) pos_lo(dst, i) = rl;
+            if (DS) {
+                pos_lo(dst, i) = rl;
+                d.fpos[i] = fpos_encode(r, rl, P.lo_inv_scale);
+            }
         }
         if (k.x != 0.0f || k.y != 0.0f || k.z != 0.0f) {
             // image counters are read and written only on a wrap
@@ -247,7 +250,10 @@ __device__ __forceinline__ float step_slot(const Dev& d, const SysParam& P, cons
     }
     if (COPY) {
         pos_hi(dst, i) = r;
-        if (DS) pos_lo(dst, i) = rl;
+        if (DS) {
+            pos_lo(dst, i) = rl;
+            if (real) d.fpos[i] = fpos_encode(r, rl, P.lo_inv_scale);
+        }
     }
     return rr;
 }

@@ -49,7 +49,7 @@ extern "C" {
  * when the potential has no r_cut); r_cut and skin are ignored */
 #define HMD_TRUNC_NONE 4
 
-/* pair potentials (mdsim/gpu/potentials/pair/*.cpp; every truncation applies to each) */
+/* pair potentials (mdsim/gpu/potentials/pair/{lennard_jones,mie,morse,power_law}.cpp; every truncation applies to each) */
 #define HMD_POTENTIAL_LENNARD_JONES 0  /* lennard_jones.cpp (default) */
 #define HMD_POTENTIAL_MIE 1            /* mie.cpp: epsilon, sigma, index_repulsion m, index_attraction n */
 #define HMD_POTENTIAL_MORSE 2          /* morse.cpp: epsilon, sigma, r_min, distortion B */

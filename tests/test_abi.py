@@ -86,3 +86,13 @@ def test_enum_constants_agree_with_the_header():
     assert pot == _lib.POTENTIAL == oracle.POTENTIAL
     short = {k: v for k, v in _lib.INTEGRATOR.items() if not k.startswith("verlet_")}
     assert integ == short
+
+
+def test_c_harness_calls_every_entry_point_and_links(lib):
+    """The C harness (tests/c_abi/harness.c) names every declared entry point
+    and compiles and links against the header and the library with a C
+    compiler; it runs on a GPU in test_gpu_c_abi.py."""
+    import _c_harness
+    missing = sorted(set(_lib.header_symbols()) - _c_harness.called_symbols())
+    assert not missing, missing
+    assert os.path.exists(_c_harness.build())
