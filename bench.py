@@ -99,9 +99,9 @@ def initial_state(w, seed=2024):
     return r, v, species, L
 
 
-def make_engine(w, L, seed=7):
+def make_engine(w, L, seed=7, precision="dsfloat"):
     import halmd_gb300 as hg
-    eng = hg.Engine("dsfloat")
+    eng = hg.Engine(precision)
     extra = {}
     if w.get("occupancy"):
         extra["neighbour_occupancy"] = w["occupancy"]
@@ -680,6 +680,77 @@ def run_phases(args, w):
     eng.close()
 
 
+def run_variants(args, w):
+    """The precision variants of one workload from the same start: float
+    positions, dsfloat positions (the default engine) and the FP64 variant
+    (HMD_PRECISION_DOUBLE), each run for --variants MD steps of NVE.  Per
+    variant: the energy drift |E(t) - E(0)| / |E(0)| fitted per 1e5 steps,
+    its difference from the FP64 run's, and the force error of the start
+    state against FP64 forces of the same state (the FP64 engine with the
+    float cut-off test, so the pair sets agree)."""
+    import halmd_gb300 as hg
+    import torch
+    steps, every = int(args.variants), max(1, int(args.variants) // 100)
+    r, v, species, L = initial_state(w)
+    wv = dict(w, rate=0.0)                      # NVE: drift is a property of the integrator and arithmetic
+    # the common start: the synthetic state (KA: relaxed) after 200 steps of
+    # the dsfloat engine, so that forces are those of a fluid, not a lattice
+    eng = make_engine(wv, L)
+    eng.set("species", species)
+    eng.set("position", r)
+    if w["nspecies"] == 2:
+        eng.minimize(RELAX_STEPS, RELAX_STEP_SIZE, RELAX_MAX_MOVE)
+    eng.set("velocity", v)
+    eng.step(200)
+    r, v = eng.get("position"), eng.get("velocity")
+    eng.close()
+
+    def engine(precision, float_cutoff=False):
+        eng = make_engine(wv, L, precision=precision)
+        if float_cutoff:
+            eng.set_option("float_cutoff", 1)
+        eng.set("species", species)
+        eng.set("position", r)
+        eng.set("velocity", v)
+        return eng
+
+    out = {}
+    ref64 = engine("double", float_cutoff=True)
+    for precision in ("float", "dsfloat", "double"):
+        eng = engine(precision)
+        eng.force(aux=True)
+        f = eng.get("force")
+        ref64.set("position", eng.get("position"))
+        ref64.force()
+        f64 = ref64.get("force")
+        norm = np.linalg.norm(f64, axis=1)
+        err = np.linalg.norm(f - f64, axis=1) / np.maximum(norm, np.sqrt(np.mean(norm ** 2)))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t, e = [], []
+        for k in range(steps // every + 1):
+            if k:
+                eng.step(every - 1)
+            eng.step(1, aux_last=True)
+            th = eng.thermo()
+            t.append(k * every)
+            e.append(0.5 * th["mv2"] + th["epot"])
+        wall = time.perf_counter() - t0
+        t, e = np.array(t, dtype=float), np.array(e)
+        (slope, _), cov = np.polyfit(t, e, 1, cov=True)
+        out[precision] = {"drift_per_1e5_steps": float(slope * 1e5 / abs(e[0])),
+                          "drift_stderr": float(np.sqrt(cov[0, 0]) * 1e5 / abs(e[0])),
+                          "max_abs_dE_over_E0": float(np.max(np.abs(e - e[0])) / abs(e[0])),
+                          "force_err_vs_fp64": {"max": float(err.max()), "median": float(np.median(err))},
+                          "ms_per_step": 1e3 * wall / steps}
+        eng.close()
+    ref64.close()
+    for precision in ("float", "dsfloat"):
+        out[precision]["drift_minus_fp64"] = out[precision]["drift_per_1e5_steps"] - out["double"]["drift_per_1e5_steps"]
+    print(json.dumps({"workload": w["name"], "n": w["n"], "md_steps": steps, "sample_every": every,
+                      "ensemble": "NVE from the same start", "variants": out}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -691,6 +762,9 @@ def main():
     ap.add_argument("--md-steps", type=int, default=100, help="MD steps per bench step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-lj1m", action="store_true", help="default workload: skip the LJ-1M sub-record")
+    ap.add_argument("--variants", type=int, default=0,
+                    help="run the float, dsfloat and FP64 variants of the workload for N MD steps from the same "
+                         "start and print their energy drift and force error, then exit")
     ap.add_argument("--phases", type=int, default=0,
                     help="run N MD steps through the module calls (integrate / force / finalize, one launch "
                          "each, no graph) with the per-phase CUDA-event timers, print the breakdown and exit; "
@@ -717,6 +791,8 @@ def main():
     w = workload(args.workload)
     if args.phases:
         return run_phases(args, w)
+    if args.variants:
+        return run_variants(args, w)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(PKG, "libhalmd_gb300.so")
 HEADER = os.path.join(REPO, "include", "halmd_gb300.h")
 
 HMD_OK = 0
-PRECISION = {"float": 0, "single": 0, "dsfloat": 1, "double-single": 1}
+PRECISION = {"float": 0, "single": 0, "dsfloat": 1, "double-single": 1, "double": 2, "fp64": 2}
 TRUNCATION = {"sharp": 0, "shifted": 1, "smooth_r4": 2, "force_shifted": 3, "none": 4}
 INTEGRATOR = {"verlet": 0, "verlet_nvt_andersen": 1, "andersen": 1, "verlet_nvt_hoover": 2, "hoover": 2,
               "verlet_nvt_boltzmann": 3, "boltzmann": 3, "euler": 4}

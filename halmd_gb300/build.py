@@ -17,7 +17,7 @@ BUILD = os.path.join(REPO, "_build")
 LIB = os.path.join(PKG, "libhalmd_gb300.so")
 
 SOURCES = ["kernels_step.cu", "kernels_force_lj.cu", "kernels_force_smooth.cu", "kernels_force_other.cu",
-           "kernels_force_pot.cu", "kernels_force_mixed.cu", "kernels_force_full.cu", "kernels_rebuild.cu", "kernels_obs.cu", "kernels_io.cu", "engine.cu", "dynamics.cu", "msd_noalloc.cu", "capi.cu"]
+           "kernels_force_pot.cu", "kernels_force_mixed.cu", "kernels_force_full.cu", "kernels_rebuild.cu", "kernels_obs.cu", "kernels_io.cu", "engine.cu", "dynamics.cu", "msd_noalloc.cu", "capi.cu", "kernels_fp64.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "--expt-relaxed-constexpr",
          "-I" + INCLUDE, "-I" + CSRC]

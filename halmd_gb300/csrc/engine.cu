@@ -22,8 +22,8 @@ static uint32_t bits_of(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u;
 
 Engine::Engine(int precision, int device) : precision_(precision), device_(device)
 {
-    if (precision != HMD_PRECISION_FLOAT && precision != HMD_PRECISION_DSFLOAT)
-        throw Error(HMD_ERR_INVALID, "precision must be HMD_PRECISION_FLOAT or HMD_PRECISION_DSFLOAT");
+    if (precision != HMD_PRECISION_FLOAT && precision != HMD_PRECISION_DSFLOAT && precision != HMD_PRECISION_DOUBLE)
+        throw Error(HMD_ERR_INVALID, "precision must be HMD_PRECISION_FLOAT, _DSFLOAT or _DOUBLE");
     int ndev = 0;
     HMD_CUDA(cudaGetDeviceCount(&ndev));
     if (device < 0 || device >= ndev) throw Error(HMD_ERR_INVALID, "no such CUDA device");
@@ -163,6 +163,8 @@ uint32_t Engine::add_system(const hmd_system_desc& d)
     const uint32_t ns = d.nspecies;
     if (d.potential < HMD_POTENTIAL_LENNARD_JONES || d.potential > HMD_POTENTIAL_POWER_LAW)
         throw Error(HMD_ERR_INVALID, "unknown potential");
+    if (fp64() && (d.potential != HMD_POTENTIAL_LENNARD_JONES || full || d.integrator != HMD_INTEGRATOR_VERLET))
+        throw Error(HMD_ERR_INVALID, "the FP64 variant takes truncated Lennard-Jones potentials and verlet");
     for (uint32_t ab = 0; ab < ns * ns; ++ab) {
         if (!(d.sigma[ab] > 0) || !(full || d.r_cut[ab] > 0) || !(d.epsilon[ab] >= 0))
             throw Error(HMD_ERR_INVALID, "bad potential parameters");
@@ -214,6 +216,7 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
     P.integrator = integrator_of(d.integrator);
     double rc_max = 0, rcs_max = 0;
     h.pairs.resize(ns * ns);
+    h.pairs64.resize(ns * ns);
     for (uint32_t ab = 0; ab < ns * ns; ++ab) {
         const double sigma = d.sigma[ab], eps = d.epsilon[ab];
         const double sigma2 = sigma * sigma;
@@ -253,11 +256,22 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
             p.q3 = (float)(d.index[ab] % 2);
         }
         p.pad = 0.0f;
+        PairParam64& q = h.pairs64[ab];
+        q.eps4 = 4 * eps;
+        q.c48 = 48 * eps / sigma2;
+        q.sigma2 = sigma2;
+        q.rr_cut = rc * rc;
+        q.r_cut = rc;
+        q.en_cut = (d.truncation == HMD_TRUNC_SHARP) ? 0.0 : ec;
+        q.f_cut = (d.truncation == HMD_TRUNC_FORCE_SHIFTED) ? fc * rc : 0.0;
+        q.pad = 0.0;
         if (full) continue;
         rc_max = std::max(rc_max, rc);
         rcs_max = std::max(rcs_max, rcs);
     }
     P.rri_smooth = (d.truncation == HMD_TRUNC_SMOOTH_R4) ? (float)std::pow(d.smoothing, -2) : 0.0f;
+    P.rri_smooth64 = (d.truncation == HMD_TRUNC_SMOOTH_R4) ? std::pow(d.smoothing, -2) : 0.0;
+    P.dt64 = d.timestep;
     P.dt = (float)d.timestep;
     P.dt_half = (float)(d.timestep / 2);
     P.rr_half_skin = full ? INFINITY : (float)(0.25 * d.skin * d.skin);   // pair_full never rebuilds
@@ -290,6 +304,11 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
         double near_max = 0;
         for (uint32_t ab = 0; ab < ns * ns; ++ab) near_max = std::max(near_max, NEAR_SIGMA * d.sigma[ab] + d.skin);
         P.exact_min = (float)(2.0 * near_max * (1.0 + 1e-6));
+        // near pairs never reach r_c when NEAR_SIGMA sigma + skin stays below it
+        bool in_range = true;
+        for (uint32_t ab = 0; ab < ns * ns; ++ab)
+            in_range = in_range && NEAR_SIGMA * d.sigma[ab] + d.skin < d.sigma[ab] * d.r_cut[ab] * (1.0 - 1e-6);
+        P.near_in_range = (in_range && !full) ? 1u : 0u;
     }
     for (int q = 0; q < 3; ++q) {
         // a list pair is within r_c + skin of each other at force time (each
@@ -404,6 +423,7 @@ void Arena::release(uint32_t at, uint32_t n)
 void Engine::reserve(uint32_t slots, uint32_t systems, uint32_t neighbour_capacity)
 {
     if (committed_) throw Error(HMD_ERR_STATE, "capacity must be reserved before commit");
+    if (fp64()) throw Error(HMD_ERR_INVALID, "the FP64 variant runs fixed engines only");
     if (slots == 0 || systems == 0) throw Error(HMD_ERR_INVALID, "capacity must be positive");
     for (const SysHost& h : sys_)
         if (h.desc.integrator != HMD_INTEGRATOR_VERLET && h.desc.integrator != HMD_INTEGRATOR_ANDERSEN)
@@ -548,6 +568,7 @@ void Engine::commit()
     const size_t S = S_;
     pos_.alloc(2 * S); vel_.alloc(2 * S); img_.alloc(S); force_.alloc(S); r0_.alloc(S);
     if (ds()) fpos_.alloc(S);
+    if (fp64()) force64_.alloc(S);
     tpos_.alloc(2 * S); tvel_.alloc(2 * S); timg_.alloc(S); tid_.alloc(S);
     en_pot_.alloc(S); stress_.alloc(6 * S);
     id_.alloc(S); rid_.alloc(S);
@@ -564,6 +585,7 @@ void Engine::commit()
     rb_.alloc(1 + table_size_ + (size_t)RB_UNITS * (table_size_ + 1));
     dsys_.alloc(table_size_); dst_.alloc(table_size_);
     dpair_.alloc((size_t)table_size_ * MAX_SPECIES * MAX_SPECIES);
+    if (fp64()) dpair64_.alloc((size_t)table_size_ * MAX_SPECIES * MAX_SPECIES);
     partial_.alloc((S / 256) * NTHERMO + 1); thermo_.alloc((size_t)table_size_ * NTHERMO);
 
     // everything starts as ghosts owned by the null system (capacity mode)
@@ -665,6 +687,9 @@ void Engine::upload_system(uint32_t s)
     HMD_CUDA(cudaMemcpyAsync(dsys_.p + s, &h.P, sizeof(SysParam), cudaMemcpyHostToDevice, stream_));
     if (!h.pairs.empty())
         HMD_CUDA(cudaMemcpyAsync(dpair_.p + h.P.pair_off, h.pairs.data(), h.pairs.size() * sizeof(PairParam),
+                                 cudaMemcpyHostToDevice, stream_));
+    if (fp64() && !h.pairs64.empty())
+        HMD_CUDA(cudaMemcpyAsync(dpair64_.p + h.P.pair_off, h.pairs64.data(), h.pairs64.size() * sizeof(PairParam64),
                                  cudaMemcpyHostToDevice, stream_));
     sync();
 }
@@ -797,6 +822,10 @@ Dev Engine::dev() const
     std::memset(&d, 0, sizeof(d));
     d.pos = pos_.p; d.vel = vel_.p; d.img = img_.p; d.force = force_.p; d.r0 = r0_.p;
     d.fpos = fpos_.p;
+    d.force64 = force64_.p;
+    d.pair64 = dpair64_.p;
+    d.fp64 = fp64() ? 1u : 0u;
+    d.float_cutoff = float_cutoff_ ? 1u : 0u;
     d.en_pot = en_pot_.p; d.stress = stress_.p; d.id = id_.p; d.rid = rid_.p;
     d.nbr = nbr_.p; d.nbr_count = nbr_count_.p; d.nbr_cap = nbr_cap_;
     d.lanes = lanes_;
@@ -1211,6 +1240,14 @@ void Engine::set_option(const std::string& name, int64_t value)
         }
         return;
     }
+    if (name == "float_cutoff") {
+        // FP64 variant: take the pair set of the float list criterion (the
+        // other engines' cut-off test) instead of r^2 < r_c^2 in double
+        float_cutoff_ = value != 0;
+        if (committed_) destroy_graphs();
+        forces_valid_ = false;
+        return;
+    }
     if (name == "fuse_steps") {
         const bool f = value != 0;
         if (f == fuse_) return;
@@ -1236,6 +1273,7 @@ int64_t Engine::get_option(const std::string& name) const
     if (name == "neighbour_scan") return nbr_scan_;
     if (name == "step_kernels") return (int64_t)step_kernels_;
     if (name == "fuse_steps") return fuse_ ? 1 : 0;
+    if (name == "float_cutoff") return float_cutoff_ ? 1 : 0;
     if (name == "neighbour_capacity") return nbr_cap_;
     if (name == "rebuild_chains") {
         uint32_t v[2];
@@ -1421,6 +1459,10 @@ void Engine::snapshot()
     HMD_CUDA(cudaMemcpyAsync(snap_vel_.p, vel_.p, vel_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(snap_img_.p, img_.p, img_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(snap_force_.p, force_.p, force_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    if (fp64()) {
+        if (!snap_force64_.p) snap_force64_.alloc(S_);
+        HMD_CUDA(cudaMemcpyAsync(snap_force64_.p, force64_.p, force64_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    }
     HMD_CUDA(cudaMemcpyAsync(snap_id_.p, id_.p, id_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(snap_rid_.p, rid_.p, rid_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(snap_st_.p, dst_.p, dst_.bytes(), cudaMemcpyDeviceToDevice, stream_));
@@ -1432,6 +1474,8 @@ void Engine::restore()
     HMD_CUDA(cudaMemcpyAsync(vel_.p, snap_vel_.p, vel_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(img_.p, snap_img_.p, img_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(force_.p, snap_force_.p, force_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    if (fp64())
+        HMD_CUDA(cudaMemcpyAsync(force64_.p, snap_force64_.p, force64_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(id_.p, snap_id_.p, id_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(rid_.p, snap_rid_.p, rid_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     HMD_CUDA(cudaMemcpyAsync(dst_.p, snap_st_.p, dst_.bytes(), cudaMemcpyDeviceToDevice, stream_));

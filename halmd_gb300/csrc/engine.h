@@ -57,6 +57,7 @@ struct SysHost {
     hmd_system_desc desc;
     SysParam P;
     std::vector<PairParam> pairs;
+    std::vector<PairParam64> pairs64;   // the same table in double (FP64 variant)
     uint32_t nbr_size = 0;   // list capacity estimate (from_binning.cpp:96-119)
     bool used = false;       // the table entry holds a system
 };
@@ -123,7 +124,9 @@ public:
     const SysHost& system(uint32_t s) const;
     uint32_t nsys() const { return (uint32_t)sys_.size(); }
     uint32_t slots() const { return S_; }
-    bool ds() const { return precision_ == HMD_PRECISION_DSFLOAT; }
+    // dsfloat storage (hi + lo words): the dsfloat engines and the FP64 variant
+    bool ds() const { return precision_ == HMD_PRECISION_DSFLOAT || precision_ == HMD_PRECISION_DOUBLE; }
+    bool fp64() const { return precision_ == HMD_PRECISION_DOUBLE; }
     void sync();
 
     std::string err;
@@ -192,6 +195,8 @@ private:
 
     DevBuf<float4> pos_, vel_, img_, force_, r0_, tpos_, tvel_, timg_;
     DevBuf<float4> fpos_;   // dsfloat engines: the force kernel's gather records
+    DevBuf<Force64> force64_, snap_force64_;   // FP64 variant: forces in double
+    DevBuf<PairParam64> dpair64_;
     DevBuf<float> en_pot_, stress_;
     DevBuf<uint32_t> id_, rid_, nbr_, nbr_count_, cell_, cell_count_, cell_sys_, chunk_sys_, tid_;
     DevBuf<uint32_t> key0_, key1_, val0_, val1_, hist_, status_, done_, any_rebuild_, rb_;
@@ -222,6 +227,7 @@ private:
     static constexpr uint64_t SEGMENT_STEPS = 5000;
     cudaGraphExec_t g_chunk_ = nullptr, g_short_ = nullptr, g_one_ = nullptr, g_one_aux_ = nullptr;
     bool fuse_ = true;                           // captured chunks fuse finalize k with integrate k+1
+    bool float_cutoff_ = false;                  // FP64 variant: float cut-off decision (set_option)
     uint64_t step_kernels_ = 0;                  // kernels of the step graphs launched (rebuild chains not counted)
 };
 

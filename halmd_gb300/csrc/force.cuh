@@ -21,11 +21,11 @@ namespace hmd {
 #define HMD_FORCE_MINB 7
 #endif
 // Resident blocks for the kernels of dsfloat engines, whose gathers carry
-// the lo words (32 bytes a neighbour): at LJ-1M 225 us with 5 blocks (96
-// registers, no spills) against 238 us with 6 and 245 us with 7 (spills);
-// at KA-64k 38.4 us against 42.4 and 43.1 us.
+// the lo words (16-byte records, hmd_device.cuh fpos_encode): at LJ-1M
+// 215 us with 5 blocks against 214 us with 6 and 216 us with 7; at KA-64k
+// 40.5 us against 43.5 and 41.8 us.
 #ifndef HMD_FORCE_MINB_DS
-#define HMD_FORCE_MINB_DS 6
+#define HMD_FORCE_MINB_DS 5
 #endif
 // 1: load a lane's next list block one iteration ahead (force_blocks2)
 #ifndef HMD_FORCE_PREFETCH
@@ -460,9 +460,15 @@ __device__ __forceinline__ void near_pair2(const PP2& p, const SysParam& P, floa
     const float2 dz = WRAP ? min_image2(sz, P.L[2], P.Linv[2]) : sz;
     const float2 px = mul2(dx, dx), py = mul2(dy, dy), pz = mul2(dz, dz);
     const float2 pxy = add2(px, py);
-    const float2 rr = add2(pxy, pz);   // == rr_exact(dx, dy, dz) per lane
-    const bool ka = va && rr.x < p.rr_cut.x;
-    const bool kb = vb && rr.y < p.rr_cut.y;
+    const float2 rr = add2(pxy, pz);
+    // the cut-off test of the list criterion, in scalar arithmetic (add2 and
+    // mul2 may come out contracted); a near pair can only reach r_c when
+    // NEAR_SIGMA sigma + skin does
+    bool ka = va, kb = vb;
+    if (!P.near_in_range) {
+        ka = ka && rr_exact(dx.x, dy.x, dz.x) < p.rr_cut.x;
+        kb = kb && rr_exact(dx.y, dy.y, dz.y) < p.rr_cut.y;
+    }
     float2 dxl = bc2(0.0f), dyl = bc2(0.0f), dzl = bc2(0.0f);
     if (!EXACT) {
         dxl = diff_err2(ri.x, ra.x, rb.x, sx);
@@ -513,8 +519,10 @@ __device__ __forceinline__ void far_pair2(const PP2& p, const SysParam& P, float
     float2 dy = WRAP ? min_image2(sy, P.L[1], P.Linv[1]) : sy;
     float2 dz = WRAP ? min_image2(sz, P.L[2], P.Linv[2]) : sz;
     float2 rr = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
-    const bool ka = va && rr.x < p.rr_cut.x;
-    const bool kb = vb && rr.y < p.rr_cut.y;
+    // the cut-off test of the list criterion, in scalar arithmetic (add2 and
+    // mul2 may come out contracted, and a pair at r_c^2 would flip)
+    const bool ka = va && rr_exact(dx.x, dy.x, dz.x) < p.rr_cut.x;
+    const bool kb = vb && rr_exact(dx.y, dy.y, dz.y) < p.rr_cut.y;
     if (WRAP || LO) {
         // the separation's residual e: across the box the rounding error of
         // ri - rj, for dsfloat positions the difference of the lo words
@@ -873,8 +881,9 @@ __device__ __forceinline__ void pot_pair2(const PairParam& pa, const PairParam& 
     float2 dy = WRAP ? min_image2(sy, P.L[1], P.Linv[1]) : sy;
     float2 dz = WRAP ? min_image2(sz, P.L[2], P.Linv[2]) : sz;
     float2 rr = rr_exact2(dx, dy, dz);
-    const bool ka = va && rr.x < pa.rr_cut;
-    const bool kb = vb && rr.y < pb.rr_cut;
+    // the cut-off test in scalar arithmetic (far_pair2)
+    const bool ka = va && rr_exact(dx.x, dy.x, dz.x) < pa.rr_cut;
+    const bool kb = vb && rr_exact(dx.y, dy.y, dz.y) < pb.rr_cut;
     const bool smooth = P.trunc == TRUNC_SMOOTH_R4;   // block-uniform
     float2 rrl = bc2(0.0f);
     if (WRAP || NEAR || LO || smooth) {

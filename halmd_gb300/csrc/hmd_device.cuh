@@ -81,6 +81,16 @@ struct PairParam {
     float pad;
 };
 
+// a force in double (FP64 variant), 32-byte aligned
+struct alignas(32) Force64 {
+    double x, y, z, w;
+};
+
+// the pair parameters in double for the FP64 variant (kernels_fp64.cu)
+struct PairParam64 {
+    double eps4, c48, sigma2, rr_cut, en_cut, r_cut, f_cut, pad;
+};
+
 // pairs closer than NEAR_SIGMA sigma at list build time are evaluated with
 // the compensated arithmetic; the rest (|F| below ~2 eps / sigma even after
 // closing in by the skin) in plain FP32
@@ -112,12 +122,15 @@ struct SysParam {
     float exact_min;           // |coordinate| from which near-pair differences are exact (k_force)
     float descent_step;        // INTEG_DESCENT: move = descent_step * F ...
     float descent_max;         // ... capped at this length per particle and step
+    uint32_t near_in_range;    // 1: a near pair (NEAR_SIGMA sigma + skin apart at most) is always inside r_c
     float lo_scale;            // unit s of the lo-word codes of Dev::fpos (a power of two)
     float lo_inv_scale;        // 1 / s
     uint32_t lo_exp_bits;      // bits of the float 2^23 s (a code field ORed in gives (2^23 + field) s)
     float lo_bias;             // (2^23 + 512) s
     uint32_t pot;              // pair potential (Pot)
     uint32_t interval;         // INTEG_BOLTZMANN: steps between velocity draws
+    double dt64;               // the time step in double (FP64 variant)
+    double rri_smooth64;       // h^-2 in double (FP64 variant)
     // INTEG_HOOVER (verlet_nvt_hoover.cpp:58-84): chain masses, dim N T, T, dt
     double nhc_mass[2];
     double nhc_target2;
@@ -154,6 +167,8 @@ struct Dev {
     float4* force;             // [S]
     float4* r0;                // [S] hi positions at the last list build
     float4* fpos;              // [S] dsfloat engines: the force kernel's gather records (fpos_encode)
+    Force64* force64;          // [S] FP64 variant: forces in double
+    const PairParam64* pair64; // FP64 variant: the pair table in double
     float* en_pot;             // [S]
     float* stress;             // [6S]
     uint32_t* id;              // [S] tag of the particle within its system
@@ -176,6 +191,8 @@ struct Dev {
     const uint32_t* chunk_sys; // [S / CHUNK]
     uint32_t S, nsys;
     uint32_t ds;               // 1: dsfloat positions and velocities (lo words in use)
+    uint32_t fp64;             // 1: the FP64 variant (kernels_fp64.cu) runs the step
+    uint32_t float_cutoff;     // FP64 variant: pair set by the float list criterion on the hi words
     // extents the launch grids cover (fixed layout: everything; capacity
     // mode: the slots, sort tiles and cells below the high-water mark of the
     // systems present, rounded up to a power of two)
@@ -283,28 +300,15 @@ __device__ __forceinline__ float rr_exact(float dx, float dy, float dz)
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
-// add and multiply with an explicit rounding modifier in PTX, so that no
-// compiler pass contracts a product and a sum into one FMA: the list
-// criterion and the cut-off test then round exactly as the oracle's float
-// restatement (a squared distance contracted to fma(z, z, x^2 + y^2) can
-// land on the other side of r_c^2)
-__device__ __forceinline__ float2 add2(float2 a, float2 b)
-{
-    unsigned long long c;
-    asm("add.rn.f32x2 %0, %1, %2;"
-        : "=l"(c) : "l"(*reinterpret_cast<const unsigned long long*>(&a)),
-          "l"(*reinterpret_cast<const unsigned long long*>(&b)));
-    return *reinterpret_cast<const float2*>(&c);
-}
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return add2(a, make_float2(-b.x, -b.y)); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b)
-{
-    unsigned long long c;
-    asm("mul.rn.f32x2 %0, %1, %2;"
-        : "=l"(c) : "l"(*reinterpret_cast<const unsigned long long*>(&a)),
-          "l"(*reinterpret_cast<const unsigned long long*>(&b)));
-    return *reinterpret_cast<const float2*>(&c);
-}
+// Products and sums of register pairs can come out contracted: on this GPU
+// a squared distance written as (x^2 + y^2) + z^2 with f32x2 multiply and
+// add (builtins or PTX with an explicit rounding modifier alike) measured
+// as fma(z, z, x^2 + y^2) for some inputs.  Decisions that must round as
+// the oracle's float restatement (the cut-off test) therefore use the
+// scalar __fmul_rn / __fadd_rn form, rr_exact.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 

@@ -27,6 +27,10 @@ void launch_finalize(const Dev& d, bool ds, cudaStream_t st);
 // finalize of step k fused with the integrate of step k + 1 (captured chunks)
 void launch_finalize_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, cudaStream_t st);
 void launch_thermo(const Dev& d, cudaStream_t st);
+// the FP64 variant of the step (kernels_fp64.cu)
+void launch_force64(const Dev& d, bool aux, cudaStream_t st);
+void launch_integrate64(const Dev& d, bool fin, cudaGraphConditionalHandle h, bool use_handle, cudaStream_t st);
+void launch_finalize64(const Dev& d, cudaStream_t st);
 // the force kernel's gather records of every real slot (dsfloat engines)
 void launch_pack_fpos(const Dev& d, cudaStream_t st);
 // largest |min_image(r - r0)|^2 of system s as float bits into *out

@@ -308,6 +308,7 @@ static_assert(HMD_STEP_THREADS >= 64 && HMD_STEP_THREADS <= 256 && HMD_STEP_THRE
 
 void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool use_handle, cudaStream_t st)
 {
+    if (d.fp64) return launch_integrate64(d, false, h, use_handle, st);
     constexpr unsigned T = HMD_STEP_THREADS;
     const unsigned grid = d.S_grid / T;
     if (ds) k_integrate<true, false><<<grid, T, 0, st>>>(d, h, use_handle ? 1 : 0);
@@ -316,6 +317,7 @@ void launch_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, bool 
 
 void launch_finalize_integrate(const Dev& d, bool ds, cudaGraphConditionalHandle h, cudaStream_t st)
 {
+    if (d.fp64) return launch_integrate64(d, true, h, true, st);
     constexpr unsigned T = HMD_STEP_THREADS;
     const unsigned grid = d.S_grid / T;
     if (ds) k_integrate<true, true><<<grid, T, 0, st>>>(d, h, 1);
@@ -332,6 +334,7 @@ void launch_mark(const Dev& d, bool rebuild_all, cudaStream_t st)
 // kernel (engines whose systems change after commit)
 void launch_force(const Dev& d, bool aux, cudaStream_t st)
 {
+    if (d.fp64) return launch_force64(d, aux, st);
     if (d.force_kinds == 0u) {
         launch_force_kind<FK_GENERIC>(d, aux, st);
         return;
@@ -349,6 +352,7 @@ void launch_force(const Dev& d, bool aux, cudaStream_t st)
 // thermostat, and the velocities are rescaled or shifted
 void launch_finalize(const Dev& d, bool ds, cudaStream_t st)
 {
+    if (d.fp64) return launch_finalize64(d, st);
     const unsigned grid = d.S_grid / 256;
     const bool thermo = (d.integ_kinds & ((1u << INTEG_HOOVER) | (1u << INTEG_BOLTZMANN))) != 0u;
     if (!thermo) {

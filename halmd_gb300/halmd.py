@@ -36,7 +36,13 @@ becomes the first positional argument.  The modules mirror:
 All modules of one script share one engine, committed when the simulation
 first needs the device (the first `sampler.run` or read of device data).
 Several `particle` instances become independent systems of that engine and
-advance together.  `reset()` starts a new script.
+advance together.  Instances coupled by pair forces, as
+`forces.pair{particle = {p1, p2}, ...}` wires them (pair_trunc.hpp:60-61,
+154-162; test/integration/modularity/two_particles.lua), become one system
+whose particles are the instances' in order: every ordered pair of the
+coupled instances needs its force, all with one potential, box, neighbour
+configuration and integrator, which is the same physics as one instance of
+several species.  `reset()` starts a new script.
 """
 import numpy as np
 
@@ -54,6 +60,7 @@ class _Script:
 
     def __init__(self):
         self.particles = []
+        self.forces = []             # (p1, p2): forces on p1 from p2
         self.engine = None
         self.observers = []          # (every, fn) called after steps that are multiples of every
         self.blocking = []
@@ -70,22 +77,106 @@ class _Script:
         precisions = {p.precision for p in self.particles}
         if len(precisions) != 1:
             raise ValueError("all particle instances of a script share one precision")
+        groups = self.groups()
         eng = Engine("dsfloat" if precisions.pop() == "double-single" else "float")
-        for p in self.particles:
-            p._index = eng.add_system(p._desc())
+        for g in groups:
+            index = eng.add_system(g[0]._desc(sum(p.nparticle for p in g)))
+            offset = 0
+            for p in g:
+                p._index, p._offset, p._group = index, offset, g
+                offset += p.nparticle
         eng.commit()
-        for p in self.particles:
+        for g in groups:
             for name in ("species", "mass", "position", "image", "velocity"):
-                if name in p._pending:
-                    eng.set(name, p._pending[name], p._index)
-            p._pending.clear()
-            for call in p._setup:
-                call(eng, p._index)
-            p._setup.clear()
+                if all(name not in p._pending for p in g):
+                    continue
+                if len(g) == 1:
+                    eng.set(name, g[0]._pending[name], g[0]._index)
+                    continue
+                if name == "position" and not all(name in p._pending for p in g):
+                    raise ValueError("positions of only some of the coupled particle instances are set")
+                parts = [p._pending[name] if name in p._pending else _default(name, p.nparticle) for p in g]
+                eng.set(name, np.concatenate([np.asarray(x) for x in parts]), g[0]._index)
+            for p in g:
+                p._pending.clear()
+                for call in p._setup:
+                    call(eng, p._index)
+                p._setup.clear()
         self.engine = eng
         for b in self.blocking:
             b._attach()
         return eng
+
+
+    def groups(self):
+        """The particle instances as engine systems: instances coupled by pair
+        forces form one group (checked to be one system of several species)."""
+        parent = {id(p): p for p in self.particles}
+
+        def root(p):
+            while parent[id(p)] is not p:
+                p = parent[id(p)]
+            return p
+
+        for a, b in self.forces:
+            ra, rb = root(a), root(b)
+            if ra is not rb:
+                parent[id(rb)] = ra
+        groups, seen = [], {}
+        for p in self.particles:
+            r = root(p)
+            if id(r) not in seen:
+                seen[id(r)] = []
+                groups.append(seen[id(r)])
+            seen[id(r)].append(p)
+        wired = {(id(a), id(b)) for a, b in self.forces}
+        for g in groups:
+            if len(g) == 1:
+                continue
+            missing = [(a.label, b.label) for a in g for b in g if (id(a), id(b)) not in wired]
+            if missing:
+                raise ValueError("coupled particle instances need a pair force for every ordered pair; missing %s"
+                                 % missing)
+            first = g[0]
+            for p in g[1:]:
+                for what in ("_box", "_potential", "_integrator"):
+                    if getattr(p, what) is None or getattr(first, what) is None:
+                        raise RuntimeError("particle '%s' needs a box, a pair force and an integrator" % p.label)
+                if p._potential is not first._potential and _potential_key(p._potential) != _potential_key(
+                        first._potential):
+                    raise ValueError("coupled particle instances must share one potential")
+                if list(p._box.length) != list(first._box.length):
+                    raise ValueError("coupled particle instances must share one box")
+                if (p._neighbour or {}) != (first._neighbour or {}):
+                    raise ValueError("coupled particle instances must share one neighbour configuration")
+                if _integrator_key(p._integrator) != _integrator_key(first._integrator):
+                    raise ValueError("coupled particle instances must use the same integrator")
+                if p.nspecies != first.nspecies:
+                    raise ValueError("coupled particle instances must declare the same number of species")
+                if p._setup:
+                    raise ValueError("set-up modules (lattice, boltzmann) act on whole systems: set the "
+                                     "positions and velocities of coupled particle instances directly")
+            if first._setup:
+                raise ValueError("set-up modules (lattice, boltzmann) act on whole systems: set the "
+                                 "positions and velocities of coupled particle instances directly")
+        return groups
+
+
+def _default(name, n):
+    if name == "species":
+        return np.zeros(n, dtype=np.uint32)
+    if name == "mass":
+        return np.ones(n)
+    return np.zeros((n, 3))
+
+
+def _potential_key(pot):
+    return (pot.potential, np.asarray(pot.epsilon).tolist(), np.asarray(pot.sigma).tolist(), pot.kind, pot.cutoff,
+            pot.h, sorted(pot.params.items()))
+
+
+def _integrator_key(integ):
+    return tuple(sorted((k, v) for k, v in vars(integ).items() if k != "particle"))
 
 
 _script = _Script()
@@ -162,22 +253,31 @@ class particle:
         self._pending = {}
         self._setup = []       # set-up calls (lattice, Boltzmann) waiting for the engine
         self._index = None
+        self._offset = 0       # first particle of this instance in its engine system
+        self._group = [self]   # the instances that share the system (coupled by pair forces)
         self._box = self._potential = self._neighbour = self._integrator = None
         _script.particles.append(self)
 
     def set(self, name, value):
         value = np.asarray(value)
-        if _script.committed():
+        if not _script.committed():
+            self._pending[name] = value
+        elif len(self._group) == 1:
             _script.engine.set(name, value, self._index)
         else:
-            self._pending[name] = value
+            full = np.array(_script.engine.get(name, self._index), copy=True)
+            full[self._offset:self._offset + self.nparticle] = value
+            _script.engine.set(name, full, self._index)
 
     def get(self, name):
         if not _script.committed() and name in self._pending:
             return self._pending[name]
-        return _script.commit().get(name, self._index)
+        full = _script.commit().get(name, self._index)
+        if len(self._group) == 1:
+            return full
+        return full[self._offset:self._offset + self.nparticle]
 
-    def _desc(self):
+    def _desc(self, nparticle=None):
         if self._box is None or self._potential is None or self._integrator is None:
             raise RuntimeError("particle '%s' needs a box, a pair force and an integrator" % self.label)
         pot, nb, integ = self._potential, self._neighbour or {}, self._integrator
@@ -194,7 +294,7 @@ class particle:
             kw.update(temperature=integ.temperature, collision_rate=integ.rate, seed=integ.seed)
         if integ.kind == "hoover":
             kw.update(temperature=integ.temperature, resonance_frequency=integ.resonance_frequency)
-        return system_desc(self.nparticle, self._box.length, nspecies=self.nspecies, **kw)
+        return system_desc(nparticle or self.nparticle, self._box.length, nspecies=self.nspecies, **kw)
 
 
 class _Potential:
@@ -284,12 +384,17 @@ def pair(args=None, **kw):
     force over all pairs (pair_full; forces/pair.lua.in:78-83)."""
     a = _args(args, kw)
     pot = a["potential"]
-    parts = a["particle"] if isinstance(a["particle"], (list, tuple)) else [a["particle"]]
-    if len(parts) != 1:
-        raise ValueError("forces between two particle instances are not supported")
-    p = parts[0]
-    p._box, p._potential, p._neighbour = a["box"], pot, dict(a.get("neighbour") or {})
-    return _Namespace(particle=p, potential=pot)
+    parts = list(a["particle"]) if isinstance(a["particle"], (list, tuple)) else [a["particle"]]
+    if len(parts) == 1:
+        parts = parts * 2
+    if len(parts) != 2:
+        raise ValueError("forces.pair: one particle instance or a pair {p1, p2} expected")
+    p1, p2 = parts
+    for p in (p1, p2):
+        if p._potential is None:
+            p._box, p._potential, p._neighbour = a["box"], pot, dict(a.get("neighbour") or {})
+    _script.forces.append((p1, p2))
+    return _Namespace(particle=p1 if p1 is p2 else (p1, p2), potential=pot)
 
 
 class _Integrator:
@@ -402,7 +507,17 @@ class thermodynamics:
 
     def _sums(self):
         eng = _script.commit()
-        return eng.thermo(self.group._index)
+        g = self.group
+        if len(g._group) == 1:
+            return eng.thermo(g._index)
+        # one of several coupled instances: FP64 sums of its particles on the
+        # host, from the per-particle arrays of the last sampled step
+        v, m = g.get("velocity"), np.asarray(g.get("mass"), dtype=np.float64)
+        stress = g.get("stress_pot")
+        mv = m[:, None] * v
+        return {"mv2": float(np.sum(mv * v)), "momentum": mv.sum(axis=0), "mass": float(m.sum()),
+                "epot": float(np.sum(g.get("potential_energy"))),
+                "virial": float(np.sum(stress[:, 0] + stress[:, 1] + stress[:, 2]))}
 
     def particle_number(self):
         return self.group.nparticle
@@ -544,15 +659,17 @@ class blocking_scheme:
         self._dyn = Dynamics(eng, self.max_lag, self.every * dt, block_size=self.size, shift=self.shift,
                              separation=self.separation, s=self.group._index)
         for c in self.correlations:
+            # tags of the instance within its engine system (coupled instances share one)
+            first, last = c.first + c.group._offset, c.last + c.group._offset
             if isinstance(c, mean_quartic_displacement):
-                self._tcf.append(self._dyn.add_mqd(c.first, c.last))
+                self._tcf.append(self._dyn.add_mqd(first, last))
             elif isinstance(c, velocity_autocorrelation):
-                self._tcf.append(self._dyn.add_vacf(c.first, c.last))
+                self._tcf.append(self._dyn.add_vacf(first, last))
             elif isinstance(c, mean_square_displacement):
-                self._tcf.append(self._dyn.add_msd(c.first, c.last))
+                self._tcf.append(self._dyn.add_msd(first, last))
             else:
                 self._tcf.append(self._dyn.add_isf(c.wavenumber, tolerance=c.tolerance, max_count=c.max_count,
-                                                   first=c.first, last=c.last, norm=c.norm))
+                                                   first=first, last=last, norm=c.norm))
         self._dyn.sample()
 
     def _stops(self, step0, steps):

@@ -39,6 +39,12 @@ extern "C" {
 
 #define HMD_PRECISION_FLOAT 0     /* particle_3_float   (particle.lua.in:46-57) */
 #define HMD_PRECISION_DSFLOAT 1   /* particle_3_dsfloat (default precision) */
+/* FP64 arithmetic in force, integrate and finalize (no counterpart among the
+ * reference's GPU particle types; the precision of its host backend, kept
+ * here as the drift and force reference run from the same start): storage
+ * as dsfloat (hi + lo words, 48 significant bits), forces in double;
+ * Lennard-Jones potentials with any truncation and velocity Verlet only */
+#define HMD_PRECISION_DOUBLE 2
 
 #define HMD_TRUNC_SHARP 0          /* truncations/sharp.hpp */
 #define HMD_TRUNC_SHIFTED 1        /* truncations/shifted.hpp (truncate.lua.in:289 default) */
@@ -175,6 +181,9 @@ HMD_API int hmd_engine_progress(hmd_engine* engine, uint64_t* step, uint32_t* st
  *                   reads list_block / force_lanes entries with one load (2 or 4 lanes: 4 or 8)
  *   "fuse_steps"    1 (default): captured chunks run the finalize of step k and the integrate of
  *                   step k+1 as one kernel; 0: separate kernels (same results)
+ *   "float_cutoff"  HMD_PRECISION_DOUBLE engines: 1 takes the pair set of the float list
+ *                   criterion on the hi words (the other engines' cut-off test), 0 (default)
+ *                   r^2 < r_c^2 in double
  *   "step_kernels"       (get only) kernels of the captured step graphs launched so far
  *                        (rebuild chains not included: rebuild_chains x hmd_system_info.rebuild_kernels)
  */

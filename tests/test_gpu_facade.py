@@ -160,3 +160,50 @@ def test_non_finite_positions_are_rejected_unchanged():
     out = np.empty_like(before)
     assert eng.get("position", out=out) is out and np.array_equal(out, before)
     eng.close()
+
+
+def _ka_two_instance_script(r, v, sp, L, coupled):
+    """The KA mixture either as one instance of two species or as two
+    instances A and B wired by forces for every ordered pair
+    (test/integration/modularity/two_particles.lua)."""
+    halmd.reset()
+    box = halmd.mdsim.box(length=[L, L, L])
+    pot = halmd.mdsim.potentials.pair.lennard_jones(epsilon=[[1, 1.5], [1.5, 0.5]], sigma=[[1, 0.8], [0.8, 0.88]])
+    pot = pot.truncate("smooth_r4", cutoff=2.5, h=0.005)
+    if not coupled:
+        p = halmd.mdsim.particle(particles=r.shape[0], species=2)
+        p.data["species"], p.data["position"], p.data["velocity"] = sp, r, v
+        halmd.mdsim.forces.pair(box=box, particle=p, potential=pot, neighbour={"skin": 0.3})
+        halmd.mdsim.integrators.verlet(box=box, particle=p, timestep=0.002)
+        return [p], box
+    parts = []
+    for label, sel in (("A", sp == 0), ("B", sp == 1)):
+        p = halmd.mdsim.particle(particles=int(sel.sum()), species=2, label=label)
+        p.data["species"], p.data["position"], p.data["velocity"] = sp[sel], r[sel], v[sel]
+        parts.append(p)
+    for p1 in parts:
+        for p2 in parts:
+            halmd.mdsim.forces.pair(box=box, particle=[p1, p2], potential=pot, neighbour={"skin": 0.3})
+    for p in parts:
+        halmd.mdsim.integrators.verlet(box=box, particle=p, timestep=0.002)
+    return parts, box
+
+
+def test_two_coupled_instances_equal_one_instance_of_two_species():
+    from _systems import ka_system
+    r, v, sp, L = ka_system(ncell=6)
+    order = np.argsort(sp, kind="stable")          # A particles first, then B
+    r, v, sp = r[order], v[order], sp[order]
+    (one,), box = _ka_two_instance_script(r, v, sp, L, coupled=False)
+    t1 = halmd.observables.thermodynamics(box=box, group=one)
+    halmd.observables.sampler.run(150)
+    ref_r, ref_v, ref_epot = one.data["position"], one.data["velocity"], t1.potential_energy() * r.shape[0]
+    parts, box = _ka_two_instance_script(r, v, sp, L, coupled=True)
+    thermos = [halmd.observables.thermodynamics(box=box, group=p) for p in parts]
+    halmd.observables.sampler.run(150)
+    got_r = np.concatenate([p.data["position"] for p in parts])
+    got_v = np.concatenate([p.data["velocity"] for p in parts])
+    assert np.array_equal(got_r, ref_r) and np.array_equal(got_v, ref_v)
+    epot = sum(t.potential_energy() * p.nparticle for t, p in zip(thermos, parts))
+    assert abs(epot - ref_epot) < 1e-9 * abs(ref_epot)
+    halmd.reset()

@@ -107,3 +107,46 @@ def test_other_potentials_defaults_and_errors(halmd):
         halmd.mdsim.potentials.pair.morse()                                  # r_min has no default
     with pytest.raises(ValueError):
         halmd.mdsim.potentials.pair.mie(index_repulsion=12)                  # both indices are required
+
+
+def two_instances(halmd, wire, na=800, nb=200, L=9.4):
+    """The KA mixture as two particle instances A and B (test/integration/
+    modularity/two_particles.lua): one box, one potential, forces for the
+    ordered pairs in `wire`, a Verlet integrator each."""
+    box = halmd.mdsim.box(length=[L, L, L])
+    pa = halmd.mdsim.particle(particles=na, species=2, label="A")
+    pb = halmd.mdsim.particle(particles=nb, species=2, label="B")
+    pot = halmd.mdsim.potentials.pair.lennard_jones(epsilon=[[1, 1.5], [1.5, 0.5]], sigma=[[1, 0.8], [0.8, 0.88]])
+    pot = pot.truncate("smooth_r4", cutoff=2.5, h=0.005)
+    inst = {"A": pa, "B": pb}
+    for l1, l2 in wire:
+        halmd.mdsim.forces.pair(box=box, particle=[inst[l1], inst[l2]], potential=pot, neighbour={"skin": 0.3})
+    for p in (pa, pb):
+        halmd.mdsim.integrators.verlet(box=box, particle=p, timestep=0.002)
+    return pa, pb
+
+
+def test_coupled_instances_form_one_system(halmd):
+    pa, pb = two_instances(halmd, [("A", "A"), ("A", "B"), ("B", "A"), ("B", "B")])
+    groups = halmd._script.groups()
+    assert len(groups) == 1 and groups[0] == [pa, pb]
+    d = pa._desc(sum(p.nparticle for p in groups[0]))
+    assert d.nparticle == 1000 and d.nspecies == 2 and d.truncation == _lib.TRUNCATION["smooth_r4"]
+
+
+def test_coupled_instances_need_every_ordered_pair(halmd):
+    two_instances(halmd, [("A", "A"), ("A", "B"), ("B", "B")])
+    with pytest.raises(ValueError, match="every ordered pair"):
+        halmd._script.groups()
+
+
+def test_coupled_instances_share_the_integrator(halmd):
+    pa, pb = two_instances(halmd, [("A", "A"), ("A", "B"), ("B", "A"), ("B", "B")])
+    halmd.mdsim.integrators.verlet(particle=pb, timestep=0.001)
+    with pytest.raises(ValueError, match="same integrator"):
+        halmd._script.groups()
+
+
+def test_uncoupled_instances_stay_separate_systems(halmd):
+    pa, pb = two_instances(halmd, [("A", "A"), ("B", "B")])
+    assert halmd._script.groups() == [[pa], [pb]]
