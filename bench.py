@@ -611,17 +611,20 @@ def run_serve(args):
     srv = Server(budget_fraction=0.8, max_slots=args.serve_max_slots, max_jobs=1024, neighbour_capacity=288,
                  chunk=args.md_steps)
     clocks = ClockSampler(0)
-    st = srv.run(jobs, realtime=True)
+    limit = args.serve_time_limit or None
+    st = srv.run(jobs, realtime=True, time_limit=limit)
     clk = clocks.stop()
-    lat = pct(gather_latency(jobs))
+    done_jobs = [j for j in jobs if j.completed is not None]
+    lat = pct(gather_latency(done_jobs)) if done_jobs else {"p50": None, "p99": None, "mean": None}
     budget = srv.budget
     srv.close()
-    work, makespan = combine(work, st["makespan"], device="cuda")
+    work, makespan = combine(st["work"], st["makespan"], device="cuda")
     chunks = int(combine(st["chunks"], 0.0, device="cuda")[0])
     fifo_jobs = my_jobs()
-    fst = run_fifo(fifo_jobs)
-    flat = pct(gather_latency(fifo_jobs))
-    fmakespan = combine(0.0, fst["makespan"], device="cuda")[1]
+    fst = run_fifo(fifo_jobs, time_limit=limit)
+    fdone = [j for j in fifo_jobs if j.completed is not None]
+    flat = pct(gather_latency(fdone)) if fdone else {"p50": None, "p99": None, "mean": None}
+    fwork, fmakespan = combine(fst["work"], fst["makespan"], device="cuda")
     njobs = int(combine(len(jobs), 0.0, device="cuda")[0])
     if dist is not None:
         dist.destroy_process_group()
@@ -636,12 +639,16 @@ def run_serve(args):
             "config": {"workload": "SERVE", "jobs": njobs, "arrival_rate_per_s": 50,
                        "parallelism": "jobs bin-packed over %d GPUs" % world if world > 1 else "single",
                        "steps_scale": args.serve_steps_scale, "particle_steps": work, "chunk_md_steps": args.md_steps,
-                       "hbm_budget": budget},
-            "latency_s": {"p50": lat["p50"], "p99": lat["p99"], "mean": lat["mean"]},
+                       "hbm_budget": budget, "time_limit_s": limit},
+            "latency_s": {"p50": lat["p50"], "p99": lat["p99"], "mean": lat["mean"],
+                          "over": "jobs completed%s" % (" within the time limit" if limit else "")},
+            "completed_jobs": st["completed"] if world == 1 else None,
             "makespan_s": st["makespan"],
-            "fifo_plain_path": {"value": work / fst["makespan"], "unit": "particle-steps/s",
-                                "latency_s": flat, "makespan_s": fst["makespan"]},
-            "throughput_ratio_vs_fifo": fst["makespan"] / st["makespan"], "clocks": clk}
+            "fifo_plain_path": {"value": fwork / fst["makespan"], "unit": "particle-steps/s",
+                                "latency_s": flat, "makespan_s": fst["makespan"],
+                                "completed_jobs": fst["completed"] if world == 1 else None,
+                                "particle_steps": fwork},
+            "throughput_ratio_vs_fifo": (work / st["makespan"]) / (fwork / fst["makespan"]), "clocks": clk}
     print(json.dumps(line))
 
 
@@ -779,6 +786,8 @@ def main():
     ap.add_argument("--serve-jobs", type=int, default=200)
     ap.add_argument("--serve-steps-scale", type=float, default=0.1)
     ap.add_argument("--serve-max-slots", type=int, default=1 << 24)
+    ap.add_argument("--serve-time-limit", type=float, default=0.0,
+                    help="SERVE: stop both runs after this many seconds (a prefix of the stream; 0: run to the end)")
     args = ap.parse_args()
     if args.workload == "serve":
         if args.impl == "reference":

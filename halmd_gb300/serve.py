@@ -123,15 +123,19 @@ class Server:
             self.done.append(job)
         return len(finished)
 
-    def run(self, jobs, clock=time.perf_counter, realtime=True):
+    def run(self, jobs, clock=time.perf_counter, realtime=True, time_limit=None):
         """Serve `jobs` (arrival times in seconds from the start).  With
         realtime=False arrivals are released as soon as the previous ones are
-        admitted (throughput mode)."""
+        admitted (throughput mode).  With a time_limit the run stops after
+        the chunk that crosses it; `work` counts the particle-steps done by
+        then (finished jobs and the steps of the running ones)."""
         pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
         t0 = clock()
         chunks = 0
         while pending or self.queue or self.running:
             now = clock() - t0
+            if time_limit is not None and now >= time_limit:
+                break
             while pending and (pending[0].arrival <= now or not realtime):
                 self.submit(pending.popleft())
             self._admit(now)
@@ -143,7 +147,12 @@ class Server:
                 time.sleep(max(0.0, min(0.01, pending[0].arrival - (clock() - t0))))
             elif self.queue:
                 raise RuntimeError("job %d does not fit the reserved capacity" % self.queue[0].jid)
-        return dict(makespan=clock() - t0, chunks=chunks)
+        makespan = clock() - t0
+        work = sum(j.work for j in self.done)
+        if self.running:
+            step, _ = self.engine.progress(self.table)
+            work += sum(job.n * int(step[k]) for k, job in self.running.items())
+        return dict(makespan=makespan, chunks=chunks, work=work, completed=len(self.done))
 
 
 def latency_stats(jobs):
@@ -151,12 +160,17 @@ def latency_stats(jobs):
     return dict(p50=float(np.percentile(lat, 50)), p99=float(np.percentile(lat, 99)), mean=float(lat.mean()))
 
 
-def run_fifo(jobs, precision="dsfloat", clock=time.perf_counter, force_lanes=None):
+def run_fifo(jobs, precision="dsfloat", clock=time.perf_counter, force_lanes=None, time_limit=None, chunk=1000):
     """The plain path: one engine per job, jobs one after another in arrival
-    order (a job starts at max(arrival, previous completion))."""
+    order (a job starts at max(arrival, previous completion)).  With a
+    time_limit a job runs in chunks of `chunk` steps and the run stops after
+    the chunk that crosses the limit; `work` counts the particle-steps done."""
     t0 = clock()
+    work, completed = 0, 0
     for job in sorted(jobs, key=lambda j: j.arrival):
         now = clock() - t0
+        if time_limit is not None and now >= time_limit:
+            break
         if job.arrival > now:
             time.sleep(job.arrival - now)
         job.admitted = clock() - t0
@@ -168,9 +182,21 @@ def run_fifo(jobs, precision="dsfloat", clock=time.perf_counter, force_lanes=Non
         eng.set("species", job.species)
         eng.set("position", job.position)
         eng.set("velocity", job.velocity)
-        eng.step(job.steps)
-        job.result = dict(position=eng.get("position"), velocity=eng.get("velocity"), image=eng.get("image"),
-                          step=int(eng.info().step))
+        if time_limit is None:
+            eng.step(job.steps)
+            done = job.steps
+        else:
+            done = 0
+            while done < job.steps and clock() - t0 < time_limit:
+                k = min(chunk, job.steps - done)
+                eng.step(k)
+                eng.info()                       # the chunk has run
+                done += k
+        work += job.n * done
+        if done == job.steps:
+            job.result = dict(position=eng.get("position"), velocity=eng.get("velocity"), image=eng.get("image"),
+                              step=int(eng.info().step))
+            job.completed = clock() - t0
+            completed += 1
         eng.close()
-        job.completed = clock() - t0
-    return dict(makespan=clock() - t0)
+    return dict(makespan=clock() - t0, work=work, completed=completed)

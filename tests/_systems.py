@@ -61,3 +61,21 @@ def state_forces(eng, species, pot, s=0, state=True, aux=True):
     pos4 = eng.get_raw("position_hi", s)[eng.get("reverse_id", s)]
     r = eng.get("position", s) if state else pos4[:, :3].astype(np.float64)
     return oracle.forces(r, species, Lf.astype(np.float64), pot, pos4=pos4, Lf=Lf, aux=aux)
+
+
+def energy_drift(eng, steps, every, s=0):
+    """Energy E = K + U sampled every `every` steps over `steps` steps:
+    returns (drift |E| per 1e5 steps from a linear fit, its standard error,
+    max |E(t) - E(0)| / |E(0)|)."""
+    t, e = [], []
+    for k in range(steps // every + 1):
+        if k:
+            eng.step(every - 1)
+        eng.step(1, aux_last=True)
+        th = eng.thermo(s)
+        t.append(k * every)
+        e.append(0.5 * th["mv2"] + th["epot"])
+    t, e = np.asarray(t, dtype=float), np.asarray(e)
+    (slope, _), cov = np.polyfit(t, e, 1, cov=True)
+    scale = 1e5 / abs(e[0])
+    return slope * scale, np.sqrt(cov[0, 0]) * scale, float(np.max(np.abs(e - e[0])) / abs(e[0]))

@@ -114,3 +114,51 @@ def test_lj1m_energy_drift():
     print("LJ-1M NVE: E0/n %.6f, drift %.3g per 1e5 steps, fluctuation %.3g" % (e[0] / n, drift, fluct))
     assert drift < 1e-5
     eng.close()
+
+
+def test_lj1m_precision_variants_against_fp64():
+    """LJ-1M in the three precision variants from one start (the dsfloat
+    state after 300 steps): float positions, dsfloat positions and the FP64
+    variant.  Each variant's force error against FP64 forces of its own state
+    (the FP64 engine with the float cut-off test: the same pair set) and its
+    energy drift per 1e5 steps against the FP64 run's, fitted over 3000 steps."""
+    from _systems import energy_drift
+    r, L = fcc(64, 0.8442, jitter=0.05, seed=9)
+    n = r.shape[0]
+    desc = hg.system_desc(n, L, r_cut=2.5, truncation="shifted", skin=0.3, timestep=0.002)
+    eng = hg.Engine("dsfloat")
+    eng.add_system(desc)
+    eng.commit()
+    eng.set("position", r)
+    eng.set("velocity", maxwell_boltzmann(n, 0.722, seed=10))
+    eng.step(300)
+    r0, v0 = eng.get("position"), eng.get("velocity")
+    eng.close()
+
+    def start(precision):
+        e = hg.Engine(precision)
+        e.add_system(desc)
+        e.commit()
+        e.set("position", r0)
+        e.set("velocity", v0)
+        return e
+
+    ref = start("double")
+    ref.set_option("float_cutoff", 1)
+    drift = {}
+    for precision in ("float", "dsfloat", "double"):
+        e = start(precision)
+        if precision != "double":
+            e.force()
+            ref.set("position", e.get("position"))
+            ref.force()
+            emax, emed = rel_force_error(e.get("force"), ref.get("force"))
+            print("LJ-1M %s: force rel err vs FP64 of its state max %.3g median %.3g" % (precision, emax, emed))
+            assert emax < FORCE_TOL
+        drift[precision] = energy_drift(e, 3000, 100)
+        print("LJ-1M %s: drift %.3g +- %.2g per 1e5 steps, max |dE|/|E| %.3g" % ((precision,) + drift[precision]))
+        e.close()
+    ref.close()
+    for precision in ("float", "dsfloat"):
+        assert abs(drift[precision][0]) < 1e-5
+        assert abs(drift[precision][0] - drift["double"][0]) < 1e-5
