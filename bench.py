@@ -479,7 +479,7 @@ def run_ensemble(args):
     chains0, kernels0 = batch.get_option("rebuild_chains"), batch.get_option("step_kernels")
     clocks = ClockSampler(0)
     total_ms = 0.0
-    for _ in range(steps):
+    for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -630,6 +630,7 @@ def run_serve(args):
         dist.destroy_process_group()
     if rank != 0:
         return
+    completed, fcompleted = st["completed"], fst["completed"]
     st = {"makespan": makespan, "chunks": chunks}
     fst = {"makespan": fmakespan}
     line = {"metric": "particle-steps/s", "value": work / st["makespan"], "unit": "particle-steps/s", "n_gpus": world,
@@ -642,11 +643,11 @@ def run_serve(args):
                        "hbm_budget": budget, "time_limit_s": limit},
             "latency_s": {"p50": lat["p50"], "p99": lat["p99"], "mean": lat["mean"],
                           "over": "jobs completed%s" % (" within the time limit" if limit else "")},
-            "completed_jobs": st["completed"] if world == 1 else None,
+            "completed_jobs": completed if world == 1 else None,
             "makespan_s": st["makespan"],
             "fifo_plain_path": {"value": fwork / fst["makespan"], "unit": "particle-steps/s",
                                 "latency_s": flat, "makespan_s": fst["makespan"],
-                                "completed_jobs": fst["completed"] if world == 1 else None,
+                                "completed_jobs": fcompleted if world == 1 else None,
                                 "particle_steps": fwork},
             "throughput_ratio_vs_fifo": (work / st["makespan"]) / (fwork / fst["makespan"]), "clocks": clk}
     print(json.dumps(line))

@@ -255,7 +255,7 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
             p.q2 = (float)(d.index[ab] / 2);
             p.q3 = (float)(d.index[ab] % 2);
         }
-        p.pad = 0.0f;
+        p.rr_tie = 8.0f * (std::nextafter(p.rr_cut, INFINITY) - p.rr_cut);
         PairParam64& q = h.pairs64[ab];
         q.eps4 = 4 * eps;
         q.c48 = 48 * eps / sigma2;

@@ -348,7 +348,7 @@ __device__ __forceinline__ void two_sum_acc2(float2& s, float2& c, float2 x)
 
 // the parameters of two pairs, lane by lane
 struct PP2 {
-    float2 eps4, c48, sigma2, rr_cut, en_cut, r_cut, f_cut, sigma2_lo, c48_lo;
+    float2 eps4, c48, sigma2, rr_cut, en_cut, r_cut, f_cut, sigma2_lo, c48_lo, rr_tie;
 };
 
 __device__ __forceinline__ PP2 pack_params(const PairParam& a, const PairParam& b)
@@ -363,6 +363,7 @@ __device__ __forceinline__ PP2 pack_params(const PairParam& a, const PairParam& 
     p.f_cut = f2(a.f_cut, b.f_cut);
     p.sigma2_lo = f2(a.sigma2_lo, b.sigma2_lo);
     p.c48_lo = f2(a.c48_lo, b.c48_lo);
+    p.rr_tie = f2(a.rr_tie, b.rr_tie);
     return p;
 }
 
@@ -519,10 +520,16 @@ __device__ __forceinline__ void far_pair2(const PP2& p, const SysParam& P, float
     float2 dy = WRAP ? min_image2(sy, P.L[1], P.Linv[1]) : sy;
     float2 dz = WRAP ? min_image2(sz, P.L[2], P.Linv[2]) : sz;
     float2 rr = add2(add2(mul2(dx, dx), mul2(dy, dy)), mul2(dz, dz));
-    // the cut-off test of the list criterion, in scalar arithmetic (add2 and
-    // mul2 may come out contracted, and a pair at r_c^2 would flip)
-    const bool ka = va && rr_exact(dx.x, dy.x, dz.x) < p.rr_cut.x;
-    const bool kb = vb && rr_exact(dx.y, dy.y, dz.y) < p.rr_cut.y;
+    // the cut-off test of the list criterion; add2 and mul2 may come out
+    // contracted, which moves r^2 by at most an ulp or two, so pairs within
+    // PairParam::rr_tie of r_c^2 are decided again in scalar arithmetic
+    bool ka = va && rr.x < p.rr_cut.x;
+    bool kb = vb && rr.y < p.rr_cut.y;
+    const float2 gap = sub2(rr, p.rr_cut);
+    if (fabsf(gap.x) <= p.rr_tie.x || fabsf(gap.y) <= p.rr_tie.y) {
+        ka = va && rr_exact(dx.x, dy.x, dz.x) < p.rr_cut.x;
+        kb = vb && rr_exact(dx.y, dy.y, dz.y) < p.rr_cut.y;
+    }
     if (WRAP || LO) {
         // the separation's residual e: across the box the rounding error of
         // ri - rj, for dsfloat positions the difference of the lo words

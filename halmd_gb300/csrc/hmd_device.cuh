@@ -78,7 +78,7 @@ struct PairParam {
     //   morse:     q0 = eps / A, q1 = A = 2 B^2 - 1, q2 = 1 / (sigma B), q3 = r_min / (sigma B)
     //   power_law: q0 = eps, q1 = n, q2 = n/2 (integer as float), q3 = 1 for odd n else 0
     float q0, q1, q2, q3;
-    float pad;
+    float rr_tie;      // 8 ulp of rr_cut: packed squared distances this close to it are tested again in scalar
 };
 
 // a force in double (FP64 variant), 32-byte aligned
