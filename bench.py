@@ -679,7 +679,7 @@ def run_phases(args, w):
     inf1 = eng.info()
     out = {"workload": w["name"], "n": w["n"], "md_steps": args.phases,
            "rebuilds": int(inf1.rebuilds - inf0.rebuilds), "force_lanes": eng.get_option("force_lanes"),
-           "list_block": eng.get_option("list_block")}
+           "list_block": eng.get_option("list_block"), "neighbour_scan": eng.get_option("neighbour_scan")}
     for ph in ("integrate", "rebuild", "force", "finalize"):
         ms, cnt = eng.profile_get(ph)
         out[ph + "_ms_per_call"] = ms / max(cnt, 1)
@@ -783,7 +783,8 @@ def main():
     ap.add_argument("--list-block", type=int, default=0, help="list block width (0 auto, 4, 8) with --force-lanes")
     ap.add_argument("--fuse-steps", type=int, default=1, help="1: fused finalize + integrate in chunks")
     ap.add_argument("--neighbour-scan", type=int, default=0,
-                    help="list build: 0 auto, 1 per lane, 2 shared per warp")
+                    help="list build: 1 per lane, 2 shared per warp; 0: autotuned in the bench, the engine's "
+                         "choice by system size in --phases")
     ap.add_argument("--serve-jobs", type=int, default=200)
     ap.add_argument("--serve-steps-scale", type=float, default=0.1)
     ap.add_argument("--serve-max-slots", type=int, default=1 << 24)
@@ -850,7 +851,10 @@ def measure(args, w, world, rank, local, dist, steps, warmup, with_cpu):
         r = eng.get("position")
     eng.set("velocity", v)
     eng.step(max(1, args.md_steps))   # equilibrate lists / first rebuilds
-    from halmd_gb300.tune import autotune_force_lanes
+    from halmd_gb300.tune import autotune_force_lanes, autotune_list_build
+    list_ms = {}
+    if not args.neighbour_scan:
+        _, list_ms = autotune_list_build(eng, use_cache=False)
     if args.force_lanes:
         eng.set_option("force_lanes", args.force_lanes)
         eng.set_option("list_block", args.list_block)
@@ -949,7 +953,9 @@ def measure(args, w, world, rank, local, dist, steps, warmup, with_cpu):
                            parallelism="replicas" if world > 1 else "single"),
             "run": {"precision": "dsfloat", "rebuilds_in_timed_region": rebuilds,
                     "force_lanes": lanes, "list_block": eng.get_option("list_block"),
-                    "autotune_force_ms": {str(k): v for k, v in lane_ms.items()}},
+                    "autotune_force_ms": {str(k): v for k, v in lane_ms.items()},
+                    "neighbour_scan": eng.get_option("neighbour_scan"),
+                    "autotune_list_ms": list_ms},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "note": "per bench step: hmd_set(position, velocity) + hmd_step(%d) + "

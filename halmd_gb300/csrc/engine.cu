@@ -555,6 +555,7 @@ void Engine::commit()
     if (!tiles.empty())
         HMD_CUDA(cudaMemcpy(tiles_.p, tiles.data(), tiles.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     hist_.alloc(std::max<uint32_t>(hist_words, 1));
+    dtot_.alloc((size_t)table_size_ * 256);
     // force-kernel shape when not set (the autotuner refines it): small
     // engines need several lanes per particle to fill 152 SMs (measured best
     // at 64k particles: 4 lanes, 2 entries per load); large ones one lane
@@ -842,7 +843,7 @@ Dev Engine::dev() const
     d.tiles_grid = capacity_ ? d.S_grid / SORT_TILE : ntiles_;
     d.sm_count = sm_count_;
     d.status = status_.p; d.done = done_.p; d.any_rebuild = any_rebuild_.p;
-    d.key[0] = key0_.p; d.key[1] = key1_.p; d.val[0] = val0_.p; d.val[1] = val1_.p; d.hist = hist_.p;
+    d.key[0] = key0_.p; d.key[1] = key1_.p; d.val[0] = val0_.p; d.val[1] = val1_.p; d.hist = hist_.p; d.dtot = dtot_.p;
     d.tiles = tiles_.p; d.ntiles = ntiles_; d.rb = rb_.p;
     d.tpos = tpos_.p; d.tvel = tvel_.p; d.timg = timg_.p; d.tid = tid_.p;
     d.partial = partial_.p; d.thermo = thermo_.p;

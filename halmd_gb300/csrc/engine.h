@@ -199,7 +199,7 @@ private:
     DevBuf<PairParam64> dpair64_;
     DevBuf<float> en_pot_, stress_;
     DevBuf<uint32_t> id_, rid_, nbr_, nbr_count_, cell_, cell_count_, cell_sys_, chunk_sys_, tid_;
-    DevBuf<uint32_t> key0_, key1_, val0_, val1_, hist_, status_, done_, any_rebuild_, rb_;
+    DevBuf<uint32_t> key0_, key1_, val0_, val1_, hist_, dtot_, status_, done_, any_rebuild_, rb_;
     DevBuf<SysParam> dsys_;
     DevBuf<SysState> dst_;
     DevBuf<PairParam> dpair_;

@@ -1051,6 +1051,12 @@ __global__ void __launch_bounds__(128, LO ? HMD_FORCE_MINB_DS : HMD_FORCE_MINB) 
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = t / W, q = t % W;
+    // the particle's own words first (every slot index is a valid address):
+    // their latency overlaps the system parameters' and the pair table's
+    float4 ri, li = make_float4(0, 0, 0, 0);
+    if (LO) ldg_pos2(d.pos, i, ri, li);
+    else ri = ldg_hi(d.pos, i);
+    const uint32_t counts = __ldg(d.nbr_count + i);
     const uint32_t s = d.chunk_sys[(blockIdx.x * (blockDim.x / W)) / CHUNK];
     const SysParam& P = d.sys[s];
     __shared__ PairParam spp[MAX_SPECIES * MAX_SPECIES];
@@ -1060,12 +1066,9 @@ __global__ void __launch_bounds__(128, LO ? HMD_FORCE_MINB_DS : HMD_FORCE_MINB) 
     if (!P.active || !d.st[s].live || *d.status != 0u) return;   // block-uniform
     if (KIND != FK_GENERIC && force_kind_of(P) != KIND) return;      // another kind's launch
     if (KIND == FK_GENERIC && force_kind_of(P) == FK_FULL) return;   // no list: k_force_full
-    float4 ri, li = make_float4(0, 0, 0, 0);
-    if (LO) ldg_pos2(d.pos, i, ri, li);
-    else ri = ldg_hi(d.pos, i);
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;
-    const uint32_t packed = real ? d.nbr_count[i] : 0u;
+    const uint32_t packed = real ? counts : 0u;
     const uint32_t nn = packed & 0xFFFFu, nf = packed >> 16;   // near / far list parts
     const bool inner = !real || (fabsf(ri.x) < P.inner[0] && fabsf(ri.y) < P.inner[1] && fabsf(ri.z) < P.inner[2]);
     const bool wrap = __any_sync(0xFFFFFFFFu, !inner);

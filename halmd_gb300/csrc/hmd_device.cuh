@@ -208,6 +208,7 @@ struct Dev {
     uint32_t* key[2];
     uint32_t* val[2];
     uint32_t* hist;
+    uint32_t* dtot;            // [nsys * 256] digit totals of a system's keys in the current radix pass
     const uint2* tiles;        // (system, first slot) of every sort tile
     uint32_t ntiles;
     // rearrange temporaries

@@ -187,14 +187,20 @@ __global__ void __launch_bounds__(1024) k_rebuild_list(Dev d)
 // Segmented stable LSD radix sort, 8-bit digits (algorithm/gpu/radix_sort_kernel.cu:76-230
 // restated per system): the slot range of every system is cut into tiles of
 // 2048 keys that never straddle two systems (tile table d.tiles); each pass
-// is one launch over all tiles (digit histograms), one block per system
-// (digit-major exclusive scan of its tiles) and one launch over all tiles
-// (stable scatter with warp-match ranking).  Only systems that rebuild with
+// is one launch over all tiles (digit histograms and per-system digit
+// totals), one launch with a warp per (system, digit) (digit-major exclusive
+// scan of its tiles) and one launch over all tiles (stable scatter with
+// warp-match ranking).  Only systems that rebuild with
 // sorting on do work; the permutation ends in val[passes % 2].
 // ---------------------------------------------------------------------------
 
-constexpr int RADIX_THREADS = 256;
-constexpr int RADIX_ROUNDS = 8;
+// A tile of 2048 keys is taken by one block of 1024 threads in two rounds:
+// a small system has few tiles (KA-64k: 32), so the rounds a block runs
+// one after the other, each a dependent chain of load, rank and store, set
+// the time of the pass.
+constexpr int RADIX_THREADS = 1024;
+constexpr int RADIX_ROUNDS = 2;
+constexpr int RADIX_WARPS = RADIX_THREADS / 32;
 constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;
 static_assert(RADIX_TILE == SORT_TILE, "tile table and kernels disagree");
 
@@ -215,6 +221,8 @@ __global__ void __launch_bounds__(256) k_seg_keys(Dev d)
         const uint32_t i = P.off + (v - L.p[1][k]) * 256u + threadIdx.x;
         d.key[0][i] = slot_key(d, P, i);
         d.val[0][i] = i;
+        // digit totals of the first pass start from zero
+        if (v == L.p[1][k]) d.dtot[(size_t)L.sys[k] * 256u + threadIdx.x] = 0u;
     }
 }
 
@@ -225,11 +233,12 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_seg_hist(Dev d, const uint32_
     __shared__ uint32_t h[256];
     for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
         const uint32_t k = rb_find(L.p[2], L.n, v);
-        const SysParam& P = d.sys[L.sys[k]];
+        const uint32_t s = L.sys[k];
+        const SysParam& P = d.sys[s];
         const uint32_t local = v - L.p[2][k];
         const uint32_t first = P.off + local * RADIX_TILE;
         const uint32_t end = min(first + (uint32_t)RADIX_TILE, P.off + P.A);
-        h[threadIdx.x] = 0;
+        if (threadIdx.x < 256) h[threadIdx.x] = 0;
         __syncthreads();
 #pragma unroll
         for (int r = 0; r < RADIX_ROUNDS; ++r) {
@@ -237,69 +246,53 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_seg_hist(Dev d, const uint32_
             if (idx < end) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
         }
         __syncthreads();
-        d.hist[P.sort_hist_off + threadIdx.x * P.sort_ntiles + local] = h[threadIdx.x];
+        if (threadIdx.x < 256) {
+            const uint32_t c = h[threadIdx.x];
+            d.hist[P.sort_hist_off + threadIdx.x * P.sort_ntiles + local] = c;
+            if (c) atomicAdd(&d.dtot[(size_t)s * 256u + threadIdx.x], c);
+        }
         __syncthreads();
     }
 }
 
-// exclusive scan of one system's histogram (digit-major over its tiles) by one
-// block of 1024 threads: each warp owns a contiguous chunk, reads it
-// lane-strided (coalesced) once to total it and once more to scan it with
-// warp shuffles and a running carry; offsets come out as absolute slots
-__device__ void seg_scan_system(const Dev& d, uint32_t s);
-
-__global__ void __launch_bounds__(1024) k_seg_scan(Dev d)
+// Exclusive scan of a system's histogram, digit-major over its tiles, one
+// warp per digit: the digit's base is the sum of the totals of the smaller
+// digits (Dev::dtot, accumulated by k_seg_hist), its row of tile counts is
+// scanned lane-strided with warp shuffles and a running carry.  A grid of
+// (systems, 32) blocks of 8 warps covers the 256 digits of every system at
+// once; offsets come out as absolute slots.
+__global__ void __launch_bounds__(256) k_seg_scan(Dev d)
 {
     const RbList L = rb_list(d);
+    const uint32_t lane = threadIdx.x & 31u, g = blockIdx.y * 8u + (threadIdx.x >> 5);
     for (uint32_t k = blockIdx.x; k < L.n; k += gridDim.x) {
         const uint32_t s = L.sys[k];
-        if (sort_live(d, s)) seg_scan_system(d, s);   // block-uniform
+        if (!sort_live(d, s)) continue;   // warp-uniform
+        const SysParam& P = d.sys[s];
+        const uint32_t* tot = d.dtot + (size_t)s * 256u;
+        uint32_t base = 0;
+        for (uint32_t q = lane; q < g; q += 32) base += tot[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) base += __shfl_xor_sync(0xFFFFFFFFu, base, o);
+        uint32_t carry = P.off + base;
+        const uint32_t nt = P.sort_ntiles;
+        uint32_t* row = d.hist + P.sort_hist_off + g * nt;
+        for (uint32_t t0 = 0; t0 < nt; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            const uint32_t v = (t < nt) ? row[t] : 0u;
+            uint32_t incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= (uint32_t)o) incl += x;
+            }
+            if (t < nt) row[t] = carry + incl - v;
+            carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
+        }
     }
 }
 
-__device__ void seg_scan_system(const Dev& d, uint32_t s)
-{
-    const SysParam& P = d.sys[s];
-    uint32_t* hist = d.hist + P.sort_hist_off;
-    const uint32_t total = 256u * P.sort_ntiles;
-    __shared__ uint32_t s_warp[32];
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const uint32_t chunk = (total + nw - 1) / nw;
-    const uint32_t b = min(warp * chunk, total), e = min(b + chunk, total);
-    uint32_t sum = 0;
-    for (uint32_t k = b + lane; k < e; k += 32) sum += hist[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, o);
-    if (lane == 0) s_warp[warp] = sum;
-    __syncthreads();
-    if (warp == 0) {
-        const uint32_t v = lane < nw ? s_warp[lane] : 0u;
-        uint32_t incl = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= (uint32_t)o) incl += x;
-        }
-        if (lane < nw) s_warp[lane] = incl - v;
-    }
-    __syncthreads();
-    uint32_t carry = P.off + s_warp[warp];
-    for (uint32_t k0 = b; k0 < e; k0 += 32) {
-        const uint32_t k = k0 + lane;
-        const uint32_t v = (k < e) ? hist[k] : 0u;
-        uint32_t incl = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= (uint32_t)o) incl += x;
-        }
-        if (k < e) hist[k] = carry + incl - v;
-        carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
-    }
-    __syncthreads();   // s_warp is reused by the next system of the block
-}
-
-__device__ __forceinline__ void seg_scatter_tile(const Dev& d, const SysParam& P, uint32_t local, const uint32_t* kin,
+__device__ __forceinline__ void seg_scatter_tile(const Dev& d, uint32_t s, uint32_t local, const uint32_t* kin,
                                                  const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t shift);
 
 __global__ void __launch_bounds__(RADIX_THREADS) k_seg_scatter(Dev d, const uint32_t* kin, const uint32_t* vin,
@@ -309,25 +302,31 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_seg_scatter(Dev d, const uint
     const uint32_t total = L.p[2][L.n];
     for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
         const uint32_t k = rb_find(L.p[2], L.n, v);
-        seg_scatter_tile(d, d.sys[L.sys[k]], v - L.p[2][k], kin, vin, kout, vout, shift);
+        seg_scatter_tile(d, L.sys[k], v - L.p[2][k], kin, vin, kout, vout, shift);
         __syncthreads();
     }
 }
 
 // one tile of 2048 keys of a system: stable scatter by the current digit
-__device__ __forceinline__ void seg_scatter_tile(const Dev& d, const SysParam& P, uint32_t local, const uint32_t* kin,
+__device__ __forceinline__ void seg_scatter_tile(const Dev& d, uint32_t s, uint32_t local, const uint32_t* kin,
                                                  const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t shift)
 {
+    const SysParam& P = d.sys[s];
+    const uint32_t th = threadIdx.x, lane = th & 31u, warp = th >> 5;
+    // the scan of this pass has read the digit totals: the next pass's
+    // histograms accumulate from zero
+    if (local == 0 && th < 256) d.dtot[(size_t)s * 256u + th] = 0u;
     const uint32_t first = P.off + local * RADIX_TILE;
     const uint32_t end = min(first + (uint32_t)RADIX_TILE, P.off + P.A);
-    __shared__ uint32_t s_w[RADIX_THREADS / 32][256];
+    __shared__ uint32_t s_w[RADIX_WARPS][256];   // per warp and digit: count, then exclusive offset
     __shared__ uint32_t s_base[256];
     __shared__ uint32_t s_goff[256];
-    const uint32_t th = threadIdx.x, lane = th & 31u, warp = th >> 5;
-    s_base[th] = 0;
-    s_goff[th] = d.hist[P.sort_hist_off + th * P.sort_ntiles + local];
-#pragma unroll
-    for (int w = 0; w < RADIX_THREADS / 32; ++w) s_w[w][th] = 0;
+    uint32_t* s_flat = &s_w[0][0];
+    if (th < 256) {
+        s_base[th] = 0;
+        s_goff[th] = d.hist[P.sort_hist_off + th * P.sort_ntiles + local];
+    }
+    for (uint32_t k = th; k < RADIX_WARPS * 256u; k += RADIX_THREADS) s_flat[k] = 0;
     __syncthreads();
     const uint32_t lt = (1u << lane) - 1u;
     for (int r = 0; r < RADIX_ROUNDS; ++r) {
@@ -339,10 +338,10 @@ __device__ __forceinline__ void seg_scatter_tile(const Dev& d, const SysParam& P
         const uint32_t rank = __popc(peers & lt);
         if (valid && rank == 0) s_w[warp][dg] = __popc(peers);
         __syncthreads();
-        {
+        if (th < 256) {
             uint32_t run = s_base[th];
-#pragma unroll
-            for (int w = 0; w < RADIX_THREADS / 32; ++w) {
+#pragma unroll 8
+            for (int w = 0; w < RADIX_WARPS; ++w) {
                 const uint32_t c = s_w[w][th];
                 s_w[w][th] = run;
                 run += c;
@@ -356,8 +355,7 @@ __device__ __forceinline__ void seg_scatter_tile(const Dev& d, const SysParam& P
             vout[pos] = val;
         }
         __syncthreads();
-#pragma unroll
-        for (int w = 0; w < RADIX_THREADS / 32; ++w) s_w[w][th] = 0;
+        for (uint32_t k = th; k < RADIX_WARPS * 256u; k += RADIX_THREADS) s_flat[k] = 0;
         __syncthreads();
     }
 }
@@ -526,13 +524,13 @@ __device__ __forceinline__ void cell_sort_one(const Dev& d, uint32_t s, uint32_t
 // (max_displacement.cpp:60-72).
 //
 // Shared scan (Dev::nbr_scan = 2; by default systems of at least
-// NBR_SHARED_MIN_N particles): one
-// warp per 32 consecutive slots.  After the Hilbert sort these are
-// spatially compact, so the warp scans the cells around its bounding box
-// once for all 32 particles: lanes load 32 candidates of a cell at a time,
-// drop those farther than r_c + skin from the box, stage the rest in shared
-// memory, and every lane tests every staged candidate against its own
-// particle.  Smaller systems, and warps whose box spans too many cells (an
+// NBR_SHARED_MIN_N particles): one warp per 32 consecutive slots.  After the
+// Hilbert sort these are spatially compact, so the warp scans the cells
+// around their bounding box once for all 32 particles: lanes load 32
+// candidates of a cell at a time, drop those farther than r_c + skin from the
+// box and buffer the rest in shared memory; every lane tests each batch of
+// 32 buffered candidates against its own particle into bit masks and then
+// appends its neighbours in batch order (cluster_batch).  Smaller systems, and warps whose box spans too many cells (an
 // unsorted system, a tiny box), scan per lane instead: the 27 cells around each particle (each
 // distinct cell once when a dimension has fewer than 3 cells).  Both scans
 // test the same float criterion, so the pair sets are identical; entries are
@@ -600,22 +598,7 @@ struct NbrBox {
         : L{P.L[0], P.L[1], P.L[2]}, Linv{P.Linv[0], P.Linv[1], P.Linv[2]}, ns(P.ns) {}
 };
 
-template <bool WRAP>
-__device__ __forceinline__ void nbr_test(const NbrBox& B, float4 ri, uint32_t i, float4 rj, uint32_t j,
-                                         const float* rrcs, const float* rrnear, NbrOut& o)
-{
-    if (j == i) return;
-    const float sx = __fsub_rn(ri.x, rj.x), sy = __fsub_rn(ri.y, rj.y), sz = __fsub_rn(ri.z, rj.z);
-    // without a wrap every |s| < L/2, where min_image returns s unchanged
-    const float dx = WRAP ? min_image(sx, B.L[0], B.Linv[0]) : sx;
-    const float dy = WRAP ? min_image(sy, B.L[1], B.Linv[1]) : sy;
-    const float dz = WRAP ? min_image(sz, B.L[2], B.Linv[2]) : sz;
-    const float rr = rr_exact(dx, dy, dz);
-    const uint32_t b = species_bits(rj.w);
-    if (b < B.ns && rr <= rrcs[b]) o.add(j, rr < rrnear[b]);
-}
-
-// Pair cut-offs of the lane's particle for the per-lane scan: held in
+// Pair cut-offs of the lane's particle for the list scans: held in
 // registers for one or two species, read from shared memory per pair above
 template <int NS>
 struct LaneCut {
@@ -638,7 +621,7 @@ struct LaneCut {
     }
 };
 
-// nbr_test of the per-lane scan: the same criterion, in the same order
+// nbr_test (below) of the per-lane scan: the same criterion, in the same order
 template <bool WRAP, int NS>
 __device__ __forceinline__ void lane_test(const NbrBox& B, float4 ri, uint32_t i, float4 rj, uint32_t j,
                                           const LaneCut<NS>& cut, NbrOutInc& o)
@@ -747,29 +730,93 @@ __device__ __noinline__ uint2 lane_scan_call(const SysParam* Pp, const float4* p
     return make_uint2(o.nn, o.nf);
 }
 
-// the cells around the warp's bounding box [lo, hi] (cell ranges c0 + [0, nc)
-// per dimension, wrapped), for all lanes at once
-template <bool WRAP>
+// Per-warp shared memory of the cluster scan: a buffer of staged candidates
+// (a batch of 32 plus the up to 31 a cell adds beyond it), and per particle
+// of the cluster the batch position of the candidate that is the particle
+// itself
+struct ClusterSmem {
+    float4 pos[64];
+    uint32_t j[64];
+    uint32_t self[32];
+};
+
+// One batch of cnt <= 32 staged candidates (FULL: cnt = 32) against the
+// lane's particle: the list criterion of each candidate goes into bit u of
+// a keep mask and a near mask (no branch per candidate), then the lane
+// appends its neighbours in batch order (ascending u).  A particle meets
+// itself at r^2 = 0; that bit is cleared through ClusterSmem::self (the
+// list criterion's j != i).
+template <bool WRAP, int NS, bool FULL>
+__device__ __forceinline__ void cluster_batch(const NbrBox& B, ClusterSmem& sm, uint32_t cnt, uint32_t i0, float4 ri,
+                                              const LaneCut<NS>& cut, uint32_t lane, bool real, NbrOutInc& o)
+{
+    sm.self[lane] = 32u;
+    __syncwarp();
+    if (lane < cnt) {
+        const uint32_t j = sm.j[lane];
+        if (j - i0 < 32u) sm.self[j - i0] = lane;
+    }
+    __syncwarp();
+    if (real) {
+        uint32_t keep = 0, near = 0;
+#pragma unroll
+        for (uint32_t u = 0; u < 32u; ++u) {
+            if (!FULL && u >= cnt) break;
+            const float4 rj = sm.pos[u];
+            const float sx = __fsub_rn(ri.x, rj.x), sy = __fsub_rn(ri.y, rj.y), sz = __fsub_rn(ri.z, rj.z);
+            const float dx = WRAP ? min_image(sx, B.L[0], B.Linv[0]) : sx;
+            const float dy = WRAP ? min_image(sy, B.L[1], B.Linv[1]) : sy;
+            const float dz = WRAP ? min_image(sz, B.L[2], B.Linv[2]) : sz;
+            const float rr = rr_exact(dx, dy, dz);
+            float c, n;
+            const bool ok = cut.get(species_bits(rj.w), c, n);
+            if (ok && rr <= c) keep |= 1u << u;
+            if (rr < n) near |= 1u << u;
+        }
+        const uint32_t self = sm.self[lane];
+        if (self < 32u) keep &= ~(1u << self);
+        near &= keep;
+        while (keep) {
+            const uint32_t u = __ffs(keep) - 1u;
+            keep &= keep - 1u;
+            o.add(sm.j[u], (near >> u) & 1u);
+        }
+    }
+    __syncwarp();
+}
+
+// The cells around the bounding box [lo, hi] of the warp's 32 particles
+// (cell ranges c0 + [0, nc) per dimension, wrapped): lanes load 32
+// candidates of a cell at a time and buffer those within r_c + skin of the
+// box (in cell order, ascending slots within a cell); every full batch of
+// 32, and the rest at the end, goes through cluster_batch.
+template <bool WRAP, int NS>
 __device__ __forceinline__ void cluster_scan(const Dev& d, const SysParam& P, float4 ri, uint32_t i, bool real,
-                                             const float* rrcs, const float* rrnear, NbrOut& o, const float* lo,
-                                             const float* hi, const int* c0, const int* ncr, float rcs2,
-                                             float4* s_pos, uint32_t* s_j, uint32_t lane)
+                                             const LaneCut<NS>& cut, NbrOut& base, const float* lo, const float* hi,
+                                             const int* c0, const int* ncr, float rcs2, ClusterSmem& sm,
+                                             uint32_t lane)
 {
     const NbrBox B(P);
+    NbrOutInc o(base);
     const float cxb = 0.5f * (lo[0] + hi[0]), cyb = 0.5f * (lo[1] + hi[1]), czb = 0.5f * (lo[2] + hi[2]);
     const float hxb = 0.5f * (hi[0] - lo[0]), hyb = 0.5f * (hi[1] - lo[1]), hzb = 0.5f * (hi[2] - lo[2]);
     const int nx = P.ncell[0], ny = P.ncell[1], nz = P.ncell[2];
     const uint32_t cs = P.cell_size;
+    // the system's cell tables, read once (the list stores could alias SysParam)
+    const uint32_t* counts = d.cell_count + P.cell_off;
+    const uint32_t* cells = d.cell + P.cell_word_off;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    for (int kz = 0; kz < ncr[2]; ++kz) {
-        const int z = (c0[2] + kz) % nz;
-        for (int ky = 0; ky < ncr[1]; ++ky) {
-            const int y = (c0[1] + ky) % ny;
-            for (int kx = 0; kx < ncr[0]; ++kx) {
-                const int x = (c0[0] + kx) % nx;
+    const uint32_t i0 = i - lane;   // the warp's slots are consecutive
+    uint32_t nb = 0;   // buffered candidates (warp-uniform)
+    int z = c0[2];
+    for (int kz = 0; kz < ncr[2]; ++kz, z = (z + 1 == nz) ? 0 : z + 1) {
+        int y = c0[1];
+        for (int ky = 0; ky < ncr[1]; ++ky, y = (y + 1 == ny) ? 0 : y + 1) {
+            int x = c0[0];
+            for (int kx = 0; kx < ncr[0]; ++kx, x = (x + 1 == nx) ? 0 : x + 1) {
                 const uint32_t c = (uint32_t)(z * ny + y) * nx + x;
-                const uint32_t nc = min(d.cell_count[P.cell_off + c], cs);
-                const uint32_t* cell = d.cell + P.cell_word_off + c * cs;
+                const uint32_t nc = min(counts[c], cs);
+                const uint32_t* cell = cells + c * cs;
                 for (uint32_t k = 0; k < nc; k += 32) {
                     const bool have = k + lane < nc;
                     const uint32_t j = have ? __ldg(cell + k + lane) : 0u;
@@ -790,25 +837,48 @@ __device__ __forceinline__ void cluster_scan(const Dev& d, const SysParam& P, fl
                     }
                     const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, keep);
                     if (keep) {
-                        const uint32_t at = __popc(ballot & lt_mask);
-                        s_pos[at] = rj;
-                        s_j[at] = j;
+                        const uint32_t at = nb + __popc(ballot & lt_mask);
+                        sm.pos[at] = rj;
+                        sm.j[at] = j;
                     }
+                    nb += __popc(ballot);
                     __syncwarp();
-                    const uint32_t nk = __popc(ballot);
-                    if (real) {
-#pragma unroll 4
-                        for (uint32_t u = 0; u < nk; ++u) nbr_test<WRAP>(B, ri, i, s_pos[u], s_j[u], rrcs, rrnear, o);
+                    if (nb >= 32u) {
+                        cluster_batch<WRAP, NS, true>(B, sm, 32u, i0, ri, cut, lane, real, o);
+                        // the candidates beyond the batch move to the front
+                        const uint32_t rest = nb - 32u;
+                        float4 tp = make_float4(0, 0, 0, 0);
+                        uint32_t tj = 0;
+                        if (lane < rest) { tp = sm.pos[32u + lane]; tj = sm.j[32u + lane]; }
+                        __syncwarp();
+                        if (lane < rest) { sm.pos[lane] = tp; sm.j[lane] = tj; }
+                        nb = rest;
+                        __syncwarp();
                     }
-                    __syncwarp();
                 }
             }
         }
     }
+    if (nb > 0u) cluster_batch<WRAP, NS, false>(B, sm, nb, i0, ri, cut, lane, real, o);
+}
+
+template <bool WRAP>
+__device__ __forceinline__ void cluster_scan_ns(const Dev& d, const SysParam& P, float4 ri, uint32_t i, bool real,
+                                                const float* rrcs, const float* rrnear, NbrOut& o, const float* lo,
+                                                const float* hi, const int* c0, const int* ncr, float rcs2,
+                                                ClusterSmem& sm, uint32_t lane)
+{
+    if (P.ns == 1)
+        cluster_scan<WRAP, 1>(d, P, ri, i, real, LaneCut<1>(rrcs, rrnear, 1u), o, lo, hi, c0, ncr, rcs2, sm, lane);
+    else if (P.ns == 2)
+        cluster_scan<WRAP, 2>(d, P, ri, i, real, LaneCut<2>(rrcs, rrnear, 2u), o, lo, hi, c0, ncr, rcs2, sm, lane);
+    else
+        cluster_scan<WRAP, 0>(d, P, ri, i, real, LaneCut<0>(rrcs, rrnear, P.ns), o, lo, hi, c0, ncr, rcs2, sm,
+                              lane);
 }
 
 __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_t i, const float* s_rrcs,
-                                               const float* s_rrnear, float4* s_pos, uint32_t* s_j, uint32_t lane);
+                                               const float* s_rrnear, ClusterSmem& sm, uint32_t lane);
 
 // two virtual blocks of 128 slots per 256-slot unit of a rebuilding system.
 // Only v stays live across the scan: the list bounds are read again each
@@ -821,8 +891,7 @@ __global__ void __launch_bounds__(128, NBR_MINB) k_neighbour(Dev d)
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
     __shared__ float s_rrnear[MAX_SPECIES * MAX_SPECIES];
-    __shared__ float4 s_pos[4][32];
-    __shared__ uint32_t s_j[4][32];
+    __shared__ ClusterSmem s_cl[4];
     for (uint32_t v = blockIdx.x;; v += gridDim.x) {
         const RbList L = rb_list(d);
         if (v >= 2u * L.p[0][L.n]) break;
@@ -838,14 +907,14 @@ __global__ void __launch_bounds__(128, NBR_MINB) k_neighbour(Dev d)
             s_rrnear[threadIdx.x] = d.pair[P.pair_off + threadIdx.x].rr_near;
         }
         __syncthreads();
-        neighbour_slot(d, s, i, s_rrcs, s_rrnear, s_pos[warp], s_j[warp], lane);
+        neighbour_slot(d, s, i, s_rrcs, s_rrnear, s_cl[warp], lane);
         if (!LOOP) break;
     }
 }
 
 // the Verlet list of slot i (one lane; the warp's 32 slots scan together)
 __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_t i, const float* s_rrcs,
-                                               const float* s_rrnear, float4* s_pos, uint32_t* s_j, uint32_t lane)
+                                               const float* s_rrnear, ClusterSmem& sm, uint32_t lane)
 {
     const SysParam& P = d.sys[s];
     const float4 ri = pos_hi(d.pos, i);
@@ -857,8 +926,6 @@ __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_
     o.bstride = (size_t)d.S << o.lw;
     o.out = d.nbr + ((size_t)i << o.lw);
     o.cap = d.nbr_cap;
-    const float* rrcs = s_rrcs + (real ? a : 0u) * P.ns;
-    const float* rrnear = s_rrnear + (real ? a : 0u) * P.ns;
     if (real) {
         d.r0[i] = ri;
         if (d.ds) d.fpos[i] = fpos_encode(ri, pos_lo(d.pos, i), P.lo_inv_scale);
@@ -904,11 +971,13 @@ __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_
         // scan: a decision of the system alone, so its lists (and their order) do
         // not depend on the other systems of the engine
         const bool shared = d.nbr_scan == 2u || (d.nbr_scan == 0u && P.n >= NBR_SHARED_MIN_N);
+        const float* rrcs = s_rrcs + (real ? a : 0u) * P.ns;
+        const float* rrnear = s_rrnear + (real ? a : 0u) * P.ns;
         if (shared && ncells <= NBR_CLUSTER_MAX_CELLS) {
             if (wrap)
-                cluster_scan<true>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos, s_j, lane);
+                cluster_scan_ns<true>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, sm, lane);
             else
-                cluster_scan<false>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, s_pos, s_j, lane);
+                cluster_scan_ns<false>(d, P, ri, i, real, rrcs, rrnear, o, lo, hi, c0, ncr, rcs * rcs, sm, lane);
         } else {
             const bool lwrap = __any_sync(0xFFFFFFFFu, real && !far_from_faces(P, ri));
             if (real) {
@@ -970,7 +1039,7 @@ void launch_sort(const Dev& d, int passes, cudaStream_t st)
         const uint32_t shift = 8u * p;
         const int cur = p & 1;
         k_seg_hist<<<rb_grid(d, d.tiles_grid), RADIX_THREADS, 0, st>>>(d, d.key[cur], shift);
-        k_seg_scan<<<rb_grid(d, d.nsys), 1024, 0, st>>>(d);
+        k_seg_scan<<<dim3(rb_grid(d, d.nsys), 32), 256, 0, st>>>(d);
         k_seg_scatter<<<rb_grid(d, d.tiles_grid), RADIX_THREADS, 0, st>>>(d, d.key[cur], d.val[cur], d.key[1 - cur],
                                                                        d.val[1 - cur], shift);
     }

@@ -54,16 +54,18 @@ template <bool DS, bool MOM>
 __global__ void __launch_bounds__(256) k_finalize(Dev d)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // the slot's words first: they do not depend on the system's parameters
+    const float w = pos_hi(d.pos, i).w;
+    float4 v = d.vel[i];
+    float4 vl = DS ? d.vel[d.S + i] : make_float4(0, 0, 0, 0);
+    const float4 f = d.force[i];
     const uint32_t s = d.chunk_sys[i / CHUNK];
     const SysParam& P = d.sys[s];
     const SysState& st = d.st[s];
     double acc[NMOM] = {0.0, 0.0, 0.0, 0.0, 0.0};
     const bool run = P.active && st.live && *d.status == 0u && P.integrator != INTEG_DESCENT;   // block-uniform
-    if (run && species_bits(pos_hi(d.pos, i).w) != PLACEHOLDER) {
-        float4 v = d.vel[i];
-        float4 vl = make_float4(0, 0, 0, 0);
-        if (DS) vl = d.vel[d.S + i];
-        finalize_slot<DS>(d, P, st, i, v, vl, d.force[i]);
+    if (run && species_bits(w) != PLACEHOLDER) {
+        finalize_slot<DS>(d, P, st, i, v, vl, f);
         d.vel[i] = v;
         if (DS) d.vel[d.S + i] = vl;
         if (MOM) moment_terms(v, vl, acc);
@@ -198,13 +200,14 @@ template <bool DS, bool FIN>
 __global__ void __launch_bounds__(256) k_integrate(Dev d, cudaGraphConditionalHandle h, int use_handle)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const SlotIn<DS> in = load_slot<DS>(d, i);
     const uint32_t s = d.chunk_sys[i / CHUNK];
     const SysParam& P = d.sys[s];
     SysState& st = d.st[s];
     const bool clean = *d.status == 0u;
     const bool live = P.active && st.steps_left != 0u && clean;
     const bool fin = FIN && P.active && st.live && clean && P.integrator != INTEG_DESCENT;
-    const float rr = step_slot<DS, FIN, false>(d, P, st, i, d.pos, d.pos, fin, live, d.force[i]);
+    const float rr = step_slot<DS, FIN>(d, P, st, i, in, fin, live);
     step_decision(d, st, rr, h, use_handle);
 }
 

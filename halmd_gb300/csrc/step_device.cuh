@@ -1,6 +1,5 @@
-// step_device.cuh — the per-slot halves of a velocity-Verlet step, shared
-// by the integrate kernels (kernels_step.cu) and the pair-force kernel's
-// fused step epilogue (force.cuh): integrate (verlet_kernel.cu:38-72),
+// step_device.cuh — the per-slot halves of a velocity-Verlet step used by
+// the integrate kernels (kernels_step.cu): integrate (verlet_kernel.cu:38-72),
 // finalize (verlet_kernel.cu:78-98, Andersen, Maxwell-Boltzmann draws),
 // steepest descent, and the end-of-step decision.
 #pragma once
@@ -174,34 +173,53 @@ __device__ __forceinline__ void finalize_slot(const Dev& d, const SysParam& P, c
     half_kick<DS>(v.z, vl.z, f.z, v.w, P.dt_half);
 }
 
+// The words of one slot that a step reads.  None depends on the per-system
+// parameters, so the step kernels load them first, unconditionally (every
+// slot index is a valid address): one round of memory latency then covers
+// both instead of the parameters' round followed by the slot's.
+template <bool DS>
+struct SlotIn {
+    float4 r, rl, v, vl, f, q;   // position hi / lo, velocity hi / lo, force, r0
+};
+
+template <bool DS>
+__device__ __forceinline__ SlotIn<DS> load_slot(const Dev& d, uint32_t i)
+{
+    SlotIn<DS> in;
+    in.r = pos_hi(d.pos, i);
+    in.rl = DS ? pos_lo(d.pos, i) : make_float4(0, 0, 0, 0);
+    in.v = d.vel[i];
+    in.vl = DS ? d.vel[d.S + i] : make_float4(0, 0, 0, 0);
+    in.f = d.force[i];
+    in.q = d.r0[i];
+    return in;
+}
+
 // One slot of a step: the finalize of the previous step (FIN and fin: its
-// force f) and the integrate of this one (live), positions read from src and
-// written to dst (COPY: dst is the other position buffer, written for every
-// slot; otherwise dst == src and only integrated slots are written).
-// Returns |r - r0|^2 of an integrated slot, else 0.
-template <bool DS, bool FIN, bool COPY>
+// force in.f) and the integrate of this one (live).  Only slots that
+// finalize or integrate are written.  Returns |r - r0|^2 of an integrated
+// slot, else 0.
+template <bool DS, bool FIN>
 __device__ __forceinline__ float step_slot(const Dev& d, const SysParam& P, const SysState& st, uint32_t i,
-                                           const float4* src, float4* dst, bool fin, bool live, float4 f)
+                                           const SlotIn<DS>& in, bool fin, bool live)
 {
     float rr = 0.0f;
-    float4 r = pos_hi(src, i);
-    float4 rl = make_float4(0, 0, 0, 0);
-    if (DS && (COPY || live)) rl = pos_lo(src, i);
+    float4 r = in.r;
+    float4 rl = in.rl;
+    const float4 f = in.f;
     const bool real = species_bits(r.w) != PLACEHOLDER;
     if (FIN && fin && !live && real) {
         // the system finished with the previous step: its last half-kick only
-        float4 v = d.vel[i];
-        float4 vl = make_float4(0, 0, 0, 0);
-        if (DS) vl = d.vel[d.S + i];
+        float4 v = in.v;
+        float4 vl = in.vl;
         finalize_slot<DS>(d, P, st, i, v, vl, f);
         d.vel[i] = v;
         if (DS) d.vel[d.S + i] = vl;
     }
     if (live && real) {
-        float4 v = d.vel[i];
+        float4 v = in.v;
         float4 k = make_float4(0, 0, 0, 0);   // box images crossed in this step
-        float4 vl = make_float4(0, 0, 0, 0);
-        if (DS) vl = d.vel[d.S + i];
+        float4 vl = in.vl;
         if (FIN && fin) finalize_slot<DS>(d, P, st, i, v, vl, f);
         if (P.integrator == INTEG_DESCENT) {   // block-uniform
             const float3 g = descent_move(f, P.descent_step, P.descent_max);
@@ -227,12 +245,10 @@ __device__ __forceinline__ float step_slot(const Dev& d, const SysParam& P, cons
             d.vel[i] = v;
             if (DS) d.vel[d.S + i] = vl;
         }
-        if (!COPY) {
-            pos_hi(dst, i) = r;
-            if (DS) {
-                pos_lo(dst, i) = rl;
-                d.fpos[i] = fpos_encode(r, rl, P.lo_inv_scale);
-            }
+        pos_hi(d.pos, i) = r;
+        if (DS) {
+            pos_lo(d.pos, i) = rl;
+            d.fpos[i] = fpos_encode(r, rl, P.lo_inv_scale);
         }
         if (k.x != 0.0f || k.y != 0.0f || k.z != 0.0f) {
             // image counters are read and written only on a wrap
@@ -242,18 +258,11 @@ __device__ __forceinline__ float step_slot(const Dev& d, const SysParam& P, cons
             im.z = __fadd_rn(im.z, k.z);
             d.img[i] = im;
         }
-        const float4 q = d.r0[i];
+        const float4 q = in.q;
         float dx = min_image(__fsub_rn(r.x, q.x), P.L[0], P.Linv[0]);
         float dy = min_image(__fsub_rn(r.y, q.y), P.L[1], P.Linv[1]);
         float dz = min_image(__fsub_rn(r.z, q.z), P.L[2], P.Linv[2]);
         rr = rr_exact(dx, dy, dz);
-    }
-    if (COPY) {
-        pos_hi(dst, i) = r;
-        if (DS) {
-            pos_lo(dst, i) = rl;
-            if (real) d.fpos[i] = fpos_encode(r, rl, P.lo_inv_scale);
-        }
     }
     return rr;
 }

@@ -3,9 +3,12 @@
 Picks the force kernel's lanes per particle (1, 2, 4 or 8 threads share one
 particle's neighbour list) and the list block width (entries one thread
 reads with one load = block / lanes) by timing the force kernel on the engine's own
-systems with CUDA events (the engine's per-phase profiler).  Results are
-cached as JSON keyed by (GPU name, slots bucket, mean list length bucket)
-so a later engine of similar size reuses the choice without timing.
+systems with CUDA events (the engine's per-phase profiler), and the list
+build's scan (per lane over the 27 cells around a particle, or shared by a
+warp of 32 particles over the cells around their bounding box) by timing
+the rebuild chain the same way.  Results are cached as JSON
+keyed by (GPU name, slots bucket, list capacity bucket) so a later engine of
+similar size reuses the choice without timing.
 """
 import json
 import math
@@ -13,6 +16,7 @@ import os
 
 CACHE = os.environ.get("HMD_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "halmd_gb300_tune.json"))
 CHOICES = ((1, 4), (2, 4), (2, 8), (4, 4), (4, 8), (8, 8))   # (lanes, list block)
+LIST_CHOICES = (1, 2)   # neighbour_scan: per lane, shared per warp
 
 
 def _gpu_name():
@@ -78,3 +82,43 @@ def autotune_force_lanes(engine, repeats=10, use_cache=True):
         db[key] = {"lanes": best[0], "block": best[1], "ms": out}
         _store(db)
     return best[0], out
+
+
+def autotune_list_build(engine, repeats=6, use_cache=True):
+    """Time the list rebuild chain for every list-build shape; keep the fastest.
+
+    Both scans build the same pair sets (one float criterion), so the choice
+    changes only the time (and the order of a particle's entries).  Returns
+    (scan, {"scan": ms per chain}) and leaves the engine on the fastest scan.
+    The engine must be committed and hold a representative state; every
+    system is flagged for a rebuild before each timed force evaluation."""
+    key = _key(engine) + "|list"
+    db = _load() if use_cache else {}
+    if use_cache and key in db and "scan" in db[key]:
+        engine.set_option("neighbour_scan", db[key]["scan"])
+        return db[key]["scan"], db[key]["ms"]
+    nsys = len(engine.systems)
+
+    def rebuild_all():
+        for s in range(nsys):
+            engine.request_rebuild(s)
+        engine.force()
+
+    timings = {}
+    for scan in LIST_CHOICES:
+        engine.set_option("neighbour_scan", scan)
+        rebuild_all()
+        engine.profile(True)
+        for _ in range(repeats):
+            rebuild_all()
+        ms, n = engine.profile_get("rebuild")
+        engine.profile(False)
+        timings[scan] = ms / max(n, 1)
+    best = min(timings, key=timings.get)
+    engine.set_option("neighbour_scan", best)
+    rebuild_all()
+    out = {str(k): v for k, v in timings.items()}
+    if use_cache:
+        db[key] = {"scan": best, "ms": out}
+        _store(db)
+    return best, out

@@ -174,7 +174,7 @@ HMD_API int hmd_engine_progress(hmd_engine* engine, uint64_t* step, uint32_t* st
  *                   (the reference's unroll_force_loop, neighbour.lua.in:98-101, is 32)
  *   "neighbour_scan" list build: 0 (auto: 2 for systems of at least 2^18 particles, else 1),
  *                   1 (each thread scans the 27 cells around its particle), 2 (each warp scans the
- *                   cells around its 32 particles once); both give the same lists
+ *                   cells around its 32 particles once); both give the same pair sets
  *   "neighbour_capacity" (get only) list slots per particle
  *   "rebuild_chains"     (get only) steps in which the rebuild chain ran (any system rebuilt)
  *   "list_block"    0 (auto), 4 or 8: entries per block of the list layout; each force thread

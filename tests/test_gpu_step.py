@@ -364,8 +364,8 @@ def test_nve_energy_conservation_lj4k(precision):
 def test_overflow_recovery_matches_ample_capacity(scan):
     a, r, v, L = lj_engine(neighbour_occupancy=20.0)   # list capacity 32 < ~78 needed
     b, *_ = lj_engine()
-    a.set_option("neighbour_scan", scan)
-    b.set_option("neighbour_scan", scan)
+    for e in (a, b):
+        e.set_option("neighbour_scan", scan)
     a.step(20)
     b.step(20)
     assert a.info().neighbour_capacity > 32
@@ -373,3 +373,4 @@ def test_overflow_recovery_matches_ample_capacity(scan):
     assert np.array_equal(a.get("velocity"), b.get("velocity"))
     a.close()
     b.close()
+
