@@ -576,16 +576,21 @@ struct NbrOutInc {
     }
     __device__ __forceinline__ void add(uint32_t j, bool near)
     {
-        if (o.nn + o.nf < o.cap) *(near ? pn : pf) = j;
-        const ptrdiff_t jump = (ptrdiff_t)(o.bstride - o.lmask);   // from the end of a block to the next
-        if (near) {
-            ++o.nn;
-            pn += (o.nn & o.lmask) ? (ptrdiff_t)1 : jump;
-        } else {
-            const uint32_t e = o.cap - 1u - o.nf;
-            ++o.nf;
-            pf -= (e & o.lmask) ? (ptrdiff_t)1 : jump;
-        }
+        if (near) add_near(j);
+        else add_far(j);
+    }
+    __device__ __forceinline__ void add_near(uint32_t j)
+    {
+        if (o.nn + o.nf < o.cap) *pn = j;
+        ++o.nn;
+        pn += (o.nn & o.lmask) ? (ptrdiff_t)1 : (ptrdiff_t)(o.bstride - o.lmask);   // to the next block
+    }
+    __device__ __forceinline__ void add_far(uint32_t j)
+    {
+        if (o.nn + o.nf < o.cap) *pf = j;
+        const uint32_t e = o.cap - 1u - o.nf;
+        ++o.nf;
+        pf -= (e & o.lmask) ? (ptrdiff_t)1 : (ptrdiff_t)(o.bstride - o.lmask);
     }
 };
 
@@ -776,10 +781,18 @@ __device__ __forceinline__ void cluster_batch(const NbrBox& B, ClusterSmem& sm, 
         const uint32_t self = sm.self[lane];
         if (self < 32u) keep &= ~(1u << self);
         near &= keep;
-        while (keep) {
-            const uint32_t u = __ffs(keep) - 1u;
-            keep &= keep - 1u;
-            o.add(sm.j[u], (near >> u) & 1u);
+        uint32_t far = keep & ~near;
+        // near entries, then far entries: each loop without a branch on the
+        // part (the parts grow from the two ends of the list independently)
+        while (near) {
+            const uint32_t u = __ffs(near) - 1u;
+            near &= near - 1u;
+            o.add_near(sm.j[u]);
+        }
+        while (far) {
+            const uint32_t u = __ffs(far) - 1u;
+            far &= far - 1u;
+            o.add_far(sm.j[u]);
         }
     }
     __syncwarp();
