@@ -649,16 +649,40 @@ __device__ __forceinline__ float4 record_lo(float w, const SysParam& P)
                        __fsub_rn(fpos_fz(w, P.lo_exp_bits), P.lo_bias), 0.0f);
 }
 
-// li - lo of two gathered records, per component, two entries per
-// instruction: the separation residuals the lo words contribute
-__device__ __forceinline__ void record_dl2(float4 li, float wa, float wb, const SysParam& P, float2& ex, float2& ey,
-                                           float2& ez)
+// the own lo words as the records decode theirs: lo + (2^23 + 512) s, the
+// lo word rounded to the code unit s (as lo_code rounds it) in the binade of
+// the decoded fields
+__device__ __forceinline__ float4 lo_anchor(float4 li, const SysParam& P)
+{
+    return make_float4(__fadd_rn(li.x, P.lo_bias), __fadd_rn(li.y, P.lo_bias), __fadd_rn(li.z, P.lo_bias), 0.0f);
+}
+
+// li - lj of two gathered records, per component, two entries per
+// instruction: the separation residuals the lo words contribute.
+// EXACT_LI (near pairs, whose forces are the most sensitive to the
+// separation): the own lo word as it is, minus the neighbour's decoded one
+// (lj = field - bias, exact).  Otherwise (far pairs): the anchor minus the
+// field, one subtraction; both lie in one binade, so the difference is
+// exactly (c_i - c_j) s, the own lo word rounded to the unit s as well (at
+// most s/2 = ulp(L/2) / 2048 from the exact form).
+template <bool EXACT_LI>
+__device__ __forceinline__ void record_dl2(float4 li, float4 anchor, float wa, float wb, const SysParam& P,
+                                           float2& ex, float2& ey, float2& ez)
 {
     const uint32_t eb = P.lo_exp_bits;
-    const float2 bias = bc2(P.lo_bias);
-    ex = sub2(bc2(li.x), sub2(f2(fpos_fx(wa, eb), fpos_fx(wb, eb)), bias));
-    ey = sub2(bc2(li.y), sub2(f2(fpos_fy(wa, eb), fpos_fy(wb, eb)), bias));
-    ez = sub2(bc2(li.z), sub2(f2(fpos_fz(wa, eb), fpos_fz(wb, eb)), bias));
+    const float2 fx = f2(fpos_fx(wa, eb), fpos_fx(wb, eb));
+    const float2 fy = f2(fpos_fy(wa, eb), fpos_fy(wb, eb));
+    const float2 fz = f2(fpos_fz(wa, eb), fpos_fz(wb, eb));
+    if (EXACT_LI) {
+        const float2 bias = bc2(P.lo_bias);
+        ex = sub2(bc2(li.x), sub2(fx, bias));
+        ey = sub2(bc2(li.y), sub2(fy, bias));
+        ez = sub2(bc2(li.z), sub2(fz, bias));
+    } else {
+        ex = sub2(bc2(anchor.x), fx);
+        ey = sub2(bc2(anchor.y), fy);
+        ez = sub2(bc2(anchor.z), fz);
+    }
 }
 
 // species of a gathered neighbour
@@ -725,6 +749,7 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
     const PairParam* row = spp + a * ns;
     PP2 p1;
     if (NS1) p1 = pack_params(spp[0], spp[0]);
+    const float4 anchor = (LO && FAR) ? lo_anchor(li, P) : li;
     const uint32_t nblk = (cnt + LB - 1) / LB;
     V jv;
     if (HMD_FORCE_PREFETCH && nblk > 0) jv = ld_list(lst);
@@ -750,7 +775,7 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
 #pragma unroll
         for (int e = 0; e < E; e += 2) {
             float2 lx = bc2(0.0f), ly = bc2(0.0f), lz = bc2(0.0f);
-            if (LO) record_dl2(li, rj[e].w, rj[e + 1].w, P, lx, ly, lz);
+            if (LO) record_dl2<!FAR>(li, anchor, rj[e].w, rj[e + 1].w, P, lx, ly, lz);
             PP2 pp;
             bool va = in[e], vb = in[e + 1];
             if (NS1) {

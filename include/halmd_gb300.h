@@ -359,8 +359,7 @@ HMD_API int hmd_dynamics_shells(hmd_dynamics* dyn, int32_t tcf, uint32_t* nshell
  * - The first call in each CUDA context (on a device: its primary context,
  *   and again after cudaDeviceReset, which makes a new one) looks up the
  *   scratch array's address, which can load this library's device code
- *   there: make that first call, on every device used, before any stream
- *   capture begins.
+ *   into that context.
  * - Nothing needs to be zeroed first.
  * - All calls on one device share the one scratch array: calls that can
  *   overlap (different streams, or host threads without ordering) race and
