@@ -336,6 +336,8 @@ void Engine::layout_system(SysHost& h, uint32_t rank, uint32_t align)
         P.lo_inv_scale = (float)std::ldexp(1.0, -es);
         P.lo_exp_bits = (uint32_t)(es + 23 + 127) << 23;  // the float 2^23 s
         P.lo_bias = (float)std::ldexp(8388608.0 + 512.0, es);
+        P.lo_exp_bits_y = (uint32_t)(es + 13 + 127) << 23;   // the float 2^13 s
+        P.lo_bias_y = (float)std::ldexp(8192.0 + 512.0, es);
     }
     // Hilbert depth (gpu/sorts/hilbert.cpp:51-54)
     P.depth = std::min(10u, (uint32_t)std::ceil(std::log((double)Lmax) / M_LN2));

@@ -645,16 +645,17 @@ __device__ __forceinline__ float4 gather_pos(const Dev& d, uint32_t j)
 __device__ __forceinline__ float4 record_lo(float w, const SysParam& P)
 {
     return make_float4(__fsub_rn(fpos_fx(w, P.lo_exp_bits), P.lo_bias),
-                       __fsub_rn(fpos_fy(w, P.lo_exp_bits), P.lo_bias),
+                       __fsub_rn(fpos_fy(w, P.lo_exp_bits_y), P.lo_bias_y),
                        __fsub_rn(fpos_fz(w, P.lo_exp_bits), P.lo_bias), 0.0f);
 }
 
-// the own lo words as the records decode theirs: lo + (2^23 + 512) s, the
-// lo word rounded to the code unit s (as lo_code rounds it) in the binade of
-// the decoded fields
+// the own lo words in the binades of the records' decoded fields:
+// lo + (2^23 + 512) s for x and z, the lo word rounded to the code unit s
+// (as lo_code rounds it), and lo + (2^13 + 512) s for y, rounded to
+// s / 1024
 __device__ __forceinline__ float4 lo_anchor(float4 li, const SysParam& P)
 {
-    return make_float4(__fadd_rn(li.x, P.lo_bias), __fadd_rn(li.y, P.lo_bias), __fadd_rn(li.z, P.lo_bias), 0.0f);
+    return make_float4(__fadd_rn(li.x, P.lo_bias), __fadd_rn(li.y, P.lo_bias_y), __fadd_rn(li.z, P.lo_bias), 0.0f);
 }
 
 // li - lj of two gathered records, per component, two entries per
@@ -663,20 +664,20 @@ __device__ __forceinline__ float4 lo_anchor(float4 li, const SysParam& P)
 // separation): the own lo word as it is, minus the neighbour's decoded one
 // (lj = field - bias, exact).  Otherwise (far pairs): the anchor minus the
 // field, one subtraction; both lie in one binade, so the difference is
-// exactly (c_i - c_j) s, the own lo word rounded to the unit s as well (at
-// most s/2 = ulp(L/2) / 2048 from the exact form).
+// exact: (c_i - c_j) s with the own lo word rounded to the unit s as well
+// (at most s/2 = ulp(L/2) / 2048 from the exact form; finer for y).
 template <bool EXACT_LI>
 __device__ __forceinline__ void record_dl2(float4 li, float4 anchor, float wa, float wb, const SysParam& P,
                                            float2& ex, float2& ey, float2& ez)
 {
-    const uint32_t eb = P.lo_exp_bits;
+    const uint32_t eb = P.lo_exp_bits, eby = P.lo_exp_bits_y;
     const float2 fx = f2(fpos_fx(wa, eb), fpos_fx(wb, eb));
-    const float2 fy = f2(fpos_fy(wa, eb), fpos_fy(wb, eb));
+    const float2 fy = f2(fpos_fy(wa, eby), fpos_fy(wb, eby));
     const float2 fz = f2(fpos_fz(wa, eb), fpos_fz(wb, eb));
     if (EXACT_LI) {
         const float2 bias = bc2(P.lo_bias);
         ex = sub2(bc2(li.x), sub2(fx, bias));
-        ey = sub2(bc2(li.y), sub2(fy, bias));
+        ey = sub2(bc2(li.y), sub2(fy, bc2(P.lo_bias_y)));
         ez = sub2(bc2(li.z), sub2(fz, bias));
     } else {
         ex = sub2(bc2(anchor.x), fx);

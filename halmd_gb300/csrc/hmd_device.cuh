@@ -125,8 +125,10 @@ struct SysParam {
     uint32_t near_in_range;    // 1: a near pair (NEAR_SIGMA sigma + skin apart at most) is always inside r_c
     float lo_scale;            // unit s of the lo-word codes of Dev::fpos (a power of two)
     float lo_inv_scale;        // 1 / s
-    uint32_t lo_exp_bits;      // bits of the float 2^23 s (a code field ORed in gives (2^23 + field) s)
+    uint32_t lo_exp_bits;      // bits of the float 2^23 s (the x or z field ORed in gives (2^23 + field) s)
     float lo_bias;             // (2^23 + 512) s
+    uint32_t lo_exp_bits_y;    // bits of the float 2^13 s (the y field in place gives (2^13 + field) s)
+    float lo_bias_y;           // (2^13 + 512) s
     uint32_t pot;              // pair potential (Pot)
     uint32_t interval;         // INTEG_BOLTZMANN: steps between velocity draws
     double dt64;               // the time step in double (FP64 variant)
@@ -233,15 +235,17 @@ __device__ __forceinline__ const float4& pos_lo(const float4* p, uint32_t i) { r
 __device__ __forceinline__ float4 ldg_hi(const float4* p, uint32_t i) { return __ldg(p + 2 * (size_t)i); }
 
 // The force kernel's gather record of a dsfloat slot, 16 bytes: the hi
-// word's x, y, z and in w the species (bits 0-1) and the lo words as
-// multiples c of the system's lo_scale s = ulp(L/2) / 1024, stored as the
-// 10-bit fields c + 512 (bits 2-11, 12-21, 22-31).  |lo| <= ulp(L/2)/2 =
-// 512 s, so c = lo / s rounded (clamped to +-511) is within s/2 of it (s a
-// power of two: the scaling is exact).  The full double-single word pair is
-// 32 bytes; the gathers of the force kernel are bound by the L1 data path,
-// and half the bytes halve that traffic.  A field ORed into the mantissa of
-// 2^23 s gives the float (2^23 + c + 512) s, so c s costs one subtraction
-// (record_lo), no integer conversion.
+// word's x, y, z and in w the lo words as multiples c of the system's
+// lo_scale s = ulp(L/2) / 1024, stored as the 10-bit fields c + 512 (x in
+// bits 0-9, y in bits 10-19, z in bits 22-31), and the species (bits
+// 20-21).  |lo| <= ulp(L/2)/2 = 512 s, so c = lo / s rounded (clamped to
+// +-511) is within s/2 of it (s a power of two: the scaling is exact).  The
+// full double-single word pair is 32 bytes; the gathers of the force kernel
+// are bound by the L1 data path, and half the bytes halve that traffic.  The
+// x field ORed into the mantissa of 2^23 s gives the float (2^23 + c + 512) s,
+// the y field left in place (mantissa bits 10-19) in that of 2^13 s gives
+// (2^13 + c + 512) s, and the z field shifted down like x: c s costs one
+// subtraction (record_lo), no integer conversion, and x and y no shift.
 __device__ __forceinline__ uint32_t lo_code(float lo, float inv_s)
 {
     const int c = __float2int_rn(__fmul_rn(lo, inv_s));
@@ -250,21 +254,22 @@ __device__ __forceinline__ uint32_t lo_code(float lo, float inv_s)
 
 __device__ __forceinline__ float4 fpos_encode(float4 hi, float4 lo, float inv_s)
 {
-    const uint32_t w = (species_bits(hi.w) & 3u) | (lo_code(lo.x, inv_s) << 2) | (lo_code(lo.y, inv_s) << 12) |
+    const uint32_t w = lo_code(lo.x, inv_s) | (lo_code(lo.y, inv_s) << 10) | ((species_bits(hi.w) & 3u) << 20) |
                        (lo_code(lo.z, inv_s) << 22);
     return make_float4(hi.x, hi.y, hi.z, __uint_as_float(w));
 }
 
 // species of a record's w word, and its three code fields as the floats
-// (2^23 + c + 512) s (exp_bits: SysParam::lo_exp_bits)
-__device__ __forceinline__ uint32_t fpos_species(float w) { return __float_as_uint(w) & 3u; }
+// (2^23 + c + 512) s for x and z (exp_bits: SysParam::lo_exp_bits) and
+// (2^13 + c + 512) s for y (SysParam::lo_exp_bits_y)
+__device__ __forceinline__ uint32_t fpos_species(float w) { return (__float_as_uint(w) >> 20) & 3u; }
 __device__ __forceinline__ float fpos_fx(float w, uint32_t exp_bits)
 {
-    return __uint_as_float(((__float_as_uint(w) >> 2) & 0x3FFu) | exp_bits);
+    return __uint_as_float((__float_as_uint(w) & 0x3FFu) | exp_bits);
 }
-__device__ __forceinline__ float fpos_fy(float w, uint32_t exp_bits)
+__device__ __forceinline__ float fpos_fy(float w, uint32_t exp_bits_y)
 {
-    return __uint_as_float(((__float_as_uint(w) >> 12) & 0x3FFu) | exp_bits);
+    return __uint_as_float((__float_as_uint(w) & 0xFFC00u) | exp_bits_y);
 }
 __device__ __forceinline__ float fpos_fz(float w, uint32_t exp_bits)
 {
