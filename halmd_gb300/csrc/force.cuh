@@ -347,8 +347,11 @@ __device__ __forceinline__ void two_sum_acc2(float2& s, float2& c, float2 x)
 }
 
 // the parameters of two pairs, lane by lane
-struct PP2 {
-    float2 eps4, c48, sigma2, rr_cut, en_cut, r_cut, f_cut, sigma2_lo, c48_lo, rr_tie;
+// (16-byte aligned, the fields a far pair reads first in pairs: a table of
+// these in shared memory is read with 16-byte loads, each half of every
+// field already in place)
+struct alignas(16) PP2 {
+    float2 sigma2, c48, rr_cut, rr_tie, eps4, en_cut, r_cut, f_cut, sigma2_lo, c48_lo;
 };
 
 __device__ __forceinline__ PP2 pack_params(const PairParam& a, const PairParam& b)
@@ -733,9 +736,14 @@ __device__ __forceinline__ void force_blocks(const Dev& d, uint32_t i, uint32_t 
 }
 
 // force_blocks with the E entries of a load taken two at a time (E even)
+// pair2: the packed parameters of every (species, neighbour species,
+// neighbour species) triple of the system in shared memory (several
+// species; pack_params of the two rows), so a pair of entries reads its
+// PP2 with four 16-byte loads instead of building it field by field
 template <int W, int E, int TRX, bool AUX, bool WRAP, bool FAR, bool LO, bool EXACT = false>
 __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t q, uint32_t cnt, const SysParam& P,
-                                              const PairParam* spp, float4 ri, float4 li, uint32_t a, ForceAcc2& A)
+                                              const PairParam* spp, const PP2* pair2, float4 ri, float4 li, uint32_t a,
+                                              ForceAcc2& A)
 {
     static_assert(E % 2 == 0, "entries are taken in pairs");
     constexpr bool NS1 = TRX >= ONE_SPECIES;
@@ -747,7 +755,7 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
     if (FAR) lst += (size_t)(d.nbr_cap / LB - 1) * bstride * W;
     const ptrdiff_t step = FAR ? -(ptrdiff_t)(bstride * W) : (ptrdiff_t)(bstride * W);
     const uint32_t ns = P.ns;
-    const PairParam* row = spp + a * ns;
+    const PP2* row2 = pair2 + a * ns * ns;
     PP2 p1;
     if (NS1) p1 = pack_params(spp[0], spp[0]);
     const float4 anchor = (LO && FAR) ? lo_anchor(li, P) : li;
@@ -787,7 +795,7 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
                 const uint32_t ba = nbr_species<LO>(rj[e].w), bb = nbr_species<LO>(rj[e + 1].w);
                 va = va && ba < ns;
                 vb = vb && bb < ns;
-                pp = pack_params(row[ba < ns ? ba : 0u], row[bb < ns ? bb : 0u]);
+                pp = row2[(ba < ns ? ba : 0u) * ns + (bb < ns ? bb : 0u)];
             }
             if (FAR) far_pair2<TR, AUX, WRAP, LO>(pp, P, ri, rj[e], rj[e + 1], va, vb, A, lx, ly, lz);
             else near_pair2<TR, AUX, WRAP, EXACT, LO>(pp, P, ri, rj[e], rj[e + 1], va, vb, A, lx, ly, lz);
@@ -799,17 +807,17 @@ __device__ __forceinline__ void force_blocks2(const Dev& d, uint32_t i, uint32_t
 template <int W, int E, int TR, bool AUX, bool LO>
 __device__ __forceinline__ void force_dispatch(const Dev& d, uint32_t i, uint32_t q, uint32_t nn, uint32_t nf,
                                                bool wrap, bool exact, const SysParam& P, const PairParam* spp,
-                                               float4 ri, float4 li, uint32_t a, ForceAcc& A)
+                                               const PP2* pair2, float4 ri, float4 li, uint32_t a, ForceAcc& A)
 {
     if constexpr (E % 2 == 0) {
         ForceAcc2 B;
         if (wrap) {
-            force_blocks2<W, E, TR, AUX, true, false, LO>(d, i, q, nn, P, spp, ri, li, a, B);
-            force_blocks2<W, E, TR, AUX, true, true, LO>(d, i, q, nf, P, spp, ri, li, a, B);
+            force_blocks2<W, E, TR, AUX, true, false, LO>(d, i, q, nn, P, spp, pair2, ri, li, a, B);
+            force_blocks2<W, E, TR, AUX, true, true, LO>(d, i, q, nf, P, spp, pair2, ri, li, a, B);
         } else {
-            if (exact) force_blocks2<W, E, TR, AUX, false, false, LO, true>(d, i, q, nn, P, spp, ri, li, a, B);
-            else force_blocks2<W, E, TR, AUX, false, false, LO>(d, i, q, nn, P, spp, ri, li, a, B);
-            force_blocks2<W, E, TR, AUX, false, true, LO>(d, i, q, nf, P, spp, ri, li, a, B);
+            if (exact) force_blocks2<W, E, TR, AUX, false, false, LO, true>(d, i, q, nn, P, spp, pair2, ri, li, a, B);
+            else force_blocks2<W, E, TR, AUX, false, false, LO>(d, i, q, nn, P, spp, pair2, ri, li, a, B);
+            force_blocks2<W, E, TR, AUX, false, true, LO>(d, i, q, nf, P, spp, pair2, ri, li, a, B);
         }
         fold_lanes2<AUX>(B, A);
     } else if (wrap) {
@@ -1086,12 +1094,23 @@ __global__ void __launch_bounds__(128, LO ? HMD_FORCE_MINB_DS : HMD_FORCE_MINB) 
     const uint32_t s = d.chunk_sys[(blockIdx.x * (blockDim.x / W)) / CHUNK];
     const SysParam& P = d.sys[s];
     __shared__ PairParam spp[MAX_SPECIES * MAX_SPECIES];
+    // packed pair parameters per (species, neighbour, neighbour) for the
+    // several-species kinds of the two-entry path (force_blocks2)
+    constexpr bool PACKED2 = (E % 2 == 0) && KIND != FK_LJ1 && KIND != FK_POT;
+    __shared__ PP2 s_pair2[PACKED2 ? MAX_SPECIES * MAX_SPECIES * MAX_SPECIES : 1];
     const uint32_t np = P.ns * P.ns;
     if (threadIdx.x < np) spp[threadIdx.x] = d.pair[P.pair_off + threadIdx.x];
     __syncthreads();
     if (!P.active || !d.st[s].live || *d.status != 0u) return;   // block-uniform
     if (KIND != FK_GENERIC && force_kind_of(P) != KIND) return;      // another kind's launch
     if (KIND == FK_GENERIC && force_kind_of(P) == FK_FULL) return;   // no list: k_force_full
+    if (PACKED2) {
+        for (uint32_t k = threadIdx.x; k < np * P.ns; k += blockDim.x) {
+            const uint32_t sa = k / np, ba = (k / P.ns) % P.ns, bb = k % P.ns;
+            s_pair2[k] = pack_params(spp[sa * P.ns + ba], spp[sa * P.ns + bb]);
+        }
+        __syncthreads();
+    }
     const uint32_t a = species_bits(ri.w);
     const bool real = a != PLACEHOLDER;
     const uint32_t packed = real ? counts : 0u;
@@ -1104,22 +1123,22 @@ __global__ void __launch_bounds__(128, LO ? HMD_FORCE_MINB_DS : HMD_FORCE_MINB) 
     ForceAcc A;
     if (real) {
         if constexpr (KIND == FK_LJ1) {
-            force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A);
+            force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, s_pair2, ri, li, a, A);
         } else if constexpr (KIND == FK_SHIFTED) {
-            force_dispatch<W, E, TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A);
+            force_dispatch<W, E, TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, s_pair2, ri, li, a, A);
         } else if constexpr (KIND == FK_SMOOTH) {
-            force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A);
+            force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, s_pair2, ri, li, a, A);
         } else if constexpr (KIND == FK_FSHIFT) {
-            force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A);
+            force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, s_pair2, ri, li, a, A);
         } else if constexpr (KIND == FK_POT) {
             force_pot<W, E, AUX, LO>(d, i, q, nn, nf, wrap, P, spp, ri, li, a, A);
         } else {
             switch (force_kind_of(P)) {
-            case FK_LJ1: force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A); break;
-            case FK_SHIFTED: force_dispatch<W, E, TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A); break;
-            case FK_SMOOTH: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A); break;
+            case FK_LJ1: force_dispatch<W, E, ONE_SPECIES + TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, s_pair2, ri, li, a, A); break;
+            case FK_SHIFTED: force_dispatch<W, E, TRUNC_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, s_pair2, ri, li, a, A); break;
+            case FK_SMOOTH: force_dispatch<W, E, TRUNC_SMOOTH_R4, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, s_pair2, ri, li, a, A); break;
             case FK_POT: force_pot<W, E, AUX, LO>(d, i, q, nn, nf, wrap, P, spp, ri, li, a, A); break;
-            default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, ri, li, a, A); break;
+            default: force_dispatch<W, E, TRUNC_FORCE_SHIFTED, AUX, LO>(d, i, q, nn, nf, wrap, exact, P, spp, s_pair2, ri, li, a, A); break;
             }
         }
     }
