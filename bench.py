@@ -99,12 +99,14 @@ def initial_state(w, seed=2024):
     return r, v, species, L
 
 
-def make_engine(w, L, seed=7, precision="dsfloat"):
+def make_engine(w, L, seed=7, precision="dsfloat", cell_occupancy=None):
     import halmd_gb300 as hg
     eng = hg.Engine(precision)
     extra = {}
     if w.get("occupancy"):
         extra["neighbour_occupancy"] = w["occupancy"]
+    if cell_occupancy:
+        extra["cell_occupancy"] = cell_occupancy
     if w["nspecies"] == 2:
         d = hg.system_desc(w["n"], L, epsilon=KA["eps"], sigma=KA["sigma"], r_cut=w.get("rc", 2.5),
                            truncation=w["trunc"], smoothing=0.005, skin=w["skin"], timestep=w["dt"],
@@ -782,6 +784,9 @@ def main():
                          "in --phases)")
     ap.add_argument("--list-block", type=int, default=0, help="list block width (0 auto, 4, 8) with --force-lanes")
     ap.add_argument("--fuse-steps", type=int, default=1, help="1: fused finalize + integrate in chunks")
+    ap.add_argument("--cell-occupancy", type=float, default=0.0,
+                    help="binning cell occupancy (the reference's parameter; 0: autotuned in the bench among "
+                         "0.5, 1 and 2, 0.5 elsewhere)")
     ap.add_argument("--neighbour-scan", type=int, default=0,
                     help="list build: 1 per lane, 2 shared per warp; 0: autotuned in the bench, the engine's "
                          "choice by system size in --phases")
@@ -839,7 +844,7 @@ def measure(args, w, world, rank, local, dist, steps, warmup, with_cpu):
     r, v, species, L = initial_state(w, seed=2024 + rank)
     if w.get("equilibrate"):
         r, v = equilibrated_state(w, r, v, species, L, seed=7 + rank)
-    eng = make_engine(w, L, seed=7 + rank)
+    eng = make_engine(w, L, seed=7 + rank, cell_occupancy=args.cell_occupancy or None)
     eng.set_option("fuse_steps", args.fuse_steps)
     if args.neighbour_scan:
         eng.set_option("neighbour_scan", args.neighbour_scan)
@@ -851,7 +856,27 @@ def measure(args, w, world, rank, local, dist, steps, warmup, with_cpu):
         r = eng.get("position")
     eng.set("velocity", v)
     eng.step(max(1, args.md_steps))   # equilibrate lists / first rebuilds
-    from halmd_gb300.tune import autotune_force_lanes, autotune_list_build
+    from halmd_gb300.tune import autotune_cell_occupancy, autotune_force_lanes, autotune_list_build
+    cell_occ, cell_ms = args.cell_occupancy or 0.5, {}
+    if not args.cell_occupancy:
+        # binning cell size: engines of each candidate cell occupancy on this state
+        r_now, v_now = eng.get("position"), eng.get("velocity")
+
+        def build(occ):
+            e = make_engine(w, L, seed=7 + rank, cell_occupancy=occ)
+            if args.neighbour_scan:
+                e.set_option("neighbour_scan", args.neighbour_scan)
+            e.set("species", species)
+            e.set("position", r_now)
+            e.set("velocity", v_now)
+            return e
+
+        cell_occ, cell_ms = autotune_cell_occupancy(build)
+        if cell_occ != 0.5:
+            eng.close()
+            eng = build(cell_occ)
+            eng.set_option("fuse_steps", args.fuse_steps)
+            eng.step(max(1, args.md_steps))
     list_ms = {}
     if not args.neighbour_scan:
         _, list_ms = autotune_list_build(eng, use_cache=False)
@@ -955,7 +980,8 @@ def measure(args, w, world, rank, local, dist, steps, warmup, with_cpu):
                     "force_lanes": lanes, "list_block": eng.get_option("list_block"),
                     "autotune_force_ms": {str(k): v for k, v in lane_ms.items()},
                     "neighbour_scan": eng.get_option("neighbour_scan"),
-                    "autotune_list_ms": list_ms},
+                    "autotune_list_ms": list_ms,
+                    "cell_occupancy": cell_occ, "autotune_cell_ms": cell_ms},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "note": "per bench step: hmd_set(position, velocity) + hmd_step(%d) + "

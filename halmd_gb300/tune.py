@@ -3,10 +3,12 @@
 Picks the force kernel's lanes per particle (1, 2, 4 or 8 threads share one
 particle's neighbour list) and the list block width (entries one thread
 reads with one load = block / lanes) by timing the force kernel on the engine's own
-systems with CUDA events (the engine's per-phase profiler), and the list
+systems with CUDA events (the engine's per-phase profiler), the list
 build's scan (per lane over the 27 cells around a particle, or shared by a
 warp of 32 particles over the cells around their bounding box) by timing
-the rebuild chain the same way.  Results are cached as JSON
+the rebuild chain the same way, and the cell size of the binning (through
+the cell occupancy the reference's sizing rule takes) by timing the
+rebuild chain of engines binned at each candidate.  Results are cached as JSON
 keyed by (GPU name, slots bucket, list capacity bucket) so a later engine of
 similar size reuses the choice without timing.
 """
@@ -17,6 +19,10 @@ import os
 CACHE = os.environ.get("HMD_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "halmd_gb300_tune.json"))
 CHOICES = ((1, 4), (2, 4), (2, 8), (4, 4), (4, 8), (8, 8))   # (lanes, list block)
 LIST_CHOICES = (1, 2)   # neighbour_scan: per lane, shared per warp
+# cell occupancy of the binning (binning.cpp:81-101): the reference's
+# default 0.5, whose cells are often capped at r_c + skin, and two that give
+# larger cells (cells never get smaller than r_c + skin)
+CELL_CHOICES = (0.5, 1.0, 2.0)
 
 
 def _gpu_name():
@@ -122,3 +128,35 @@ def autotune_list_build(engine, repeats=6, use_cache=True):
         db[key] = {"scan": best, "ms": out}
         _store(db)
     return best, out
+
+
+def autotune_cell_occupancy(build, candidates=CELL_CHOICES, repeats=5):
+    """Time the list rebuild chain of engines binned at each cell occupancy;
+    return the fastest.
+
+    build(occupancy) returns a committed engine holding the state to tune
+    on (positions set); it is closed here.  Every cell size gives the same
+    pair sets (the list criterion does not depend on the binning).  Returns
+    (occupancy, {"occupancy": ms per chain})."""
+    timings = {}
+    for occ in candidates:
+        eng = build(occ)
+        try:
+            nsys = len(eng.systems)
+
+            def rebuild_all():
+                for s in range(nsys):
+                    eng.request_rebuild(s)
+                eng.force()
+
+            rebuild_all()   # first build (and any growth of the cell capacity)
+            eng.profile(True)
+            for _ in range(repeats):
+                rebuild_all()
+            ms, n = eng.profile_get("rebuild")
+            eng.profile(False)
+            timings[occ] = ms / max(n, 1)
+        finally:
+            eng.close()
+    best = min(timings, key=timings.get)
+    return best, {str(k): v for k, v in timings.items()}
