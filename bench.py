@@ -829,7 +829,7 @@ def main():
         sub = measure(args, workload("lj1m"), world, rank, local, dist, min(args.steps, 10), 3,
                       not args.no_cpu_baseline)
         line["lj1m"] = {k: sub[k] for k in ("value", "unit", "ms_per_step", "steps", "warmup", "config", "e2e",
-                                            "gpu_launches", "roofline", "clocks", "cpu_baseline", "accuracy")
+                                            "gpu_launches", "roofline", "clocks", "cpu_baseline", "accuracy", "run")
                         if k in sub}
     if rank == 0:
         print(json.dumps(line))

@@ -20,6 +20,12 @@ namespace hmd {
 #ifndef HMD_FORCE_MINB
 #define HMD_FORCE_MINB 7
 #endif
+// threads per block of the force kernel (a multiple of 32 that divides 256:
+// systems are padded to 256 slots, so a block never straddles two)
+#ifndef HMD_FORCE_THREADS
+#define HMD_FORCE_THREADS 128
+#endif
+static_assert(HMD_FORCE_THREADS % 32 == 0 && 256 % HMD_FORCE_THREADS == 0, "force block size");
 // Resident blocks for the kernels of dsfloat engines, whose gathers carry
 // the lo words (16-byte records, hmd_device.cuh fpos_encode): at LJ-1M
 // 215 us with 5 blocks against 214 us with 6 and 216 us with 7; at KA-64k
@@ -1081,7 +1087,8 @@ __device__ __forceinline__ void force_pot(const Dev& d, uint32_t i, uint32_t q, 
 
 // LO: the engine holds dsfloat positions (the separations carry the lo words)
 template <int W, int E, int KIND, bool AUX, bool LO>
-__global__ void __launch_bounds__(128, LO ? HMD_FORCE_MINB_DS : HMD_FORCE_MINB) k_force(Dev d)
+__global__ void __launch_bounds__(HMD_FORCE_THREADS, (LO ? HMD_FORCE_MINB_DS : HMD_FORCE_MINB) * 128 / HMD_FORCE_THREADS)
+k_force(Dev d)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i = t / W, q = t % W;
@@ -1168,13 +1175,14 @@ __global__ void __launch_bounds__(128, LO ? HMD_FORCE_MINB_DS : HMD_FORCE_MINB) 
 template <int W, int E, int KIND>
 static void launch_force_shape(const Dev& d, bool aux, cudaStream_t st)
 {
-    const unsigned grid = (unsigned)((size_t)d.S_grid * W / 128);
+    constexpr unsigned T = HMD_FORCE_THREADS;
+    const unsigned grid = (unsigned)((size_t)d.S_grid * W / T);
     if (d.ds) {
-        if (aux) k_force<W, E, KIND, true, true><<<grid, 128, 0, st>>>(d);
-        else k_force<W, E, KIND, false, true><<<grid, 128, 0, st>>>(d);
+        if (aux) k_force<W, E, KIND, true, true><<<grid, T, 0, st>>>(d);
+        else k_force<W, E, KIND, false, true><<<grid, T, 0, st>>>(d);
     } else {
-        if (aux) k_force<W, E, KIND, true, false><<<grid, 128, 0, st>>>(d);
-        else k_force<W, E, KIND, false, false><<<grid, 128, 0, st>>>(d);
+        if (aux) k_force<W, E, KIND, true, false><<<grid, T, 0, st>>>(d);
+        else k_force<W, E, KIND, false, false><<<grid, T, 0, st>>>(d);
     }
 }
 
