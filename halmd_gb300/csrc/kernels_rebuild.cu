@@ -543,6 +543,13 @@ __device__ __forceinline__ void cell_sort_one(const Dev& d, uint32_t s, uint32_t
 // pushed spill traffic into the shared scan's inner loop: 14 % more
 // instructions, and 72 registers without spills measured 1 % slower than 64).
 constexpr int NBR_MINB = 8;
+// A one-system engine whose grid fills at most NBR_SMALL_MINB blocks per SM
+// (KA-64k: 500 blocks on 152 SMs) gains nothing from 8 resident blocks; its
+// build runs with 4, and up to 128 registers, which the compiler spends on
+// more loads in flight (KA-64k chain 0.30 against 0.32 ms with the per-lane
+// scan, 0.29 against 0.33 ms with the shared scan; at LJ-1M, whose grid is
+// 13 waves, 4 blocks measured 1.20 against 0.99 ms).
+constexpr int NBR_SMALL_MINB = 4;
 
 constexpr uint32_t NBR_CLUSTER_MAX_CELLS = 150;   // larger cell ranges: per-lane scan
 struct NbrOut {
@@ -898,8 +905,8 @@ __device__ __forceinline__ void neighbour_slot(const Dev& d, uint32_t s, uint32_
 // round (the list stores may alias them, so they are not kept in
 // registers) and the pair table is staged again per virtual block.
 // LOOP = false: the grid has a block per virtual block (one-system engines).
-template <bool LOOP>
-__global__ void __launch_bounds__(128, NBR_MINB) k_neighbour(Dev d)
+template <bool LOOP, int MINB = NBR_MINB>
+__global__ void __launch_bounds__(128, MINB) k_neighbour(Dev d)
 {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ float s_rrcs[MAX_SPECIES * MAX_SPECIES];
@@ -1079,7 +1086,8 @@ void launch_neighbour(const Dev& d, cudaStream_t st)
     // one-system engines launch a block per virtual block; otherwise one
     // wave of resident blocks loops over the virtual blocks
     const unsigned all = std::max(1u, d.S_grid / 128);
-    if (d.nsys == 1) k_neighbour<false><<<all, 128, 0, st>>>(d);
+    if (d.nsys == 1 && all <= d.sm_count * NBR_SMALL_MINB) k_neighbour<false, NBR_SMALL_MINB><<<all, 128, 0, st>>>(d);
+    else if (d.nsys == 1) k_neighbour<false><<<all, 128, 0, st>>>(d);
     else k_neighbour<true><<<std::min(all, d.sm_count * NBR_MINB), 128, 0, st>>>(d);
 }
 
