@@ -658,7 +658,7 @@ def run_serve(args):
 def run_phases(args, w):
     """Per-phase breakdown of the MD step through the module-level calls."""
     r, v, species, L = initial_state(w)
-    eng = make_engine(w, L)
+    eng = make_engine(w, L, cell_occupancy=args.cell_occupancy or None)
     if args.force_lanes:
         eng.set_option("force_lanes", args.force_lanes)
         eng.set_option("list_block", args.list_block)
@@ -681,7 +681,8 @@ def run_phases(args, w):
     inf1 = eng.info()
     out = {"workload": w["name"], "n": w["n"], "md_steps": args.phases,
            "rebuilds": int(inf1.rebuilds - inf0.rebuilds), "force_lanes": eng.get_option("force_lanes"),
-           "list_block": eng.get_option("list_block"), "neighbour_scan": eng.get_option("neighbour_scan")}
+           "list_block": eng.get_option("list_block"), "neighbour_scan": eng.get_option("neighbour_scan"),
+           "cell_occupancy": args.cell_occupancy or 0.5}
     for ph in ("integrate", "rebuild", "force", "finalize"):
         ms, cnt = eng.profile_get(ph)
         out[ph + "_ms_per_call"] = ms / max(cnt, 1)
