@@ -787,7 +787,7 @@ def main():
     ap.add_argument("--fuse-steps", type=int, default=1, help="1: fused finalize + integrate in chunks")
     ap.add_argument("--cell-occupancy", type=float, default=0.0,
                     help="binning cell occupancy (the reference's parameter; 0: autotuned in the bench among "
-                         "0.5, 1 and 2, 0.5 elsewhere)")
+                         "0.5, 1, 1.5 and 2, 0.5 elsewhere)")
     ap.add_argument("--neighbour-scan", type=int, default=0,
                     help="list build: 1 per lane, 2 shared per warp; 0: autotuned in the bench, the engine's "
                          "choice by system size in --phases")

@@ -20,9 +20,9 @@ CACHE = os.environ.get("HMD_TUNE_CACHE", os.path.join(os.path.expanduser("~"), "
 CHOICES = ((1, 4), (2, 4), (2, 8), (4, 4), (4, 8), (8, 8))   # (lanes, list block)
 LIST_CHOICES = (1, 2)   # neighbour_scan: per lane, shared per warp
 # cell occupancy of the binning (binning.cpp:81-101): the reference's
-# default 0.5, whose cells are often capped at r_c + skin, and two that give
-# larger cells (cells never get smaller than r_c + skin)
-CELL_CHOICES = (0.5, 1.0, 2.0)
+# default 0.5, whose cells are often capped at r_c + skin, and three that
+# give larger cells (cells never get smaller than r_c + skin)
+CELL_CHOICES = (0.5, 1.0, 1.5, 2.0)
 
 
 def _gpu_name():
