@@ -91,7 +91,7 @@ def test_cell_occupancy_tuner_closes_every_engine_and_returns_the_fastest():
     built = []
 
     def build(occ):
-        e = FakeEngine(rebuild_ms=lambda o, occ: {0.5: 0.9, 1.0: 0.7, 2.0: 0.8}[occ], occupancy=occ)
+        e = FakeEngine(rebuild_ms=lambda o, occ: 0.7 + 0.1 * abs(occ - 1.0), occupancy=occ)
         built.append(e)
         return e
 
