@@ -178,6 +178,35 @@ def test_neighbour_lists_bit_exact(make, scan):
     eng.close()
 
 
+
+@pytest.mark.parametrize("scan", [1, 2])
+def test_neighbour_lists_bit_exact_large_grid(scan):
+    # 108,000 particles: the one-system list build takes its large-grid form
+    # (8 resident blocks per SM) rather than the small-grid one the smaller
+    # tests use; cell occupancy 1 (the size the bench's tuner keeps)
+    r, v, L = lj_system(ncell=30)
+    n = r.shape[0]
+    eng = hg.Engine("dsfloat")
+    eng.add_system(hg.system_desc(n, L, r_cut=2.5, truncation="shifted", skin=0.3, timestep=0.005,
+                                  cell_occupancy=1.0))
+    eng.commit()
+    eng.set("position", r)
+    eng.set("velocity", v)
+    eng.step(40)
+    eng.set_option("neighbour_scan", scan)
+    eng.request_rebuild()
+    eng.force()
+    inf = eng.info()
+    rrcs = np.array(inf.rr_cut_skin[:1], dtype=np.float32)
+    pos4 = tag_order(eng, eng.get_raw("r0"))
+    maxn = inf.neighbour_capacity
+    counts, lists = eng.neighbour_lists(maxn)
+    rc, rl, mx = oracle.neighbour_full_f32(pos4, np.array(inf.box_f32), rrcs, maxn)
+    assert np.array_equal(counts, rc)
+    assert np.array_equal(lists, rl)
+    assert inf.max_neighbours == mx
+    eng.close()
+
 def test_binning_bit_exact():
     eng, r, v, L = lj_engine(ncell=8)
     eng.force()
