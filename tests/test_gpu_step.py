@@ -204,7 +204,8 @@ def test_neighbour_lists_bit_exact_large_grid(scan):
     rc, rl, mx = oracle.neighbour_full_f32(pos4, np.array(inf.box_f32), rrcs, maxn)
     assert np.array_equal(counts, rc)
     assert np.array_equal(lists, rl)
-    assert inf.max_neighbours == mx
+    # the engine keeps the largest list length of every build since commit
+    assert counts.max() == mx and inf.max_neighbours >= mx
     eng.close()
 
 def test_binning_bit_exact():
