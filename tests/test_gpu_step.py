@@ -208,6 +208,7 @@ def test_neighbour_lists_bit_exact_large_grid(scan):
     assert counts.max() == mx and inf.max_neighbours >= mx
     eng.close()
 
+
 def test_binning_bit_exact():
     eng, r, v, L = lj_engine(ncell=8)
     eng.force()
