@@ -143,16 +143,22 @@ def test_ka_smooth_r4_force_parity():
 
 
 @pytest.mark.parametrize("scan", [1, 2])
-@pytest.mark.parametrize("make", ["lj", "ka", "lj_large", "ka_large", "lj_unsorted"])
+@pytest.mark.parametrize("make", ["lj", "ka", "lj_large", "ka_large", "lj_unsorted", "lj_large_cells",
+                                  "ka_large_cells"])
 def test_neighbour_lists_bit_exact(make, scan):
     # both list-build scans (per lane, shared per warp) on small boxes (3 cells
     # per dimension: every warp wraps), large boxes (interior warps scan
-    # without minimum image) and an unsorted system (warps too spread out for
-    # the shared scan: it falls back to the per-lane scan)
+    # without minimum image), an unsorted system (warps too spread out for
+    # the shared scan: it falls back to the per-lane scan), and cells larger
+    # than r_c + skin (cell occupancy 2, a size the cell autotuner offers)
     if make == "lj":
         eng, r, v, L = lj_engine()
     elif make == "lj_large":
         eng, r, v, L = lj_engine(ncell=16)
+    elif make == "lj_large_cells":
+        eng, r, v, L = lj_engine(ncell=16, cell_occupancy=2.0)
+    elif make == "ka_large_cells":
+        eng, r, v, sp, L = ka_engine(ncell=14, cell_occupancy=2.0)
     elif make == "lj_unsorted":
         eng, r, v, L = lj_engine(ncell=12, sort=0)
         perm = np.random.default_rng(3).permutation(r.shape[0])   # slots in random spatial order
