@@ -428,7 +428,7 @@ def run_ensemble(args):
     import torch
     import halmd_gb300 as hg
     from halmd_gb300.shard import combine, partition, rank_env
-    from halmd_gb300.tune import autotune_force_lanes
+    from halmd_gb300.tune import autotune_force_lanes, autotune_list_build
     rank, world, local = rank_env()
     torch.cuda.set_device(local)
     if world > 1:
@@ -455,6 +455,9 @@ def run_ensemble(args):
     for k, s in enumerate(specs):
         load(batch, k, s)
     batch.step(M)
+    list_ms = {}
+    if not args.neighbour_scan:
+        _, list_ms = autotune_list_build(batch, use_cache=False)
     lanes, lane_ms = autotune_force_lanes(batch, use_cache=False)
     if args.phases:
         # module-path breakdown of the batched step (one launch per phase for all replicas)
@@ -499,14 +502,17 @@ def run_ensemble(args):
     ntot_all = combine(ntot, 0.0, device="cuda")[0]
     # step-graph kernels, plus the rebuild chain in every step where any replica rebuilt
     launches = (batch.get_option("step_kernels") - kernels0) + chains * inf.rebuild_kernels
+    scan_used = batch.get_option("neighbour_scan")
     batch.close()
 
-    # the plain path: one engine per replica, stepped one after another
+    # the plain path: one engine per replica, stepped one after another (the
+    # same list-build scan as the batch)
     engines = []
     for s in specs:
         e = hg.Engine("dsfloat")
         e.add_system(hg.system_desc(s["n"], s["L"], **s["desc"]))
         e.commit()
+        e.set_option("neighbour_scan", scan_used)
         load(e, 0, s)
         e.step(M)
         engines.append(e)
@@ -536,6 +542,7 @@ def run_ensemble(args):
                        "parallelism": "replicas bin-packed over %d GPUs" % world if world > 1 else "single",
                        "md_steps_per_bench_step": M, "force_lanes": lanes,
                        "autotune_force_ms": {str(k): v for k, v in lane_ms.items()},
+                       "neighbour_scan": scan_used, "autotune_list_ms": list_ms,
                        "l2": "flushed (256 MB write) between timed bench steps"},
             "looped_plain_path": {"value": looped, "unit": "particle-steps/s",
                                   "note": "256 engines of one replica each, hmd_step(%d) in turn" % M},
