@@ -422,9 +422,10 @@ def ensemble_specs(count=256, seed=256):
     return out
 
 
-def run_ensemble(args):
+def run_ensemble(args, emit=True):
     """ENS-256: all replicas in one engine (one launch per phase, graph-captured
-    step chunks) against looping the one-system path over the same replicas."""
+    step chunks) against looping the one-system path over the same replicas.
+    Returns the line (rank 0), printed unless emit is false."""
     import torch
     import halmd_gb300 as hg
     from halmd_gb300.shard import combine, partition, rank_env
@@ -547,7 +548,9 @@ def run_ensemble(args):
             "looped_plain_path": {"value": looped, "unit": "particle-steps/s",
                                   "note": "256 engines of one replica each, hmd_step(%d) in turn" % M},
             "batch_speedup": batched / looped, "gpu_launches": launches, "clocks": clk}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def serve_jobs(count, steps_scale, rate=50.0, seed=2000):
@@ -585,7 +588,7 @@ def serve_jobs(count, steps_scale, rate=50.0, seed=2000):
     return jobs
 
 
-def run_serve(args):
+def run_serve(args, emit=True):
     """SERVE: continuous batching under an 80% HBM budget against a FIFO run
     of the one-system path, same job stream."""
     import torch
@@ -659,7 +662,9 @@ def run_serve(args):
                                 "completed_jobs": fcompleted if world == 1 else None,
                                 "particle_steps": fwork},
             "throughput_ratio_vs_fifo": (work / st["makespan"]) / (fwork / fst["makespan"]), "clocks": clk}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def run_phases(args, w):
@@ -780,6 +785,11 @@ def main():
     ap.add_argument("--md-steps", type=int, default=100, help="MD steps per bench step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-lj1m", action="store_true", help="default workload: skip the LJ-1M sub-record")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="default workload: skip the ENS-256 and SERVE sub-records")
+    ap.add_argument("--sub-serve-time-limit", type=float, default=30.0,
+                    help="default workload: seconds of the SERVE sub-record's stream prefix (each of the served "
+                         "and FIFO runs)")
     ap.add_argument("--variants", type=int, default=0,
                     help="run the float, dsfloat and FP64 variants of the workload for N MD steps from the same "
                          "start and print their energy drift and force error, then exit")
@@ -839,6 +849,27 @@ def main():
         line["lj1m"] = {k: sub[k] for k in ("value", "unit", "ms_per_step", "steps", "warmup", "config", "e2e",
                                             "gpu_launches", "roofline", "clocks", "cpu_baseline", "accuracy", "run")
                         if k in sub}
+    if world == 1 and args.workload == "ka64k" and not args.no_batched:
+        # the batched and served forms of the metric, short: ENS-256 with 3
+        # bench steps, and SERVE's 2000-job stream over a time-bounded prefix
+        import copy
+        a = copy.copy(args)
+        a.steps, a.warmup, a.phases, a.neighbour_scan = 3, 3, 0, 0
+        try:
+            ens = run_ensemble(a, emit=False)
+            line["ens256"] = {k: ens[k] for k in ("value", "unit", "ms_per_step", "steps", "config",
+                                                  "looped_plain_path", "batch_speedup", "gpu_launches", "clocks")}
+        except Exception as ex:   # a failed sub-record must not take the headline with it
+            line["ens256"] = {"error": "%s: %s" % (type(ex).__name__, str(ex)[:200])}
+        a = copy.copy(args)
+        a.serve_jobs, a.serve_steps_scale, a.serve_time_limit = 2000, 1.0, args.sub_serve_time_limit
+        try:
+            srv = run_serve(a, emit=False)
+            line["serve"] = {k: srv[k] for k in ("value", "unit", "config", "latency_s", "completed_jobs",
+                                                 "makespan_s", "fifo_plain_path", "throughput_ratio_vs_fifo",
+                                                 "clocks")}
+        except Exception as ex:
+            line["serve"] = {"error": "%s: %s" % (type(ex).__name__, str(ex)[:200])}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
